@@ -1,0 +1,1154 @@
+// gb_build.cu -- GPU BVH builder behind rtcCommitScene.
+//
+// Replaces the reference's CPU binned-SAH builder (kernels/bvh/bvh_builder_sah.cpp:111-189,
+// kernels/builders/bvh_builder_sah.h:222-319) with a GPU pipeline:
+//   1. primrefs: per-triangle validity + AABB, scene and centroid bounds
+//      (validity rule of kernels/common/scene_triangle_mesh.h:127-147)
+//   2. 63-bit Morton codes of the centroids (21 bits per axis)
+//   3. stable LSD radix sort of (code, primref index), 8-bit digits; passes
+//      whose digit is constant over all keys are skipped.  Stable sorting by
+//      key with the index as value gives exactly std::stable_sort's order.
+//   4. PLOC agglomerative clustering (nearest neighbour by merged-box surface
+//      area within a window of +-16 clusters, mutual pairs merge) -> binary tree
+//   5. top-down collapse into 8-wide nodes (largest-area child opened first),
+//      child boxes quantised to 8 bits per plane, children placed in slots
+//      so that the ray's direction octant gives a near-to-far visiting order,
+//      leaves of <= 3 triangles written as v0/e1/e2 records.
+// Everything is deterministic: the same input gives the same bytes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "gb_build.h"
+#include "gb_common.h"
+#include "gb_launch.h"
+
+namespace gb {
+
+#define GB_CHECK(x)                                \
+  do {                                             \
+    cudaError_t e_ = (x);                          \
+    if (e_ != cudaSuccess) return e_;              \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float ord2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+#else
+  uint32_t b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+  float f;
+  memcpy(&f, &b, 4);
+  return f;
+#endif
+}
+
+struct BoundsAcc {
+  uint32_t glo[3], ghi[3];  // ordered-uint min/max of geometry bounds
+  uint32_t clo[3], chi[3];  // of centroids
+  uint32_t nvalid;
+  uint32_t pad;
+  unsigned long long kand, kor;
+};
+
+__device__ __forceinline__ float half_area(float3 lo, float3 hi) {
+  const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+  return dx * (dy + dz) + dy * dz;
+}
+
+__device__ __forceinline__ float3 f3min(float3 a, float3 b) {
+  return make_float3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z));
+}
+__device__ __forceinline__ float3 f3max(float3 a, float3 b) {
+  return make_float3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z));
+}
+
+// ---------------------------------------------------------------------------
+// 1. primrefs
+// ---------------------------------------------------------------------------
+
+constexpr float kFltLarge = 1.844E18f;  // common/math/constants.h:34
+
+__device__ __forceinline__ bool vtx_ok(float x, float y, float z) {
+  return x > -kFltLarge && x < kFltLarge && y > -kFltLarge && y < kFltLarge && z > -kFltLarge && z < kFltLarge;
+}
+
+__device__ __forceinline__ float3 load_vtx(const GeomDesc& g, uint32_t i) {
+  const float* p = reinterpret_cast<const float*>(g.verts + (uint64_t)i * g.vstride);
+  return make_float3(p[0], p[1], p[2]);
+}
+
+__device__ __forceinline__ uint3 load_tri(const GeomDesc& g, uint32_t j) {
+  const uint32_t* p = reinterpret_cast<const uint32_t*>(g.idx + (uint64_t)j * g.istride);
+  return make_uint3(p[0], p[1], p[2]);
+}
+
+__device__ __forceinline__ int find_geom(const GeomDesc* geoms, int ngeoms, uint32_t gi) {
+  int lo = 0, hi = ngeoms - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (geoms[mid].prim_offset <= gi) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// plo[i] = (lo.xyz, geometry slot), phi[i] = (hi.xyz, primID); invalid
+// triangles get an empty box (+inf,-inf).
+__global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ geoms, int ngeoms, uint32_t total,
+                                                  float4* __restrict__ plo, float4* __restrict__ phi,
+                                                  BoundsAcc* acc) {
+  __shared__ uint32_t s_b[12];
+  __shared__ uint32_t s_cnt;
+  if (threadIdx.x < 12) s_b[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0xFFFFFFFFu : 0u;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = false;
+  float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+  if (gi < total) {
+    const int gs = find_geom(geoms, ngeoms, gi);
+    const GeomDesc g = geoms[gs];
+    const uint32_t j = gi - g.prim_offset;
+    const uint3 t = load_tri(g, j);
+    if (t.x < g.nverts && t.y < g.nverts && t.z < g.nverts) {
+      const float3 a = load_vtx(g, t.x), b = load_vtx(g, t.y), c = load_vtx(g, t.z);
+      if (vtx_ok(a.x, a.y, a.z) && vtx_ok(b.x, b.y, b.z) && vtx_ok(c.x, c.y, c.z)) {
+        ok = true;
+        lo = f3min(f3min(a, b), c);
+        hi = f3max(f3max(a, b), c);
+      }
+    }
+    plo[gi] = make_float4(lo.x, lo.y, lo.z, __uint_as_float((uint32_t)gs));
+    phi[gi] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(j));
+  }
+  // warp-reduce bounds then shared atomics
+  float v[12];
+  const float3 c = make_float3((lo.x + hi.x) * 0.5f, (lo.y + hi.y) * 0.5f, (lo.z + hi.z) * 0.5f);
+  v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = hi.x; v[4] = hi.y; v[5] = hi.z;
+  if (ok) { v[6] = c.x; v[7] = c.y; v[8] = c.z; v[9] = c.x; v[10] = c.y; v[11] = c.z; }
+  else { v[6] = v[7] = v[8] = INFINITY; v[9] = v[10] = v[11] = -INFINITY; }
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    float x = v[k];
+    const bool isMin = (k % 6) < 3;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      float y = __shfl_xor_sync(0xFFFFFFFFu, x, o);
+      x = isMin ? fminf(x, y) : fmaxf(x, y);
+    }
+    v[k] = x;
+  }
+  const unsigned nok = __popc(__ballot_sync(0xFFFFFFFFu, ok));
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      if ((k % 6) < 3) atomicMin(&s_b[k], f2ord(v[k]));
+      else atomicMax(&s_b[k], f2ord(v[k]));
+    }
+    atomicAdd(&s_cnt, nok);
+  }
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    const int k = threadIdx.x;
+    uint32_t* dst = (k < 3) ? &acc->glo[k] : (k < 6) ? &acc->ghi[k - 3] : (k < 9) ? &acc->clo[k - 6] : &acc->chi[k - 9];
+    if ((k % 6) < 3) atomicMin(dst, s_b[k]); else atomicMax(dst, s_b[k]);
+  }
+  if (threadIdx.x == 0) atomicAdd(&acc->nvalid, s_cnt);
+}
+
+// ---------------------------------------------------------------------------
+// 2. Morton codes
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint64_t spread21(uint32_t x) {
+  uint64_t v = x & 0x1FFFFFu;
+  v = (v | (v << 32)) & 0x1F00000000FFFFull;
+  v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+  v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+  v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, const float4* __restrict__ phi,
+                                                uint32_t n, BoundsAcc* acc, uint64_t* __restrict__ keys,
+                                                uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t key = ~0ull;
+  if (i < n) {
+    const float4 a = plo[i], b = phi[i];
+    if (a.x <= b.x) {
+      const float lo[3] = {ord2f(acc->clo[0]), ord2f(acc->clo[1]), ord2f(acc->clo[2])};
+      const float hi[3] = {ord2f(acc->chi[0]), ord2f(acc->chi[1]), ord2f(acc->chi[2])};
+      const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+      uint64_t code = 0;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const float ext = hi[d] - lo[d];
+        float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
+        x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
+        code |= spread21((uint32_t)x) << (2 - d);
+      }
+      key = code;
+    }
+    keys[i] = key;
+    vals[i] = i;
+  }
+  // AND / OR over all keys to find constant digits
+  unsigned long long ka = (i < n) ? key : ~0ull, ko = (i < n) ? key : 0ull;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ka &= __shfl_xor_sync(0xFFFFFFFFu, ka, o);
+    ko |= __shfl_xor_sync(0xFFFFFFFFu, ko, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAnd(&acc->kand, ka);
+    atomicOr(&acc->kor, ko);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3. stable LSD radix sort (64-bit keys, 32-bit values)
+// ---------------------------------------------------------------------------
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift,
+                                                        uint32_t* __restrict__ hist, uint32_t nblocks) {
+  __shared__ uint32_t s_h[256];
+  s_h[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * RS_TILE;
+#pragma unroll 4
+  for (int r = 0; r < RS_ITEMS; r++) {
+    const uint32_t i = base + r * RS_THREADS + threadIdx.x;
+    if (i < n) atomicAdd(&s_h[(uint32_t)(keys[i] >> shift) & 0xFFu], 1u);
+  }
+  __syncthreads();
+  hist[threadIdx.x * nblocks + blockIdx.x] = s_h[threadIdx.x];
+}
+
+// Exclusive scan of a uint32 array by a single block of 1024 threads.
+// Optionally writes the total to *total.
+__global__ void __launch_bounds__(1024) k_scan_excl(uint32_t* __restrict__ a, uint32_t n, uint32_t* total) {
+  __shared__ uint32_t s_w[32];
+  __shared__ uint32_t s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int PER = 8;
+  for (uint32_t base = 0; base < n; base += 1024 * PER) {
+    uint32_t v[PER];
+    uint32_t sum = 0;
+    const uint32_t i0 = base + threadIdx.x * PER;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      v[k] = (i0 + k < n) ? a[i0 + k] : 0u;
+      sum += v[k];
+    }
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = s_w[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        if (lane >= o) w += y;
+      }
+      s_w[lane] = w;
+    }
+    __syncthreads();
+    uint32_t excl = s_carry + (warp ? s_w[warp - 1] : 0u) + (x - sum);
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      if (i0 + k < n) a[i0 + k] = excl;
+      excl += v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 1023) s_carry = excl;
+    __syncthreads();
+  }
+  if (total && threadIdx.x == 0) *total = s_carry;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin,
+                                                           const uint32_t* __restrict__ vin,
+                                                           uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           uint32_t n, int shift, const uint32_t* __restrict__ offs,
+                                                           uint32_t nblocks) {
+  __shared__ uint32_t s_run[256];
+  __shared__ uint32_t s_cnt[8][256];
+  __shared__ uint32_t s_off[8][256];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  s_run[tid] = offs[tid * nblocks + blockIdx.x];
+#pragma unroll
+  for (int w = 0; w < 8; w++) s_cnt[w][tid] = 0;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * RS_TILE;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (int r = 0; r < RS_ITEMS; r++) {
+    const uint32_t i = base + r * RS_THREADS + tid;
+    const bool in = i < n;
+    uint64_t k = 0;
+    uint32_t v = 0, d = 256u;
+    if (in) {
+      k = kin[i];
+      v = vin[i];
+      d = (uint32_t)(k >> shift) & 0xFFu;
+    }
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    const uint32_t rank = __popc(peers & lt);
+    if (in && rank == 0) s_cnt[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t run = s_run[tid];
+#pragma unroll
+      for (int w = 0; w < 8; w++) {
+        const uint32_t c = s_cnt[w][tid];
+        s_off[w][tid] = run;
+        run += c;
+        s_cnt[w][tid] = 0;
+      }
+      s_run[tid] = run;
+    }
+    __syncthreads();
+    if (in) {
+      const uint32_t pos = s_off[warp][d] + rank;
+      if (pos < n) {
+        kout[pos] = k;
+        vout[pos] = v;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 4. PLOC
+// ---------------------------------------------------------------------------
+
+constexpr int PLOC_R = 16;
+constexpr int PLOC_BLOCK = 256;
+constexpr uint32_t PLOC_SMALL = 4096;   // finish on one CTA below this many clusters
+constexpr int PLOC_SMALL_THREADS = 1024;
+
+// binary nodes: bnlo[k] = (lo.xyz, left), bnhi[k] = (hi.xyz, right);
+// leaves k < N: left = -1, right = primref index
+__global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ plo, const float4* __restrict__ phi,
+                                                   const uint32_t* __restrict__ sorted, uint32_t n,
+                                                   float4* __restrict__ bnlo, float4* __restrict__ bnhi,
+                                                   uint32_t* __restrict__ bncnt, uint32_t* __restrict__ cidx,
+                                                   float4* __restrict__ clo, float4* __restrict__ chi) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t p = sorted[i];
+  const float4 a = plo[p], b = phi[p];
+  bnlo[i] = make_float4(a.x, a.y, a.z, __int_as_float(-1));
+  bnhi[i] = make_float4(b.x, b.y, b.z, __uint_as_float(p));
+  bncnt[i] = 1;
+  cidx[i] = i;
+  clo[i] = make_float4(a.x, a.y, a.z, 0.f);
+  chi[i] = make_float4(b.x, b.y, b.z, 0.f);
+}
+
+__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict__ clo, const float4* __restrict__ chi,
+                                                        uint32_t n, uint32_t* __restrict__ nn) {
+  __shared__ float3 s_lo[PLOC_BLOCK + 2 * PLOC_R], s_hi[PLOC_BLOCK + 2 * PLOC_R];
+  const int base = blockIdx.x * PLOC_BLOCK;
+  for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
+    const int j = base - PLOC_R + k;
+    if (j >= 0 && j < (int)n) {
+      const float4 a = clo[j], b = chi[j];
+      s_lo[k] = make_float3(a.x, a.y, a.z);
+      s_hi[k] = make_float3(b.x, b.y, b.z);
+    }
+  }
+  __syncthreads();
+  const int i = base + threadIdx.x;
+  if (i >= (int)n) return;
+  const float3 lo = s_lo[threadIdx.x + PLOC_R], hi = s_hi[threadIdx.x + PLOC_R];
+  unsigned long long best = ~0ull;
+#pragma unroll 4
+  for (int o = -PLOC_R; o <= PLOC_R; o++) {
+    const int j = i + o;
+    if (o == 0 || j < 0 || j >= (int)n) continue;
+    const float a = half_area(f3min(lo, s_lo[threadIdx.x + PLOC_R + o]), f3max(hi, s_hi[threadIdx.x + PLOC_R + o]));
+    const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
+    best = key < best ? key : best;
+  }
+  nn[i] = (n > 1) ? (uint32_t)best : (uint32_t)i;
+}
+
+__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_count(const uint32_t* __restrict__ nn, uint32_t n,
+                                                           uint32_t* __restrict__ bsurv, uint32_t* __restrict__ bmerge) {
+  const uint32_t i = blockIdx.x * PLOC_BLOCK + threadIdx.x;
+  int surv = 0, merge = 0;
+  if (i < n) {
+    const uint32_t j = nn[i];
+    const bool mutual = (j != i) && nn[j] == i;
+    merge = mutual && i < j;
+    surv = !(mutual && j < i);
+  }
+  const int cs = __syncthreads_count(surv);
+  const int cm = __syncthreads_count(merge);
+  if (threadIdx.x == 0) {
+    bsurv[blockIdx.x] = cs;
+    bmerge[blockIdx.x] = cm;
+  }
+}
+
+__device__ __forceinline__ uint32_t block_excl_scan_flag(int flag, uint32_t* s_warp) {
+  // exclusive rank of this thread among flagged threads of the block
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t bal = __ballot_sync(0xFFFFFFFFu, flag);
+  if (lane == 0) s_warp[warp] = __popc(bal);
+  __syncthreads();
+  uint32_t pre = 0;
+  for (int w = 0; w < warp; w++) pre += s_warp[w];
+  __syncthreads();
+  return pre + __popc(bal & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const float4* __restrict__ clo, const float4* __restrict__ chi,
+                                                          const uint32_t* __restrict__ cidx,
+                                                          const uint32_t* __restrict__ nn, uint32_t n,
+                                                          const uint32_t* __restrict__ bsurv_off,
+                                                          const uint32_t* __restrict__ bmerge_off, uint32_t node_next,
+                                                          float4* __restrict__ bnlo, float4* __restrict__ bnhi,
+                                                          uint32_t* __restrict__ bncnt, float4* __restrict__ olo,
+                                                          float4* __restrict__ ohi, uint32_t* __restrict__ oidx,
+                                                          uint32_t node_cap, uint32_t* err) {
+  __shared__ uint32_t s_w[PLOC_BLOCK / 32];
+  const uint32_t i = blockIdx.x * PLOC_BLOCK + threadIdx.x;
+  int surv = 0, merge = 0;
+  uint32_t j = 0;
+  if (i < n) {
+    j = nn[i];
+    const bool mutual = (j != i) && nn[j] == i;
+    merge = mutual && i < j;
+    surv = !(mutual && j < i);
+  }
+  const uint32_t rs = block_excl_scan_flag(surv, s_w);
+  const uint32_t rm = block_excl_scan_flag(merge, s_w);
+  if (i >= n || !surv) return;
+  const uint32_t pos = bsurv_off[blockIdx.x] + rs;
+  const float4 a = clo[i], b = chi[i];
+  if (pos >= n) {
+    atomicOr(err, kErrBuild);
+    return;
+  }
+  if (merge) {
+    const float4 c = clo[j], d = chi[j];
+    const uint32_t id = node_next + bmerge_off[blockIdx.x] + rm;
+    if (id >= node_cap) {
+      atomicOr(err, kErrBuild);
+      return;
+    }
+    const uint32_t l = cidx[i], r = cidx[j];
+    const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), 0.f);
+    const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
+    bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
+    bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
+    bncnt[id] = bncnt[l] + bncnt[r];
+    olo[pos] = lo;
+    ohi[pos] = hi;
+    oidx[pos] = id;
+  } else {
+    olo[pos] = a;
+    ohi[pos] = b;
+    oidx[pos] = cidx[i];
+  }
+}
+
+// Finishes clustering of n <= PLOC_SMALL clusters inside one CTA.
+__global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4* __restrict__ clo,
+                                                                  const float4* __restrict__ chi,
+                                                                  const uint32_t* __restrict__ cidx, uint32_t n0,
+                                                                  uint32_t node_next0, float4* __restrict__ bnlo,
+                                                                  float4* __restrict__ bnhi,
+                                                                  uint32_t* __restrict__ bncnt, uint32_t* root_out,
+                                                                  uint32_t* iters_out, uint32_t node_cap,
+                                                                  uint32_t* err) {
+  extern __shared__ unsigned char smem[];
+  float3* s_lo = reinterpret_cast<float3*>(smem);
+  float3* s_hi = s_lo + PLOC_SMALL;
+  uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_hi + PLOC_SMALL);
+  uint32_t* s_nn = s_idx + PLOC_SMALL;
+  __shared__ uint32_t s_w[32];
+  __shared__ uint32_t s_tot[2];
+  constexpr int EPT = PLOC_SMALL / PLOC_SMALL_THREADS;  // elements per thread (contiguous)
+  for (uint32_t k = threadIdx.x; k < n0; k += blockDim.x) {
+    const float4 a = clo[k], b = chi[k];
+    s_lo[k] = make_float3(a.x, a.y, a.z);
+    s_hi[k] = make_float3(b.x, b.y, b.z);
+    s_idx[k] = cidx[k];
+  }
+  uint32_t n = n0, node_next = node_next0, iters = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // every round merges at least the globally closest pair, so n0 - 1 rounds
+  // always suffice; the bound only guards against a logic error
+  while (n > 1) {
+    if (iters >= PLOC_SMALL) {
+      if (threadIdx.x == 0) atomicOr(err, kErrBuild);
+      break;
+    }
+    iters++;
+    // nearest neighbours
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const float3 lo = s_lo[i], hi = s_hi[i];
+      unsigned long long best = ~0ull;
+      for (int o = -PLOC_R; o <= PLOC_R; o++) {
+        const int j = (int)i + o;
+        if (o == 0 || j < 0 || j >= (int)n) continue;
+        const float a = half_area(f3min(lo, s_lo[j]), f3max(hi, s_hi[j]));
+        const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
+        best = key < best ? key : best;
+      }
+      s_nn[i] = (uint32_t)best;
+    }
+    __syncthreads();
+    // flags for this thread's contiguous chunk
+    uint32_t cs = 0, cm = 0;
+    int fs[EPT], fm[EPT];
+    const uint32_t i0 = threadIdx.x * EPT;
+#pragma unroll
+    for (int e = 0; e < EPT; e++) {
+      const uint32_t i = i0 + e;
+      fs[e] = fm[e] = 0;
+      if (i < n) {
+        const uint32_t j = s_nn[i];
+        const bool mutual = s_nn[j] == i;
+        fm[e] = mutual && i < j;
+        fs[e] = !(mutual && j < i);
+      }
+      cs += fs[e];
+      cm += fm[e];
+    }
+    // block exclusive scan of (cs, cm) packed into one 32-bit word (both < 2^16)
+    uint32_t x = cs | (cm << 16);
+    const uint32_t mine = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = s_w[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        if (lane >= o) w += y;
+      }
+      s_w[lane] = w;
+      if (lane == 31) { s_tot[0] = w & 0xFFFFu; s_tot[1] = w >> 16; }
+    }
+    __syncthreads();
+    const uint32_t excl = (warp ? s_w[warp - 1] : 0u) + (x - mine);
+    uint32_t ps = excl & 0xFFFFu, pm = excl >> 16;
+    // gather outputs into registers
+    float3 olo[EPT], ohi[EPT];
+    uint32_t oidx[EPT], opos[EPT];
+#pragma unroll
+    for (int e = 0; e < EPT; e++) {
+      const uint32_t i = i0 + e;
+      opos[e] = 0xFFFFFFFFu;
+      if (i < n && fs[e]) {
+        float3 lo = s_lo[i], hi = s_hi[i];
+        uint32_t id = s_idx[i];
+        if (fm[e]) {
+          const uint32_t j = s_nn[i];
+          const uint32_t nid = node_next + pm;
+          const uint32_t l = id, r = s_idx[j];
+          if (nid >= node_cap) {
+            atomicOr(err, kErrBuild);
+            break;
+          }
+          lo = f3min(lo, s_lo[j]);
+          hi = f3max(hi, s_hi[j]);
+          bnlo[nid] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
+          bnhi[nid] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
+          bncnt[nid] = bncnt[l] + bncnt[r];
+          id = nid;
+          pm++;
+        }
+        olo[e] = lo;
+        ohi[e] = hi;
+        oidx[e] = id;
+        opos[e] = ps++;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < EPT; e++) {
+      if (opos[e] != 0xFFFFFFFFu) {
+        s_lo[opos[e]] = olo[e];
+        s_hi[opos[e]] = ohi[e];
+        s_idx[opos[e]] = oidx[e];
+      }
+    }
+    node_next += s_tot[1];
+    n = s_tot[0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *root_out = s_idx[0];
+    *iters_out += iters;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 5. collapse to 8-wide quantised nodes
+// ---------------------------------------------------------------------------
+
+struct BinTree {
+  const float4* lo;
+  const float4* hi;
+  const uint32_t* cnt;
+  uint32_t nleaves;
+};
+
+__device__ __forceinline__ bool bt_leaf(const BinTree& t, uint32_t k) { return k < t.nleaves; }
+__device__ __forceinline__ uint32_t bt_left(const BinTree& t, uint32_t k) { return __float_as_uint(t.lo[k].w); }
+__device__ __forceinline__ uint32_t bt_right(const BinTree& t, uint32_t k) { return __float_as_uint(t.hi[k].w); }
+__device__ __forceinline__ float3 bt_lo(const BinTree& t, uint32_t k) {
+  const float4 a = t.lo[k];
+  return make_float3(a.x, a.y, a.z);
+}
+__device__ __forceinline__ float3 bt_hi(const BinTree& t, uint32_t k) {
+  const float4 a = t.hi[k];
+  return make_float3(a.x, a.y, a.z);
+}
+
+// Chooses up to 8 children for the wide node that replaces binary node b.
+__device__ int gather_children(const BinTree& t, uint32_t b, uint32_t kids[8]) {
+  if (bt_leaf(t, b)) {
+    kids[0] = b;
+    return 1;
+  }
+  kids[0] = bt_left(t, b);
+  kids[1] = bt_right(t, b);
+  int nk = 2;
+  while (nk < 8) {
+    int best = -1;
+    bool bestMand = false;
+    float bestA = -1.0f;
+    for (int i = 0; i < nk; i++) {
+      const uint32_t c = kids[i];
+      if (bt_leaf(t, c)) continue;
+      const bool mand = t.cnt[c] > (uint32_t)kLeafMax;
+      const float A = half_area(bt_lo(t, c), bt_hi(t, c));
+      if (!mand) {
+        // opening a small subtree pays off only if its children's boxes
+        // cover less area than its own box
+        const uint32_t l = bt_left(t, c), r = bt_right(t, c);
+        const float Al = half_area(bt_lo(t, l), bt_hi(t, l)), Ar = half_area(bt_lo(t, r), bt_hi(t, r));
+        if (!(Al + Ar < A)) continue;
+      }
+      if ((mand && !bestMand) || (mand == bestMand && A > bestA)) {
+        best = i;
+        bestMand = mand;
+        bestA = A;
+      }
+    }
+    if (best < 0) break;
+    const uint32_t c = kids[best];
+    kids[best] = bt_left(t, c);
+    kids[nk++] = bt_right(t, c);
+  }
+  return nk;
+}
+
+__global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const uint32_t* __restrict__ items, uint32_t nitems,
+                                                        uint32_t* __restrict__ kids_out, uint32_t* __restrict__ nint,
+                                                        uint32_t* __restrict__ ntri) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nitems) return;
+  uint32_t kids[8];
+  const int nk = gather_children(t, items[k], kids);
+  uint32_t ni = 0, nt = 0;
+  for (int i = 0; i < 8; i++) {
+    if (i < nk) {
+      const uint32_t c = kids[i];
+      const uint32_t cnt = t.cnt[c];
+      if (cnt > (uint32_t)kLeafMax) ni++; else nt += cnt;
+      kids_out[8 * (size_t)k + i] = c;
+    } else {
+      kids_out[8 * (size_t)k + i] = 0xFFFFFFFFu;
+    }
+  }
+  nint[k] = ni;
+  ntri[k] = nt;
+}
+
+__device__ __forceinline__ uint32_t exp_for(float ext) {
+  // smallest power of two 2^(E-127) with 255 * 2^(E-127) >= ext
+  const float x = __fdiv_ru(ext, 255.0f);
+  const uint32_t bits = __float_as_uint(x);
+  uint32_t E = (bits >> 23) & 0xFFu;
+  if (bits & 0x7FFFFFu) E += 1;
+  if (E < 1) E = 1;
+  if (E > 253) E = 253;
+  return E;
+}
+
+__device__ __forceinline__ void write_tri(const GeomDesc* __restrict__ geoms, const float4* __restrict__ plo,
+                                          const float4* __restrict__ phi, uint32_t prim, TriRecord* dst) {
+  const uint32_t gs = __float_as_uint(plo[prim].w);
+  const uint32_t j = __float_as_uint(phi[prim].w);
+  const GeomDesc g = geoms[gs];
+  const uint3 t = load_tri(g, j);
+  const float3 p0 = load_vtx(g, t.x), p1 = load_vtx(g, t.y), p2 = load_vtx(g, t.z);
+  // Triangle4: e1 = v0 - v1, e2 = v2 - v0 (triangle.h:40-41)
+  const float3 e1 = make_float3(__fsub_rn(p0.x, p1.x), __fsub_rn(p0.y, p1.y), __fsub_rn(p0.z, p1.z));
+  const float3 e2 = make_float3(__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z));
+  dst->a = make_float4(p0.x, p0.y, p0.z, __uint_as_float(j));
+  dst->b = make_float4(e1.x, e1.y, e1.z, __uint_as_float(g.geomID));
+  dst->c = make_float4(e2.x, e2.y, e2.z, 0.f);
+}
+
+__global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc* __restrict__ geoms,
+                                                       const float4* __restrict__ plo, const float4* __restrict__ phi,
+                                                       const uint32_t* __restrict__ kids_in, uint32_t nitems,
+                                                       const uint32_t* __restrict__ off_int,
+                                                       const uint32_t* __restrict__ off_tri, uint32_t level_base,
+                                                       uint32_t next_base, uint32_t tri_next,
+                                                       WideNode* __restrict__ nodes, TriRecord* __restrict__ tris,
+                                                       uint32_t* __restrict__ next_items, double* sah_acc,
+                                                       uint32_t* leaf_count, uint32_t node_cap, uint32_t tri_cap,
+                                                       uint32_t* err) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nitems) return;
+  uint32_t kids[8];
+  int nk = 0;
+  for (int i = 0; i < 8; i++) {
+    kids[i] = kids_in[8 * (size_t)k + i];
+    if (kids[i] != 0xFFFFFFFFu) nk = i + 1;
+  }
+  // union box and quantisation frame
+  float3 ulo = make_float3(INFINITY, INFINITY, INFINITY), uhi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+  for (int i = 0; i < nk; i++) {
+    ulo = f3min(ulo, bt_lo(t, kids[i]));
+    uhi = f3max(uhi, bt_hi(t, kids[i]));
+  }
+  const uint32_t Ex = exp_for(__fsub_ru(uhi.x, ulo.x));
+  const uint32_t Ey = exp_for(__fsub_ru(uhi.y, ulo.y));
+  const uint32_t Ez = exp_for(__fsub_ru(uhi.z, ulo.z));
+  const float sx = __uint_as_float(Ex << 23), sy = __uint_as_float(Ey << 23), sz = __uint_as_float(Ez << 23);
+  const float ix = __uint_as_float((254u - Ex) << 23), iy = __uint_as_float((254u - Ey) << 23),
+              iz = __uint_as_float((254u - Ez) << 23);
+  // slot assignment: slot s prefers children far along the octant direction
+  // with sign bits s (bit set = negative axis), so that visiting slots in
+  // ascending order of (slot ^ ray octant) is roughly near-to-far.
+  const float3 pc = make_float3((ulo.x + uhi.x) * 0.5f, (ulo.y + uhi.y) * 0.5f, (ulo.z + uhi.z) * 0.5f);
+  float cost[8][8];
+  for (int i = 0; i < nk; i++) {
+    const float3 a = bt_lo(t, kids[i]), b = bt_hi(t, kids[i]);
+    const float3 d = make_float3((a.x + b.x) * 0.5f - pc.x, (a.y + b.y) * 0.5f - pc.y, (a.z + b.z) * 0.5f - pc.z);
+    for (int s = 0; s < 8; s++)
+      cost[i][s] = ((s & 1) ? -d.x : d.x) + ((s & 2) ? -d.y : d.y) + ((s & 4) ? -d.z : d.z);
+  }
+  int slot_of[8];
+  uint32_t used = 0, assigned = 0;
+  for (int it = 0; it < nk; it++) {
+    float bc = INFINITY;
+    int bi = -1, bs = -1;
+    for (int i = 0; i < nk; i++) {
+      if (assigned >> i & 1) continue;
+      for (int s = 0; s < 8; s++) {
+        if (used >> s & 1) continue;
+        if (bi < 0 || cost[i][s] < bc) { bc = cost[i][s]; bi = i; bs = s; }
+      }
+    }
+    slot_of[bi] = bs;
+    assigned |= 1u << bi;
+    used |= 1u << bs;
+  }
+  int kid_at[8];
+  for (int s = 0; s < 8; s++) kid_at[s] = -1;
+  for (int i = 0; i < nk; i++) kid_at[slot_of[i]] = i;
+
+  WideNode node;
+  node.px = ulo.x;
+  node.py = ulo.y;
+  node.pz = ulo.z;
+  node.ex = (uint8_t)Ex;
+  node.ey = (uint8_t)Ey;
+  node.ez = (uint8_t)Ez;
+  node.imask = 0;
+  node.child_base = next_base + off_int[k];
+  node.tri_base = tri_next + off_tri[k];
+  uint32_t int_rank = 0, tri_off = 0;
+  double sah = 0.0;
+  uint32_t nleaf = 0;
+  for (int s = 0; s < 8; s++) {
+    const int i = kid_at[s];
+    if (i < 0) {
+      node.meta[s] = 0;
+      node.qlo_x[s] = node.qlo_y[s] = node.qlo_z[s] = 255;
+      node.qhi_x[s] = node.qhi_y[s] = node.qhi_z[s] = 0;
+      continue;
+    }
+    const uint32_t c = kids[i];
+    const float3 a = bt_lo(t, c), b = bt_hi(t, c);
+    const float qlx = fminf(fmaxf(floorf(__fsub_rd(a.x, ulo.x) * ix), 0.f), 255.f);
+    const float qly = fminf(fmaxf(floorf(__fsub_rd(a.y, ulo.y) * iy), 0.f), 255.f);
+    const float qlz = fminf(fmaxf(floorf(__fsub_rd(a.z, ulo.z) * iz), 0.f), 255.f);
+    const float qhx = fminf(fmaxf(ceilf(__fsub_ru(b.x, ulo.x) * ix), 0.f), 255.f);
+    const float qhy = fminf(fmaxf(ceilf(__fsub_ru(b.y, ulo.y) * iy), 0.f), 255.f);
+    const float qhz = fminf(fmaxf(ceilf(__fsub_ru(b.z, ulo.z) * iz), 0.f), 255.f);
+    node.qlo_x[s] = (uint8_t)qlx; node.qlo_y[s] = (uint8_t)qly; node.qlo_z[s] = (uint8_t)qlz;
+    node.qhi_x[s] = (uint8_t)qhx; node.qhi_y[s] = (uint8_t)qhy; node.qhi_z[s] = (uint8_t)qhz;
+    // decoded (outward-rounded) box, as traversal sees it
+    const float3 dlo = make_float3(__fmaf_rd(qlx, sx, ulo.x), __fmaf_rd(qly, sy, ulo.y), __fmaf_rd(qlz, sz, ulo.z));
+    const float3 dhi = make_float3(__fmaf_ru(qhx, sx, ulo.x), __fmaf_ru(qhy, sy, ulo.y), __fmaf_ru(qhz, sz, ulo.z));
+    const double A = (double)fmaxf(0.f, half_area(dlo, dhi));
+    const uint32_t cnt = t.cnt[c];
+    if (cnt > (uint32_t)kLeafMax) {
+      node.meta[s] = (uint8_t)(0x20u | (24u + (uint32_t)s));
+      node.imask |= (uint8_t)(1u << s);
+      if (off_int[k] + int_rank >= node_cap || node.child_base + int_rank >= node_cap) {
+        atomicOr(err, kErrBuild);
+        return;
+      }
+      next_items[off_int[k] + int_rank] = c;
+      int_rank++;
+      sah += A;  // inner node term
+    } else {
+      node.meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | tri_off);
+      // collect the subtree's primitives (<= 3) in depth-first order
+      uint32_t st[4];
+      int sp = 0;
+      st[sp++] = c;
+      uint32_t w = 0;
+      while (sp > 0) {
+        const uint32_t x = st[--sp];
+        if (bt_leaf(t, x)) {
+          if (node.tri_base + tri_off + w >= tri_cap || w >= cnt) {
+            atomicOr(err, kErrBuild);
+            return;
+          }
+          write_tri(geoms, plo, phi, bt_right(t, x), &tris[node.tri_base + tri_off + w]);
+          w++;
+        } else {
+          if (sp + 2 > 4) {
+            atomicOr(err, kErrBuild);
+            return;
+          }
+          st[sp++] = bt_right(t, x);
+          st[sp++] = bt_left(t, x);
+        }
+      }
+      tri_off += cnt;
+      sah += A * (double)((cnt + 3) / 4);  // leaf term: area x Triangle4 blocks
+      nleaf++;
+    }
+  }
+  if (level_base + k >= node_cap) {
+    atomicOr(err, kErrBuild);
+    return;
+  }
+  nodes[level_base + k] = node;
+  atomicAdd(sah_acc, sah);
+  atomicAdd(leaf_count, nleaf);
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+
+template <typename T>
+static cudaError_t dalloc(T** p, size_t count, cudaStream_t st) {
+  return cudaMallocAsync((void**)p, std::max<size_t>(count, 1) * sizeof(T), st);
+}
+
+static inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* out, BuildStats* stats) {
+  *out = DeviceBVH();
+  *stats = BuildStats();
+  for (int d = 0; d < 3; d++) { out->lo[d] = INFINITY; out->hi[d] = -INFINITY; }
+  uint64_t total64 = 0;
+  for (int g = 0; g < ngeoms; g++) total64 += h_geoms[g].ntris;
+  if (total64 == 0) return cudaSuccess;
+  if (total64 >= 0x7FFFFFFFull) return cudaErrorInvalidValue;
+  const uint32_t total = (uint32_t)total64;
+
+  cudaEvent_t ev0, ev1;
+  GB_CHECK(cudaEventCreate(&ev0));
+  GB_CHECK(cudaEventCreate(&ev1));
+  GB_CHECK(cudaEventRecord(ev0, st));
+
+  GeomDesc* d_geoms = nullptr;
+  GB_CHECK(dalloc(&d_geoms, ngeoms, st));
+  GB_CHECK(cudaMemcpyAsync(d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
+
+  float4 *plo = nullptr, *phi = nullptr;
+  BoundsAcc* acc = nullptr;
+  GB_CHECK(dalloc(&plo, total, st));
+  GB_CHECK(dalloc(&phi, total, st));
+  GB_CHECK(dalloc(&acc, 1, st));
+  BoundsAcc h_acc;
+  for (int d = 0; d < 3; d++) { h_acc.glo[d] = h_acc.clo[d] = 0xFFFFFFFFu; h_acc.ghi[d] = h_acc.chi[d] = 0u; }
+  h_acc.nvalid = 0;
+  h_acc.pad = 0;
+  h_acc.kand = ~0ull;
+  h_acc.kor = 0ull;
+  GB_CHECK(cudaMemcpyAsync(acc, &h_acc, sizeof(BoundsAcc), cudaMemcpyHostToDevice, st));
+  k_primrefs<<<cdiv(total, 256), 256, 0, st>>>(d_geoms, ngeoms, total, plo, phi, acc); note_launches(1);
+
+  uint64_t *keys_a = nullptr, *keys_b = nullptr;
+  uint32_t *vals_a = nullptr, *vals_b = nullptr;
+  GB_CHECK(dalloc(&keys_a, total, st));
+  GB_CHECK(dalloc(&keys_b, total, st));
+  GB_CHECK(dalloc(&vals_a, total, st));
+  GB_CHECK(dalloc(&vals_b, total, st));
+  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a); note_launches(1);
+  GB_CHECK(cudaGetLastError());
+  GB_CHECK(cudaMemcpyAsync(&h_acc, acc, sizeof(BoundsAcc), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaStreamSynchronize(st));
+  const uint32_t N = h_acc.nvalid;
+  for (int d = 0; d < 3; d++) { out->lo[d] = ord2f(h_acc.glo[d]); out->hi[d] = ord2f(h_acc.ghi[d]); }
+  if (N == 0) {
+    for (int d = 0; d < 3; d++) { out->lo[d] = INFINITY; out->hi[d] = -INFINITY; }
+    cudaFreeAsync(d_geoms, st); cudaFreeAsync(plo, st); cudaFreeAsync(phi, st); cudaFreeAsync(acc, st);
+    cudaFreeAsync(keys_a, st); cudaFreeAsync(keys_b, st); cudaFreeAsync(vals_a, st); cudaFreeAsync(vals_b, st);
+    cudaEventDestroy(ev0); cudaEventDestroy(ev1);
+    return cudaStreamSynchronize(st);
+  }
+
+  // ---- radix sort (all `total` keys; invalid ones carry ~0 and sort last)
+  {
+    const uint32_t nb = cdiv(total, RS_TILE);
+    uint32_t* hist = nullptr;
+    GB_CHECK(dalloc(&hist, (size_t)256 * nb, st));
+    for (int pass = 0; pass < 8; pass++) {
+      const int shift = 8 * pass;
+      const uint64_t a = (h_acc.kand >> shift) & 0xFF, o = (h_acc.kor >> shift) & 0xFF;
+      if (a == o) continue;  // digit constant over all keys
+      k_rs_hist<<<nb, RS_THREADS, 0, st>>>(keys_a, total, shift, hist, nb); note_launches(1);
+      k_scan_excl<<<1, 1024, 0, st>>>(hist, 256 * nb, nullptr); note_launches(1);
+      k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(keys_a, vals_a, keys_b, vals_b, total, shift, hist, nb); note_launches(1);
+      std::swap(keys_a, keys_b);
+      std::swap(vals_a, vals_b);
+    }
+    GB_CHECK(cudaGetLastError());
+    cudaFreeAsync(hist, st);
+  }
+
+  // ---- PLOC over the N valid primitives (sorted positions 0..N-1)
+  float4 *bnlo = nullptr, *bnhi = nullptr;
+  uint32_t* bncnt = nullptr;
+  const uint32_t nnodes_bin = 2 * N - 1;
+  GB_CHECK(dalloc(&bnlo, nnodes_bin, st));
+  GB_CHECK(dalloc(&bnhi, nnodes_bin, st));
+  GB_CHECK(dalloc(&bncnt, nnodes_bin, st));
+  float4 *clo_a, *chi_a, *clo_b, *chi_b;
+  uint32_t *cidx_a, *cidx_b, *nn;
+  GB_CHECK(dalloc(&clo_a, N, st));
+  GB_CHECK(dalloc(&chi_a, N, st));
+  GB_CHECK(dalloc(&clo_b, N, st));
+  GB_CHECK(dalloc(&chi_b, N, st));
+  GB_CHECK(dalloc(&cidx_a, N, st));
+  GB_CHECK(dalloc(&cidx_b, N, st));
+  GB_CHECK(dalloc(&nn, N, st));
+  k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, bnlo, bnhi, bncnt, cidx_a, clo_a, chi_a); note_launches(1);
+  uint32_t *bsurv, *bmerge, *d_tot, *d_root, *d_iters;
+  const uint32_t maxb = cdiv(N, PLOC_BLOCK);
+  GB_CHECK(dalloc(&bsurv, maxb, st));
+  GB_CHECK(dalloc(&bmerge, maxb, st));
+  GB_CHECK(dalloc(&d_tot, 4, st));
+  GB_CHECK(dalloc(&d_root, 1, st));
+  GB_CHECK(dalloc(&d_iters, 1, st));
+  GB_CHECK(cudaMemsetAsync(d_iters, 0, sizeof(uint32_t), st));
+  uint32_t n = N, node_next = N, iters = 0;
+  uint32_t* h_tot = nullptr;
+  GB_CHECK(cudaMallocHost((void**)&h_tot, 4 * sizeof(uint32_t)));
+  while (n > PLOC_SMALL) {
+    const uint32_t nb = cdiv(n, PLOC_BLOCK);
+    k_ploc_nn<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, n, nn); note_launches(1);
+    k_ploc_count<<<nb, PLOC_BLOCK, 0, st>>>(nn, n, bsurv, bmerge); note_launches(1);
+    k_scan_excl<<<1, 1024, 0, st>>>(bsurv, nb, d_tot + 0); note_launches(1);
+    k_scan_excl<<<1, 1024, 0, st>>>(bmerge, nb, d_tot + 1); note_launches(1);
+    k_ploc_emit<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, cidx_a, nn, n, bsurv, bmerge, node_next, bnlo, bnhi, bncnt,
+                                           clo_b, chi_b, cidx_b, nnodes_bin, &acc->pad); note_launches(1);
+    GB_CHECK(cudaGetLastError());
+    GB_CHECK(cudaMemcpyAsync(h_tot, d_tot, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GB_CHECK(cudaStreamSynchronize(st));
+    if (h_tot[1] == 0) {  // cannot happen (the globally closest pair is mutual)
+      cudaFreeHost(h_tot);
+      return cudaErrorUnknown;
+    }
+    node_next += h_tot[1];
+    n = h_tot[0];
+    iters++;
+    std::swap(clo_a, clo_b);
+    std::swap(chi_a, chi_b);
+    std::swap(cidx_a, cidx_b);
+  }
+  {
+    const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 2 * sizeof(uint32_t));
+    GB_CHECK(cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(clo_a, chi_a, cidx_a, n, node_next, bnlo, bnhi, bncnt, d_root,
+                                                      d_iters, nnodes_bin, &acc->pad); note_launches(1);
+    GB_CHECK(cudaGetLastError());
+  }
+  uint32_t root = 0, small_iters = 0, berr = 0;
+  GB_CHECK(cudaMemcpyAsync(&root, d_root, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(&small_iters, d_iters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(&berr, &acc->pad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaStreamSynchronize(st));
+  if (berr || root >= nnodes_bin) {
+    cudaFreeHost(h_tot);
+    return cudaErrorUnknown;
+  }
+  stats->ploc_iterations = iters + small_iters;
+  cudaFreeAsync(clo_b, st); cudaFreeAsync(chi_b, st); cudaFreeAsync(cidx_b, st);
+  cudaFreeAsync(clo_a, st); cudaFreeAsync(chi_a, st); cudaFreeAsync(cidx_a, st);
+  cudaFreeAsync(nn, st); cudaFreeAsync(bsurv, st); cudaFreeAsync(bmerge, st);
+
+  // ---- collapse, level by level (breadth-first node order)
+  BinTree bt{bnlo, bnhi, bncnt, N};
+  WideNode* wnodes = nullptr;
+  TriRecord* wtris = nullptr;
+  const uint32_t maxw = N;  // wide internal nodes <= binary internal nodes + 1
+  GB_CHECK(dalloc(&wnodes, maxw, st));
+  GB_CHECK(dalloc(&wtris, N, st));
+  uint32_t *items_a, *items_b, *kids, *nint, *ntri;
+  GB_CHECK(dalloc(&items_a, maxw, st));
+  GB_CHECK(dalloc(&items_b, maxw, st));
+  GB_CHECK(dalloc(&kids, (size_t)8 * maxw, st));
+  GB_CHECK(dalloc(&nint, maxw, st));
+  GB_CHECK(dalloc(&ntri, maxw, st));
+  double* d_sah = nullptr;
+  uint32_t* d_leaves = nullptr;
+  GB_CHECK(dalloc(&d_sah, 1, st));
+  GB_CHECK(dalloc(&d_leaves, 1, st));
+  GB_CHECK(cudaMemsetAsync(d_sah, 0, sizeof(double), st));
+  GB_CHECK(cudaMemsetAsync(d_leaves, 0, sizeof(uint32_t), st));
+  GB_CHECK(cudaMemcpyAsync(items_a, &root, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  uint32_t nitems = 1, level_base = 0, tri_next = 0, depth = 0;
+  while (nitems > 0) {
+    const uint32_t nb = cdiv(nitems, 128);
+    k_collapse_count<<<nb, 128, 0, st>>>(bt, items_a, nitems, kids, nint, ntri); note_launches(1);
+    k_scan_excl<<<1, 1024, 0, st>>>(nint, nitems, d_tot + 0); note_launches(1);
+    k_scan_excl<<<1, 1024, 0, st>>>(ntri, nitems, d_tot + 1); note_launches(1);
+    const uint32_t next_base = level_base + nitems;
+    k_collapse_emit<<<nb, 128, 0, st>>>(bt, d_geoms, plo, phi, kids, nitems, nint, ntri, level_base, next_base,
+                                        tri_next, wnodes, wtris, items_b, d_sah, d_leaves, maxw, N, &acc->pad); note_launches(1);
+    GB_CHECK(cudaGetLastError());
+    GB_CHECK(cudaMemcpyAsync(h_tot, d_tot, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GB_CHECK(cudaStreamSynchronize(st));
+    depth++;
+    level_base = next_base;
+    tri_next += h_tot[1];
+    nitems = h_tot[0];
+    if (level_base + nitems > maxw) { cudaFreeHost(h_tot); return cudaErrorUnknown; }
+    std::swap(items_a, items_b);
+  }
+  const uint32_t num_nodes = level_base;
+  GB_CHECK(cudaMemcpyAsync(&berr, &acc->pad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaStreamSynchronize(st));
+  if (berr || tri_next != N) {
+    cudaFreeHost(h_tot);
+    return cudaErrorUnknown;
+  }
+  double sah_sum = 0;
+  uint32_t nleaves = 0;
+  GB_CHECK(cudaMemcpyAsync(&sah_sum, d_sah, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(&nleaves, d_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+
+  // exact-size outputs
+  GB_CHECK(cudaMalloc((void**)&out->nodes, (size_t)num_nodes * sizeof(WideNode)));
+  GB_CHECK(cudaMalloc((void**)&out->tris, (size_t)N * sizeof(TriRecord)));
+  GB_CHECK(cudaMemcpyAsync(out->nodes, wnodes, (size_t)num_nodes * sizeof(WideNode), cudaMemcpyDeviceToDevice, st));
+  GB_CHECK(cudaMemcpyAsync(out->tris, wtris, (size_t)N * sizeof(TriRecord), cudaMemcpyDeviceToDevice, st));
+  out->num_nodes = num_nodes;
+  out->num_tris = N;
+  out->depth = depth;
+
+  cudaFreeAsync(wnodes, st); cudaFreeAsync(wtris, st);
+  cudaFreeAsync(items_a, st); cudaFreeAsync(items_b, st); cudaFreeAsync(kids, st);
+  cudaFreeAsync(nint, st); cudaFreeAsync(ntri, st); cudaFreeAsync(d_sah, st); cudaFreeAsync(d_leaves, st);
+  cudaFreeAsync(d_tot, st); cudaFreeAsync(d_root, st); cudaFreeAsync(d_iters, st);
+  cudaFreeAsync(bnlo, st); cudaFreeAsync(bnhi, st); cudaFreeAsync(bncnt, st);
+  cudaFreeAsync(plo, st); cudaFreeAsync(phi, st); cudaFreeAsync(acc, st); cudaFreeAsync(d_geoms, st);
+  cudaFreeAsync(keys_a, st); cudaFreeAsync(keys_b, st); cudaFreeAsync(vals_a, st); cudaFreeAsync(vals_b, st);
+  GB_CHECK(cudaEventRecord(ev1, st));
+  GB_CHECK(cudaStreamSynchronize(st));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  cudaFreeHost(h_tot);
+
+  // SAH relative to the root box (bvh_statistics.cpp: root node counts once)
+  const float gx = out->hi[0] - out->lo[0], gy = out->hi[1] - out->lo[1], gz = out->hi[2] - out->lo[2];
+  const double Aroot = std::max(0.0, (double)(gx * (gy + gz) + gy * gz));
+  stats->sah = Aroot > 0 ? (Aroot + sah_sum) / Aroot : 0.0;
+  stats->build_ms = ms;
+  stats->num_nodes = num_nodes;
+  stats->num_leaves = nleaves;
+  stats->num_prims = N;
+  stats->depth = depth;
+  return cudaSuccess;
+}
+
+// Sorts (key, value) pairs with the builder's radix sort (all 8 digits,
+// constant digits skipped).  Device pointers; results in keys/vals.
+cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  uint64_t* kb = nullptr;
+  uint32_t* vb = nullptr;
+  uint32_t* hist = nullptr;
+  const uint32_t nb = cdiv(n, RS_TILE);
+  GB_CHECK(dalloc(&kb, n, st));
+  GB_CHECK(dalloc(&vb, n, st));
+  GB_CHECK(dalloc(&hist, (size_t)256 * nb, st));
+  uint64_t* ka = keys;
+  uint32_t* va = vals;
+  for (int pass = 0; pass < 8; pass++) {
+    const int shift = 8 * pass;
+    k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, shift, hist, nb);
+    k_scan_excl<<<1, 1024, 0, st>>>(hist, 256 * nb, nullptr);
+    k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
+    note_launches(3);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  GB_CHECK(cudaGetLastError());
+  // 8 passes: the result is back in the caller's buffers
+  cudaFreeAsync(kb, st);
+  cudaFreeAsync(vb, st);
+  cudaFreeAsync(hist, st);
+  return cudaStreamSynchronize(st);
+}
+
+void free_bvh(DeviceBVH* b) {
+  if (b->nodes) cudaFree(b->nodes);
+  if (b->tris) cudaFree(b->tris);
+  b->nodes = nullptr;
+  b->tris = nullptr;
+  b->num_nodes = b->num_tris = 0;
+}
+
+}  // namespace gb

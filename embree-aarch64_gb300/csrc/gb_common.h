@@ -1,0 +1,96 @@
+// gb_common.h -- data layouts shared by the GPU builder, the traversal kernels
+// and the C-ABI host layer of the GB300 triangle ray-query library.
+//
+// HBM layout of one committed scene (all arrays 16-byte aligned):
+//   WideNode  nodes[num_nodes]   80 B each: 8-wide node, child boxes quantised
+//                                to 8 bits per plane relative to a per-node
+//                                origin and power-of-two scale (5 x 16-B loads)
+//   TriRecord tris[num_tris]     48 B each: v0, e1 = v0-v1, e2 = v2-v0 (the
+//                                reference's Triangle4 lane contents,
+//                                kernels/geometry/triangle.h:40-41) + ids
+// Children of a node are stored contiguously: internal children at
+// child_base + rank among internal slots, leaf triangles at tri_base + offset.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gb {
+
+constexpr uint32_t kInvalidID = 0xFFFFFFFFu;
+constexpr int kLeafMax = 3;          // triangles per leaf child (unary count in meta)
+constexpr int kStackSize = 64;       // traversal stack entries (node groups)
+
+// 80-byte wide node.
+//   meta[s]: 0 = empty slot; internal child: 0b001'11sss (24 + slot);
+//            leaf: unary triangle count in bits 5..7 (001, 011, 111) and the
+//            first triangle's offset from tri_base in bits 0..4 (0..23).
+//   imask:   bit s set when slot s holds an internal child.
+//   ex/ey/ez: IEEE-754 biased exponent of the per-axis scale 2^(e-127).
+//   decoded child box: lo = p + qlo * scale, hi = p + qhi * scale (rounded
+//   outward at traversal time so the decoded box always contains the child).
+struct alignas(16) WideNode {
+  float px, py, pz;
+  uint8_t ex, ey, ez, imask;
+  uint32_t child_base;
+  uint32_t tri_base;
+  uint8_t meta[8];
+  uint8_t qlo_x[8], qlo_y[8], qlo_z[8];
+  uint8_t qhi_x[8], qhi_y[8], qhi_z[8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
+
+// 48-byte triangle record: (v0.xyz, primID), (e1.xyz, geomID), (e2.xyz, pad).
+struct alignas(16) TriRecord {
+  float4 a;
+  float4 b;
+  float4 c;
+};
+static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
+
+// One geometry as the builder sees it (device pointers, byte strides).
+struct GeomDesc {
+  const char* verts;
+  const char* idx;
+  uint64_t vstride;
+  uint64_t istride;
+  uint32_t nverts;
+  uint32_t ntris;
+  uint32_t geomID;     // user-visible geometry ID
+  uint32_t prim_offset; // exclusive prefix of ntris over the scene's geometries
+};
+
+// A committed BVH in device memory.
+struct DeviceBVH {
+  WideNode* nodes = nullptr;
+  TriRecord* tris = nullptr;
+  uint32_t num_nodes = 0;
+  uint32_t num_tris = 0;     // valid primitives in the BVH
+  uint32_t depth = 0;        // wide levels
+  float lo[3] = {0, 0, 0};   // geometry bounds (empty scene: +inf / -inf)
+  float hi[3] = {0, 0, 0};
+};
+
+// Build statistics reported through the extension API.
+struct BuildStats {
+  double sah = 0;            // bvh_statistics.cpp semantics on the decoded boxes
+  double build_ms = 0;       // device time of the whole build
+  uint32_t num_nodes = 0, num_leaves = 0, num_prims = 0, depth = 0;
+  uint32_t ploc_iterations = 0;
+};
+
+// Traversal work counters (counting variant of the kernels).
+struct TraceCounters {
+  unsigned long long nodes;
+  unsigned long long tris;
+  unsigned long long rays;
+};
+
+// Device-side error flags (bit mask).
+enum : uint32_t {
+  kErrStackOverflow = 1u,
+  kErrIterationLimit = 2u,
+  kErrBuild = 4u,
+};
+
+}  // namespace gb

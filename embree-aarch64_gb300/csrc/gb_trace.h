@@ -1,0 +1,24 @@
+// gb_trace.h -- host entry point of the traversal kernels (gb_trace.cu).
+#pragma once
+#include "gb_common.h"
+
+namespace gb {
+
+struct TraceParams {
+  const WideNode* nodes;
+  const TriRecord* tris;
+  char* rays;                 // RTCRayHit (closest) or RTCRay (any hit) records, device memory
+  uint64_t stride;            // byte stride between records (multiple of 4)
+  uint32_t nrays;
+  unsigned int* ray_counter;  // zeroed before launch; persistent warps fetch rays from it
+  unsigned int* err;          // error flags (kErr*)
+  TraceCounters* counters;    // counting variant only
+  uint32_t max_iters;         // per-ray loop bound
+  uint32_t num_nodes;         // bounds of the node and triangle arrays
+  uint32_t num_tris;
+};
+
+// Launches the persistent closest-hit (anyhit = false) or any-hit kernel.
+cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStream_t st);
+
+}  // namespace gb

@@ -1,0 +1,1153 @@
+// rtcore_api.cpp -- the C ABI (rtc* entry points) over the GPU builder and
+// traversal kernels.
+//
+// Object model and error convention follow the reference's API layer
+// (kernels/common/rtcore.cpp, kernels/common/device.cpp:258-318,
+// kernels/common/rtcore.h:28-122): reference-counted handles, every entry
+// point catches its own exceptions and turns them into an RTCError that is
+// passed to the device's error callback and stored per (device, thread)
+// until rtcGetDeviceError reads and clears it.  Errors without a device go
+// to a per-thread slot read by rtcGetDeviceError(NULL).
+//
+// GPU residency: rtcCommitScene copies each enabled triangle geometry's
+// buffers to HBM (device pointers are used in place) and runs the GPU
+// builder on the calling thread's stream.  Queries copy host rays to a
+// per-thread device buffer (or trace device rays in place), launch the
+// persistent traversal kernel and return after the stream is synchronised.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <exception>
+#include <map>
+#include <mutex>
+#include <set>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "rtcore_gb300.h"
+#include "rtcore_gb300_ext.h"
+#include "gb_build.h"
+#include "gb_common.h"
+#include "gb_launch.h"
+#include "gb_trace.h"
+
+namespace {
+
+struct rtc_error : public std::exception {
+  RTCError code;
+  std::string msg;
+  rtc_error(RTCError c, std::string m) : code(c), msg(std::move(m)) {}
+  const char* what() const noexcept override { return msg.c_str(); }
+};
+
+[[noreturn]] void fail(RTCError c, const char* m) { throw rtc_error(c, m); }
+
+void cuda_ok(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return;
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation) throw rtc_error(RTC_ERROR_OUT_OF_MEMORY, m);
+  throw rtc_error(RTC_ERROR_UNKNOWN, m);
+}
+
+struct RefCounted {
+  std::atomic<long> refs{1};
+  virtual ~RefCounted() {}
+  void inc() { refs.fetch_add(1); }
+  void dec() {
+    if (refs.fetch_sub(1) == 1) delete this;
+  }
+};
+
+std::mutex g_mutex;  // device creation / properties (rtcore.cpp:20-25)
+
+// ---------------------------------------------------------------------------
+// device
+// ---------------------------------------------------------------------------
+
+struct Device : RefCounted {
+  RTCErrorFunction error_fn = nullptr;
+  void* error_user = nullptr;
+  RTCMemoryMonitorFunction mem_fn = nullptr;
+  void* mem_user = nullptr;
+  int verbose = 0;
+  int benchmark = 0;
+  int cuda_device = -1;
+  std::mutex mtx;
+
+  explicit Device(const char* cfg) {
+    if (cfg) parse(cfg);
+    if (cuda_device < 0) cuda_ok(cudaGetDevice(&cuda_device), "cudaGetDevice");
+    int n = 0;
+    cuda_ok(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (cuda_device >= n) fail(RTC_ERROR_INVALID_ARGUMENT, "gpu.device out of range");
+  }
+
+  // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
+  // Honoured: verbose, benchmark, gpu.device; the CPU tasking and ISA keys
+  // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
+  void parse(const char* cfg) {
+    std::string s(cfg);
+    size_t i = 0;
+    while (i < s.size()) {
+      size_t j = s.find(',', i);
+      if (j == std::string::npos) j = s.size();
+      std::string tok = s.substr(i, j - i);
+      size_t eq = tok.find('=');
+      auto trim = [](std::string x) {
+        size_t a = x.find_first_not_of(" \t"), b = x.find_last_not_of(" \t");
+        return a == std::string::npos ? std::string() : x.substr(a, b - a + 1);
+      };
+      if (eq != std::string::npos) {
+        std::string k = trim(tok.substr(0, eq)), v = trim(tok.substr(eq + 1));
+        if (k == "verbose") verbose = atoi(v.c_str());
+        else if (k == "benchmark") benchmark = atoi(v.c_str());
+        else if (k == "gpu.device") cuda_device = atoi(v.c_str());
+      }
+      i = j + 1;
+    }
+  }
+
+  void set_current() const { cuda_ok(cudaSetDevice(cuda_device), "cudaSetDevice"); }
+
+  // memory monitor hook (device.cpp:318-328): a veto becomes OUT_OF_MEMORY
+  void memory(ssize_t bytes, bool post) {
+    if (mem_fn && bytes != 0 && !mem_fn(mem_user, bytes, post) && bytes > 0)
+      fail(RTC_ERROR_OUT_OF_MEMORY, "memory monitor forced termination");
+  }
+};
+
+thread_local RTCError t_thread_error = RTC_ERROR_NONE;
+thread_local std::unordered_map<const Device*, RTCError> t_device_error;
+
+void process_error(Device* d, RTCError e, const char* str) {
+  if (!d) {
+    if (t_thread_error == RTC_ERROR_NONE) t_thread_error = e;
+    return;
+  }
+  if (d->verbose >= 1) fprintf(stderr, "rtcore-gb300: error %d (%s)\n", (int)e, str ? str : "");
+  if (d->error_fn) d->error_fn(d->error_user, e, str);
+  RTCError& slot = t_device_error[d];
+  if (slot == RTC_ERROR_NONE) slot = e;
+}
+
+#define API_BEGIN try {
+#define API_END(dev)                                                   \
+  }                                                                    \
+  catch (rtc_error & e) {                                              \
+    process_error(dev, e.code, e.what());                              \
+  }                                                                    \
+  catch (std::bad_alloc&) {                                            \
+    process_error(dev, RTC_ERROR_OUT_OF_MEMORY, "out of memory");      \
+  }                                                                    \
+  catch (std::exception & e) {                                         \
+    process_error(dev, RTC_ERROR_UNKNOWN, e.what());                   \
+  }                                                                    \
+  catch (...) {                                                        \
+    process_error(dev, RTC_ERROR_UNKNOWN, "unknown exception caught"); \
+  }
+
+#define VERIFY_HANDLE(h) \
+  if ((h) == nullptr) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+
+// ---------------------------------------------------------------------------
+// buffers and geometry
+// ---------------------------------------------------------------------------
+
+struct Buffer : RefCounted {
+  Device* device;
+  char* ptr;
+  size_t bytes;
+  bool shared;
+  Buffer(Device* d, size_t n, void* p) : device(d), ptr((char*)p), bytes(n), shared(p != nullptr) {
+    device->inc();
+    if (!shared) {
+      ptr = (char*)malloc(std::max<size_t>(n, 16));
+      if (!ptr) fail(RTC_ERROR_OUT_OF_MEMORY, "out of memory");
+    }
+  }
+  ~Buffer() override {
+    if (!shared) free(ptr);
+    device->dec();
+  }
+};
+
+struct View {
+  Buffer* buf = nullptr;  // keeps a reference
+  const char* ptr = nullptr;
+  size_t stride = 0;
+  size_t num = 0;
+  RTCFormat format = RTC_FORMAT_UNDEFINED;
+  void set(Buffer* b, size_t offset, size_t s, size_t n, RTCFormat f) {
+    if (b) b->inc();
+    if (buf) buf->dec();
+    buf = b;
+    ptr = b ? b->ptr + offset : nullptr;
+    stride = s;
+    num = n;
+    format = f;
+  }
+  View() = default;
+  View(const View&) = delete;
+  View& operator=(const View&) = delete;
+  ~View() {
+    if (buf) buf->dec();
+  }
+};
+
+bool is_device_pointer(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+struct Geometry : RefCounted {
+  Device* device;
+  RTCGeometryType type;
+  View vertices, indices;
+  bool enabled = true;
+  unsigned mask = 0xFFFFFFFFu;
+  RTCBuildQuality quality = RTC_BUILD_QUALITY_MEDIUM;
+  void* user = nullptr;
+  unsigned time_steps = 1;
+  // device copies of host buffers
+  char* d_verts = nullptr;
+  char* d_idx = nullptr;
+  size_t cap_verts = 0, cap_idx = 0;
+
+  Geometry(Device* d, RTCGeometryType t) : device(d), type(t) { device->inc(); }
+  ~Geometry() override {
+    if (d_verts) cudaFree(d_verts);
+    if (d_idx) cudaFree(d_idx);
+    device->dec();
+  }
+
+  // TriangleMesh::setBuffer checks (kernels/common/scene_triangle_mesh.cpp:35-84)
+  void set_buffer(RTCBufferType type, unsigned slot, RTCFormat format, Buffer* b, size_t offset, size_t stride,
+                  size_t num) {
+    if ((((size_t)(b ? b->ptr : nullptr) + offset) & 0x3) || (stride & 0x3))
+      fail(RTC_ERROR_INVALID_OPERATION, "data must be 4 bytes aligned");
+    if (type == RTC_BUFFER_TYPE_VERTEX) {
+      if (format != RTC_FORMAT_FLOAT3) fail(RTC_ERROR_INVALID_OPERATION, "invalid vertex buffer format");
+      if (stride * num > 16ull * 1024ull * 1024ull * 1024ull)
+        fail(RTC_ERROR_INVALID_OPERATION, "vertex buffer can be at most 16GB large");
+      if (slot >= time_steps) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid vertex buffer slot");
+      vertices.set(b, offset, stride, num, format);
+    } else if (type == RTC_BUFFER_TYPE_VERTEX_ATTRIBUTE) {
+      // no vertex attribute slots exist (rtcSetGeometryVertexAttributeCount is not provided)
+      if (format < RTC_FORMAT_FLOAT || format > RTC_FORMAT_FLOAT16)
+        fail(RTC_ERROR_INVALID_OPERATION, "invalid vertex attribute buffer format");
+      fail(RTC_ERROR_INVALID_OPERATION, "invalid vertex attribute buffer slot");
+    } else if (type == RTC_BUFFER_TYPE_INDEX) {
+      if (slot != 0) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid buffer slot");
+      if (format != RTC_FORMAT_UINT3) fail(RTC_ERROR_INVALID_OPERATION, "invalid index buffer format");
+      indices.set(b, offset, stride, num, format);
+    } else {
+      fail(RTC_ERROR_INVALID_ARGUMENT, "unknown buffer type");
+    }
+  }
+
+  View* view(RTCBufferType type, unsigned slot) {
+    if (type == RTC_BUFFER_TYPE_INDEX) {
+      if (slot != 0) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid buffer slot");
+      return &indices;
+    }
+    if (type == RTC_BUFFER_TYPE_VERTEX) {
+      if (slot >= time_steps) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid buffer slot");
+      return &vertices;
+    }
+    fail(RTC_ERROR_INVALID_ARGUMENT, "unknown buffer type");
+  }
+
+  // Device view of one buffer: in place for device memory, else a copy.
+  const char* upload(const View& v, char** dbuf, size_t* cap, cudaStream_t st) {
+    if (!v.ptr || v.num == 0) return nullptr;
+    if (is_device_pointer(v.ptr)) return v.ptr;
+    const size_t bytes = (v.num - 1) * v.stride + (v.format == RTC_FORMAT_FLOAT3 || v.format == RTC_FORMAT_UINT3 ? 12 : v.stride);
+    if (bytes > *cap) {
+      if (*dbuf) cudaFree(*dbuf);
+      *dbuf = nullptr;
+      *cap = 0;
+      device->memory((ssize_t)bytes, false);
+      cuda_ok(cudaMalloc((void**)dbuf, bytes), "cudaMalloc geometry");
+      *cap = bytes;
+    }
+    cuda_ok(cudaMemcpyAsync(*dbuf, v.ptr, bytes, cudaMemcpyHostToDevice, st), "upload geometry");
+    return *dbuf;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// per-thread query context
+// ---------------------------------------------------------------------------
+
+struct ThreadCtx {
+  cudaStream_t own = nullptr;
+  cudaStream_t user = nullptr;
+  bool user_set = false;
+  char* dbuf = nullptr;
+  size_t cap = 0;
+  unsigned int* dscratch = nullptr;     // [0] ray counter, [1] error flags, [2..] counters
+  unsigned int* hscratch = nullptr;     // pinned mirror
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+  bool counting = false;
+  RTCGBQueryStats last{};
+  int device = -1;
+
+  cudaStream_t stream() {
+    if (user_set) return user;
+    if (!own) cuda_ok(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking), "cudaStreamCreate");
+    return own;
+  }
+  void ensure(int dev) {
+    if (device == dev && dscratch) return;
+    device = dev;
+    cuda_ok(cudaMalloc((void**)&dscratch, 64), "cudaMalloc scratch");
+    cuda_ok(cudaMallocHost((void**)&hscratch, 64), "cudaMallocHost");
+    cuda_ok(cudaEventCreate(&e0), "event");
+    cuda_ok(cudaEventCreate(&e1), "event");
+    cuda_ok(cudaEventCreate(&e2), "event");
+    cuda_ok(cudaEventCreate(&e3), "event");
+  }
+  char* buffer(size_t bytes) {
+    if (bytes > cap) {
+      if (dbuf) cudaFree(dbuf);
+      dbuf = nullptr;
+      cap = 0;
+      size_t want = std::max(bytes, cap * 2);
+      cuda_ok(cudaMalloc((void**)&dbuf, want), "cudaMalloc rays");
+      cap = want;
+    }
+    return dbuf;
+  }
+  ~ThreadCtx() {
+    if (dbuf) cudaFree(dbuf);
+    if (dscratch) cudaFree(dscratch);
+    if (hscratch) cudaFreeHost(hscratch);
+    if (own) cudaStreamDestroy(own);
+    for (cudaEvent_t e : {e0, e1, e2, e3})
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+thread_local ThreadCtx t_ctx;
+
+// ---------------------------------------------------------------------------
+// scene
+// ---------------------------------------------------------------------------
+
+struct Scene : RefCounted {
+  Device* device;
+  std::mutex mtx;
+  std::vector<Geometry*> geoms;  // index = geomID
+  std::set<unsigned> free_ids;
+  RTCSceneFlags flags = RTC_SCENE_FLAG_NONE;
+  RTCBuildQuality quality = RTC_BUILD_QUALITY_MEDIUM;
+  RTCProgressMonitorFunction progress = nullptr;
+  void* progress_ptr = nullptr;
+  bool committed = false;
+  gb::DeviceBVH bvh;
+  gb::BuildStats stats;
+
+  explicit Scene(Device* d) : device(d) { device->inc(); }
+  ~Scene() override {
+    for (Geometry* g : geoms)
+      if (g) g->dec();
+    gb::free_bvh(&bvh);
+    device->dec();
+  }
+
+  // Scene::bind (kernels/common/scene.cpp:595-623) with the ID pool's
+  // smallest-free-ID policy.
+  unsigned attach(Geometry* g, unsigned id) {
+    std::lock_guard<std::mutex> lk(mtx);
+    if (id == RTC_INVALID_GEOMETRY_ID) {
+      if (!free_ids.empty()) {
+        id = *free_ids.begin();
+        free_ids.erase(free_ids.begin());
+      } else {
+        id = (unsigned)geoms.size();
+        geoms.push_back(nullptr);
+      }
+    } else {
+      if (id < geoms.size() && geoms[id]) fail(RTC_ERROR_INVALID_ARGUMENT, "geometry ID already assigned");
+      while (geoms.size() <= id) {
+        free_ids.insert((unsigned)geoms.size());
+        geoms.push_back(nullptr);
+      }
+      free_ids.erase(id);
+    }
+    g->inc();
+    geoms[id] = g;
+    return id;
+  }
+
+  void detach(unsigned id) {
+    std::lock_guard<std::mutex> lk(mtx);
+    if (id >= geoms.size() || !geoms[id]) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid geometry ID");
+    geoms[id]->dec();
+    geoms[id] = nullptr;
+    free_ids.insert(id);
+  }
+
+  void commit() {
+    std::lock_guard<std::mutex> lk(mtx);
+    device->set_current();
+    t_ctx.ensure(device->cuda_device);
+    cudaStream_t st = t_ctx.stream();
+    if (progress && !progress(progress_ptr, 0.0)) fail(RTC_ERROR_CANCELLED, "progress monitor forced termination");
+    std::vector<gb::GeomDesc> descs;
+    uint64_t total = 0;
+    for (unsigned id = 0; id < geoms.size(); id++) {
+      Geometry* g = geoms[id];
+      if (!g || !g->enabled || g->type != RTC_GEOMETRY_TYPE_TRIANGLE) continue;
+      if (!g->vertices.ptr || !g->indices.ptr || g->indices.num == 0) continue;
+      gb::GeomDesc d{};
+      d.verts = g->upload(g->vertices, &g->d_verts, &g->cap_verts, st);
+      d.idx = g->upload(g->indices, &g->d_idx, &g->cap_idx, st);
+      d.vstride = g->vertices.stride;
+      d.istride = g->indices.stride;
+      d.nverts = (uint32_t)g->vertices.num;
+      d.ntris = (uint32_t)g->indices.num;
+      d.geomID = id;
+      d.prim_offset = (uint32_t)total;
+      total += d.ntris;
+      descs.push_back(d);
+    }
+    if (total >= 0x7FFFFFFFull) fail(RTC_ERROR_INVALID_OPERATION, "too many primitives");
+    // estimated device bytes of the build (scratch + result)
+    device->memory((ssize_t)(total * 256 + 4096), false);
+    gb::free_bvh(&bvh);
+    committed = false;
+    gb::BuildStats bs;
+    cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, &bvh, &bs), "rtcCommitScene");
+    stats = bs;
+    committed = true;
+    if (progress) progress(progress_ptr, 1.0);
+    if (device->benchmark)
+      printf("BENCHMARK_BUILD %f %f %f %u\n", bs.build_ms * 1e-3, bs.build_ms > 0 ? bs.num_prims / (bs.build_ms * 1e-3) : 0.0,
+             bs.sah, (unsigned)(bvh.num_nodes * sizeof(gb::WideNode) + bvh.num_tris * sizeof(gb::TriRecord)));
+    if (device->verbose >= 2)
+      fprintf(stderr, "rtcore-gb300: built %u prims, %u nodes, depth %u, SAH %.3f, %.3f ms\n", bs.num_prims,
+              bs.num_nodes, bs.depth, bs.sah, bs.build_ms);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// queries
+// ---------------------------------------------------------------------------
+
+void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit, size_t recsize) {
+  VERIFY_HANDLE(scene);
+  if (!scene->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  if (M == 0) return;
+  if (!rays) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  if (((size_t)rays & 0x3) || (stride & 0x3)) fail(RTC_ERROR_INVALID_ARGUMENT, "ray not aligned to 4 bytes");
+  if (stride < recsize) fail(RTC_ERROR_INVALID_ARGUMENT, "byteStride smaller than the ray record");
+  ThreadCtx& c = t_ctx;
+  c.last = RTCGBQueryStats{};
+  const gb::DeviceBVH& bvh = scene->bvh;
+  if (bvh.num_nodes == 0) return;  // empty scene: nothing is hit
+  scene->device->set_current();
+  c.ensure(scene->device->cuda_device);
+  cudaStream_t st = c.stream();
+  const size_t span = (size_t)(M - 1) * stride + recsize;
+  const bool on_device = is_device_pointer(rays);
+  char* d_rays = (char*)rays;
+  cuda_ok(cudaEventRecord(c.e0, st), "event");
+  if (!on_device) {
+    d_rays = c.buffer(span);
+    cuda_ok(cudaMemcpyAsync(d_rays, rays, span, cudaMemcpyHostToDevice, st), "H2D rays");
+    c.last.h2d_bytes = span;
+  }
+  cuda_ok(cudaMemsetAsync(c.dscratch, 0, 64, st), "memset");
+  gb::TraceParams P{};
+  P.nodes = bvh.nodes;
+  P.tris = bvh.tris;
+  P.rays = d_rays;
+  P.stride = stride;
+  P.nrays = M;
+  P.ray_counter = c.dscratch;
+  P.err = c.dscratch + 1;
+  P.counters = reinterpret_cast<gb::TraceCounters*>(c.dscratch + 2);
+  P.max_iters = 2 * bvh.num_nodes + 64;
+  P.num_nodes = bvh.num_nodes;
+  P.num_tris = bvh.num_tris;
+  cuda_ok(cudaEventRecord(c.e1, st), "event");
+  cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
+  gb::note_launches(2);  // memset + traversal
+  cuda_ok(cudaEventRecord(c.e2, st), "event");
+  if (!on_device) {
+    cuda_ok(cudaMemcpyAsync(rays, d_rays, span, cudaMemcpyDeviceToHost, st), "D2H rays");
+    c.last.d2h_bytes = span;
+  }
+  cuda_ok(cudaMemcpyAsync(c.hscratch, c.dscratch, 64, cudaMemcpyDeviceToHost, st), "D2H status");
+  cuda_ok(cudaEventRecord(c.e3, st), "event");
+  cuda_ok(cudaStreamSynchronize(st), "traversal");
+  float k_ms = 0, t_ms = 0;
+  cudaEventElapsedTime(&k_ms, c.e1, c.e2);
+  cudaEventElapsedTime(&t_ms, c.e0, c.e3);
+  c.last.kernel_ms = k_ms;
+  c.last.total_ms = t_ms;
+  if (c.counting) {
+    const gb::TraceCounters* tc = reinterpret_cast<const gb::TraceCounters*>(c.hscratch + 2);
+    c.last.nodes = tc->nodes;
+    c.last.tris = tc->tris;
+    c.last.rays = tc->rays;
+  }
+  const unsigned err = c.hscratch[1];
+  if (err & gb::kErrStackOverflow) fail(RTC_ERROR_UNKNOWN, "traversal stack overflow");
+  if (err & gb::kErrIterationLimit) fail(RTC_ERROR_UNKNOWN, "traversal iteration limit reached");
+  if (err & gb::kErrBuild) fail(RTC_ERROR_UNKNOWN, "traversal found an invalid BVH reference");
+}
+
+// array-of-pointers variants gather into a packed host array first
+template <typename Rec>
+void run_query_pointers(Scene* scene, Rec** recs, unsigned M, bool anyhit) {
+  VERIFY_HANDLE(scene);
+  if (M == 0) return;
+  if (!recs) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  std::vector<Rec> tmp(M);
+  for (unsigned i = 0; i < M; i++) tmp[i] = *recs[i];
+  run_query(scene, tmp.data(), M, sizeof(Rec), anyhit, sizeof(Rec));
+  for (unsigned i = 0; i < M; i++) *recs[i] = tmp[i];
+}
+
+}  // namespace
+
+namespace gb {
+std::atomic<unsigned long long> g_launch_count{0};
+void note_launches(unsigned n) { g_launch_count.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace gb
+
+// ===========================================================================
+// exported C ABI
+// ===========================================================================
+
+extern "C" {
+
+RTC_API RTCDevice rtcNewDevice(const char* config) {
+  API_BEGIN
+  std::lock_guard<std::mutex> lk(g_mutex);
+  Device* d = new Device(config);
+  return (RTCDevice)d;
+  API_END(nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcRetainDevice(RTCDevice hdevice) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  d->inc();
+  API_END(nullptr)
+}
+
+RTC_API void rtcReleaseDevice(RTCDevice hdevice) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  d->dec();
+  API_END(nullptr)
+}
+
+RTC_API ssize_t rtcGetDeviceProperty(RTCDevice hdevice, enum RTCDeviceProperty prop) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  switch (prop) {
+    case RTC_DEVICE_PROPERTY_VERSION: return RTC_VERSION;
+    case RTC_DEVICE_PROPERTY_VERSION_MAJOR: return RTC_VERSION_MAJOR;
+    case RTC_DEVICE_PROPERTY_VERSION_MINOR: return RTC_VERSION_MINOR;
+    case RTC_DEVICE_PROPERTY_VERSION_PATCH: return RTC_VERSION_PATCH;
+    case RTC_DEVICE_PROPERTY_NATIVE_RAY4_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_NATIVE_RAY8_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_NATIVE_RAY16_SUPPORTED: return 0;
+    case RTC_DEVICE_PROPERTY_RAY_STREAM_SUPPORTED: return 1;
+    case RTC_DEVICE_PROPERTY_BACKFACE_CULLING_CURVES_ENABLED:
+    case RTC_DEVICE_PROPERTY_RAY_MASK_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_BACKFACE_CULLING_ENABLED:
+    case RTC_DEVICE_PROPERTY_FILTER_FUNCTION_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_IGNORE_INVALID_RAYS_ENABLED:
+    case RTC_DEVICE_PROPERTY_COMPACT_POLYS_ENABLED: return 0;
+    case RTC_DEVICE_PROPERTY_TRIANGLE_GEOMETRY_SUPPORTED: return 1;
+    case RTC_DEVICE_PROPERTY_QUAD_GEOMETRY_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_SUBDIVISION_GEOMETRY_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_CURVE_GEOMETRY_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_USER_GEOMETRY_SUPPORTED:
+    case RTC_DEVICE_PROPERTY_POINT_GEOMETRY_SUPPORTED: return 0;
+    case RTC_DEVICE_PROPERTY_TASKING_SYSTEM: return 0;
+    case RTC_DEVICE_PROPERTY_JOIN_COMMIT_SUPPORTED: return 1;
+    case RTC_DEVICE_PROPERTY_PARALLEL_COMMIT_SUPPORTED: return 1;
+    default: fail(RTC_ERROR_INVALID_ARGUMENT, "unknown readable property");
+  }
+  API_END(d)
+  return 0;
+}
+
+RTC_API void rtcSetDeviceProperty(RTCDevice hdevice, const enum RTCDeviceProperty prop, ssize_t value) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  (void)prop;
+  (void)value;
+  fail(RTC_ERROR_INVALID_ARGUMENT, "unknown writable property");
+  API_END(d)
+}
+
+RTC_API enum RTCError rtcGetDeviceError(RTCDevice hdevice) {
+  Device* d = (Device*)hdevice;
+  if (!d) {
+    RTCError e = t_thread_error;
+    t_thread_error = RTC_ERROR_NONE;
+    return e;
+  }
+  auto it = t_device_error.find(d);
+  if (it == t_device_error.end()) return RTC_ERROR_NONE;
+  RTCError e = it->second;
+  it->second = RTC_ERROR_NONE;
+  return e;
+}
+
+RTC_API void rtcSetDeviceErrorFunction(RTCDevice hdevice, RTCErrorFunction error, void* userPtr) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  d->error_fn = error;
+  d->error_user = userPtr;
+  API_END(d)
+}
+
+RTC_API void rtcSetDeviceMemoryMonitorFunction(RTCDevice hdevice, RTCMemoryMonitorFunction fn, void* userPtr) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  d->mem_fn = fn;
+  d->mem_user = userPtr;
+  API_END(d)
+}
+
+// ---- buffers
+
+RTC_API RTCBuffer rtcNewBuffer(RTCDevice hdevice, size_t byteSize) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  return (RTCBuffer) new Buffer(d, byteSize, nullptr);
+  API_END(d)
+  return nullptr;
+}
+
+RTC_API RTCBuffer rtcNewSharedBuffer(RTCDevice hdevice, void* ptr, size_t byteSize) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  return (RTCBuffer) new Buffer(d, byteSize, ptr);
+  API_END(d)
+  return nullptr;
+}
+
+RTC_API void* rtcGetBufferData(RTCBuffer hbuffer) {
+  Buffer* b = (Buffer*)hbuffer;
+  API_BEGIN
+  VERIFY_HANDLE(hbuffer);
+  return b->ptr;
+  API_END(b ? b->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcRetainBuffer(RTCBuffer hbuffer) {
+  Buffer* b = (Buffer*)hbuffer;
+  API_BEGIN
+  VERIFY_HANDLE(hbuffer);
+  b->inc();
+  API_END(b ? b->device : nullptr)
+}
+
+RTC_API void rtcReleaseBuffer(RTCBuffer hbuffer) {
+  Buffer* b = (Buffer*)hbuffer;
+  API_BEGIN
+  VERIFY_HANDLE(hbuffer);
+  b->dec();
+  API_END(nullptr)
+}
+
+// ---- geometry
+
+RTC_API RTCGeometry rtcNewGeometry(RTCDevice hdevice, enum RTCGeometryType type) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  if (type != RTC_GEOMETRY_TYPE_TRIANGLE) fail(RTC_ERROR_UNKNOWN, "geometry type is not supported");
+  return (RTCGeometry) new Geometry(d, type);
+  API_END(d)
+  return nullptr;
+}
+
+RTC_API void rtcRetainGeometry(RTCGeometry hg) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  g->inc();
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcReleaseGeometry(RTCGeometry hg) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  g->dec();
+  API_END(nullptr)
+}
+
+RTC_API void rtcCommitGeometry(RTCGeometry hg) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcEnableGeometry(RTCGeometry hg) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  g->enabled = true;
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcDisableGeometry(RTCGeometry hg) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  g->enabled = false;
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetGeometryTimeStepCount(RTCGeometry hg, unsigned int timeStepCount) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  if (timeStepCount != 1) fail(RTC_ERROR_INVALID_OPERATION, "motion blur is not supported");
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetGeometryMask(RTCGeometry hg, unsigned int mask) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  g->mask = mask;
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetGeometryBuildQuality(RTCGeometry hg, enum RTCBuildQuality quality) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  if (quality != RTC_BUILD_QUALITY_LOW && quality != RTC_BUILD_QUALITY_MEDIUM && quality != RTC_BUILD_QUALITY_HIGH &&
+      quality != RTC_BUILD_QUALITY_REFIT)
+    fail(RTC_ERROR_INVALID_ARGUMENT, "invalid build quality");
+  g->quality = quality;
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetGeometryBuffer(RTCGeometry hg, enum RTCBufferType type, unsigned int slot, enum RTCFormat format,
+                                  RTCBuffer hbuffer, size_t byteOffset, size_t byteStride, size_t itemCount) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  VERIFY_HANDLE(hbuffer);
+  Buffer* b = (Buffer*)hbuffer;
+  if (g->device != b->device) fail(RTC_ERROR_INVALID_ARGUMENT, "inputs are from different devices");
+  if (itemCount > 0xFFFFFFFFu) fail(RTC_ERROR_INVALID_ARGUMENT, "buffer too large");
+  g->set_buffer(type, slot, format, b, byteOffset, byteStride, itemCount);
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetSharedGeometryBuffer(RTCGeometry hg, enum RTCBufferType type, unsigned int slot,
+                                        enum RTCFormat format, const void* ptr, size_t byteOffset, size_t byteStride,
+                                        size_t itemCount) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  if (itemCount > 0xFFFFFFFFu) fail(RTC_ERROR_INVALID_ARGUMENT, "buffer too large");
+  Buffer* b = new Buffer(g->device, itemCount * byteStride, (char*)ptr + byteOffset);
+  try {
+    g->set_buffer(type, slot, format, b, 0, byteStride, itemCount);
+  } catch (...) {
+    b->dec();
+    throw;
+  }
+  b->dec();
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void* rtcSetNewGeometryBuffer(RTCGeometry hg, enum RTCBufferType type, unsigned int slot,
+                                      enum RTCFormat format, size_t byteStride, size_t itemCount) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  if (itemCount > 0xFFFFFFFFu) fail(RTC_ERROR_INVALID_ARGUMENT, "buffer too large");
+  // vertex buffers are over-allocated to a 16-byte multiple, as in rtcore.cpp:1470-1486
+  size_t bytes = itemCount * byteStride;
+  if (type == RTC_BUFFER_TYPE_VERTEX || type == RTC_BUFFER_TYPE_VERTEX_ATTRIBUTE) bytes += (16 - (byteStride % 16)) % 16;
+  Buffer* b = new Buffer(g->device, bytes, nullptr);
+  try {
+    g->set_buffer(type, slot, format, b, 0, byteStride, itemCount);
+  } catch (...) {
+    b->dec();
+    throw;
+  }
+  b->dec();
+  return b->ptr;
+  API_END(g ? g->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void* rtcGetGeometryBufferData(RTCGeometry hg, enum RTCBufferType type, unsigned int slot) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  return (void*)g->view(type, slot)->ptr;
+  API_END(g ? g->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcUpdateGeometryBuffer(RTCGeometry hg, enum RTCBufferType type, unsigned int slot) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  g->view(type, slot);  // validates; buffers are re-uploaded at every commit
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetGeometryIntersectFilterFunction(RTCGeometry hg, RTCFilterFunctionN filter) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  if (filter) fail(RTC_ERROR_INVALID_OPERATION, "filter functions are not supported by the GPU path");
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetGeometryOccludedFilterFunction(RTCGeometry hg, RTCFilterFunctionN filter) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  if (filter) fail(RTC_ERROR_INVALID_OPERATION, "filter functions are not supported by the GPU path");
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcSetGeometryUserData(RTCGeometry hg, void* ptr) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  g->user = ptr;
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void* rtcGetGeometryUserData(RTCGeometry hg) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  return g->user;
+  API_END(g ? g->device : nullptr)
+  return nullptr;
+}
+
+// ---- scene
+
+RTC_API RTCScene rtcNewScene(RTCDevice hdevice) {
+  Device* d = (Device*)hdevice;
+  API_BEGIN
+  VERIFY_HANDLE(hdevice);
+  return (RTCScene) new Scene(d);
+  API_END(d)
+  return nullptr;
+}
+
+RTC_API RTCDevice rtcGetSceneDevice(RTCScene hs) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  s->device->inc();
+  return (RTCDevice)s->device;
+  API_END(s ? s->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcRetainScene(RTCScene hs) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  s->inc();
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcReleaseScene(RTCScene hs) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  s->dec();
+  API_END(nullptr)
+}
+
+RTC_API unsigned int rtcAttachGeometry(RTCScene hs, RTCGeometry hg) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  VERIFY_HANDLE(hg);
+  Geometry* g = (Geometry*)hg;
+  if (s->device != g->device) fail(RTC_ERROR_INVALID_ARGUMENT, "inputs are from different devices");
+  return s->attach(g, RTC_INVALID_GEOMETRY_ID);
+  API_END(s ? s->device : nullptr)
+  return RTC_INVALID_GEOMETRY_ID;
+}
+
+RTC_API void rtcAttachGeometryByID(RTCScene hs, RTCGeometry hg, unsigned int geomID) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  VERIFY_HANDLE(hg);
+  if (geomID == RTC_INVALID_GEOMETRY_ID) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  Geometry* g = (Geometry*)hg;
+  if (s->device != g->device) fail(RTC_ERROR_INVALID_ARGUMENT, "inputs are from different devices");
+  s->attach(g, geomID);
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcDetachGeometry(RTCScene hs, unsigned int geomID) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (geomID == RTC_INVALID_GEOMETRY_ID) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  s->detach(geomID);
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API RTCGeometry rtcGetGeometry(RTCScene hs, unsigned int geomID) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  std::lock_guard<std::mutex> lk(s->mtx);
+  if (geomID >= s->geoms.size()) return nullptr;
+  return (RTCGeometry)s->geoms[geomID];
+  API_END(s ? s->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcCommitScene(RTCScene hs) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  s->commit();
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcJoinCommitScene(RTCScene hs) { rtcCommitScene(hs); }
+
+RTC_API void rtcSetSceneProgressMonitorFunction(RTCScene hs, RTCProgressMonitorFunction progress, void* ptr) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  s->progress = progress;
+  s->progress_ptr = ptr;
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcSetSceneBuildQuality(RTCScene hs, enum RTCBuildQuality quality) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (quality != RTC_BUILD_QUALITY_LOW && quality != RTC_BUILD_QUALITY_MEDIUM && quality != RTC_BUILD_QUALITY_HIGH)
+    fail(RTC_ERROR_UNKNOWN, "invalid build quality");
+  s->quality = quality;
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcSetSceneFlags(RTCScene hs, enum RTCSceneFlags flags) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  s->flags = flags;
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API enum RTCSceneFlags rtcGetSceneFlags(RTCScene hs) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  return s->flags;
+  API_END(s ? s->device : nullptr)
+  return RTC_SCENE_FLAG_NONE;
+}
+
+RTC_API void rtcGetSceneBounds(RTCScene hs, struct RTCBounds* b) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  b->lower_x = s->bvh.lo[0];
+  b->lower_y = s->bvh.lo[1];
+  b->lower_z = s->bvh.lo[2];
+  b->align0 = 0;
+  b->upper_x = s->bvh.hi[0];
+  b->upper_y = s->bvh.hi[1];
+  b->upper_z = s->bvh.hi[2];
+  b->align1 = 0;
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcGetSceneLinearBounds(RTCScene hs, struct RTCLinearBounds* b) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!b) fail(RTC_ERROR_INVALID_OPERATION, "invalid destination pointer");
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  RTCBounds one{};
+  one.lower_x = s->bvh.lo[0]; one.lower_y = s->bvh.lo[1]; one.lower_z = s->bvh.lo[2];
+  one.upper_x = s->bvh.hi[0]; one.upper_y = s->bvh.hi[1]; one.upper_z = s->bvh.hi[2];
+  b->bounds0 = one;
+  b->bounds1 = one;
+  API_END(s ? s->device : nullptr)
+}
+
+// ---- queries
+
+RTC_API void rtcIntersect1(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRayHit* rayhit) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  VERIFY_HANDLE(hs);
+  if (!rayhit) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  // rtcore.cpp:609-612: a single ray is traced only when tnear <= tfar
+  if (!(rayhit->ray.tnear <= rayhit->ray.tfar)) return;
+  run_query(s, rayhit, 1, sizeof(RTCRayHit), false, sizeof(RTCRayHit));
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcIntersect1M(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRayHit* rayhit, unsigned int M,
+                            size_t byteStride) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit));
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcIntersect1Mp(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRayHit** rayhit, unsigned int M) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  run_query_pointers<RTCRayHit>(s, rayhit, M, false);
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcOccluded1(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRay* ray) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  VERIFY_HANDLE(hs);
+  if (!ray) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  if (!(ray->tnear <= ray->tfar)) return;
+  run_query(s, ray, 1, sizeof(RTCRay), true, sizeof(RTCRay));
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcOccluded1M(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRay* ray, unsigned int M,
+                           size_t byteStride) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  run_query(s, ray, M, byteStride, true, sizeof(RTCRay));
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcOccluded1Mp(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRay** ray, unsigned int M) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  run_query_pointers<RTCRay>(s, ray, M, true);
+  API_END(s ? s->device : nullptr)
+}
+
+// ---- extensions
+
+RTC_API void rtcgbGetSceneBuildStats(RTCScene hs, RTCGBBuildStats* out) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!out) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  memset(out, 0, sizeof(*out));
+  out->sah = s->stats.sah;
+  out->build_ms = s->stats.build_ms;
+  out->num_nodes = s->stats.num_nodes;
+  out->num_leaves = s->stats.num_leaves;
+  out->num_prims = s->stats.num_prims;
+  out->depth = s->stats.depth;
+  out->ploc_iterations = s->stats.ploc_iterations;
+  out->bvh_bytes = (unsigned long long)s->bvh.num_nodes * sizeof(gb::WideNode) +
+                   (unsigned long long)s->bvh.num_tris * sizeof(gb::TriRecord);
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcgbGetLastQueryStats(RTCGBQueryStats* out) {
+  if (out) *out = t_ctx.last;
+}
+
+RTC_API void rtcgbSetQueryCounting(int enable) { t_ctx.counting = enable != 0; }
+
+RTC_API unsigned long long rtcgbGetKernelLaunchCount(void) { return gb::g_launch_count.load(); }
+
+RTC_API void rtcgbSetThreadStream(void* cuda_stream) {
+  t_ctx.user = (cudaStream_t)cuda_stream;
+  t_ctx.user_set = cuda_stream != nullptr;
+}
+
+RTC_API unsigned int rtcgbGetSceneBVH(RTCScene hs, void* nodes, unsigned int max_nodes, void* tris,
+                                      unsigned int max_tris, unsigned int* num_tris) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  s->device->set_current();
+  const unsigned nn = std::min(max_nodes, s->bvh.num_nodes), nt = std::min(max_tris, s->bvh.num_tris);
+  if (nodes && nn) cuda_ok(cudaMemcpy(nodes, s->bvh.nodes, (size_t)nn * sizeof(gb::WideNode), cudaMemcpyDeviceToHost), "copy nodes");
+  if (tris && nt) cuda_ok(cudaMemcpy(tris, s->bvh.tris, (size_t)nt * sizeof(gb::TriRecord), cudaMemcpyDeviceToHost), "copy tris");
+  if (num_tris) *num_tris = s->bvh.num_tris;
+  return s->bvh.num_nodes;
+  API_END(s ? s->device : nullptr)
+  return 0;
+}
+
+RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, unsigned int n) {
+  if (n == 0) return 0;
+  if (!keys || !values) return 1;
+  t_ctx.ensure(0);
+  cudaStream_t st = t_ctx.stream();
+  uint64_t* dk = nullptr;
+  uint32_t* dv = nullptr;
+  if (cudaMalloc((void**)&dk, (size_t)n * 8) != cudaSuccess) return 2;
+  if (cudaMalloc((void**)&dv, (size_t)n * 4) != cudaSuccess) { cudaFree(dk); return 2; }
+  int rc = 0;
+  if (cudaMemcpyAsync(dk, keys, (size_t)n * 8, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(dv, values, (size_t)n * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      gb::sort_pairs(dk, dv, n, st) != cudaSuccess ||
+      cudaMemcpyAsync(keys, dk, (size_t)n * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(values, dv, (size_t)n * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    rc = 3;
+  cudaFree(dk);
+  cudaFree(dv);
+  return rc;
+}
+
+}  // extern "C"

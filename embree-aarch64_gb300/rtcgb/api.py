@@ -1,0 +1,276 @@
+"""ctypes binding of librtcore_gb300.so (the reference-compatible C ABI).
+
+This is how Python callers -- the tests and the benchmark -- reach the
+library: through the same `rtc*` entry points a C++ host program links.
+There is no other compute path: if the shared library cannot be loaded the
+import fails loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from .rays import RAYHIT_DTYPE, RAY_DTYPE
+
+RTC_GEOMETRY_TYPE_TRIANGLE = 0
+RTC_BUFFER_TYPE_INDEX = 0
+RTC_BUFFER_TYPE_VERTEX = 1
+RTC_FORMAT_UINT3 = 0x5003
+RTC_FORMAT_FLOAT3 = 0x9003
+RTC_INVALID_GEOMETRY_ID = 0xFFFFFFFF
+
+ERRORS = {0: "NONE", 1: "UNKNOWN", 2: "INVALID_ARGUMENT", 3: "INVALID_OPERATION", 4: "OUT_OF_MEMORY",
+          5: "UNSUPPORTED_CPU", 6: "CANCELLED"}
+
+# every entry point declared in include/rtcore_gb300.h and include/rtcore_gb300_ext.h
+EXPORTS = """rtcNewDevice rtcRetainDevice rtcReleaseDevice rtcGetDeviceProperty rtcSetDeviceProperty
+rtcGetDeviceError rtcSetDeviceErrorFunction rtcSetDeviceMemoryMonitorFunction rtcNewBuffer rtcNewSharedBuffer
+rtcGetBufferData rtcRetainBuffer rtcReleaseBuffer rtcNewGeometry rtcRetainGeometry rtcReleaseGeometry
+rtcCommitGeometry rtcEnableGeometry rtcDisableGeometry rtcSetGeometryTimeStepCount rtcSetGeometryMask
+rtcSetGeometryBuildQuality rtcSetGeometryBuffer rtcSetSharedGeometryBuffer rtcSetNewGeometryBuffer
+rtcGetGeometryBufferData rtcUpdateGeometryBuffer rtcSetGeometryIntersectFilterFunction
+rtcSetGeometryOccludedFilterFunction rtcSetGeometryUserData rtcGetGeometryUserData rtcNewScene rtcGetSceneDevice
+rtcRetainScene rtcReleaseScene rtcAttachGeometry rtcAttachGeometryByID rtcDetachGeometry rtcGetGeometry
+rtcCommitScene rtcJoinCommitScene rtcSetSceneProgressMonitorFunction rtcSetSceneBuildQuality rtcSetSceneFlags
+rtcGetSceneFlags rtcGetSceneBounds rtcGetSceneLinearBounds rtcIntersect1 rtcIntersect1M rtcIntersect1Mp
+rtcOccluded1 rtcOccluded1M rtcOccluded1Mp rtcgbGetSceneBuildStats rtcgbGetLastQueryStats rtcgbSetQueryCounting
+rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs""".split()
+
+
+class RTCBounds(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("lower_x", "lower_y", "lower_z", "align0",
+                                              "upper_x", "upper_y", "upper_z", "align1")]
+
+
+class RTCIntersectContext(ctypes.Structure):
+    _fields_ = [("flags", ctypes.c_int), ("filter", ctypes.c_void_p), ("instID", ctypes.c_uint * 1)]
+
+
+class RTCGBBuildStats(ctypes.Structure):
+    _fields_ = [("sah", ctypes.c_double), ("build_ms", ctypes.c_double), ("num_nodes", ctypes.c_uint),
+                ("num_leaves", ctypes.c_uint), ("num_prims", ctypes.c_uint), ("depth", ctypes.c_uint),
+                ("ploc_iterations", ctypes.c_uint), ("pad", ctypes.c_uint), ("bvh_bytes", ctypes.c_ulonglong)]
+
+
+class RTCGBQueryStats(ctypes.Structure):
+    _fields_ = [("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("rays", ctypes.c_ulonglong),
+                ("nodes", ctypes.c_ulonglong), ("tris", ctypes.c_ulonglong), ("h2d_bytes", ctypes.c_ulonglong),
+                ("d2h_bytes", ctypes.c_ulonglong)]
+
+
+ERROR_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p)
+MEMORY_FN = ctypes.CFUNCTYPE(ctypes.c_bool, ctypes.c_void_p, ctypes.c_ssize_t, ctypes.c_bool)
+PROGRESS_FN = ctypes.CFUNCTYPE(ctypes.c_bool, ctypes.c_void_p, ctypes.c_double)
+
+_lib = None
+
+
+def load(build=True):
+    """Loads (building first if needed) the shared library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"librtcore_gb300.so missing at {path}; run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    vp, u, sz, i = ctypes.c_void_p, ctypes.c_uint, ctypes.c_size_t, ctypes.c_int
+    sig = {
+        "rtcNewDevice": (vp, [ctypes.c_char_p]),
+        "rtcReleaseDevice": (None, [vp]), "rtcRetainDevice": (None, [vp]),
+        "rtcGetDeviceProperty": (ctypes.c_ssize_t, [vp, i]),
+        "rtcSetDeviceProperty": (None, [vp, i, ctypes.c_ssize_t]),
+        "rtcGetDeviceError": (i, [vp]),
+        "rtcSetDeviceErrorFunction": (None, [vp, ERROR_FN, vp]),
+        "rtcSetDeviceMemoryMonitorFunction": (None, [vp, MEMORY_FN, vp]),
+        "rtcNewBuffer": (vp, [vp, sz]), "rtcNewSharedBuffer": (vp, [vp, vp, sz]),
+        "rtcGetBufferData": (vp, [vp]), "rtcRetainBuffer": (None, [vp]), "rtcReleaseBuffer": (None, [vp]),
+        "rtcNewGeometry": (vp, [vp, i]), "rtcRetainGeometry": (None, [vp]), "rtcReleaseGeometry": (None, [vp]),
+        "rtcCommitGeometry": (None, [vp]), "rtcEnableGeometry": (None, [vp]), "rtcDisableGeometry": (None, [vp]),
+        "rtcSetGeometryTimeStepCount": (None, [vp, u]), "rtcSetGeometryMask": (None, [vp, u]),
+        "rtcSetGeometryBuildQuality": (None, [vp, i]),
+        "rtcSetGeometryBuffer": (None, [vp, i, u, i, vp, sz, sz, sz]),
+        "rtcSetSharedGeometryBuffer": (None, [vp, i, u, i, vp, sz, sz, sz]),
+        "rtcSetNewGeometryBuffer": (vp, [vp, i, u, i, sz, sz]),
+        "rtcGetGeometryBufferData": (vp, [vp, i, u]), "rtcUpdateGeometryBuffer": (None, [vp, i, u]),
+        "rtcSetGeometryIntersectFilterFunction": (None, [vp, vp]),
+        "rtcSetGeometryOccludedFilterFunction": (None, [vp, vp]),
+        "rtcSetGeometryUserData": (None, [vp, vp]), "rtcGetGeometryUserData": (vp, [vp]),
+        "rtcNewScene": (vp, [vp]), "rtcGetSceneDevice": (vp, [vp]),
+        "rtcRetainScene": (None, [vp]), "rtcReleaseScene": (None, [vp]),
+        "rtcAttachGeometry": (u, [vp, vp]), "rtcAttachGeometryByID": (None, [vp, vp, u]),
+        "rtcDetachGeometry": (None, [vp, u]), "rtcGetGeometry": (vp, [vp, u]),
+        "rtcCommitScene": (None, [vp]), "rtcJoinCommitScene": (None, [vp]),
+        "rtcSetSceneProgressMonitorFunction": (None, [vp, PROGRESS_FN, vp]),
+        "rtcSetSceneBuildQuality": (None, [vp, i]), "rtcSetSceneFlags": (None, [vp, i]),
+        "rtcGetSceneFlags": (i, [vp]),
+        "rtcGetSceneBounds": (None, [vp, ctypes.POINTER(RTCBounds)]),
+        "rtcGetSceneLinearBounds": (None, [vp, vp]),
+        "rtcIntersect1": (None, [vp, vp, vp]), "rtcIntersect1M": (None, [vp, vp, vp, u, sz]),
+        "rtcIntersect1Mp": (None, [vp, vp, vp, u]),
+        "rtcOccluded1": (None, [vp, vp, vp]), "rtcOccluded1M": (None, [vp, vp, vp, u, sz]),
+        "rtcOccluded1Mp": (None, [vp, vp, vp, u]),
+        "rtcgbGetSceneBuildStats": (None, [vp, ctypes.POINTER(RTCGBBuildStats)]),
+        "rtcgbGetLastQueryStats": (None, [ctypes.POINTER(RTCGBQueryStats)]),
+        "rtcgbSetQueryCounting": (None, [i]),
+        "rtcgbGetKernelLaunchCount": (ctypes.c_ulonglong, []),
+        "rtcgbSetThreadStream": (None, [vp]),
+        "rtcgbGetSceneBVH": (u, [vp, vp, u, vp, u, ctypes.POINTER(u)]),
+        "rtcgbRadixSortPairs": (i, [vp, vp, u]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class RTCError(RuntimeError):
+    def __init__(self, code, where):
+        super().__init__(f"{where}: RTC_ERROR_{ERRORS.get(code, code)}")
+        self.code = code
+
+
+class Device:
+    def __init__(self, config=b""):
+        self.L = load()
+        self.h = ctypes.c_void_p(self.L.rtcNewDevice(config))
+        if not self.h:
+            raise RTCError(self.L.rtcGetDeviceError(None), "rtcNewDevice")
+
+    def error(self):
+        return self.L.rtcGetDeviceError(self.h)
+
+    def check(self, where):
+        e = self.error()
+        if e:
+            raise RTCError(e, where)
+
+    def release(self):
+        if self.h:
+            self.L.rtcReleaseDevice(self.h)
+            self.h = None
+
+
+class Scene:
+    """A scene of triangle meshes built with rtcCommitScene."""
+
+    def __init__(self, device):
+        self.dev = device
+        self.L = device.L
+        self.h = ctypes.c_void_p(self.L.rtcNewScene(device.h))
+        self._keep = []
+        device.check("rtcNewScene")
+
+    def add_mesh(self, verts, idx, geom_id=None):
+        """Attaches a triangle mesh using shared buffers (kept alive here)."""
+        verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(idx, np.uint32).reshape(-1, 3)
+        self._keep.append((verts, idx))
+        L = self.L
+        g = ctypes.c_void_p(L.rtcNewGeometry(self.dev.h, RTC_GEOMETRY_TYPE_TRIANGLE))
+        L.rtcSetSharedGeometryBuffer(g, RTC_BUFFER_TYPE_VERTEX, 0, RTC_FORMAT_FLOAT3, _ptr(verts), 0, 12,
+                                     verts.shape[0])
+        L.rtcSetSharedGeometryBuffer(g, RTC_BUFFER_TYPE_INDEX, 0, RTC_FORMAT_UINT3, _ptr(idx), 0, 12, idx.shape[0])
+        L.rtcCommitGeometry(g)
+        if geom_id is None:
+            gid = L.rtcAttachGeometry(self.h, g)
+        else:
+            L.rtcAttachGeometryByID(self.h, g, geom_id)
+            gid = geom_id
+        L.rtcReleaseGeometry(g)
+        self.dev.check("add_mesh")
+        return gid
+
+    def commit(self):
+        self.L.rtcCommitScene(self.h)
+        self.dev.check("rtcCommitScene")
+
+    def bounds(self):
+        b = RTCBounds()
+        self.L.rtcGetSceneBounds(self.h, ctypes.byref(b))
+        self.dev.check("rtcGetSceneBounds")
+        return np.array([b.lower_x, b.lower_y, b.lower_z]), np.array([b.upper_x, b.upper_y, b.upper_z])
+
+    def build_stats(self):
+        s = RTCGBBuildStats()
+        self.L.rtcgbGetSceneBuildStats(self.h, ctypes.byref(s))
+        self.dev.check("rtcgbGetSceneBuildStats")
+        return {f: getattr(s, f) for f, _ in s._fields_ if f != "pad"}
+
+    def intersect(self, rays, stride=None, count=None):
+        """rtcIntersect1M on a host RTCRayHit array (in place)."""
+        ctx = RTCIntersectContext(0, None, (ctypes.c_uint * 1)(RTC_INVALID_GEOMETRY_ID))
+        n = rays.shape[0] if count is None else count
+        self.L.rtcIntersect1M(self.h, ctypes.byref(ctx), _ptr(rays), n, stride or rays.dtype.itemsize)
+        self.dev.check("rtcIntersect1M")
+        return rays
+
+    def occluded(self, rays, stride=None, count=None):
+        """rtcOccluded1M on a host RTCRay (or RTCRayHit) array (in place)."""
+        ctx = RTCIntersectContext(0, None, (ctypes.c_uint * 1)(RTC_INVALID_GEOMETRY_ID))
+        n = rays.shape[0] if count is None else count
+        self.L.rtcOccluded1M(self.h, ctypes.byref(ctx), _ptr(rays), n, stride or rays.dtype.itemsize)
+        self.dev.check("rtcOccluded1M")
+        return rays
+
+    def intersect_ptr(self, ptr, n, stride=80):
+        """rtcIntersect1M on raw memory (host or CUDA device pointer)."""
+        ctx = RTCIntersectContext(0, None, (ctypes.c_uint * 1)(RTC_INVALID_GEOMETRY_ID))
+        self.L.rtcIntersect1M(self.h, ctypes.byref(ctx), ctypes.c_void_p(ptr), n, stride)
+        self.dev.check("rtcIntersect1M")
+
+    def occluded_ptr(self, ptr, n, stride=48):
+        ctx = RTCIntersectContext(0, None, (ctypes.c_uint * 1)(RTC_INVALID_GEOMETRY_ID))
+        self.L.rtcOccluded1M(self.h, ctypes.byref(ctx), ctypes.c_void_p(ptr), n, stride)
+        self.dev.check("rtcOccluded1M")
+
+    def bvh(self):
+        """Copies the committed BVH: (nodes uint8 [n,80], tris float32 [m,12])."""
+        nt = ctypes.c_uint()
+        n = self.L.rtcgbGetSceneBVH(self.h, None, 0, None, 0, ctypes.byref(nt))
+        nodes = np.zeros((max(n, 1), 80), np.uint8)
+        tris = np.zeros((max(nt.value, 1), 12), np.float32)
+        self.L.rtcgbGetSceneBVH(self.h, _ptr(nodes), n, _ptr(tris), nt.value, ctypes.byref(nt))
+        self.dev.check("rtcgbGetSceneBVH")
+        return nodes[:n], tris[:nt.value]
+
+    def release(self):
+        if self.h:
+            self.L.rtcReleaseScene(self.h)
+            self.h = None
+
+
+def last_query_stats():
+    L = load()
+    s = RTCGBQueryStats()
+    L.rtcgbGetLastQueryStats(ctypes.byref(s))
+    return {f: getattr(s, f) for f, _ in s._fields_}
+
+
+def set_counting(on):
+    load().rtcgbSetQueryCounting(1 if on else 0)
+
+
+def launch_count():
+    return load().rtcgbGetKernelLaunchCount()
+
+
+def radix_sort_pairs(keys, values):
+    """GPU stable radix sort of uint64 keys with uint32 values (returns copies)."""
+    k = np.ascontiguousarray(keys, np.uint64).copy()
+    v = np.ascontiguousarray(values, np.uint32).copy()
+    rc = load().rtcgbRadixSortPairs(_ptr(k), _ptr(v), k.shape[0])
+    if rc:
+        raise RuntimeError(f"rtcgbRadixSortPairs failed ({rc})")
+    return k, v
+
+
+def set_thread_stream(stream_ptr):
+    load().rtcgbSetThreadStream(ctypes.c_void_p(stream_ptr) if stream_ptr else None)

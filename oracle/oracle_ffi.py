@@ -1,0 +1,139 @@
+"""ctypes bridge to the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by `__graft_entry__.smoke()` and
+by the CPU-baseline leg of bench.py, always as the checker / the CPU
+reference arm, never as part of the product path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+
+def build(force=False):
+    """Compiles liboracle.so with the committed Makefile."""
+    src = os.path.join(HERE, "oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "liboracle.so"], check=True)
+    return LIB_PATH
+
+
+class OrcStats(ctypes.Structure):
+    _fields_ = [("sah", ctypes.c_double), ("node_sah", ctypes.c_double), ("leaf_sah", ctypes.c_double),
+                ("num_nodes", ctypes.c_uint64), ("num_leaves", ctypes.c_uint64),
+                ("num_blocks", ctypes.c_uint64), ("num_prims", ctypes.c_uint64),
+                ("depth", ctypes.c_uint32), ("bounds", ctypes.c_float * 6)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp, sz, u, i, f = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint, ctypes.c_int, ctypes.c_float
+        L.orc_scene_new.restype = vp
+        L.orc_scene_free.argtypes = [vp]
+        L.orc_scene_add_mesh.argtypes = [vp, u, vp, sz, u, vp, sz, u]
+        L.orc_scene_commit.argtypes = [vp]
+        L.orc_scene_commit.restype = ctypes.c_long
+        L.orc_scene_stats.argtypes = [vp, ctypes.POINTER(OrcStats)]
+        for fn in (L.orc_intersect1M, L.orc_occluded1M):
+            fn.argtypes = [vp, vp, u, sz, i]
+        for fn in (L.orc_brute_intersect1M, L.orc_brute_occluded1M):
+            fn.argtypes = [vp, vp, u, sz]
+        L.orc_counters.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
+        L.orc_adjudicate.argtypes = [vp, vp, u, u, f, u, u, f, i]
+        L.orc_adjudicate.restype = i
+        L.orc_fp64_hit.argtypes = [vp, vp, u, u, ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.orc_fp64_hit.restype = i
+        L.orc_moeller1.argtypes = [ctypes.POINTER(f)] * 5 + [f, f] + [ctypes.POINTER(f)] * 3
+        L.orc_moeller1.restype = i
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class OracleScene:
+    """A committed oracle scene built from (geomID, verts, idx) meshes."""
+
+    def __init__(self, meshes):
+        L = lib()
+        self._h = ctypes.c_void_p(L.orc_scene_new())
+        self._keep = []
+        for gid, verts, idx in meshes:
+            verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+            idx = np.ascontiguousarray(idx, np.uint32).reshape(-1, 3)
+            self._keep.append((verts, idx))
+            L.orc_scene_add_mesh(self._h, gid, _ptr(verts), 12, verts.shape[0], _ptr(idx), 12, idx.shape[0])
+        self.num_prims = L.orc_scene_commit(self._h)
+
+    def close(self):
+        if self._h:
+            lib().orc_scene_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stats(self):
+        st = OrcStats()
+        lib().orc_scene_stats(self._h, ctypes.byref(st))
+        return st
+
+    def intersect(self, rayhits, nthreads=0):
+        """In-place closest hit on an RTCRayHit record array."""
+        assert rayhits.dtype.itemsize == 80 and rayhits.flags.c_contiguous
+        lib().orc_intersect1M(self._h, _ptr(rayhits), rayhits.shape[0], 80, nthreads)
+        return rayhits
+
+    def occluded(self, rays, nthreads=0):
+        stride = rays.dtype.itemsize
+        assert rays.flags.c_contiguous
+        lib().orc_occluded1M(self._h, _ptr(rays), rays.shape[0], stride, nthreads)
+        return rays
+
+    def brute_intersect(self, rayhits):
+        lib().orc_brute_intersect1M(self._h, _ptr(rayhits), rayhits.shape[0], 80)
+        return rayhits
+
+    def brute_occluded(self, rays):
+        lib().orc_brute_occluded1M(self._h, _ptr(rays), rays.shape[0], rays.dtype.itemsize)
+        return rays
+
+    def counters(self):
+        c = (ctypes.c_uint64 * 3)()
+        lib().orc_counters(c)
+        return dict(nodes=c[0], leaves=c[1], tris=c[2])
+
+    def adjudicate(self, ray_in, hitA, hitB, tie_ulps=16):
+        """ray_in: one RTCRayHit record as originally submitted.
+        hitA/hitB: (geomID, primID, t)."""
+        rec = np.ascontiguousarray(np.asarray(ray_in).reshape(1))
+        return lib().orc_adjudicate(self._h, _ptr(rec), int(hitA[0]), int(hitA[1]), float(hitA[2]),
+                                    int(hitB[0]), int(hitB[1]), float(hitB[2]), int(tie_ulps))
+
+    def fp64_hit(self, ray_in, geomID, primID):
+        rec = np.ascontiguousarray(np.asarray(ray_in).reshape(1))
+        t, u, v = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        ok = lib().orc_fp64_hit(self._h, _ptr(rec), geomID, primID, ctypes.byref(t), ctypes.byref(u), ctypes.byref(v))
+        return bool(ok), t.value, u.value, v.value
+
+
+def moeller1(v0, v1, v2, org, d, tnear=0.0, tfar=float("inf")):
+    f3 = ctypes.c_float * 3
+    out4, tuv, ng = (ctypes.c_float * 4)(), f3(), f3()
+    ok = lib().orc_moeller1(f3(*v0), f3(*v1), f3(*v2), f3(*org), f3(*d), tnear, tfar, out4, tuv, ng)
+    return bool(ok), tuple(out4), tuple(tuv), tuple(ng)

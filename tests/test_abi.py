@@ -1,0 +1,99 @@
+"""The C ABI without a GPU: the library builds, loads, exports every entry
+point that include/*.h declares, and the record layouts match the reference's
+(include/embree3/rtcore_ray.h:11-49, rtcore_common.h:88-224)."""
+import os
+import re
+import subprocess
+import textwrap
+
+import numpy as np
+import pytest
+
+from rtcgb import build
+from rtcgb import rays as R
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(REPO, "include")
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(INC):
+        if f.endswith(".h"):
+            txt = open(os.path.join(INC, f)).read()
+            names.update(re.findall(r"^RTC_API\s+[^;(]*?\b(rtc\w+)\s*\(", txt, re.M))
+    return names
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    lib = build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True, check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if " T " in l}
+    declared = declared_symbols()
+    assert len(declared) >= 55
+    missing = declared - exported
+    assert not missing, missing
+    # nothing but the API leaks out of the library
+    extra = {s for s in exported if s.startswith("rtc")} - declared
+    assert not extra, extra
+
+
+def test_library_loads_without_gpu():
+    import ctypes
+    lib = ctypes.CDLL(build.build())
+    for name in declared_symbols():
+        assert hasattr(lib, name)
+
+
+def test_ctypes_binding_covers_all_symbols():
+    from rtcgb import api
+    assert set(api.EXPORTS) == declared_symbols()
+
+
+LAYOUT_C = textwrap.dedent(r"""
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "rtcore_gb300.h"
+    #include "rtcore_gb300_ext.h"
+    int main(void) {
+      printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n",
+             sizeof(struct RTCRay), sizeof(struct RTCHit), sizeof(struct RTCRayHit),
+             offsetof(struct RTCRayHit, hit), offsetof(struct RTCRay, tfar),
+             offsetof(struct RTCHit, primID), offsetof(struct RTCHit, geomID),
+             offsetof(struct RTCHit, instID), sizeof(struct RTCIntersectContext),
+             sizeof(struct RTCBounds), _Alignof(struct RTCRay));
+      return 0;
+    }
+""")
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_header_layout(tmp_path, lang):
+    src = tmp_path / ("layout.c" if lang == "c" else "layout.cpp")
+    src.write_text(LAYOUT_C.replace("_Alignof", "alignof") if lang == "c++" else LAYOUT_C)
+    exe = tmp_path / "layout"
+    cc = "gcc" if lang == "c" else "g++"
+    subprocess.run([cc, "-Wall", "-Werror", "-I", INC, str(src), "-o", str(exe)], check=True)
+    vals = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
+    assert vals == [48, 32, 80, 48, 32, 20, 24, 28, 24, 32, 16]
+    assert R.RAYHIT_DTYPE.fields["tfar"][1] == 32
+    assert R.RAYHIT_DTYPE.fields["primID"][1] == 48 + 20
+    assert R.RAYHIT_DTYPE.fields["geomID"][1] == 48 + 24
+
+
+def test_drop_in_include_path(tmp_path):
+    """A program written against <embree3/rtcore.h> compiles unchanged."""
+    src = tmp_path / "prog.cpp"
+    src.write_text(textwrap.dedent("""
+        #include <embree3/rtcore.h>
+        int main() {
+          RTCDevice d = rtcNewDevice(nullptr);
+          RTCScene s = rtcNewScene(d);
+          RTCGeometry g = rtcNewGeometry(d, RTC_GEOMETRY_TYPE_TRIANGLE);
+          rtcAttachGeometry(s, g); rtcReleaseGeometry(g); rtcCommitScene(s);
+          RTCIntersectContext ctx; rtcInitIntersectContext(&ctx);
+          RTCRayHit rh; rtcIntersect1M(s, &ctx, &rh, 1, sizeof(rh));
+          rtcReleaseScene(s); rtcReleaseDevice(d); return 0;
+        }
+    """))
+    subprocess.run(["g++", "-c", "-Wall", "-I", INC, str(src), "-o", str(tmp_path / "prog.o")], check=True)

@@ -1,0 +1,93 @@
+"""The GPU BVH builder: structural invariants of the 8-wide quantised BVH,
+determinism, and SAH quality against the oracle's restatement of the
+reference's binned-SAH builder (bvh_statistics.cpp semantics on both)."""
+import numpy as np
+import pytest
+
+from rtcgb import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def decode(nodes):
+    """80-byte node records -> dict of arrays (layout of csrc/gb_common.h)."""
+    n = nodes.shape[0]
+    f = nodes[:, 0:12].copy().view(np.float32).reshape(n, 3)
+    e = nodes[:, 12:15].astype(np.uint32)
+    imask = nodes[:, 15]
+    child_base = nodes[:, 16:20].copy().view(np.uint32).reshape(n)
+    tri_base = nodes[:, 20:24].copy().view(np.uint32).reshape(n)
+    meta = nodes[:, 24:32]
+    q = nodes[:, 32:80].reshape(n, 6, 8).astype(np.float64)
+    scale = np.ldexp(1.0, e.astype(np.int64) - 127)
+    lo = f[:, None, :].astype(np.float64) + q[:, 0:3, :].transpose(0, 2, 1) * scale[:, None, :]
+    hi = f[:, None, :].astype(np.float64) + q[:, 3:6, :].transpose(0, 2, 1) * scale[:, None, :]
+    return dict(imask=imask, child_base=child_base, tri_base=tri_base, meta=meta, lo=lo, hi=hi)
+
+
+def check_structure(nodes, tris, verts, idx):
+    d = decode(nodes)
+    n = nodes.shape[0]
+    seen = np.zeros(tris.shape[0], np.int32)
+    reached = np.zeros(n, np.int32)
+    reached[0] = 1
+    prim = tris[:, 3].view(np.uint32)
+    for k in range(n):
+        internal_rank = 0
+        for s in range(8):
+            m = int(d["meta"][k, s])
+            if m == 0:
+                continue
+            lo, hi = d["lo"][k, s], d["hi"][k, s]
+            if d["imask"][k] >> s & 1:
+                c = d["child_base"][k] + internal_rank
+                internal_rank += 1
+                assert c < n
+                reached[c] += 1
+            else:
+                cnt = bin(m >> 5).count("1")
+                assert (m >> 5) in (1, 3, 7)
+                first = d["tri_base"][k] + (m & 31)
+                for t in range(first, first + cnt):
+                    seen[t] += 1
+                    pv = verts[idx[prim[t]]]  # 3x3 vertices of the triangle
+                    assert np.all(pv >= lo - 1e-30) and np.all(pv <= hi + 1e-30), (k, s)
+    assert np.all(seen == 1)      # every valid triangle exactly once
+    assert np.all(reached == 1)   # every node has exactly one parent (root: itself)
+
+
+def test_structure_and_determinism(rtc, device):
+    for verts, idx in (W.heightfield(48), W.gaussian_soup(20000, seed=3), W.triangle_sphere((0, 0, 0), 1.0, 30)):
+        sc = rtc.Scene(device)
+        sc.add_mesh(verts, idx)
+        sc.commit()
+        nodes, tris = sc.bvh()
+        assert tris.shape[0] == idx.shape[0]
+        check_structure(nodes, tris, verts, idx)
+        # e1 = v0 - v1, e2 = v2 - v0 exactly as Triangle4 (triangle.h:40-41)
+        p = tris[:, 3].view(np.uint32)
+        v = verts[idx[p]]
+        assert np.array_equal(tris[:, 0:3], v[:, 0])
+        assert np.array_equal(tris[:, 4:7], v[:, 0] - v[:, 1])
+        assert np.array_equal(tris[:, 8:11], v[:, 2] - v[:, 0])
+        sc.commit()
+        nodes2, tris2 = sc.bvh()
+        assert np.array_equal(nodes, nodes2) and np.array_equal(tris, tris2)
+
+
+@pytest.mark.parametrize("name", ["heightfield", "soup"])
+def test_sah_against_reference_builder(rtc, device, oracle, name):
+    """SAH of the GPU BVH vs the oracle's binned-SAH builder (target <= 1.15x)."""
+    if name == "heightfield":
+        verts, idx = W.heightfield(256)
+    else:
+        verts, idx = W.gaussian_soup(500_000, seed=11)
+    sc = rtc.Scene(device)
+    sc.add_mesh(verts, idx)
+    sc.commit()
+    gpu = sc.build_stats()
+    ref = oracle.OracleScene([(0, verts, idx)]).stats()
+    ratio = gpu["sah"] / ref.sah
+    print(name, "gpu SAH", gpu["sah"], "reference-builder SAH", ref.sah, "ratio", ratio)
+    assert gpu["num_prims"] == ref.num_prims
+    assert ratio <= 1.15
