@@ -43,7 +43,7 @@ def test_error_callback_and_null_handles(rtc, device):
     L.rtcNewGeometry(device.h, 1)  # QUAD: not supported
     assert device.error() == E_UNKNOWN
     assert seen and seen[-1][0] == E_UNKNOWN
-    L.rtcSetDeviceErrorFunction(device.h, rtc.ERROR_FN(), None)
+    L.rtcSetDeviceErrorFunction(device.h, rtc.ERROR_FN(), None)  # NULL callback
     L.rtcCommitScene(None)
     assert L.rtcGetDeviceError(None) == E_ARG
 
@@ -152,7 +152,8 @@ def test_progress_monitor_cancel(rtc, device):
     L.rtcSetSceneProgressMonitorFunction(s, cb, None)
     L.rtcCommitScene(s)
     assert device.error() == E_CANCEL
-    L.rtcSetSceneProgressMonitorFunction(s, rtc.PROGRESS_FN(lambda ptr, n: True), None)
+    ok_cb = rtc.PROGRESS_FN(lambda ptr, n: True)  # must outlive the commit below
+    L.rtcSetSceneProgressMonitorFunction(s, ok_cb, None)
     L.rtcCommitScene(s)
     assert device.error() == E_NONE
     L.rtcReleaseScene(s)
