@@ -3,10 +3,10 @@
 //
 // Replaces the reference's single-ray / hybrid traversal
 // (kernels/bvh/bvh_intersector1.cpp:30-195, bvh_intersector_hybrid.cpp:36-375)
-// with persistent CTAs: each warp fetches 32 rays with one atomic, every lane
-// walks the 8-wide quantised BVH with a short stack of node groups
-// (child base + hit bits), visiting children in the order given by the ray's
-// direction octant.
+// with persistent CTAs: warps refill idle lanes with rays fetched by one
+// atomic, every lane walks the 8-wide quantised BVH with a short stack of node
+// groups (child base + hit bits) and postponed triangle groups, visiting
+// children in the order given by the ray's direction octant.
 //
 // Arithmetic that decides hits is the reference's, bit for bit:
 //   Moeller-Trumbore  kernels/geometry/triangle_intersector_moeller.h:62-104
@@ -15,10 +15,9 @@
 // with rcp the correctly rounded reciprocal.  This file is compiled with
 // --fmad=false and every rounding step is spelled out with intrinsics.
 //
-// The node test only prunes: it decodes each child box rounded outward and
-// widens the slab interval by (1 + 2*gamma_3) (Ize, "Robust BVH Ray
-// Traversal", JCGT 2013), so a box that contains an accepted intersection
-// is never culled.
+// The node test only prunes: its slab distances are widened by a bound on
+// their rounding error, so a box that contains an accepted intersection is
+// never culled.
 #include <cuda_runtime.h>
 
 #include "gb_common.h"
@@ -27,8 +26,6 @@
 namespace gb {
 
 constexpr int TRACE_THREADS = 128;
-// 1 + 2*gamma_3 rounded up to float: gamma_3 = 3u/(1-3u), u = 2^-24
-constexpr float kSlabGrow = 1.00000036f;
 constexpr float kMinRcpInput = 1E-18f;  // common/math/constants.h:31
 
 __device__ __forceinline__ float dot3(const float3 a, const float3 b) {
@@ -75,13 +72,24 @@ __device__ __forceinline__ void init_ray(TRay& r) {
   r.tnear_c = fmaxf(r.tnear, 0.0f);
 }
 
-__device__ __forceinline__ uint32_t byte_of(uint2 v, int s) {
-  return ((s < 4 ? v.x : v.y) >> (8 * (s & 3))) & 0xFFu;
+// Byte k of w as a float (exact): 0x4B0000bb reinterpreted is 2^23 + bb.
+__device__ __forceinline__ float ubyte_f(uint32_t w, uint32_t k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k)) - 8388608.0f;
 }
 
-// Intersects the 8 children of `np`.  Returns the node group of hit internal
-// children (hit bits 24..31 keyed by slot ^ oct, imask in bits 0..7) and the
-// triangle group of hit leaves (24 triangle bits).
+// Rounding slack of the slab test, relative to (|p - o| + 256 s) |1/d|: the
+// computed slab distances carry at most ~5 unit roundoffs of that magnitude
+// (one each from p - o, the product with 1/d, 1/d itself, the FMA and the
+// subtraction of the slack); 8u = 2^-21 covers them with margin.
+constexpr float kSlabEps = 4.76837158e-7f;
+
+// Intersects the 8 children of `np`.  Child box planes are p + q * 2^e; with
+// a = (p - o) / d and b = 2^e / d precomputed per node and axis, a plane
+// distance is one FMA q * b + a, widened by the rounding slack (near planes
+// down, far planes up) so a box that contains an accepted intersection is
+// never culled.  Returns the node group of hit internal children (hit bits
+// 24..31 keyed by slot ^ oct, imask in bits 0..7) and the triangle group of
+// hit leaves (24 triangle bits).
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, const TRay& r, const float tfar,
                                                uint32_t& g_base, uint32_t& g_bits, uint32_t& t_base,
                                                uint32_t& t_bits) {
@@ -91,28 +99,45 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
   const uint4 n2 = __ldg(q + 2);
   const uint4 n3 = __ldg(q + 3);
   const uint4 n4 = __ldg(q + 4);
-  const float px = __uint_as_float(n0.x), py = __uint_as_float(n0.y), pz = __uint_as_float(n0.z);
-  const uint32_t ex = n0.w & 0xFFu, ey = (n0.w >> 8) & 0xFFu, ez = (n0.w >> 16) & 0xFFu, imask = n0.w >> 24;
-  const float sx = __uint_as_float(ex << 23), sy = __uint_as_float(ey << 23), sz = __uint_as_float(ez << 23);
-  const uint2 meta = make_uint2(n1.z, n1.w);
-  const uint2 qlx = make_uint2(n2.x, n2.y), qly = make_uint2(n2.z, n2.w);
-  const uint2 qlz = make_uint2(n3.x, n3.y), qhx = make_uint2(n3.z, n3.w);
-  const uint2 qhy = make_uint2(n4.x, n4.y), qhz = make_uint2(n4.z, n4.w);
+  const uint32_t imask = n0.w >> 24;
+  float bx, by, bz, anx, afx, any_, afy, anz, afz;
+  {
+    const float sx = __uint_as_float((n0.w & 0xFFu) << 23);
+    const float sy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23);
+    const float sz = __uint_as_float(((n0.w >> 16) & 0xFFu) << 23);
+    const float xo = __fsub_rn(__uint_as_float(n0.x), r.org.x);
+    const float yo = __fsub_rn(__uint_as_float(n0.y), r.org.y);
+    const float zo = __fsub_rn(__uint_as_float(n0.z), r.org.z);
+    const float ax = __fmul_rn(xo, r.rdir.x), ay = __fmul_rn(yo, r.rdir.y), az = __fmul_rn(zo, r.rdir.z);
+    bx = __fmul_rn(sx, r.rdir.x);
+    by = __fmul_rn(sy, r.rdir.y);
+    bz = __fmul_rn(sz, r.rdir.z);
+    const float ex = __fmul_ru(__fmul_ru(__fmaf_ru(256.0f, sx, fabsf(xo)), fabsf(r.rdir.x)), kSlabEps);
+    const float ey = __fmul_ru(__fmul_ru(__fmaf_ru(256.0f, sy, fabsf(yo)), fabsf(r.rdir.y)), kSlabEps);
+    const float ez = __fmul_ru(__fmul_ru(__fmaf_ru(256.0f, sz, fabsf(zo)), fabsf(r.rdir.z)), kSlabEps);
+    anx = __fsub_rd(ax, ex); afx = __fadd_ru(ax, ex);
+    any_ = __fsub_rd(ay, ey); afy = __fadd_ru(ay, ey);
+    anz = __fsub_rd(az, ez); afz = __fadd_ru(az, ez);
+  }
+  // near / far quantised planes by the ray direction's sign per axis
+  const bool px = r.rdir.x >= 0.0f, py = r.rdir.y >= 0.0f, pz = r.rdir.z >= 0.0f;
+  const uint32_t nx0 = px ? n2.x : n3.z, nx1 = px ? n2.y : n3.w, fx0 = px ? n3.z : n2.x, fx1 = px ? n3.w : n2.y;
+  const uint32_t ny0 = py ? n2.z : n4.x, ny1 = py ? n2.w : n4.y, fy0 = py ? n4.x : n2.z, fy1 = py ? n4.y : n2.w;
+  const uint32_t nz0 = pz ? n3.x : n4.z, nz1 = pz ? n3.y : n4.w, fz0 = pz ? n4.z : n3.x, fz1 = pz ? n4.w : n3.y;
   const float tfar_c = fmaxf(tfar, 0.0f);
   uint32_t hits = 0, tb = 0;
 #pragma unroll
   for (int s = 0; s < 8; s++) {
-    const uint32_t m = byte_of(meta, s);
-    // outward-rounded decode of the child box
-    const float lx = __fmaf_rd((float)byte_of(qlx, s), sx, px), hx = __fmaf_ru((float)byte_of(qhx, s), sx, px);
-    const float ly = __fmaf_rd((float)byte_of(qly, s), sy, py), hy = __fmaf_ru((float)byte_of(qhy, s), sy, py);
-    const float lz = __fmaf_rd((float)byte_of(qlz, s), sz, pz), hz = __fmaf_ru((float)byte_of(qhz, s), sz, pz);
-    const float t0x = __fmul_rn(__fsub_rn(lx, r.org.x), r.rdir.x), t1x = __fmul_rn(__fsub_rn(hx, r.org.x), r.rdir.x);
-    const float t0y = __fmul_rn(__fsub_rn(ly, r.org.y), r.rdir.y), t1y = __fmul_rn(__fsub_rn(hy, r.org.y), r.rdir.y);
-    const float t0z = __fmul_rn(__fsub_rn(lz, r.org.z), r.rdir.z), t1z = __fmul_rn(__fsub_rn(hz, r.org.z), r.rdir.z);
-    const float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), r.tnear_c));
-    const float tmax = __fmul_ru(fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tfar_c)),
-                                 kSlabGrow);
+    const uint32_t k = s & 3;
+    const float tnx = __fmaf_rn(ubyte_f(s < 4 ? nx0 : nx1, k), bx, anx);
+    const float tfx = __fmaf_rn(ubyte_f(s < 4 ? fx0 : fx1, k), bx, afx);
+    const float tny = __fmaf_rn(ubyte_f(s < 4 ? ny0 : ny1, k), by, any_);
+    const float tfy = __fmaf_rn(ubyte_f(s < 4 ? fy0 : fy1, k), by, afy);
+    const float tnz = __fmaf_rn(ubyte_f(s < 4 ? nz0 : nz1, k), bz, anz);
+    const float tfz = __fmaf_rn(ubyte_f(s < 4 ? fz0 : fz1, k), bz, afz);
+    const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear_c));
+    const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_c));
+    const uint32_t m = ((s < 4 ? n1.z : n1.w) >> (8 * k)) & 0xFFu;
     if (m != 0 && tmin <= tmax) {
       if (imask >> s & 1u) hits |= 1u << (24 + (s ^ r.oct));
       else tb |= (m >> 5) << (m & 31u);
@@ -133,73 +158,9 @@ struct Ctx {
   uint32_t num_tris;
 };
 
-template <bool ANYHIT, bool COUNT>
-__device__ __forceinline__ bool traverse(const Ctx& c, const TRay& r, float& t_best, uint32_t& hit_tri, float& hit_u,
-                                         float& hit_v, unsigned long long& n_nodes, unsigned long long& n_tris) {
-  uint2 stack[kStackSize];
-  int sp = 0;
-  // virtual group holding the root as internal slot 0
-  uint32_t g_base = 0, g_bits = (1u << (24 + r.oct)) | 1u;
-  uint32_t t_base = 0, t_bits = 0;
-  uint32_t iters = 0;
-  for (;;) {
-    if (++iters > c.max_iters) {
-      atomicOr(c.err, kErrIterationLimit);
-      return false;
-    }
-    if (g_bits & 0xFF000000u) {
-      const uint32_t k = __ffs(g_bits >> 24) - 1;
-      g_bits &= ~(1u << (24 + k));
-      const uint32_t slot = k ^ r.oct;
-      const uint32_t child = g_base + __popc(g_bits & ((1u << slot) - 1u) & 0xFFu);
-      if (g_bits & 0xFF000000u) {
-        if (sp >= kStackSize) {
-          atomicOr(c.err, kErrStackOverflow);
-          return false;
-        }
-        stack[sp++] = make_uint2(g_base, g_bits);
-      }
-      if (child >= c.num_nodes) {  // corrupt BVH: report, never read out of bounds
-        atomicOr(c.err, kErrBuild);
-        return false;
-      }
-      if (COUNT) n_nodes++;
-      intersect_node(c.nodes + child, r, t_best, g_base, g_bits, t_base, t_bits);
-    }
-    while (t_bits) {
-      const uint32_t idx = __ffs(t_bits) - 1;
-      t_bits &= t_bits - 1;
-      const uint32_t ti = t_base + idx;
-      if (ti >= c.num_tris) {
-        atomicOr(c.err, kErrBuild);
-        return false;
-      }
-      const float4* tp = reinterpret_cast<const float4*>(c.tris + ti);
-      const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
-      if (COUNT) n_tris++;
-      float U, V, T, absDen;
-      if (moeller(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org, r.dir,
-                  r.tnear, t_best, U, V, T, absDen)) {
-        if (ANYHIT) {
-          hit_tri = ti;
-          return true;
-        }
-        const float rcp = __frcp_rn(absDen);
-        t_best = __fmul_rn(T, rcp);
-        hit_u = __fmul_rn(U, rcp);
-        hit_v = __fmul_rn(V, rcp);
-        hit_tri = ti;
-      }
-    }
-    if (!(g_bits & 0xFF000000u)) {
-      if (sp == 0) break;
-      const uint2 e = stack[--sp];
-      g_base = e.x;
-      g_bits = e.y;
-    }
-  }
-  return hit_tri != kInvalidID;
-}
+constexpr int kRefillIdle = 8;      // a warp fetches new rays once this many lanes are idle
+constexpr int kPostponePct = 20;    // triangle work waits while fewer active lanes have it
+constexpr uint32_t kTriGroup = 0x80000000u;  // stack entry flag: triangle group
 
 template <bool ALIGNED>
 __device__ __forceinline__ void load_ray(const char* p, TRay& r, float& tfar) {
@@ -219,51 +180,144 @@ __device__ __forceinline__ void load_ray(const char* p, TRay& r, float& tfar) {
   }
 }
 
+// Persistent traversal.  Every lane owns one ray at a time; a warp refills
+// its idle lanes with one atomic once kRefillIdle of them are idle.  Each
+// loop iteration an active lane (1) visits one node of its current group,
+// (2) tests its pending triangles -- unless few lanes of the warp have
+// triangle work, in which case the group is pushed and tested later -- and
+// (3) pops the stack when its group is exhausted.
 template <bool ANYHIT, bool COUNT, bool ALIGNED>
 __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
-  Ctx c{P.nodes, P.tris, P.err, P.max_iters, P.num_nodes, P.num_tris};
+  const Ctx c{P.nodes, P.tris, P.err, P.max_iters, P.num_nodes, P.num_tris};
   const int lane = threadIdx.x & 31;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint2 stack[kStackSize];
+  int sp = 0;
+  bool active = false, exhausted = false;
+  char* rec = nullptr;
+  TRay r;
+  float t_best = 0.f, hu = 0.f, hv = 0.f;
+  uint32_t hit_tri = kInvalidID, g_base = 0, g_bits = 0, t_base = 0, t_bits = 0, iters = 0;
   unsigned long long n_nodes = 0, n_tris = 0, n_rays = 0;
   for (;;) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(P.ray_counter, 32u);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= P.nrays) break;
-    const uint32_t rid = base + lane;
-    if (rid >= P.nrays) continue;
-    char* rec = P.rays + (uint64_t)rid * P.stride;
-    TRay r;
-    float tfar;
-    load_ray<ALIGNED>(rec, r, tfar);
-    if (ANYHIT) {
-      // bvh_intersector_stream_filters.cpp:75: skip invalid and already occluded rays
-      if (!(r.tnear <= tfar) || tfar < 0.0f) continue;
-    } else {
-      if (!(r.tnear <= tfar)) continue;
+    // ---- refill idle lanes
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
+    if (!exhausted && __popc(idle) >= kRefillIdle) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(P.ray_counter, (unsigned)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (base + __popc(idle) >= P.nrays) exhausted = true;
+      if (!active) {
+        const uint32_t rid = base + __popc(idle & lt_mask);
+        if (rid < P.nrays) {
+          rec = P.rays + (uint64_t)rid * P.stride;
+          float tfar;
+          load_ray<ALIGNED>(rec, r, tfar);
+          // stream semantics: only tnear <= tfar rays are traced; any-hit also
+          // skips already occluded rays (bvh_intersector_stream_filters.cpp:75)
+          const bool valid = ANYHIT ? ((r.tnear <= tfar) && !(tfar < 0.0f)) : (r.tnear <= tfar);
+          if (valid) {
+            init_ray(r);
+            t_best = tfar;
+            hit_tri = kInvalidID;
+            g_base = 0;
+            g_bits = (1u << (24 + r.oct)) | 1u;  // virtual group: the root as internal slot 0
+            t_bits = 0;
+            sp = 0;
+            iters = 0;
+            active = true;
+            if (COUNT) n_rays++;
+          }
+        }
+      }
     }
-    if (COUNT) n_rays++;
-    init_ray(r);
-    float t_best = tfar, u = 0.f, v = 0.f;
-    uint32_t hit_tri = kInvalidID;
-    const bool hit = traverse<ANYHIT, COUNT>(c, r, t_best, hit_tri, u, v, n_nodes, n_tris);
-    if (!hit) continue;
-    if (ANYHIT) {
-      *reinterpret_cast<float*>(rec + 32) = -INFINITY;
+    if (!__any_sync(0xFFFFFFFFu, active)) {
+      if (exhausted) break;
       continue;
     }
-    const float4* tp = reinterpret_cast<const float4*>(c.tris + hit_tri);
-    const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
-    const float3 Ng = cross3(make_float3(d.x, d.y, d.z), make_float3(b.x, b.y, b.z));
-    *reinterpret_cast<float*>(rec + 32) = t_best;
-    if (ALIGNED) {
-      *reinterpret_cast<float4*>(rec + 48) = make_float4(Ng.x, Ng.y, Ng.z, u);
-      *reinterpret_cast<uint4*>(rec + 64) =
-          make_uint4(__float_as_uint(v), __float_as_uint(a.w), __float_as_uint(b.w), kInvalidID);
-    } else {
-      float* f = reinterpret_cast<float*>(rec + 48);
-      f[0] = Ng.x; f[1] = Ng.y; f[2] = Ng.z; f[3] = u; f[4] = v;
-      uint32_t* w = reinterpret_cast<uint32_t*>(rec + 68);
-      w[0] = __float_as_uint(a.w); w[1] = __float_as_uint(b.w); w[2] = kInvalidID;
+    bool done = false, visited = false;
+    if (active && ++iters > c.max_iters) {
+      atomicOr(c.err, kErrIterationLimit);
+      active = false;
+    }
+    // ---- (1) one node of the current group
+    if (active && t_bits == 0 && (g_bits & 0xFF000000u)) {
+      const uint32_t k = __ffs(g_bits >> 24) - 1;
+      g_bits &= ~(1u << (24 + k));
+      const uint32_t slot = k ^ r.oct;
+      const uint32_t child = g_base + __popc(g_bits & ((1u << slot) - 1u) & 0xFFu);
+      if (g_bits & 0xFF000000u) {
+        if (sp < kStackSize) stack[sp++] = make_uint2(g_base, g_bits);
+        else { atomicOr(c.err, kErrStackOverflow); active = false; }
+      }
+      if (active && child >= c.num_nodes) { atomicOr(c.err, kErrBuild); active = false; }
+      if (active) {
+        if (COUNT) n_nodes++;
+        intersect_node(c.nodes + child, r, t_best, g_base, g_bits, t_base, t_bits);
+        visited = true;
+      }
+    }
+    // ---- (2) triangles, postponed while few lanes have any
+    const uint32_t want = __ballot_sync(0xFFFFFFFFu, active && t_bits != 0);
+    const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
+    if (visited && t_bits != 0 && __popc(want) * 100 < __popc(act) * kPostponePct) {
+      if (sp < kStackSize) {
+        stack[sp++] = make_uint2(t_base | kTriGroup, t_bits);
+        t_bits = 0;
+      }
+    }
+    while (active && t_bits) {
+      const uint32_t idx = __ffs(t_bits) - 1;
+      t_bits &= t_bits - 1;
+      const uint32_t ti = t_base + idx;
+      if (ti >= c.num_tris) { atomicOr(c.err, kErrBuild); active = false; break; }
+      const float4* tp = reinterpret_cast<const float4*>(c.tris + ti);
+      const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
+      if (COUNT) n_tris++;
+      float U, V, T, absDen;
+      if (moeller(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org, r.dir,
+                  r.tnear, t_best, U, V, T, absDen)) {
+        hit_tri = ti;
+        if (ANYHIT) { done = true; t_bits = 0; break; }
+        const float rcp = __frcp_rn(absDen);
+        t_best = __fmul_rn(T, rcp);
+        hu = __fmul_rn(U, rcp);
+        hv = __fmul_rn(V, rcp);
+      }
+    }
+    // ---- (3) next group from the stack, or finish
+    if (active && !done && t_bits == 0 && !(g_bits & 0xFF000000u)) {
+      if (sp > 0) {
+        const uint2 e = stack[--sp];
+        if (e.x & kTriGroup) { t_base = e.x & ~kTriGroup; t_bits = e.y; g_bits = 0; }
+        else { g_base = e.x; g_bits = e.y; }
+      } else {
+        done = true;
+      }
+    }
+    if (active && done) {
+      active = false;
+      if (hit_tri != kInvalidID) {
+        if (ANYHIT) {
+          *reinterpret_cast<float*>(rec + 32) = -INFINITY;
+        } else {
+          const float4* tp = reinterpret_cast<const float4*>(c.tris + hit_tri);
+          const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
+          const float3 Ng = cross3(make_float3(d.x, d.y, d.z), make_float3(b.x, b.y, b.z));
+          *reinterpret_cast<float*>(rec + 32) = t_best;
+          if (ALIGNED) {
+            *reinterpret_cast<float4*>(rec + 48) = make_float4(Ng.x, Ng.y, Ng.z, hu);
+            *reinterpret_cast<uint4*>(rec + 64) =
+                make_uint4(__float_as_uint(hv), __float_as_uint(a.w), __float_as_uint(b.w), kInvalidID);
+          } else {
+            float* f = reinterpret_cast<float*>(rec + 48);
+            f[0] = Ng.x; f[1] = Ng.y; f[2] = Ng.z; f[3] = hu; f[4] = hv;
+            uint32_t* w = reinterpret_cast<uint32_t*>(rec + 68);
+            w[0] = __float_as_uint(a.w); w[1] = __float_as_uint(b.w); w[2] = kInvalidID;
+          }
+        }
+      }
     }
   }
   if (COUNT) {

@@ -479,7 +479,7 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   P.ray_counter = c.dscratch;
   P.err = c.dscratch + 1;
   P.counters = reinterpret_cast<gb::TraceCounters*>(c.dscratch + 2);
-  P.max_iters = 2 * bvh.num_nodes + 64;
+  P.max_iters = 4 * bvh.num_nodes + 64;  // node visits, triangle phases and pops per ray
   P.num_nodes = bvh.num_nodes;
   P.num_tris = bvh.num_tris;
   cuda_ok(cudaEventRecord(c.e1, st), "event");
