@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="", help="extra rtcNewDevice config tokens, e.g. gpu.leaf_max=2")
     return ap.parse_args()
 
 
@@ -209,7 +210,7 @@ def run_gpu(args, rank, world):
 
     verts, idx, rays, label = workload(args.workload, args.scale, rank)
     nrays = rays.shape[0]
-    dev = api.Device(f"gpu.device={local}".encode())
+    dev = api.Device(f"gpu.device={local}{',' + args.config if args.config else ''}".encode())
     stream = torch.cuda.current_stream()
     api.set_thread_stream(stream.cuda_stream)
     sc = api.Scene(dev)

@@ -13,7 +13,7 @@
 //   5. top-down collapse into 8-wide nodes (largest-area child opened first),
 //      child boxes quantised to 8 bits per plane, children placed in slots
 //      so that the ray's direction octant gives a near-to-far visiting order,
-//      leaves of <= 3 triangles written as v0/e1/e2 records.
+//      leaves of <= 4 triangles written as v0/e1/e2 records.
 // Everything is deterministic: the same input gives the same bytes.
 #include <cuda_runtime.h>
 
@@ -182,7 +182,7 @@ __device__ __forceinline__ uint64_t spread21(uint32_t x) {
 
 __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                 uint32_t n, BoundsAcc* acc, uint64_t* __restrict__ keys,
-                                                uint32_t* __restrict__ vals) {
+                                                uint32_t* __restrict__ vals, int cube) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t key = ~0ull;
   if (i < n) {
@@ -191,10 +191,14 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
       const float lo[3] = {ord2f(acc->clo[0]), ord2f(acc->clo[1]), ord2f(acc->clo[2])};
       const float hi[3] = {ord2f(acc->chi[0]), ord2f(acc->chi[1]), ord2f(acc->chi[2])};
       const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+      // cube: one scale for all axes (the centroid box's largest extent) keeps
+      // the scene's aspect ratio, so flat scenes are ordered mostly in-plane;
+      // otherwise every axis is scaled to its own extent
+      const float emax = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
       uint64_t code = 0;
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        const float ext = hi[d] - lo[d];
+        const float ext = cube ? emax : hi[d] - lo[d];
         float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
         x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
         code |= spread21((uint32_t)x) << (2 - d);
@@ -625,6 +629,7 @@ struct BinTree {
   const float4* hi;
   const uint32_t* cnt;
   uint32_t nleaves;
+  uint32_t leaf_max;  // subtrees of at most this many triangles may become leaves
 };
 
 __device__ __forceinline__ bool bt_leaf(const BinTree& t, uint32_t k) { return k < t.nleaves; }
@@ -655,7 +660,7 @@ __device__ int gather_children(const BinTree& t, uint32_t b, uint32_t kids[8]) {
     for (int i = 0; i < nk; i++) {
       const uint32_t c = kids[i];
       if (bt_leaf(t, c)) continue;
-      const bool mand = t.cnt[c] > (uint32_t)kLeafMax;
+      const bool mand = t.cnt[c] > t.leaf_max;
       const float A = half_area(bt_lo(t, c), bt_hi(t, c));
       if (!mand) {
         // opening a small subtree pays off only if its children's boxes
@@ -690,7 +695,7 @@ __global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const uint32_
     if (i < nk) {
       const uint32_t c = kids[i];
       const uint32_t cnt = t.cnt[c];
-      if (cnt > (uint32_t)kLeafMax) ni++; else nt += cnt;
+      if (cnt > t.leaf_max) ni++; else nt += cnt;
       kids_out[8 * (size_t)k + i] = c;
     } else {
       kids_out[8 * (size_t)k + i] = 0xFFFFFFFFu;
@@ -823,8 +828,8 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
     const float3 dhi = make_float3(__fmaf_ru(qhx, sx, ulo.x), __fmaf_ru(qhy, sy, ulo.y), __fmaf_ru(qhz, sz, ulo.z));
     const double A = (double)fmaxf(0.f, half_area(dlo, dhi));
     const uint32_t cnt = t.cnt[c];
-    if (cnt > (uint32_t)kLeafMax) {
-      node.meta[s] = (uint8_t)(0x20u | (24u + (uint32_t)s));
+    if (cnt > t.leaf_max) {
+      node.meta[s] = (uint8_t)(0x80u | (uint32_t)s);
       node.imask |= (uint8_t)(1u << s);
       if (off_int[k] + int_rank >= node_cap || node.child_base + int_rank >= node_cap) {
         atomicOr(err, kErrBuild);
@@ -834,9 +839,9 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
       int_rank++;
       sah += A;  // inner node term
     } else {
-      node.meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | tri_off);
-      // collect the subtree's primitives (<= 3) in depth-first order
-      uint32_t st[4];
+      node.meta[s] = (uint8_t)(0x80u | ((cnt - 1u) << 5) | tri_off);
+      // collect the subtree's primitives (<= leaf_max) in depth-first order
+      uint32_t st[8];
       int sp = 0;
       st[sp++] = c;
       uint32_t w = 0;
@@ -850,7 +855,7 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
           write_tri(geoms, plo, phi, bt_right(t, x), &tris[node.tri_base + tri_off + w]);
           w++;
         } else {
-          if (sp + 2 > 4) {
+          if (sp + 2 > 8) {
             atomicOr(err, kErrBuild);
             return;
           }
@@ -883,7 +888,8 @@ static cudaError_t dalloc(T** p, size_t count, cudaStream_t st) {
 
 static inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
-cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* out, BuildStats* stats) {
+cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, const BuildOptions& opt, DeviceBVH* out,
+                      BuildStats* stats) {
   *out = DeviceBVH();
   *stats = BuildStats();
   for (int d = 0; d < 3; d++) { out->lo[d] = INFINITY; out->hi[d] = -INFINITY; }
@@ -922,7 +928,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   GB_CHECK(dalloc(&keys_b, total, st));
   GB_CHECK(dalloc(&vals_a, total, st));
   GB_CHECK(dalloc(&vals_b, total, st));
-  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a); note_launches(1);
+  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube); note_launches(1);
   GB_CHECK(cudaGetLastError());
   GB_CHECK(cudaMemcpyAsync(&h_acc, acc, sizeof(BoundsAcc), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
@@ -1027,7 +1033,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   cudaFreeAsync(nn, st); cudaFreeAsync(bsurv, st); cudaFreeAsync(bmerge, st);
 
   // ---- collapse, level by level (breadth-first node order)
-  BinTree bt{bnlo, bnhi, bncnt, N};
+  BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(opt.leaf_max, 1), kLeafMaxLimit)};
   WideNode* wnodes = nullptr;
   TriRecord* wtris = nullptr;
   const uint32_t maxw = N;  // wide internal nodes <= binary internal nodes + 1

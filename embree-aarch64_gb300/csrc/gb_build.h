@@ -7,7 +7,8 @@ namespace gb {
 // Builds the BVH of the given geometries (device buffers) on stream `st`.
 // Synchronises `st` before returning; `out` owns two device allocations that
 // free_bvh releases.  An empty or all-invalid scene yields num_nodes == 0.
-cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* out, BuildStats* stats);
+cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, const BuildOptions& opt, DeviceBVH* out,
+                      BuildStats* stats);
 void free_bvh(DeviceBVH* b);
 
 // Stable LSD radix sort of 64-bit keys with 32-bit values (device buffers).

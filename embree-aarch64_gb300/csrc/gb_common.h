@@ -18,17 +18,18 @@
 namespace gb {
 
 constexpr uint32_t kInvalidID = 0xFFFFFFFFu;
-constexpr int kLeafMax = 3;          // triangles per leaf child (unary count in meta)
+constexpr int kLeafMaxLimit = 4;     // largest leaf the node encoding allows
+constexpr int kLeafMaxDefault = 2;   // default triangles per leaf child (fastest measured)
 constexpr int kStackSize = 64;       // traversal stack entries (node groups)
 
 // 80-byte wide node.
-//   meta[s]: 0 = empty slot; internal child: 0b001'11sss (24 + slot);
-//            leaf: unary triangle count in bits 5..7 (001, 011, 111) and the
-//            first triangle's offset from tri_base in bits 0..4 (0..23).
+//   meta[s]: 0 = empty slot; otherwise bit 7 is set and, for a leaf, bits
+//            5..6 hold (triangle count - 1) and bits 0..4 the first
+//            triangle's offset from tri_base (0..28).
 //   imask:   bit s set when slot s holds an internal child.
 //   ex/ey/ez: IEEE-754 biased exponent of the per-axis scale 2^(e-127).
-//   decoded child box: lo = p + qlo * scale, hi = p + qhi * scale (rounded
-//   outward at traversal time so the decoded box always contains the child).
+//   decoded child box: lo = p + qlo * scale, hi = p + qhi * scale (the
+//   quantisation rounds outward, so the decoded box contains the child).
 struct alignas(16) WideNode {
   float px, py, pz;
   uint8_t ex, ey, ez, imask;
@@ -69,6 +70,12 @@ struct DeviceBVH {
   uint32_t depth = 0;        // wide levels
   float lo[3] = {0, 0, 0};   // geometry bounds (empty scene: +inf / -inf)
   float hi[3] = {0, 0, 0};
+};
+
+// Builder options (device config keys gpu.leaf_max=1..4, gpu.morton=axis|cube).
+struct BuildOptions {
+  int leaf_max = kLeafMaxDefault;
+  int morton_cube = 0;  // 1: one Morton scale for all axes (gpu.morton=cube)
 };
 
 // Build statistics reported through the extension API.

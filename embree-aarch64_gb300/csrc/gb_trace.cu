@@ -89,7 +89,7 @@ constexpr float kSlabEps = 4.76837158e-7f;
 // down, far planes up) so a box that contains an accepted intersection is
 // never culled.  Returns the node group of hit internal children (hit bits
 // 24..31 keyed by slot ^ oct, imask in bits 0..7) and the triangle group of
-// hit leaves (24 triangle bits).
+// hit leaves (up to 32 triangle bits).
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, const TRay& r, const float tfar,
                                                uint32_t& g_base, uint32_t& g_bits, uint32_t& t_base,
                                                uint32_t& t_bits) {
@@ -140,7 +140,7 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
     const uint32_t m = ((s < 4 ? n1.z : n1.w) >> (8 * k)) & 0xFFu;
     if (m != 0 && tmin <= tmax) {
       if (imask >> s & 1u) hits |= 1u << (24 + (s ^ r.oct));
-      else tb |= (m >> 5) << (m & 31u);
+      else tb |= ((2u << ((m >> 5) & 3u)) - 1u) << (m & 31u);
     }
   }
   g_base = n1.x;

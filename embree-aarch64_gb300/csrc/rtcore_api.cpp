@@ -78,6 +78,7 @@ struct Device : RefCounted {
   int verbose = 0;
   int benchmark = 0;
   int cuda_device = -1;
+  gb::BuildOptions build_opt;
   std::mutex mtx;
 
   explicit Device(const char* cfg) {
@@ -89,7 +90,7 @@ struct Device : RefCounted {
   }
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
-  // Honoured: verbose, benchmark, gpu.device; the CPU tasking and ISA keys
+  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton; the CPU tasking and ISA keys
   // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
   void parse(const char* cfg) {
     std::string s(cfg);
@@ -108,6 +109,8 @@ struct Device : RefCounted {
         if (k == "verbose") verbose = atoi(v.c_str());
         else if (k == "benchmark") benchmark = atoi(v.c_str());
         else if (k == "gpu.device") cuda_device = atoi(v.c_str());
+        else if (k == "gpu.leaf_max") build_opt.leaf_max = atoi(v.c_str());
+        else if (k == "gpu.morton") build_opt.morton_cube = (v == "cube");
       }
       i = j + 1;
     }
@@ -429,7 +432,7 @@ struct Scene : RefCounted {
     gb::free_bvh(&bvh);
     committed = false;
     gb::BuildStats bs;
-    cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, &bvh, &bs), "rtcCommitScene");
+    cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, device->build_opt, &bvh, &bs), "rtcCommitScene");
     stats = bs;
     committed = true;
     if (progress) progress(progress_ptr, 1.0);
