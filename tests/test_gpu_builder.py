@@ -75,7 +75,7 @@ def test_structure_and_determinism(rtc, device):
         assert np.array_equal(nodes, nodes2) and np.array_equal(tris, tris2)
 
 
-@pytest.mark.parametrize("name,config,limit", [("heightfield", b"", 1.30), ("heightfield", b"gpu.leaf_max=4,gpu.morton=cube", 1.22),
+@pytest.mark.parametrize("name,config,limit", [("heightfield", b"", 1.36), ("heightfield", b"gpu.leaf_max=4,gpu.morton=cube", 1.22),
                                                ("soup", b"", 1.15)])
 def test_sah_against_reference_builder(rtc, oracle, name, config, limit):
     """SAH of the GPU BVH vs the oracle's binned-SAH builder.  The soup carries
