@@ -20,6 +20,8 @@
 // never culled.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "gb_common.h"
 #include "gb_trace.h"
 
@@ -361,6 +363,85 @@ cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStre
   }
   if (count) return aligned ? launch_one<false, true, true>(P, st) : launch_one<false, true, false>(P, st);
   return aligned ? launch_one<false, false, true>(P, st) : launch_one<false, false, false>(P, st);
+}
+
+// ---------------------------------------------------------------------------
+// Query without allocations.
+//
+// For callers that must not allocate device memory during a query -- a
+// process whose memory is fully reserved by its own allocator (so cudaMalloc
+// would fail), a real-time loop that cannot take cudaMalloc's implicit device
+// synchronisation, or a service held to a fixed memory budget -- the scratch
+// of the closest-hit query lives in this file-scope array, which every GPU
+// that loads the library holds until the process exits: 256 bytes of query
+// state (fetch counter, error flags, counters) followed by kNoAllocStagingBytes
+// (32 MiB) of staging for host-resident rays.  All calls share it and it keeps
+// the last call's contents: each call clears the state words it relies on,
+// and calls whose GPU work overlaps (concurrent streams or host threads) race
+// on it, so callers serialise them.
+// ---------------------------------------------------------------------------
+
+constexpr uint64_t kNoAllocStateBytes = 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocStateBytes + kNoAllocStagingBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the symbol name is only a host-side stand-in for it).
+static cudaError_t noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+cudaError_t noalloc_closest(const DeviceBVH& bvh, char* rays, bool rays_on_device, uint32_t M, uint64_t stride,
+                            cudaStream_t st, uint32_t* err_flags) {
+  *err_flags = 0;
+  if (M == 0 || bvh.num_nodes == 0) return cudaSuccess;
+  const uint64_t span = (uint64_t)(M - 1) * stride + sizeof(float) * 20;
+  if (!rays_on_device && span > kNoAllocStagingBytes) return cudaErrorInvalidValue;
+  unsigned char* scratch = nullptr;
+  cudaError_t e = noalloc_scratch(&scratch);
+  if (e != cudaSuccess) return e;
+  unsigned int* state = reinterpret_cast<unsigned int*>(scratch);
+  char* staging = reinterpret_cast<char*>(scratch + kNoAllocStateBytes);
+  if ((e = cudaMemsetAsync(state, 0, kNoAllocStateBytes, st)) != cudaSuccess) return e;
+  if (!rays_on_device && (e = cudaMemcpyAsync(staging, rays, span, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return e;
+  TraceParams P{};
+  P.nodes = bvh.nodes;
+  P.tris = bvh.tris;
+  P.rays = rays_on_device ? rays : staging;
+  P.stride = stride;
+  P.nrays = M;
+  P.ray_counter = state;
+  P.err = state + 1;
+  P.counters = reinterpret_cast<TraceCounters*>(state + 2);
+  P.max_iters = 4 * bvh.num_nodes + 64;
+  P.num_nodes = bvh.num_nodes;
+  P.num_tris = bvh.num_tris;
+  if ((e = launch_trace(P, false, false, st)) != cudaSuccess) return e;
+  if (!rays_on_device && (e = cudaMemcpyAsync(rays, staging, span, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  unsigned int flags = 0;
+  if ((e = cudaMemcpyAsync(&flags, state + 1, sizeof(flags), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  *err_flags = flags;
+  return cudaSuccess;
 }
 
 }  // namespace gb

@@ -21,4 +21,15 @@ struct TraceParams {
 // Launches the persistent closest-hit (anyhit = false) or any-hit kernel.
 cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStream_t st);
 
+// Size of the staging area for host-resident rays in the no-allocation query.
+constexpr uint64_t kNoAllocStagingBytes = 32ull << 20;
+
+// Closest-hit query whose scratch (fetch counter, error flags, staging for
+// host rays) is a static device array: it allocates no memory.  `rays` is
+// device-accessible memory when rays_on_device, else host memory whose span
+// must fit in kNoAllocStagingBytes.  Synchronises `st`; *err_flags receives
+// the kernel's kErr* bits.
+cudaError_t noalloc_closest(const DeviceBVH& bvh, char* rays, bool rays_on_device, uint32_t M, uint64_t stride,
+                            cudaStream_t st, uint32_t* err_flags);
+
 }  // namespace gb

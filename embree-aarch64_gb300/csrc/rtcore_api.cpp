@@ -1131,6 +1131,34 @@ RTC_API unsigned int rtcgbGetSceneBVH(RTCScene hs, void* nodes, unsigned int max
   return 0;
 }
 
+RTC_API void rtcgbIntersect1MNoAlloc(RTCScene hs, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride,
+                                     void* cuda_stream) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  if (M == 0) return;
+  if (!rayhit) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  if (((size_t)rayhit & 0x3) || (byteStride & 0x3)) fail(RTC_ERROR_INVALID_ARGUMENT, "ray not aligned to 4 bytes");
+  if (byteStride < sizeof(RTCRayHit)) fail(RTC_ERROR_INVALID_ARGUMENT, "byteStride smaller than the ray record");
+  if (s->bvh.num_nodes == 0) return;
+  s->device->set_current();
+  const bool on_device = is_device_pointer(rayhit);
+  const size_t span = (size_t)(M - 1) * byteStride + sizeof(RTCRayHit);
+  if (!on_device && span > gb::kNoAllocStagingBytes)
+    fail(RTC_ERROR_INVALID_ARGUMENT,
+         "rtcgbIntersect1MNoAlloc: host rays span more than its 32 MiB staging area; pass device memory or "
+         "split the stream");
+  uint32_t flags = 0;
+  cuda_ok(gb::noalloc_closest(s->bvh, (char*)rayhit, on_device, M, byteStride, (cudaStream_t)cuda_stream, &flags),
+          "rtcgbIntersect1MNoAlloc");
+  gb::note_launches(2);  // memset + traversal
+  if (flags & gb::kErrStackOverflow) fail(RTC_ERROR_UNKNOWN, "traversal stack overflow");
+  if (flags & gb::kErrIterationLimit) fail(RTC_ERROR_UNKNOWN, "traversal iteration limit reached");
+  if (flags & gb::kErrBuild) fail(RTC_ERROR_UNKNOWN, "traversal found an invalid BVH reference");
+  API_END(s ? s->device : nullptr)
+}
+
 RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, unsigned int n) {
   if (n == 0) return 0;
   if (!keys || !values) return 1;

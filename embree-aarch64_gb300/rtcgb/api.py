@@ -35,7 +35,7 @@ rtcRetainScene rtcReleaseScene rtcAttachGeometry rtcAttachGeometryByID rtcDetach
 rtcCommitScene rtcJoinCommitScene rtcSetSceneProgressMonitorFunction rtcSetSceneBuildQuality rtcSetSceneFlags
 rtcGetSceneFlags rtcGetSceneBounds rtcGetSceneLinearBounds rtcIntersect1 rtcIntersect1M rtcIntersect1Mp
 rtcOccluded1 rtcOccluded1M rtcOccluded1Mp rtcgbGetSceneBuildStats rtcgbGetLastQueryStats rtcgbSetQueryCounting
-rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs""".split()
+rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs rtcgbIntersect1MNoAlloc""".split()
 
 
 class RTCBounds(ctypes.Structure):
@@ -118,6 +118,7 @@ def load(build=True):
         "rtcgbSetThreadStream": (None, [vp]),
         "rtcgbGetSceneBVH": (u, [vp, vp, u, vp, u, ctypes.POINTER(u)]),
         "rtcgbRadixSortPairs": (i, [vp, vp, u]),
+        "rtcgbIntersect1MNoAlloc": (None, [vp, vp, u, sz, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

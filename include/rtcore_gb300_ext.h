@@ -63,4 +63,24 @@ RTC_API unsigned int rtcgbGetSceneBVH(RTCScene scene, void* nodes, unsigned int 
    success. */
 RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, unsigned int n);
 
+/* Closest-hit query that allocates no memory.  No counterpart in the
+   reference.  For callers that cannot call cudaMalloc during a query: a
+   process whose device memory is already reserved by its own allocator, a
+   real-time loop that cannot afford cudaMalloc's implicit synchronisation, a
+   service held to a fixed memory budget.  Same semantics as rtcIntersect1M
+   on `cuda_stream` (NULL: the default stream; synchronised before return),
+   but all scratch lives in a static device array that each GPU loading the
+   library holds until exit: 256 bytes of query state plus
+   RTCGB_NOALLOC_STAGING_BYTES (32 MiB) for staging host-resident rays.  Rays
+   in device memory are traced in place at any size; host rays whose span
+   ((M-1)*byteStride + 80 bytes) exceeds the staging area are rejected with
+   RTC_ERROR_INVALID_ARGUMENT.  The array's device address is looked up on
+   the first call on each device, so make that first call before any stream
+   capture.  All calls share the array and it keeps the last call's contents:
+   each call clears the state it needs, and calls whose GPU work overlaps
+   (different streams or host threads at the same time) race on it. */
+#define RTCGB_NOALLOC_STAGING_BYTES 33554432u
+RTC_API void rtcgbIntersect1MNoAlloc(RTCScene scene, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride,
+                                     void* cuda_stream);
+
 #endif
