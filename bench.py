@@ -312,7 +312,9 @@ def run_gpu(args, rank, world):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_s = float(t.item())
         e2e = {"value": world * nrays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(q["h2d_bytes"]),
-               "d2h_bytes_per_step": int(q["d2h_bytes"]), "ms_per_step": e2e_s * 1e3}
+               "d2h_bytes_per_step": int(q["d2h_bytes"]), "ms_per_step": e2e_s * 1e3,
+               "host_buffer": "pinned", "host_access": int(api.load().rtcgbGetDeviceHostAccess(dev.h)),
+               "path": "rtcIntersect1M on host memory (" + (args.config or "gpu.host_rays default") + ")"}
 
     line = None
     if rank == 0:

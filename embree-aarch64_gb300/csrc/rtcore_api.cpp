@@ -79,6 +79,14 @@ struct Device : RefCounted {
   int benchmark = 0;
   int cuda_device = -1;
   gb::BuildOptions build_opt;
+  // host-resident rays: 0 copy all / trace / copy back, 1 chunked 3-stream
+  // pipeline, 2 direct (the kernel reads and writes host memory itself where
+  // the device can address it, else the pipeline).  Direct is the default: on
+  // GB300 the kernel reaches host memory over NVLink-C2C at the pace it
+  // consumes rays, so no copy phase is exposed.
+  int host_mode = 2;
+  int pageable_access = 0;     // cudaDevAttrPageableMemoryAccess
+  int host_ptr_registered = 0; // cudaDevAttrCanUseHostPointerForRegisteredMem
   std::mutex mtx;
 
   explicit Device(const char* cfg) {
@@ -87,10 +95,13 @@ struct Device : RefCounted {
     int n = 0;
     cuda_ok(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
     if (cuda_device >= n) fail(RTC_ERROR_INVALID_ARGUMENT, "gpu.device out of range");
+    cudaDeviceGetAttribute(&pageable_access, cudaDevAttrPageableMemoryAccess, cuda_device);
+    cudaDeviceGetAttribute(&host_ptr_registered, cudaDevAttrCanUseHostPointerForRegisteredMem, cuda_device);
+    cudaGetLastError();
   }
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
-  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton; the CPU tasking and ISA keys
+  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.host_rays; the CPU tasking and ISA keys
   // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
   void parse(const char* cfg) {
     std::string s(cfg);
@@ -111,6 +122,7 @@ struct Device : RefCounted {
         else if (k == "gpu.device") cuda_device = atoi(v.c_str());
         else if (k == "gpu.leaf_max") build_opt.leaf_max = atoi(v.c_str());
         else if (k == "gpu.morton") build_opt.morton_cube = (v == "cube");
+        else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
       }
       i = j + 1;
     }
@@ -203,14 +215,19 @@ struct View {
   }
 };
 
-bool is_device_pointer(const void* p) {
-  if (!p) return false;
+cudaMemoryType pointer_type(const void* p) {
+  if (!p) return cudaMemoryTypeUnregistered;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return cudaMemoryTypeUnregistered;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  return a.type;
+}
+
+bool is_device_pointer(const void* p) {
+  const cudaMemoryType t = pointer_type(p);
+  return t == cudaMemoryTypeDevice || t == cudaMemoryTypeManaged;
 }
 
 struct Geometry : RefCounted {
@@ -302,6 +319,9 @@ struct ThreadCtx {
   unsigned int* dscratch = nullptr;     // [0] ray counter, [1] error flags, [2..] counters
   unsigned int* hscratch = nullptr;     // pinned mirror
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+  static constexpr int kMaxChunks = 32;
+  cudaStream_t s_in = nullptr, s_out = nullptr;     // copy streams of the pipeline
+  cudaEvent_t ev_in[kMaxChunks] = {}, ev_tr[kMaxChunks] = {};
   bool counting = false;
   RTCGBQueryStats last{};
   int device = -1;
@@ -321,6 +341,15 @@ struct ThreadCtx {
     cuda_ok(cudaEventCreate(&e2), "event");
     cuda_ok(cudaEventCreate(&e3), "event");
   }
+  void ensure_pipeline() {
+    if (s_in) return;
+    cuda_ok(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_ok(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (int i = 0; i < kMaxChunks; i++) {
+      cuda_ok(cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming), "event");
+      cuda_ok(cudaEventCreateWithFlags(&ev_tr[i], cudaEventDisableTiming), "event");
+    }
+  }
   char* buffer(size_t bytes) {
     if (bytes > cap) {
       if (dbuf) cudaFree(dbuf);
@@ -337,8 +366,14 @@ struct ThreadCtx {
     if (dscratch) cudaFree(dscratch);
     if (hscratch) cudaFreeHost(hscratch);
     if (own) cudaStreamDestroy(own);
+    if (s_in) cudaStreamDestroy(s_in);
+    if (s_out) cudaStreamDestroy(s_out);
     for (cudaEvent_t e : {e0, e1, e2, e3})
       if (e) cudaEventDestroy(e);
+    for (int i = 0; i < kMaxChunks; i++) {
+      if (ev_in[i]) cudaEventDestroy(ev_in[i]);
+      if (ev_tr[i]) cudaEventDestroy(ev_tr[i]);
+    }
   }
 };
 
@@ -460,39 +495,90 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   c.last = RTCGBQueryStats{};
   const gb::DeviceBVH& bvh = scene->bvh;
   if (bvh.num_nodes == 0) return;  // empty scene: nothing is hit
-  scene->device->set_current();
-  c.ensure(scene->device->cuda_device);
+  Device* dev = scene->device;
+  dev->set_current();
+  c.ensure(dev->cuda_device);
   cudaStream_t st = c.stream();
   const size_t span = (size_t)(M - 1) * stride + recsize;
-  const bool on_device = is_device_pointer(rays);
-  char* d_rays = (char*)rays;
-  cuda_ok(cudaEventRecord(c.e0, st), "event");
-  if (!on_device) {
-    d_rays = c.buffer(span);
-    cuda_ok(cudaMemcpyAsync(d_rays, rays, span, cudaMemcpyHostToDevice, st), "H2D rays");
-    c.last.h2d_bytes = span;
-  }
-  cuda_ok(cudaMemsetAsync(c.dscratch, 0, 64, st), "memset");
+  const cudaMemoryType mt = pointer_type(rays);
+  const bool on_device = mt == cudaMemoryTypeDevice || mt == cudaMemoryTypeManaged;
+  // host memory the kernel may address directly (NVLink-C2C / ATS)
+  const bool direct = !on_device && dev->host_mode == 2 &&
+                      ((mt == cudaMemoryTypeHost && dev->host_ptr_registered) ||
+                       (mt == cudaMemoryTypeUnregistered && dev->pageable_access));
   gb::TraceParams P{};
   P.nodes = bvh.nodes;
   P.tris = bvh.tris;
-  P.rays = d_rays;
   P.stride = stride;
-  P.nrays = M;
   P.ray_counter = c.dscratch;
   P.err = c.dscratch + 1;
   P.counters = reinterpret_cast<gb::TraceCounters*>(c.dscratch + 2);
   P.max_iters = 4 * bvh.num_nodes + 64;  // node visits, triangle phases and pops per ray
   P.num_nodes = bvh.num_nodes;
   P.num_tris = bvh.num_tris;
-  cuda_ok(cudaEventRecord(c.e1, st), "event");
-  cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
-  gb::note_launches(2);  // memset + traversal
-  cuda_ok(cudaEventRecord(c.e2, st), "event");
-  if (!on_device) {
+  cuda_ok(cudaEventRecord(c.e0, st), "event");
+  cuda_ok(cudaMemsetAsync(c.dscratch, 0, 64, st), "memset");
+  unsigned launches = 1;
+  const uint32_t kChunk = 1u << 21;  // rays per pipeline stage
+  if (on_device || direct) {
+    P.rays = (char*)rays;
+    P.nrays = M;
+    cuda_ok(cudaEventRecord(c.e1, st), "event");
+    cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
+    launches++;
+    cuda_ok(cudaEventRecord(c.e2, st), "event");
+    if (direct) {
+      c.last.h2d_bytes = (unsigned long long)M * 48;                     // ray records read by the kernel
+      c.last.d2h_bytes = (unsigned long long)M * (anyhit ? 4 : 36);      // at most tfar (+ hit) written
+    }
+  } else if (dev->host_mode >= 1 && M > kChunk) {
+    // chunked pipeline: H2D of chunk i+1 and D2H of chunk i-1 overlap the trace of chunk i
+    c.ensure_pipeline();
+    char* d_rays = c.buffer(span);
+    const uint32_t nchunks = std::min<uint32_t>((M + kChunk - 1) / kChunk, ThreadCtx::kMaxChunks);
+    const uint32_t per = (M + nchunks - 1) / nchunks;
+    cuda_ok(cudaEventRecord(c.e3, st), "event");
+    cuda_ok(cudaStreamWaitEvent(c.s_in, c.e3, 0), "wait");
+    for (uint32_t i = 0; i < nchunks; i++) {
+      const uint32_t first = i * per, n = std::min(per, M - first);
+      const size_t off = (size_t)first * stride, bytes = (size_t)(n - 1) * stride + recsize;
+      cuda_ok(cudaMemcpyAsync(d_rays + off, (char*)rays + off, bytes, cudaMemcpyHostToDevice, c.s_in), "H2D rays");
+      cuda_ok(cudaEventRecord(c.ev_in[i], c.s_in), "event");
+    }
+    cuda_ok(cudaEventRecord(c.e1, st), "event");
+    for (uint32_t i = 0; i < nchunks; i++) {
+      const uint32_t first = i * per, n = std::min(per, M - first);
+      const size_t off = (size_t)first * stride, bytes = (size_t)(n - 1) * stride + recsize;
+      cuda_ok(cudaStreamWaitEvent(st, c.ev_in[i], 0), "wait");
+      cuda_ok(cudaMemsetAsync(c.dscratch, 0, sizeof(unsigned int), st), "memset");  // fetch counter only
+      gb::TraceParams Pi = P;
+      Pi.rays = d_rays + off;
+      Pi.nrays = n;
+      cuda_ok(gb::launch_trace(Pi, anyhit, c.counting, st), "traversal launch");
+      launches += 2;
+      cuda_ok(cudaEventRecord(c.ev_tr[i], st), "event");
+      cuda_ok(cudaStreamWaitEvent(c.s_out, c.ev_tr[i], 0), "wait");
+      cuda_ok(cudaMemcpyAsync((char*)rays + off, d_rays + off, bytes, cudaMemcpyDeviceToHost, c.s_out), "D2H rays");
+    }
+    cuda_ok(cudaEventRecord(c.e2, st), "event");
+    cuda_ok(cudaEventRecord(c.e3, c.s_out), "event");
+    cuda_ok(cudaStreamWaitEvent(st, c.e3, 0), "wait");
+    c.last.h2d_bytes = span;
+    c.last.d2h_bytes = span;
+  } else {
+    char* d_rays = c.buffer(span);
+    cuda_ok(cudaMemcpyAsync(d_rays, rays, span, cudaMemcpyHostToDevice, st), "H2D rays");
+    P.rays = d_rays;
+    P.nrays = M;
+    cuda_ok(cudaEventRecord(c.e1, st), "event");
+    cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
+    launches++;
+    cuda_ok(cudaEventRecord(c.e2, st), "event");
     cuda_ok(cudaMemcpyAsync(rays, d_rays, span, cudaMemcpyDeviceToHost, st), "D2H rays");
+    c.last.h2d_bytes = span;
     c.last.d2h_bytes = span;
   }
+  gb::note_launches(launches);
   cuda_ok(cudaMemcpyAsync(c.hscratch, c.dscratch, 64, cudaMemcpyDeviceToHost, st), "D2H status");
   cuda_ok(cudaEventRecord(c.e3, st), "event");
   cuda_ok(cudaStreamSynchronize(st), "traversal");
@@ -1157,6 +1243,12 @@ RTC_API void rtcgbIntersect1MNoAlloc(RTCScene hs, struct RTCRayHit* rayhit, unsi
   if (flags & gb::kErrIterationLimit) fail(RTC_ERROR_UNKNOWN, "traversal iteration limit reached");
   if (flags & gb::kErrBuild) fail(RTC_ERROR_UNKNOWN, "traversal found an invalid BVH reference");
   API_END(s ? s->device : nullptr)
+}
+
+RTC_API int rtcgbGetDeviceHostAccess(RTCDevice hdevice) {
+  Device* d = (Device*)hdevice;
+  if (!d) return -1;
+  return (d->pageable_access ? 1 : 0) | (d->host_ptr_registered ? 2 : 0);
 }
 
 RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, unsigned int n) {

@@ -35,7 +35,7 @@ rtcRetainScene rtcReleaseScene rtcAttachGeometry rtcAttachGeometryByID rtcDetach
 rtcCommitScene rtcJoinCommitScene rtcSetSceneProgressMonitorFunction rtcSetSceneBuildQuality rtcSetSceneFlags
 rtcGetSceneFlags rtcGetSceneBounds rtcGetSceneLinearBounds rtcIntersect1 rtcIntersect1M rtcIntersect1Mp
 rtcOccluded1 rtcOccluded1M rtcOccluded1Mp rtcgbGetSceneBuildStats rtcgbGetLastQueryStats rtcgbSetQueryCounting
-rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs rtcgbIntersect1MNoAlloc""".split()
+rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs rtcgbIntersect1MNoAlloc rtcgbGetDeviceHostAccess""".split()
 
 
 class RTCBounds(ctypes.Structure):
@@ -119,6 +119,7 @@ def load(build=True):
         "rtcgbGetSceneBVH": (u, [vp, vp, u, vp, u, ctypes.POINTER(u)]),
         "rtcgbRadixSortPairs": (i, [vp, vp, u]),
         "rtcgbIntersect1MNoAlloc": (None, [vp, vp, u, sz, vp]),
+        "rtcgbGetDeviceHostAccess": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -57,6 +57,15 @@ RTC_API void rtcgbSetThreadStream(void* cuda_stream);
 RTC_API unsigned int rtcgbGetSceneBVH(RTCScene scene, void* nodes, unsigned int max_nodes, void* tris,
                                       unsigned int max_tris, unsigned int* num_tris);
 
+/* Host-memory access of the device: bit 0 set when kernels can address
+   pageable host memory (cudaDevAttrPageableMemoryAccess), bit 1 when they can
+   use host pointers of pinned / registered memory directly.  With the device
+   config key gpu.host_rays=direct (default), queries on such host rays are
+   traced in place (other host rays use the pipeline); gpu.host_rays=pipeline
+   overlaps chunked copies with the traversal; gpu.host_rays=copy copies all
+   rays, traces, and copies back. */
+RTC_API int rtcgbGetDeviceHostAccess(RTCDevice device);
+
 /* Sorts n (key, value) pairs (host arrays, in place) with the builder's
    stable LSD radix sort on the GPU.  The result equals a stable host sort by
    key; exposed so that property can be tested directly.  Returns 0 on

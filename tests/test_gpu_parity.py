@@ -276,3 +276,42 @@ def test_radix_sort_bit_exact_vs_host_stable_sort(rtc):
         order = np.argsort(keys, kind="stable")
         assert np.array_equal(k, keys[order])
         assert np.array_equal(v, vals[order])
+
+
+@pytest.mark.parametrize("mode", ["copy", "pipeline", "direct"])
+def test_host_ray_modes(rtc, mode):
+    """Host-resident rays through each host path (copy all, chunked copy/trace
+    pipeline, direct access where the device can address host memory) give
+    the bytes of tracing the same rays in device memory, for pageable and
+    pinned host buffers."""
+    torch = pytest.importorskip("torch")
+    dev = rtc.Device(f"gpu.host_rays={mode}".encode())
+    access = rtc.load().rtcgbGetDeviceHostAccess(dev.h)
+    verts, idx = W.gaussian_soup(50_000, seed=41)
+    rays = W.sphere_rays(2_500_000, seed=42)        # more than one 2M-ray pipeline chunk
+    sc = rtc.Scene(dev)
+    sc.add_mesh(verts, idx)
+    sc.commit()
+    t = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    sc.intersect_ptr(t.data_ptr(), rays.shape[0], 80)
+    ref = t.cpu().numpy().view(R.RAYHIT_DTYPE)
+    pageable = rays.copy()
+    sc.intersect(pageable)
+    assert (pageable.view(np.uint8) == ref.view(np.uint8)).all()
+    pinned = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory()
+    sc.intersect_ptr(pinned.data_ptr(), rays.shape[0], 80)
+    assert (pinned.numpy() == ref.view(np.uint8)).all()
+    st = rtc.last_query_stats()
+    if mode == "direct" and access & 2:
+        assert st["h2d_bytes"] == rays.shape[0] * 48
+    else:
+        assert st["h2d_bytes"] == rays.nbytes
+    # occlusion through the same path
+    shadow, _ = W.shadow_rays(ref, seed=43)
+    a = shadow.copy()
+    sc.occluded(a)
+    ts = torch.from_numpy(shadow.view(np.uint8).copy()).cuda()
+    sc.occluded_ptr(ts.data_ptr(), shadow.shape[0], 48)
+    assert (a.view(np.uint8) == ts.cpu().numpy()).all()
+    sc.release()
+    dev.release()
