@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--robust", action="store_true", help="RTC_SCENE_FLAG_ROBUST scene (Pluecker test)")
     ap.add_argument("--config", default="", help="extra rtcNewDevice config tokens, e.g. gpu.leaf_max=2")
     return ap.parse_args()
 
@@ -140,13 +141,13 @@ def peaks():
 # CPU arm (the oracle port of the reference path)
 # ---------------------------------------------------------------------------
 
-def cpu_rate(verts, idx, rays, budget_s, shadow=False, orc=None):
+def cpu_rate(verts, idx, rays, budget_s, shadow=False, orc=None, robust=False):
     """Mrays/s of the oracle on all host threads over a bounded sample."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle_ffi
     t0 = time.perf_counter()
     if orc is None:
-        orc = oracle_ffi.OracleScene([(0, verts, idx)])
+        orc = oracle_ffi.OracleScene([(0, verts, idx)], robust=robust)
     build_s = time.perf_counter() - t0
     cores = os.cpu_count() or 1
     n0 = min(rays.shape[0], 65536)
@@ -169,7 +170,7 @@ def run_reference(args, rank, world):
         return
     verts, idx, rays, label = workload(args.workload, args.scale)
     per = []
-    base, orc, _ = cpu_rate(verts, idx, rays, 1.0)
+    base, orc, _ = cpu_rate(verts, idx, rays, 1.0, robust=args.robust)
     for s in range(args.warmup + args.steps):
         r, orc, sample = cpu_rate(verts, idx, rays, max(1.0, args.cpu_seconds / max(1, args.steps)), orc=orc)
         if s >= args.warmup:
@@ -213,7 +214,9 @@ def run_gpu(args, rank, world):
     dev = api.Device(f"gpu.device={local}{',' + args.config if args.config else ''}".encode())
     stream = torch.cuda.current_stream()
     api.set_thread_stream(stream.cuda_stream)
-    sc = api.Scene(dev)
+    sc = api.Scene(dev, flags=api.RTC_SCENE_FLAG_ROBUST if args.robust else 0)
+    if args.robust:
+        label += " (robust scene: Pluecker test)"
     sc.add_mesh(verts, idx)
     t = time.perf_counter()
     sc.commit()
@@ -346,7 +349,7 @@ def run_gpu(args, rank, world):
         }
 
     if rank == 0 and not args.no_cpu:
-        base, orc, sample = cpu_rate(verts, idx, rays, args.cpu_seconds)
+        base, orc, sample = cpu_rate(verts, idx, rays, args.cpu_seconds, robust=args.robust)
         st = orc.stats()
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["build"]["sah_reference_builder"] = st.sah

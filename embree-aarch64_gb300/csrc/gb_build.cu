@@ -630,6 +630,7 @@ struct BinTree {
   const uint32_t* cnt;
   uint32_t nleaves;
   uint32_t leaf_max;  // subtrees of at most this many triangles may become leaves
+  uint32_t robust;    // write raw vertices into triangle records
 };
 
 __device__ __forceinline__ bool bt_leaf(const BinTree& t, uint32_t k) { return k < t.nleaves; }
@@ -717,15 +718,16 @@ __device__ __forceinline__ uint32_t exp_for(float ext) {
 }
 
 __device__ __forceinline__ void write_tri(const GeomDesc* __restrict__ geoms, const float4* __restrict__ plo,
-                                          const float4* __restrict__ phi, uint32_t prim, TriRecord* dst) {
+                                          const float4* __restrict__ phi, uint32_t prim, TriRecord* dst, bool robust) {
   const uint32_t gs = __float_as_uint(plo[prim].w);
   const uint32_t j = __float_as_uint(phi[prim].w);
   const GeomDesc g = geoms[gs];
   const uint3 t = load_tri(g, j);
   const float3 p0 = load_vtx(g, t.x), p1 = load_vtx(g, t.y), p2 = load_vtx(g, t.z);
-  // Triangle4: e1 = v0 - v1, e2 = v2 - v0 (triangle.h:40-41)
-  const float3 e1 = make_float3(__fsub_rn(p0.x, p1.x), __fsub_rn(p0.y, p1.y), __fsub_rn(p0.z, p1.z));
-  const float3 e2 = make_float3(__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z));
+  // Triangle4: e1 = v0 - v1, e2 = v2 - v0 (triangle.h:40-41); Triangle4v of
+  // robust scenes keeps v1 and v2 themselves (trianglev.h:93-115)
+  const float3 e1 = robust ? p1 : make_float3(__fsub_rn(p0.x, p1.x), __fsub_rn(p0.y, p1.y), __fsub_rn(p0.z, p1.z));
+  const float3 e2 = robust ? p2 : make_float3(__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z));
   dst->a = make_float4(p0.x, p0.y, p0.z, __uint_as_float(j));
   dst->b = make_float4(e1.x, e1.y, e1.z, __uint_as_float(g.geomID));
   dst->c = make_float4(e2.x, e2.y, e2.z, 0.f);
@@ -852,7 +854,7 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
             atomicOr(err, kErrBuild);
             return;
           }
-          write_tri(geoms, plo, phi, bt_right(t, x), &tris[node.tri_base + tri_off + w]);
+          write_tri(geoms, plo, phi, bt_right(t, x), &tris[node.tri_base + tri_off + w], t.robust != 0);
           w++;
         } else {
           if (sp + 2 > 8) {
@@ -1033,7 +1035,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   cudaFreeAsync(nn, st); cudaFreeAsync(bsurv, st); cudaFreeAsync(bmerge, st);
 
   // ---- collapse, level by level (breadth-first node order)
-  BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(opt.leaf_max, 1), kLeafMaxLimit)};
+  BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(opt.leaf_max, 1), kLeafMaxLimit),
+             (uint32_t)(opt.robust != 0)};
   WideNode* wnodes = nullptr;
   TriRecord* wtris = nullptr;
   const uint32_t maxw = N;  // wide internal nodes <= binary internal nodes + 1
@@ -1091,6 +1094,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   out->num_nodes = num_nodes;
   out->num_tris = N;
   out->depth = depth;
+  out->robust = opt.robust != 0;
 
   cudaFreeAsync(wnodes, st); cudaFreeAsync(wtris, st);
   cudaFreeAsync(items_a, st); cudaFreeAsync(items_b, st); cudaFreeAsync(kids, st);

@@ -41,7 +41,9 @@ struct alignas(16) WideNode {
 };
 static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
 
-// 48-byte triangle record: (v0.xyz, primID), (e1.xyz, geomID), (e2.xyz, pad).
+// 48-byte triangle record: (v0.xyz, primID), (e1.xyz, geomID), (e2.xyz, pad);
+// in robust scenes (v0.xyz, primID), (v1.xyz, geomID), (v2.xyz, pad), the
+// reference's Triangle4v values (kernels/geometry/trianglev.h:93-115).
 struct alignas(16) TriRecord {
   float4 a;
   float4 b;
@@ -68,6 +70,7 @@ struct DeviceBVH {
   uint32_t num_nodes = 0;
   uint32_t num_tris = 0;     // valid primitives in the BVH
   uint32_t depth = 0;        // wide levels
+  int robust = 0;            // triangle records hold (v0, v1, v2) for the Pluecker test
   float lo[3] = {0, 0, 0};   // geometry bounds (empty scene: +inf / -inf)
   float hi[3] = {0, 0, 0};
 };
@@ -76,6 +79,7 @@ struct DeviceBVH {
 struct BuildOptions {
   int leaf_max = kLeafMaxDefault;
   int morton_cube = 0;  // 1: one Morton scale for all axes (gpu.morton=cube)
+  int robust = 0;       // RTC_SCENE_FLAG_ROBUST: triangle records hold v0, v1, v2
 };
 
 // Build statistics reported through the extension API.

@@ -55,6 +55,51 @@ __device__ __forceinline__ bool moeller(const float3 v0, const float3 e1, const 
   return (__fmul_rn(absDen, tnear) < T) & (T <= __fmul_rn(absDen, tfar));
 }
 
+// stable_triangle_normal (common/math/vec3.h:210-222): per component the
+// cross product of (a,b) or (b,c) whose cancelling product is smaller.
+__device__ __forceinline__ float3 stable_normal(const float3 a, const float3 b, const float3 c) {
+  const float ab_x = __fmul_rn(a.z, b.y), ab_y = __fmul_rn(a.x, b.z), ab_z = __fmul_rn(a.y, b.x);
+  const float bc_x = __fmul_rn(b.z, c.y), bc_y = __fmul_rn(b.x, c.z), bc_z = __fmul_rn(b.y, c.x);
+  const float3 cab = make_float3(__fmaf_rn(a.y, b.z, -ab_x), __fmaf_rn(a.z, b.x, -ab_y), __fmaf_rn(a.x, b.y, -ab_z));
+  const float3 cbc = make_float3(__fmaf_rn(b.y, c.z, -bc_x), __fmaf_rn(b.z, c.x, -bc_y), __fmaf_rn(b.x, c.y, -bc_z));
+  return make_float3(fabsf(ab_x) < fabsf(bc_x) ? cab.x : cbc.x, fabsf(ab_y) < fabsf(bc_y) ? cab.y : cbc.y,
+                     fabsf(ab_z) < fabsf(bc_z) ? cab.z : cbc.z);
+}
+
+__device__ __forceinline__ float3 f3sub(const float3 a, const float3 b) {
+  return make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 f3add(const float3 a, const float3 b) {
+  return make_float3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+
+// Pluecker test of robust scenes (triangle_intersector_pluecker.h:60-111):
+// vertices relative to the origin, edge functions U,V,W accepted within
+// ulp*|U+V+W| of zero, t = rcp(2 Ng.D) * 2 v0.Ng inside [tnear, tfar].
+__device__ __forceinline__ bool pluecker(const float3 tv0, const float3 tv1, const float3 tv2, const float3 O,
+                                         const float3 D, const float tnear, const float tfar, float& U, float& V,
+                                         float& UVW, float& t) {
+  const float3 v0 = f3sub(tv0, O), v1 = f3sub(tv1, O), v2 = f3sub(tv2, O);
+  const float3 e0 = f3sub(v2, v0), e1 = f3sub(v0, v1), e2 = f3sub(v1, v2);
+  U = dot3(cross3(e0, f3add(v2, v0)), D);
+  V = dot3(cross3(e1, f3add(v0, v1)), D);
+  const float W = dot3(cross3(e2, f3add(v1, v2)), D);
+  UVW = __fadd_rn(__fadd_rn(U, V), W);
+  const float eps = __fmul_rn(1.1920928955078125e-07f, fabsf(UVW));
+  if (!((fminf(fminf(U, V), W) >= -eps) | (fmaxf(fmaxf(U, V), W) <= eps))) return false;
+  const float3 Ng = stable_normal(e0, e1, e2);
+  const float dd = dot3(Ng, D), den = __fadd_rn(dd, dd);
+  const float tt = dot3(v0, Ng), T = __fadd_rn(tt, tt);
+  t = __fmul_rn(__frcp_rn(den), T);
+  return (tnear <= t) & (t <= tfar) & (den != 0.0f);
+}
+
+// Geometric normal of a robust-scene hit, as the test computed it.
+__device__ __forceinline__ float3 pluecker_normal(const float3 tv0, const float3 tv1, const float3 tv2, const float3 O) {
+  const float3 v0 = f3sub(tv0, O), v1 = f3sub(tv1, O), v2 = f3sub(tv2, O);
+  return stable_normal(f3sub(v2, v0), f3sub(v0, v1), f3sub(v1, v2));
+}
+
 struct TRay {
   float3 org, dir, rdir;
   float tnear;     // raw ray tnear (triangle test)
@@ -188,7 +233,7 @@ __device__ __forceinline__ void load_ray(const char* p, TRay& r, float& tfar) {
 // (2) tests its pending triangles -- unless few lanes of the warp have
 // triangle work, in which case the group is pushed and tested later -- and
 // (3) pops the stack when its group is exhausted.
-template <bool ANYHIT, bool COUNT, bool ALIGNED>
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST>
 __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
   const Ctx c{P.nodes, P.tris, P.err, P.max_iters, P.num_nodes, P.num_tris};
   const int lane = threadIdx.x & 31;
@@ -277,15 +322,29 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
       const float4* tp = reinterpret_cast<const float4*>(c.tris + ti);
       const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
       if (COUNT) n_tris++;
-      float U, V, T, absDen;
-      if (moeller(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org, r.dir,
-                  r.tnear, t_best, U, V, T, absDen)) {
-        hit_tri = ti;
-        if (ANYHIT) { done = true; t_bits = 0; break; }
-        const float rcp = __frcp_rn(absDen);
-        t_best = __fmul_rn(T, rcp);
-        hu = __fmul_rn(U, rcp);
-        hv = __fmul_rn(V, rcp);
+      if (ROBUST) {
+        float U, V, UVW, t;
+        if (pluecker(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org,
+                     r.dir, r.tnear, t_best, U, V, UVW, t)) {
+          hit_tri = ti;
+          if (ANYHIT) { done = true; t_bits = 0; break; }
+          // PlueckerHitM::finalize: u,v = U,V * rcp(UVW), 0 when |UVW| < 1e-18
+          const float rcp = fabsf(UVW) < kMinRcpInput ? 0.0f : __frcp_rn(UVW);
+          t_best = t;
+          hu = __fmul_rn(U, rcp);
+          hv = __fmul_rn(V, rcp);
+        }
+      } else {
+        float U, V, T, absDen;
+        if (moeller(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org, r.dir,
+                    r.tnear, t_best, U, V, T, absDen)) {
+          hit_tri = ti;
+          if (ANYHIT) { done = true; t_bits = 0; break; }
+          const float rcp = __frcp_rn(absDen);
+          t_best = __fmul_rn(T, rcp);
+          hu = __fmul_rn(U, rcp);
+          hv = __fmul_rn(V, rcp);
+        }
       }
     }
     // ---- (3) next group from the stack, or finish
@@ -306,7 +365,9 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
         } else {
           const float4* tp = reinterpret_cast<const float4*>(c.tris + hit_tri);
           const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
-          const float3 Ng = cross3(make_float3(d.x, d.y, d.z), make_float3(b.x, b.y, b.z));
+          const float3 Ng = ROBUST ? pluecker_normal(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
+                                                     make_float3(d.x, d.y, d.z), r.org)
+                                   : cross3(make_float3(d.x, d.y, d.z), make_float3(b.x, b.y, b.z));
           *reinterpret_cast<float*>(rec + 32) = t_best;
           if (ALIGNED) {
             *reinterpret_cast<float4*>(rec + 48) = make_float4(Ng.x, Ng.y, Ng.z, hu);
@@ -337,32 +398,35 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
   }
 }
 
-template <bool ANYHIT, bool COUNT, bool ALIGNED>
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST>
 static cudaError_t launch_one(const TraceParams& P, cudaStream_t st) {
   static int blocks_per_sm = -1, num_sms = 0;
   if (blocks_per_sm < 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED>, TRACE_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED, ROBUST>,
+                                                  TRACE_THREADS, 0);
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
   uint64_t want = ((uint64_t)P.nrays + TRACE_THREADS - 1) / TRACE_THREADS;
   uint64_t grid = (uint64_t)num_sms * blocks_per_sm;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
-  k_trace<ANYHIT, COUNT, ALIGNED><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
+  k_trace<ANYHIT, COUNT, ALIGNED, ROBUST><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
   return cudaGetLastError();
+}
+
+template <bool ANYHIT, bool COUNT>
+static cudaError_t launch_variant(const TraceParams& P, bool aligned, cudaStream_t st) {
+  if (P.robust) return aligned ? launch_one<ANYHIT, COUNT, true, true>(P, st) : launch_one<ANYHIT, COUNT, false, true>(P, st);
+  return aligned ? launch_one<ANYHIT, COUNT, true, false>(P, st) : launch_one<ANYHIT, COUNT, false, false>(P, st);
 }
 
 cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStream_t st) {
   const bool aligned = ((uintptr_t)P.rays % 16 == 0) && (P.stride % 16 == 0);
-  if (anyhit) {
-    if (count) return aligned ? launch_one<true, true, true>(P, st) : launch_one<true, true, false>(P, st);
-    return aligned ? launch_one<true, false, true>(P, st) : launch_one<true, false, false>(P, st);
-  }
-  if (count) return aligned ? launch_one<false, true, true>(P, st) : launch_one<false, true, false>(P, st);
-  return aligned ? launch_one<false, false, true>(P, st) : launch_one<false, false, false>(P, st);
+  if (anyhit) return count ? launch_variant<true, true>(P, aligned, st) : launch_variant<true, false>(P, aligned, st);
+  return count ? launch_variant<false, true>(P, aligned, st) : launch_variant<false, false>(P, aligned, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -434,6 +498,7 @@ cudaError_t noalloc_closest(const DeviceBVH& bvh, char* rays, bool rays_on_devic
   P.max_iters = 4 * bvh.num_nodes + 64;
   P.num_nodes = bvh.num_nodes;
   P.num_tris = bvh.num_tris;
+  P.robust = bvh.robust;
   if ((e = launch_trace(P, false, false, st)) != cudaSuccess) return e;
   if (!rays_on_device && (e = cudaMemcpyAsync(rays, staging, span, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     return e;

@@ -16,6 +16,7 @@ struct TraceParams {
   uint32_t max_iters;         // per-ray loop bound
   uint32_t num_nodes;         // bounds of the node and triangle arrays
   uint32_t num_tris;
+  int robust;                 // Pluecker test on (v0, v1, v2) records
 };
 
 // Launches the persistent closest-hit (anyhit = false) or any-hit kernel.

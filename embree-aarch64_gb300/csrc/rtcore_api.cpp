@@ -467,7 +467,9 @@ struct Scene : RefCounted {
     gb::free_bvh(&bvh);
     committed = false;
     gb::BuildStats bs;
-    cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, device->build_opt, &bvh, &bs), "rtcCommitScene");
+    gb::BuildOptions opt = device->build_opt;
+    opt.robust = (flags & RTC_SCENE_FLAG_ROBUST) != 0;  // scene.cpp:119-125: Triangle4v + Pluecker
+    cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, opt, &bvh, &bs), "rtcCommitScene");
     stats = bs;
     committed = true;
     if (progress) progress(progress_ptr, 1.0);
@@ -516,6 +518,7 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   P.max_iters = 4 * bvh.num_nodes + 64;  // node visits, triangle phases and pops per ray
   P.num_nodes = bvh.num_nodes;
   P.num_tris = bvh.num_tris;
+  P.robust = bvh.robust;
   cuda_ok(cudaEventRecord(c.e0, st), "event");
   cuda_ok(cudaMemsetAsync(c.dscratch, 0, 64, st), "memset");
   unsigned launches = 1;

@@ -19,6 +19,7 @@ RTC_BUFFER_TYPE_VERTEX = 1
 RTC_FORMAT_UINT3 = 0x5003
 RTC_FORMAT_FLOAT3 = 0x9003
 RTC_INVALID_GEOMETRY_ID = 0xFFFFFFFF
+RTC_SCENE_FLAG_ROBUST = 1 << 2
 
 ERRORS = {0: "NONE", 1: "UNKNOWN", 2: "INVALID_ARGUMENT", 3: "INVALID_OPERATION", 4: "OUT_OF_MEMORY",
           5: "UNSUPPORTED_CPU", 6: "CANCELLED"}
@@ -163,11 +164,13 @@ class Device:
 class Scene:
     """A scene of triangle meshes built with rtcCommitScene."""
 
-    def __init__(self, device):
+    def __init__(self, device, flags=0):
         self.dev = device
         self.L = device.L
         self.h = ctypes.c_void_p(self.L.rtcNewScene(device.h))
         self._keep = []
+        if flags:
+            self.L.rtcSetSceneFlags(self.h, flags)
         device.check("rtcNewScene")
 
     def add_mesh(self, verts, idx, geom_id=None):

@@ -100,6 +100,7 @@ struct OracleScene {
   uint32_t root;
   float glo[3], ghi[3];
   int committed;
+  int robust; /* RTC_SCENE_FLAG_ROBUST: Triangle4v leaves + Pluecker test */
   pthread_mutex_t lock;
 };
 
@@ -143,6 +144,11 @@ int orc_scene_add_mesh(OracleScene* s, unsigned geomID, const void* verts, size_
   for (unsigned i = 0; i < ntris; i++) memcpy(&m->idx[3 * (size_t)i], (const char*)idx + i * istride, 12);
   s->committed = 0;
   return 0;
+}
+
+void orc_scene_set_robust(OracleScene* s, int robust) {
+  s->robust = robust;
+  s->committed = 0;
 }
 
 static int cmp_mesh(const void* a, const void* b) {
@@ -386,7 +392,9 @@ static uint32_t create_leaf(OracleScene* s, const BRec* r) {
         const OMesh* m = find_mesh(s, p->geomID);
         const unsigned* tri = &m->idx[3 * (size_t)p->primID];
         v3 p0 = mesh_vertex(m, tri[0]), p1 = mesh_vertex(m, tri[1]), p2 = mesh_vertex(m, tri[2]);
-        v3 e1 = v3sub(p0, p1), e2 = v3sub(p2, p0);
+        /* Triangle4 keeps edges (triangle.h:40-41); Triangle4v of robust
+           scenes keeps the vertices (trianglev.h:93-115) in the same slots */
+        v3 e1 = s->robust ? p1 : v3sub(p0, p1), e2 = s->robust ? p2 : v3sub(p2, p0);
         t->v0[0][i] = p0.x; t->v0[1][i] = p0.y; t->v0[2][i] = p0.z;
         t->e1[0][i] = e1.x; t->e1[1][i] = e1.y; t->e1[2][i] = e1.z;
         t->e2[0][i] = e2.x; t->e2[1][i] = e2.y; t->e2[2][i] = e2.z;
@@ -628,6 +636,66 @@ static inline int moeller(v3 v0, v3 e1, v3 e2, v3 O, v3 D, float tnear, float tf
   return 1;
 }
 
+/* stable_triangle_normal  common/math/vec3.h:210-222 */
+static inline v3 stable_normal(v3 a, v3 b, v3 c) {
+  const float ab_x = a.z * b.y, ab_y = a.x * b.z, ab_z = a.y * b.x;
+  const float bc_x = b.z * c.y, bc_y = b.x * c.z, bc_z = b.y * c.x;
+  const v3 cab = {fmaf(a.y, b.z, -ab_x), fmaf(a.z, b.x, -ab_y), fmaf(a.x, b.y, -ab_z)};
+  const v3 cbc = {fmaf(b.y, c.z, -bc_x), fmaf(b.z, c.x, -bc_y), fmaf(b.x, c.y, -bc_z)};
+  v3 r;
+  r.x = fabsf(ab_x) < fabsf(bc_x) ? cab.x : cbc.x;
+  r.y = fabsf(ab_y) < fabsf(bc_y) ? cab.y : cbc.y;
+  r.z = fabsf(ab_z) < fabsf(bc_z) ? cab.z : cbc.z;
+  return r;
+}
+
+typedef struct {
+  float U, V, UVW, t;
+  v3 Ng;
+} PHit;
+
+static inline v3 v3add(v3 a, v3 b) { v3 r = {a.x + b.x, a.y + b.y, a.z + b.z}; return r; }
+static inline float fmin3(float a, float b, float c) { return fmin2(fmin2(a, b), c); }
+static inline float fmax3(float a, float b, float c) { return fmax2(fmax2(a, b), c); }
+
+/* PlueckerIntersector1::intersect  kernels/geometry/triangle_intersector_pluecker.h:60-111 */
+static inline int pluecker(v3 tv0, v3 tv1, v3 tv2, v3 O, v3 D, float tnear, float tfar, PHit* h) {
+  const v3 v0 = v3sub(tv0, O), v1 = v3sub(tv1, O), v2 = v3sub(tv2, O);
+  const v3 e0 = v3sub(v2, v0), e1 = v3sub(v0, v1), e2 = v3sub(v1, v2);
+  const float U = dot3(cross3(e0, v3add(v2, v0)), D);
+  const float V = dot3(cross3(e1, v3add(v0, v1)), D);
+  const float W = dot3(cross3(e2, v3add(v1, v2)), D);
+  const float UVW = U + V + W;
+  const float eps = FLT_EPSILON * fabsf(UVW);
+  if (!((fmin3(U, V, W) >= -eps) | (fmax3(U, V, W) <= eps))) return 0;
+  const v3 Ng = stable_normal(e0, e1, e2);
+  const float dd = dot3(Ng, D), den = dd + dd;
+  const float tt = dot3(v0, Ng), T = tt + tt;
+  const float t = (1.0f / den) * T;
+  if (!((tnear <= t) & (t <= tfar) & (den != 0.0f))) return 0;
+  h->U = U; h->V = V; h->UVW = UVW; h->t = t; h->Ng = Ng;
+  return 1;
+}
+
+/* PlueckerHitM::finalize: u,v = U,V * rcp(UVW), 0 when |UVW| < min_rcp_input */
+static inline void pluecker_uv(const PHit* h, float* u, float* v) {
+  const float r = fabsf(h->UVW) < REF_MIN_RCP_INPUT ? 0.0f : 1.0f / h->UVW;
+  *u = h->U * r;
+  *v = h->V * r;
+}
+
+int orc_pluecker1(const float v0[3], const float v1[3], const float v2[3], const float org[3], const float dir[3],
+                  float tnear, float tfar, float out_tuv[3], float out_Ng[3]) {
+  v3 a = {v0[0], v0[1], v0[2]}, b = {v1[0], v1[1], v1[2]}, c = {v2[0], v2[1], v2[2]};
+  v3 O = {org[0], org[1], org[2]}, D = {dir[0], dir[1], dir[2]};
+  PHit h;
+  if (!pluecker(a, b, c, O, D, tnear, tfar, &h)) return 0;
+  out_tuv[0] = h.t;
+  pluecker_uv(&h, &out_tuv[1], &out_tuv[2]);
+  out_Ng[0] = h.Ng.x; out_Ng[1] = h.Ng.y; out_Ng[2] = h.Ng.z;
+  return 1;
+}
+
 int orc_moeller1(const float v0[3], const float v1[3], const float v2[3], const float org[3], const float dir[3],
                  float tnear, float tfar, float out_UVTden[4], float out_tuv[3], float out_Ng[3]) {
   v3 a = {v0[0], v0[1], v0[2]}, b = {v1[0], v1[1], v1[2]}, c = {v2[0], v2[1], v2[2]};
@@ -658,7 +726,9 @@ void orc_counters(uint64_t out[3]) {
 
 typedef struct {
   v3 org, rdir, org_rdir;
+  v3 rdir_near, rdir_far;  /* robust: 1/d scaled by (1 -+ 3 ulp) */
   int nearX, nearY, nearZ; /* 0: lower plane is near, 1: upper */
+  int robust;
   float tnear, tfar;       /* clamped to >= 0 */
 } TravRay;
 
@@ -668,15 +738,31 @@ static inline float rcp_safe(float d) {
   return 1.0f / d;
 }
 
-static inline void trav_init(TravRay* t, const ORay* r) {
+static inline float zero_fix(float d) { return fabsf(d) < REF_MIN_RCP_INPUT ? REF_MIN_RCP_INPUT : d; }
+
+static inline void trav_init(TravRay* t, const ORay* r, int robust) {
+  t->robust = robust;
+  if (robust) {
+    /* TravRayBase<N,Nx,true>  node_intersector1.h:122-153 */
+    const float round_down = 1.0f - 3.0f * FLT_EPSILON, round_up = 1.0f + 3.0f * FLT_EPSILON;
+    const v3 rd = {1.0f / zero_fix(r->dir.x), 1.0f / zero_fix(r->dir.y), 1.0f / zero_fix(r->dir.z)};
+    t->rdir_near.x = round_down * rd.x; t->rdir_near.y = round_down * rd.y; t->rdir_near.z = round_down * rd.z;
+    t->rdir_far.x = round_up * rd.x; t->rdir_far.y = round_up * rd.y; t->rdir_far.z = round_up * rd.z;
+  }
   t->org = r->org;
   t->rdir.x = rcp_safe(r->dir.x);
   t->rdir.y = rcp_safe(r->dir.y);
   t->rdir.z = rcp_safe(r->dir.z);
   t->org_rdir = v3mul(r->org, t->rdir);
-  t->nearX = t->rdir.x >= 0.0f ? 0 : 1;
-  t->nearY = t->rdir.y >= 0.0f ? 0 : 1;
-  t->nearZ = t->rdir.z >= 0.0f ? 0 : 1;
+  if (robust) {
+    t->nearX = t->rdir_near.x >= 0.0f ? 0 : 1;
+    t->nearY = t->rdir_near.y >= 0.0f ? 0 : 1;
+    t->nearZ = t->rdir_near.z >= 0.0f ? 0 : 1;
+  } else {
+    t->nearX = t->rdir.x >= 0.0f ? 0 : 1;
+    t->nearY = t->rdir.y >= 0.0f ? 0 : 1;
+    t->nearZ = t->rdir.z >= 0.0f ? 0 : 1;
+  }
   t->tnear = fmax2(r->tnear, 0.0f);
   t->tfar = fmax2(r->tfar, 0.0f);
 }
@@ -690,6 +776,22 @@ static inline unsigned node_test(const ONode8* n, const TravRay* t, float dist[8
   const float* nz = t->nearZ ? n->hi[2] : n->lo[2];
   const float* fz = t->nearZ ? n->lo[2] : n->hi[2];
   unsigned mask = 0;
+  if (t->robust) {
+    /* intersectNodeRobust  node_intersector1.h:622-637 */
+    for (int i = 0; i < 8; i++) {
+      float tNx = (nx[i] - t->org.x) * t->rdir_near.x;
+      float tNy = (ny[i] - t->org.y) * t->rdir_near.y;
+      float tNz = (nz[i] - t->org.z) * t->rdir_near.z;
+      float tFx = (fx[i] - t->org.x) * t->rdir_far.x;
+      float tFy = (fy[i] - t->org.y) * t->rdir_far.y;
+      float tFz = (fz[i] - t->org.z) * t->rdir_far.z;
+      float tN = fmax2(fmax2(tNx, tNy), fmax2(tNz, t->tnear));
+      float tF = fmin2(fmin2(tFx, tFy), fmin2(tFz, t->tfar));
+      dist[i] = tN;
+      mask |= (unsigned)(tN <= tF) << i;
+    }
+    return mask;
+  }
   for (int i = 0; i < 8; i++) {
     float tNx = fmaf(nx[i], t->rdir.x, -t->org_rdir.x);
     float tNy = fmaf(ny[i], t->rdir.y, -t->org_rdir.y);
@@ -707,56 +809,71 @@ static inline unsigned node_test(const ONode8* n, const TravRay* t, float dist[8
 
 /* One Triangle4 block: all lanes against the same tfar, then the nearest
    valid lane (lowest lane on ties, vfloat4_sse2.h:887-892) is committed. */
-static inline int leaf_block_closest(const OTri4* tri, const ORay* r, float tfar_now, OHit* hit, OCount* cnt) {
-  MHit h[4];
+static inline int leaf_block_closest(const OTri4* tri, const ORay* r, float tfar_now, OHit* hit, OCount* cnt,
+                                     int robust) {
   int valid[4];
+  float tv[4];
+  MHit h[4];
+  PHit ph[4];
   int any = 0;
   for (int i = 0; i < 4; i++) {
     valid[i] = 0;
+    tv[i] = INFINITY;
     if (tri->geomID[i] == INVALID_ID) continue;
     cnt->tris++;
-    v3 v0 = {tri->v0[0][i], tri->v0[1][i], tri->v0[2][i]};
-    v3 e1 = {tri->e1[0][i], tri->e1[1][i], tri->e1[2][i]};
-    v3 e2 = {tri->e2[0][i], tri->e2[1][i], tri->e2[2][i]};
-    valid[i] = moeller(v0, e1, e2, r->org, r->dir, r->tnear, tfar_now, &h[i]);
+    v3 a = {tri->v0[0][i], tri->v0[1][i], tri->v0[2][i]};
+    v3 b = {tri->e1[0][i], tri->e1[1][i], tri->e1[2][i]};
+    v3 c = {tri->e2[0][i], tri->e2[1][i], tri->e2[2][i]};
+    if (robust) {
+      valid[i] = pluecker(a, b, c, r->org, r->dir, r->tnear, tfar_now, &ph[i]);
+      if (valid[i]) tv[i] = ph[i].t;
+    } else {
+      valid[i] = moeller(a, b, c, r->org, r->dir, r->tnear, tfar_now, &h[i]);
+      if (valid[i]) tv[i] = h[i].T * (1.0f / h[i].absDen);
+    }
     any |= valid[i];
   }
   if (!any) return 0;
-  float tv[4];
   float best = INFINITY;
-  for (int i = 0; i < 4; i++) {
-    tv[i] = INFINITY;
-    if (!valid[i]) continue;
-    const float rcp = 1.0f / h[i].absDen;
-    tv[i] = h[i].T * rcp;
-    if (tv[i] < best) best = tv[i];
-  }
+  for (int i = 0; i < 4; i++)
+    if (valid[i] && tv[i] < best) best = tv[i];
   int sel = -1;
   for (int i = 0; i < 4 && sel < 0; i++)
     if (valid[i] && tv[i] == best) sel = i;
   if (sel < 0)
     for (int i = 0; i < 4 && sel < 0; i++)
       if (valid[i]) sel = i;
-  const float rcp = 1.0f / h[sel].absDen;
   hit->valid = 1;
-  hit->t = h[sel].T * rcp;
-  hit->u = h[sel].U * rcp;
-  hit->v = h[sel].V * rcp;
-  hit->Ng = h[sel].Ng;
+  if (robust) {
+    hit->t = ph[sel].t;
+    pluecker_uv(&ph[sel], &hit->u, &hit->v);
+    hit->Ng = ph[sel].Ng;
+  } else {
+    const float rcp = 1.0f / h[sel].absDen;
+    hit->t = h[sel].T * rcp;
+    hit->u = h[sel].U * rcp;
+    hit->v = h[sel].V * rcp;
+    hit->Ng = h[sel].Ng;
+  }
   hit->geomID = tri->geomID[sel];
   hit->primID = tri->primID[sel];
   return 1;
 }
 
-static inline int leaf_block_any(const OTri4* tri, const ORay* r, OCount* cnt) {
+static inline int leaf_block_any(const OTri4* tri, const ORay* r, OCount* cnt, int robust) {
   for (int i = 0; i < 4; i++) {
     if (tri->geomID[i] == INVALID_ID) continue;
     cnt->tris++;
-    v3 v0 = {tri->v0[0][i], tri->v0[1][i], tri->v0[2][i]};
-    v3 e1 = {tri->e1[0][i], tri->e1[1][i], tri->e1[2][i]};
-    v3 e2 = {tri->e2[0][i], tri->e2[1][i], tri->e2[2][i]};
-    MHit h;
-    if (moeller(v0, e1, e2, r->org, r->dir, r->tnear, r->tfar, &h)) return 1;
+    v3 a = {tri->v0[0][i], tri->v0[1][i], tri->v0[2][i]};
+    v3 b = {tri->e1[0][i], tri->e1[1][i], tri->e1[2][i]};
+    v3 c = {tri->e2[0][i], tri->e2[1][i], tri->e2[2][i]};
+    if (robust) {
+      PHit h;
+      if (pluecker(a, b, c, r->org, r->dir, r->tnear, r->tfar, &h)) return 1;
+    } else {
+      MHit h;
+      if (moeller(a, b, c, r->org, r->dir, r->tnear, r->tfar, &h)) return 1;
+    }
   }
   return 0;
 }
@@ -772,7 +889,7 @@ static void trace_closest(const OracleScene* s, char* rec, OCount* cnt) {
   if (!(r.tnear <= r.tfar)) return;
   if (s->root == EMPTY_REF) return;
   TravRay t;
-  trav_init(&t, &r);
+  trav_init(&t, &r, s->robust);
   OHit hit;
   memset(&hit, 0, sizeof(hit));
   hit.valid = 0;
@@ -810,7 +927,7 @@ static void trace_closest(const OracleScene* s, char* rec, OCount* cnt) {
     cnt->leaves++;
     const OLeaf* lf = &s->leaves[cur & ~LEAF_BIT];
     for (uint32_t b = 0; b < lf->nblocks; b++) {
-      if (leaf_block_closest(&s->tris[lf->first + b], &r, r.tfar, &hit, cnt)) r.tfar = hit.t;
+      if (leaf_block_closest(&s->tris[lf->first + b], &r, r.tfar, &hit, cnt, s->robust)) r.tfar = hit.t;
     }
     t.tfar = r.tfar;
   }
@@ -825,7 +942,7 @@ static void trace_occluded(const OracleScene* s, char* rec, OCount* cnt) {
   if (!(r.tnear <= r.tfar)) return;
   if (s->root == EMPTY_REF) return;
   TravRay t;
-  trav_init(&t, &r);
+  trav_init(&t, &r, s->robust);
   uint32_t stack[STACK_SIZE];
   int sp = 0;
   stack[sp++] = s->root;
@@ -850,7 +967,7 @@ static void trace_occluded(const OracleScene* s, char* rec, OCount* cnt) {
     cnt->leaves++;
     const OLeaf* lf = &s->leaves[cur & ~LEAF_BIT];
     for (uint32_t b = 0; b < lf->nblocks; b++) {
-      if (leaf_block_any(&s->tris[lf->first + b], &r, cnt)) {
+      if (leaf_block_any(&s->tris[lf->first + b], &r, cnt, s->robust)) {
         float ninf = -INFINITY;
         memcpy(rec + 32, &ninf, 4);
         return;
@@ -922,6 +1039,7 @@ void orc_occluded1M(const OracleScene* s, void* rays, unsigned M, size_t stride,
 /* brute force                                                              */
 /* ------------------------------------------------------------------------ */
 
+/* the leaf values of one primitive: (v0, e1, e2), or (v0, v1, v2) when robust */
 static int prim_tri(const OracleScene* s, unsigned geomID, unsigned primID, v3* v0, v3* e1, v3* e2) {
   const OMesh* m = find_mesh(s, geomID);
   if (!m || primID >= m->nt) return 0;
@@ -929,8 +1047,8 @@ static int prim_tri(const OracleScene* s, unsigned geomID, unsigned primID, v3* 
   if (tri[0] >= m->nv || tri[1] >= m->nv || tri[2] >= m->nv) return 0;
   v3 p0 = mesh_vertex(m, tri[0]), p1 = mesh_vertex(m, tri[1]), p2 = mesh_vertex(m, tri[2]);
   *v0 = p0;
-  *e1 = v3sub(p0, p1);
-  *e2 = v3sub(p2, p0);
+  *e1 = s->robust ? p1 : v3sub(p0, p1);
+  *e2 = s->robust ? p2 : v3sub(p2, p0);
   return 1;
 }
 
@@ -946,14 +1064,23 @@ void orc_brute_intersect1M(const OracleScene* s, void* rays, unsigned M, size_t 
     for (size_t k = 0; k < s->nprims; k++) {
       v3 v0, e1, e2;
       if (!prim_tri(s, s->prims[k].geomID, s->prims[k].primID, &v0, &e1, &e2)) continue;
-      MHit h;
-      if (!moeller(v0, e1, e2, r.org, r.dir, r.tnear, r.tfar, &h)) continue;
-      const float rcp = 1.0f / h.absDen;
-      hit.valid = 1;
-      hit.t = h.T * rcp;
-      hit.u = h.U * rcp;
-      hit.v = h.V * rcp;
-      hit.Ng = h.Ng;
+      if (s->robust) {
+        PHit h;
+        if (!pluecker(v0, e1, e2, r.org, r.dir, r.tnear, r.tfar, &h)) continue;
+        hit.valid = 1;
+        hit.t = h.t;
+        pluecker_uv(&h, &hit.u, &hit.v);
+        hit.Ng = h.Ng;
+      } else {
+        MHit h;
+        if (!moeller(v0, e1, e2, r.org, r.dir, r.tnear, r.tfar, &h)) continue;
+        const float rcp = 1.0f / h.absDen;
+        hit.valid = 1;
+        hit.t = h.T * rcp;
+        hit.u = h.U * rcp;
+        hit.v = h.V * rcp;
+        hit.Ng = h.Ng;
+      }
       hit.geomID = s->prims[k].geomID;
       hit.primID = s->prims[k].primID;
       r.tfar = hit.t;
@@ -972,7 +1099,9 @@ void orc_brute_occluded1M(const OracleScene* s, void* rays, unsigned M, size_t s
       v3 v0, e1, e2;
       if (!prim_tri(s, s->prims[k].geomID, s->prims[k].primID, &v0, &e1, &e2)) continue;
       MHit h;
-      if (moeller(v0, e1, e2, r.org, r.dir, r.tnear, r.tfar, &h)) {
+      PHit ph;
+      if (s->robust ? pluecker(v0, e1, e2, r.org, r.dir, r.tnear, r.tfar, &ph)
+                    : moeller(v0, e1, e2, r.org, r.dir, r.tnear, r.tfar, &h)) {
         float ninf = -INFINITY;
         memcpy(rec + 32, &ninf, 4);
         break;

@@ -17,6 +17,9 @@
  *   - Triangle4 leaf fill  kernels/geometry/triangle.h:40-41, 98-120
  *   - single-ray traversal kernels/bvh/bvh_intersector1.cpp:30-195,
  *       node test kernels/bvh/node_intersector1.h:30-60, 527-585
+ *   - robust mode (Triangle4v + Pluecker, rounding-aware node test)
+ *       kernels/geometry/triangle_intersector_pluecker.h:60-111,
+ *       kernels/geometry/trianglev.h:93-115, node_intersector1.h:122-153,622-637
  *   - Moeller-Trumbore leaf test
  *       kernels/geometry/triangle_intersector_moeller.h:62-104,
  *       epilog kernels/geometry/intersector_epilog.h:215-296,
@@ -56,6 +59,12 @@ void orc_scene_free(OracleScene* s);
 int orc_scene_add_mesh(OracleScene* s, unsigned geomID,
                        const void* verts, size_t vstride, unsigned nverts,
                        const void* idx, size_t istride, unsigned ntris);
+
+/* RTC_SCENE_FLAG_ROBUST: Triangle4v leaves (raw vertices) and the Pluecker
+   test (kernels/common/scene.cpp:119-125, triangle_intersector_pluecker.h)
+   with the rounding-aware node test (node_intersector1.h:122-153,622-637).
+   Takes effect at the next commit. */
+void orc_scene_set_robust(OracleScene* s, int robust);
 
 /* Builds the BVH8 (binned SAH).  Returns the number of valid primitives. */
 long orc_scene_commit(OracleScene* s);
@@ -111,6 +120,10 @@ int orc_fp64_hit(const OracleScene* s, const void* rayhit_in, unsigned geomID,
 int orc_moeller1(const float v0[3], const float v1[3], const float v2[3],
                  const float org[3], const float dir[3], float tnear, float tfar,
                  float out_UVTden[4], float out_tuv[3], float out_Ng[3]);
+
+/* Single-triangle Pluecker test (robust mode); out_tuv = t, u, v. */
+int orc_pluecker1(const float v0[3], const float v1[3], const float v2[3], const float org[3], const float dir[3],
+                  float tnear, float tfar, float out_tuv[3], float out_Ng[3]);
 
 #ifdef __cplusplus
 }

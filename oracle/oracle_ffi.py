@@ -55,6 +55,9 @@ def lib():
         L.orc_fp64_hit.restype = i
         L.orc_moeller1.argtypes = [ctypes.POINTER(f)] * 5 + [f, f] + [ctypes.POINTER(f)] * 3
         L.orc_moeller1.restype = i
+        L.orc_scene_set_robust.argtypes = [vp, i]
+        L.orc_pluecker1.argtypes = [ctypes.POINTER(f)] * 5 + [f, f] + [ctypes.POINTER(f)] * 2
+        L.orc_pluecker1.restype = i
         _lib = L
     return _lib
 
@@ -66,9 +69,10 @@ def _ptr(a):
 class OracleScene:
     """A committed oracle scene built from (geomID, verts, idx) meshes."""
 
-    def __init__(self, meshes):
+    def __init__(self, meshes, robust=False):
         L = lib()
         self._h = ctypes.c_void_p(L.orc_scene_new())
+        L.orc_scene_set_robust(self._h, 1 if robust else 0)
         self._keep = []
         for gid, verts, idx in meshes:
             verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
@@ -130,6 +134,13 @@ class OracleScene:
         t, u, v = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         ok = lib().orc_fp64_hit(self._h, _ptr(rec), geomID, primID, ctypes.byref(t), ctypes.byref(u), ctypes.byref(v))
         return bool(ok), t.value, u.value, v.value
+
+
+def pluecker1(v0, v1, v2, org, d, tnear=0.0, tfar=float("inf")):
+    f3 = ctypes.c_float * 3
+    tuv, ng = f3(), f3()
+    ok = lib().orc_pluecker1(f3(*v0), f3(*v1), f3(*v2), f3(*org), f3(*d), tnear, tfar, tuv, ng)
+    return bool(ok), tuple(tuv), tuple(ng)
 
 
 def moeller1(v0, v1, v2, org, d, tnear=0.0, tfar=float("inf")):

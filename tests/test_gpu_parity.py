@@ -315,3 +315,32 @@ def test_host_ray_modes(rtc, mode):
     assert (a.view(np.uint8) == ts.cpu().numpy()).all()
     sc.release()
     dev.release()
+
+
+def test_robust_mode_parity(rtc, device, oracle):
+    """RTC_SCENE_FLAG_ROBUST (Triangle4v + Pluecker): GPU vs the oracle's
+    robust path on a heightfield, a soup and the verify suite's far-away
+    watertight sphere, whose rays must not leak (miss rate <= 2e-5)."""
+    from test_oracle import WATERTIGHT_FAR, watertight_rays
+    cases = [(W.heightfield(128), W.camera_rays(256, 256)),
+             (W.gaussian_soup(100_000, seed=51), W.sphere_rays(200_000, seed=52))]
+    vs, ix, wr = watertight_rays("sphere", WATERTIGHT_FAR, 100_000, 53)
+    cases.append(((vs, ix), wr))
+    for (verts, idx), rays in cases:
+        sg = rtc.Scene(device, flags=rtc.RTC_SCENE_FLAG_ROBUST)
+        sg.add_mesh(verts, idx)
+        sg.commit()
+        so = oracle.OracleScene([(0, verts, idx)], robust=True)
+        g, r = rays.copy(), rays.copy()
+        sg.intersect(g)
+        so.intersect(r)
+        rep = compare_closest(so, rays, g, r)
+        print(rep)
+        assert_clean(rep)
+        shadow, _ = W.shadow_rays(r, seed=54)
+        a, b = shadow.copy(), shadow.copy()
+        sg.occluded(a)
+        so.occluded(b)
+        assert_clean(compare_occluded(so, shadow, a, b, sg))
+        sg.release()
+    assert np.mean(g["geomID"] == 0xFFFFFFFF) <= 2e-5

@@ -213,3 +213,52 @@ def test_adjudicator_codes(oracle):
     assert sc.adjudicate(ray, (0, 0, 1.0), (0, 1, 2.0)) == 3   # A closer
     assert sc.adjudicate(ray, (0, 1, 2.0), (0, 0, 1.0)) == 4   # B closer
     assert sc.adjudicate(ray, (0xFFFFFFFF, 0, 0), (0, 0, 1.0)) == 4  # A missed a robust hit
+
+
+WATERTIGHT_FAR = np.array([148376.0, 1234.0, -223423.0], np.float32)  # verify.cpp:5498
+
+
+def watertight_rays(model, pos, n, seed):
+    """Rays of WatertightTest (verify.cpp:2898-2979)."""
+    rng = np.random.default_rng(seed)
+    if model == "sphere":
+        verts, idx = W.triangle_sphere(pos, 2.0, 500)
+        org = pos + (2 * rng.random((n, 3), dtype=np.float32) - 1)
+        d = 2 * rng.random((n, 3), dtype=np.float32) - 1
+    else:
+        verts, idx = W.triangle_plane((pos[0], -6, -6), (0, 0, 12), (0, 12, 0), 500, 500)
+        org = np.broadcast_to(np.array([pos[0] - 3, 0, 0], np.float32), (n, 3))
+        d = 2 * rng.random((n, 3), dtype=np.float32) - 1
+        d[:, 0] = 1.0
+    return verts, idx, R.make_rayhits(org, d)
+
+
+@pytest.mark.parametrize("model", ["sphere", "plane"])
+def test_watertight_robust_far_from_origin(oracle, model):
+    """The verify suite runs WatertightTest on robust scenes far from the
+    origin (verify.cpp:5496-5504): the Pluecker path must stay watertight
+    there (miss rate <= 2e-5)."""
+    verts, idx, rays = watertight_rays(model, WATERTIGHT_FAR, 50000, 17)
+    sc = oracle.OracleScene([(0, verts, idx)], robust=True)
+    sc.intersect(rays)
+    assert np.mean(rays["geomID"] == 0xFFFFFFFF) <= 2e-5
+
+
+def test_triangle_hit_known_answer_robust(oracle):
+    """TriangleHitTest on a robust scene (Triangle4v + Pluecker)."""
+    verts, idx, rays, u, v = _single_triangle_rays()
+    sc = oracle.OracleScene([(0, verts, idx)], robust=True)
+    sc.intersect(rays, nthreads=1)
+    check_triangle_hit(rays, u, v, verts)
+
+
+def test_robust_bvh_matches_brute_force(oracle):
+    verts, idx = W.gaussian_soup(3000, seed=5)
+    rays = W.sphere_rays(3000, seed=6)
+    sc = oracle.OracleScene([(0, verts, idx)], robust=True)
+    a, b = rays.copy(), rays.copy()
+    sc.intersect(a)
+    sc.brute_intersect(b)
+    assert R.hits_equal_bits(a, b).mean() > 0.999
+    ok, tuv, ng = oracle.pluecker1((0, 0, 0), (1, 0, 0), (0, 1, 0), (0.25, 0.25, -1), (0, 0, 1))
+    assert ok and tuv == (1.0, 0.25, 0.25) and ng == (0.0, 0.0, 1.0)
