@@ -1056,7 +1056,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(cudaMemsetAsync(d_leaves, 0, sizeof(uint32_t), st));
   GB_CHECK(cudaMemcpyAsync(items_a, &root, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
   uint32_t nitems = 1, level_base = 0, tri_next = 0, depth = 0;
+  std::vector<uint32_t> level_start;
   while (nitems > 0) {
+    level_start.push_back(level_base);
     const uint32_t nb = cdiv(nitems, 128);
     k_collapse_count<<<nb, 128, 0, st>>>(bt, items_a, nitems, kids, nint, ntri); note_launches(1);
     k_scan_excl<<<1, 1024, 0, st>>>(nint, nitems, d_tot + 0); note_launches(1);
@@ -1095,6 +1097,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   out->num_tris = N;
   out->depth = depth;
   out->robust = opt.robust != 0;
+  level_start.push_back(num_nodes);
+  out->level_start = level_start;
 
   cudaFreeAsync(wnodes, st); cudaFreeAsync(wtris, st);
   cudaFreeAsync(items_a, st); cudaFreeAsync(items_b, st); cudaFreeAsync(kids, st);
@@ -1151,6 +1155,206 @@ cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t 
   cudaFreeAsync(vb, st);
   cudaFreeAsync(hist, st);
   return cudaStreamSynchronize(st);
+}
+
+
+// ---------------------------------------------------------------------------
+// 6. refit: same topology, new vertex positions
+//
+// Replaces the reference's BVH refitter (kernels/bvh/bvh_refit.cpp:30-247),
+// which recomputes node bounds bottom-up for meshes whose topology did not
+// change.  Triangle records are re-gathered from the updated vertex buffers,
+// then every breadth-first level, deepest first, recomputes its children's
+// boxes (leaves from their triangles' vertices, inner children from the box
+// the deeper level stored) and requantises them in the node's new frame.
+// Slot order and leaf grouping stay as built.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ bool refit_tri_vertices(const GeomDesc* __restrict__ geoms,
+                                                   const uint32_t* __restrict__ slot_of, uint32_t nslots,
+                                                   const TriRecord& rec, float3& p0, float3& p1, float3& p2) {
+  const uint32_t primID = __float_as_uint(rec.a.w), geomID = __float_as_uint(rec.b.w);
+  if (geomID >= nslots) return false;
+  const uint32_t slot = slot_of[geomID];
+  if (slot == kInvalidID) return false;
+  const GeomDesc g = geoms[slot];
+  if (primID >= g.ntris) return false;
+  const uint3 t = load_tri(g, primID);
+  if (t.x >= g.nverts || t.y >= g.nverts || t.z >= g.nverts) return false;
+  p0 = load_vtx(g, t.x);
+  p1 = load_vtx(g, t.y);
+  p2 = load_vtx(g, t.z);
+  return vtx_ok(p0.x, p0.y, p0.z) && vtx_ok(p1.x, p1.y, p1.z) && vtx_ok(p2.x, p2.y, p2.z);
+}
+
+__global__ void __launch_bounds__(256) k_refit_tris(const GeomDesc* __restrict__ geoms,
+                                                    const uint32_t* __restrict__ slot_of, uint32_t nslots,
+                                                    TriRecord* __restrict__ tris, uint32_t n, int robust,
+                                                    uint32_t* err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  TriRecord rec = tris[i];
+  float3 p0, p1, p2;
+  if (!refit_tri_vertices(geoms, slot_of, nslots, rec, p0, p1, p2)) {
+    atomicOr(err, kErrBuild);  // the host falls back to a full build
+    return;
+  }
+  const float3 e1 = robust ? p1 : make_float3(__fsub_rn(p0.x, p1.x), __fsub_rn(p0.y, p1.y), __fsub_rn(p0.z, p1.z));
+  const float3 e2 = robust ? p2 : make_float3(__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z));
+  rec.a = make_float4(p0.x, p0.y, p0.z, rec.a.w);
+  rec.b = make_float4(e1.x, e1.y, e1.z, rec.b.w);
+  rec.c = make_float4(e2.x, e2.y, e2.z, 0.f);
+  tris[i] = rec;
+}
+
+__global__ void __launch_bounds__(128) k_refit_level(const GeomDesc* __restrict__ geoms,
+                                                     const uint32_t* __restrict__ slot_of, uint32_t nslots,
+                                                     const TriRecord* __restrict__ tris, uint32_t num_tris,
+                                                     WideNode* __restrict__ nodes, uint32_t num_nodes,
+                                                     float* __restrict__ node_box, uint32_t begin, uint32_t end,
+                                                     double* sah_acc, uint32_t* err) {
+  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end || k >= num_nodes) return;
+  WideNode node = nodes[k];
+  float3 clo[8], chi[8];
+  float3 ulo = make_float3(INFINITY, INFINITY, INFINITY), uhi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+  uint32_t rank = 0;
+  for (int s = 0; s < 8; s++) {
+    clo[s] = make_float3(INFINITY, INFINITY, INFINITY);
+    chi[s] = make_float3(-INFINITY, -INFINITY, -INFINITY);
+    const uint32_t m = node.meta[s];
+    if (m == 0) continue;
+    if (node.imask >> s & 1u) {
+      const uint32_t c = node.child_base + rank++;
+      if (c >= num_nodes || c <= k) {
+        atomicOr(err, kErrBuild);
+        return;
+      }
+      clo[s] = make_float3(node_box[6 * (size_t)c + 0], node_box[6 * (size_t)c + 1], node_box[6 * (size_t)c + 2]);
+      chi[s] = make_float3(node_box[6 * (size_t)c + 3], node_box[6 * (size_t)c + 4], node_box[6 * (size_t)c + 5]);
+    } else {
+      const uint32_t cnt = ((m >> 5) & 3u) + 1u, first = node.tri_base + (m & 31u);
+      for (uint32_t t = first; t < first + cnt; t++) {
+        float3 p0, p1, p2;
+        if (t >= num_tris || !refit_tri_vertices(geoms, slot_of, nslots, tris[t], p0, p1, p2)) {
+          atomicOr(err, kErrBuild);
+          return;
+        }
+        clo[s] = f3min(clo[s], f3min(f3min(p0, p1), p2));
+        chi[s] = f3max(chi[s], f3max(f3max(p0, p1), p2));
+      }
+    }
+    ulo = f3min(ulo, clo[s]);
+    uhi = f3max(uhi, chi[s]);
+  }
+  const uint32_t Ex = exp_for(__fsub_ru(uhi.x, ulo.x));
+  const uint32_t Ey = exp_for(__fsub_ru(uhi.y, ulo.y));
+  const uint32_t Ez = exp_for(__fsub_ru(uhi.z, ulo.z));
+  const float sx = __uint_as_float(Ex << 23), sy = __uint_as_float(Ey << 23), sz = __uint_as_float(Ez << 23);
+  const float ix = __uint_as_float((254u - Ex) << 23), iy = __uint_as_float((254u - Ey) << 23),
+              iz = __uint_as_float((254u - Ez) << 23);
+  node.px = ulo.x;
+  node.py = ulo.y;
+  node.pz = ulo.z;
+  node.ex = (uint8_t)Ex;
+  node.ey = (uint8_t)Ey;
+  node.ez = (uint8_t)Ez;
+  double sah = 0.0;
+  for (int s = 0; s < 8; s++) {
+    if (node.meta[s] == 0) continue;
+    const float3 a = clo[s], b = chi[s];
+    const float qlx = fminf(fmaxf(floorf(__fsub_rd(a.x, ulo.x) * ix), 0.f), 255.f);
+    const float qly = fminf(fmaxf(floorf(__fsub_rd(a.y, ulo.y) * iy), 0.f), 255.f);
+    const float qlz = fminf(fmaxf(floorf(__fsub_rd(a.z, ulo.z) * iz), 0.f), 255.f);
+    const float qhx = fminf(fmaxf(ceilf(__fsub_ru(b.x, ulo.x) * ix), 0.f), 255.f);
+    const float qhy = fminf(fmaxf(ceilf(__fsub_ru(b.y, ulo.y) * iy), 0.f), 255.f);
+    const float qhz = fminf(fmaxf(ceilf(__fsub_ru(b.z, ulo.z) * iz), 0.f), 255.f);
+    node.qlo_x[s] = (uint8_t)qlx; node.qlo_y[s] = (uint8_t)qly; node.qlo_z[s] = (uint8_t)qlz;
+    node.qhi_x[s] = (uint8_t)qhx; node.qhi_y[s] = (uint8_t)qhy; node.qhi_z[s] = (uint8_t)qhz;
+    const float3 dlo = make_float3(__fmaf_rd(qlx, sx, ulo.x), __fmaf_rd(qly, sy, ulo.y), __fmaf_rd(qlz, sz, ulo.z));
+    const float3 dhi = make_float3(__fmaf_ru(qhx, sx, ulo.x), __fmaf_ru(qhy, sy, ulo.y), __fmaf_ru(qhz, sz, ulo.z));
+    sah += (double)fmaxf(0.f, half_area(dlo, dhi));  // leaves of <= 4 triangles: one block each
+  }
+  nodes[k] = node;
+  node_box[6 * (size_t)k + 0] = ulo.x; node_box[6 * (size_t)k + 1] = ulo.y; node_box[6 * (size_t)k + 2] = ulo.z;
+  node_box[6 * (size_t)k + 3] = uhi.x; node_box[6 * (size_t)k + 4] = uhi.y; node_box[6 * (size_t)k + 5] = uhi.z;
+  atomicAdd(sah_acc, sah);
+}
+
+cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* bvh, BuildStats* stats,
+                      bool* fallback) {
+  *fallback = false;
+  if (bvh->num_nodes == 0 || bvh->level_start.size() < 2) {
+    *fallback = true;
+    return cudaSuccess;
+  }
+  cudaEvent_t ev0, ev1;
+  GB_CHECK(cudaEventCreate(&ev0));
+  GB_CHECK(cudaEventCreate(&ev1));
+  GB_CHECK(cudaEventRecord(ev0, st));
+  uint32_t nslots = 0;
+  for (int g = 0; g < ngeoms; g++) nslots = std::max(nslots, h_geoms[g].geomID + 1);
+  std::vector<uint32_t> slot_of(std::max(nslots, 1u), kInvalidID);
+  for (int g = 0; g < ngeoms; g++) slot_of[h_geoms[g].geomID] = (uint32_t)g;
+  GeomDesc* d_geoms = nullptr;
+  uint32_t *d_slot = nullptr, *d_err = nullptr;
+  float* node_box = nullptr;
+  double* d_sah = nullptr;
+  GB_CHECK(dalloc(&d_geoms, ngeoms, st));
+  GB_CHECK(dalloc(&d_slot, slot_of.size(), st));
+  GB_CHECK(dalloc(&d_err, 1, st));
+  GB_CHECK(dalloc(&node_box, (size_t)6 * bvh->num_nodes, st));
+  GB_CHECK(dalloc(&d_sah, 1, st));
+  GB_CHECK(cudaMemcpyAsync(d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
+  GB_CHECK(cudaMemcpyAsync(d_slot, slot_of.data(), sizeof(uint32_t) * slot_of.size(), cudaMemcpyHostToDevice, st));
+  GB_CHECK(cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st));
+  GB_CHECK(cudaMemsetAsync(d_sah, 0, sizeof(double), st));
+  k_refit_tris<<<cdiv(bvh->num_tris, 256), 256, 0, st>>>(d_geoms, d_slot, (uint32_t)slot_of.size(), bvh->tris,
+                                                         bvh->num_tris, bvh->robust, d_err);
+  note_launches(1);
+  for (size_t l = bvh->level_start.size() - 1; l-- > 0;) {
+    const uint32_t b = bvh->level_start[l], e = bvh->level_start[l + 1];
+    if (e <= b) continue;
+    k_refit_level<<<cdiv(e - b, 128), 128, 0, st>>>(d_geoms, d_slot, (uint32_t)slot_of.size(), bvh->tris,
+                                                   bvh->num_tris, bvh->nodes, bvh->num_nodes, node_box, b, e, d_sah,
+                                                   d_err);
+    note_launches(1);
+  }
+  GB_CHECK(cudaGetLastError());
+  uint32_t err = 0;
+  float root[6];
+  double sah_sum = 0;
+  GB_CHECK(cudaMemcpyAsync(&err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(root, node_box, sizeof(root), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(&sah_sum, d_sah, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaEventRecord(ev1, st));
+  cudaFreeAsync(d_geoms, st);
+  cudaFreeAsync(d_slot, st);
+  cudaFreeAsync(d_err, st);
+  cudaFreeAsync(node_box, st);
+  cudaFreeAsync(d_sah, st);
+  GB_CHECK(cudaStreamSynchronize(st));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (err) {  // a vertex became invalid or the records are inconsistent: rebuild
+    *fallback = true;
+    return cudaSuccess;
+  }
+  for (int d = 0; d < 3; d++) {
+    bvh->lo[d] = root[d];
+    bvh->hi[d] = root[3 + d];
+  }
+  const float gx = bvh->hi[0] - bvh->lo[0], gy = bvh->hi[1] - bvh->lo[1], gz = bvh->hi[2] - bvh->lo[2];
+  const double Aroot = std::max(0.0, (double)(gx * (gy + gz) + gy * gz));
+  stats->sah = Aroot > 0 ? (Aroot + sah_sum) / Aroot : 0.0;
+  stats->build_ms = ms;
+  stats->num_nodes = bvh->num_nodes;
+  stats->num_prims = bvh->num_tris;
+  stats->depth = bvh->depth;
+  stats->refit = 1;
+  return cudaSuccess;
 }
 
 void free_bvh(DeviceBVH* b) {

@@ -15,6 +15,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <vector>
+
 namespace gb {
 
 constexpr uint32_t kInvalidID = 0xFFFFFFFFu;
@@ -73,6 +75,7 @@ struct DeviceBVH {
   int robust = 0;            // triangle records hold (v0, v1, v2) for the Pluecker test
   float lo[3] = {0, 0, 0};   // geometry bounds (empty scene: +inf / -inf)
   float hi[3] = {0, 0, 0};
+  std::vector<uint32_t> level_start;  // first node of each breadth-first level + end (for refit)
 };
 
 // Builder options (device config keys gpu.leaf_max=1..4, gpu.morton=axis|cube).
@@ -88,6 +91,7 @@ struct BuildStats {
   double build_ms = 0;       // device time of the whole build
   uint32_t num_nodes = 0, num_leaves = 0, num_prims = 0, depth = 0;
   uint32_t ploc_iterations = 0;
+  uint32_t refit = 0;        // 1 when the last commit refitted instead of rebuilding
 };
 
 // Traversal work counters (counting variant of the kernels).

@@ -239,6 +239,7 @@ struct Geometry : RefCounted {
   RTCBuildQuality quality = RTC_BUILD_QUALITY_MEDIUM;
   void* user = nullptr;
   unsigned time_steps = 1;
+  uint64_t topo_version = 0;  // bumped when the index buffer is set or updated
   // device copies of host buffers
   char* d_verts = nullptr;
   char* d_idx = nullptr;
@@ -271,6 +272,7 @@ struct Geometry : RefCounted {
       if (slot != 0) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid buffer slot");
       if (format != RTC_FORMAT_UINT3) fail(RTC_ERROR_INVALID_OPERATION, "invalid index buffer format");
       indices.set(b, offset, stride, num, format);
+      topo_version++;
     } else {
       fail(RTC_ERROR_INVALID_ARGUMENT, "unknown buffer type");
     }
@@ -395,6 +397,18 @@ struct Scene : RefCounted {
   bool committed = false;
   gb::DeviceBVH bvh;
   gb::BuildStats stats;
+  // topology of the last full build: (geomID, geometry, index version, triangles, vertices)
+  struct SigEntry {
+    unsigned id;
+    const Geometry* g;
+    uint64_t topo;
+    size_t ntris, nverts;
+    bool operator==(const SigEntry& o) const {
+      return id == o.id && g == o.g && topo == o.topo && ntris == o.ntris && nverts == o.nverts;
+    }
+  };
+  std::vector<SigEntry> built_sig;
+  bool built_robust = false;
 
   explicit Scene(Device* d) : device(d) { device->inc(); }
   ~Scene() override {
@@ -462,16 +476,38 @@ struct Scene : RefCounted {
       descs.push_back(d);
     }
     if (total >= 0x7FFFFFFFull) fail(RTC_ERROR_INVALID_OPERATION, "too many primitives");
+    std::vector<SigEntry> sig;
+    bool all_refit = !descs.empty();
+    for (const gb::GeomDesc& d : descs) {
+      const Geometry* g = geoms[d.geomID];
+      sig.push_back(SigEntry{d.geomID, g, g->topo_version, d.ntris, d.nverts});
+      all_refit &= g->quality == RTC_BUILD_QUALITY_REFIT;
+    }
+    const bool robust = (flags & RTC_SCENE_FLAG_ROBUST) != 0;  // scene.cpp:119-125: Triangle4v + Pluecker
+    // geometries marked RTC_BUILD_QUALITY_REFIT whose topology is unchanged
+    // since the last build are refitted (kernels/bvh/bvh_refit.cpp:30-247)
+    if (committed && all_refit && bvh.num_nodes > 0 && sig == built_sig && robust == built_robust) {
+      gb::BuildStats bs = stats;
+      bool fallback = false;
+      cuda_ok(gb::refit_bvh(descs.data(), (int)descs.size(), st, &bvh, &bs, &fallback), "rtcCommitScene (refit)");
+      if (!fallback) {
+        stats = bs;
+        if (progress) progress(progress_ptr, 1.0);
+        return;
+      }
+    }
     // estimated device bytes of the build (scratch + result)
     device->memory((ssize_t)(total * 256 + 4096), false);
     gb::free_bvh(&bvh);
     committed = false;
     gb::BuildStats bs;
     gb::BuildOptions opt = device->build_opt;
-    opt.robust = (flags & RTC_SCENE_FLAG_ROBUST) != 0;  // scene.cpp:119-125: Triangle4v + Pluecker
+    opt.robust = robust;
     cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, opt, &bvh, &bs), "rtcCommitScene");
     stats = bs;
     committed = true;
+    built_sig = sig;
+    built_robust = robust;
     if (progress) progress(progress_ptr, 1.0);
     if (device->benchmark)
       printf("BENCHMARK_BUILD %f %f %f %u\n", bs.build_ms * 1e-3, bs.build_ms > 0 ? bs.num_prims / (bs.build_ms * 1e-3) : 0.0,
@@ -918,6 +954,7 @@ RTC_API void rtcUpdateGeometryBuffer(RTCGeometry hg, enum RTCBufferType type, un
   API_BEGIN
   VERIFY_HANDLE(hg);
   g->view(type, slot);  // validates; buffers are re-uploaded at every commit
+  if (type == RTC_BUFFER_TYPE_INDEX) g->topo_version++;
   API_END(g ? g->device : nullptr)
 }
 
@@ -1186,6 +1223,7 @@ RTC_API void rtcgbGetSceneBuildStats(RTCScene hs, RTCGBBuildStats* out) {
   out->num_prims = s->stats.num_prims;
   out->depth = s->stats.depth;
   out->ploc_iterations = s->stats.ploc_iterations;
+  out->refit = s->stats.refit;
   out->bvh_bytes = (unsigned long long)s->bvh.num_nodes * sizeof(gb::WideNode) +
                    (unsigned long long)s->bvh.num_tris * sizeof(gb::TriRecord);
   API_END(s ? s->device : nullptr)

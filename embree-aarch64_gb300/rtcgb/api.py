@@ -20,6 +20,7 @@ RTC_FORMAT_UINT3 = 0x5003
 RTC_FORMAT_FLOAT3 = 0x9003
 RTC_INVALID_GEOMETRY_ID = 0xFFFFFFFF
 RTC_SCENE_FLAG_ROBUST = 1 << 2
+RTC_BUILD_QUALITY_REFIT = 3
 
 ERRORS = {0: "NONE", 1: "UNKNOWN", 2: "INVALID_ARGUMENT", 3: "INVALID_OPERATION", 4: "OUT_OF_MEMORY",
           5: "UNSUPPORTED_CPU", 6: "CANCELLED"}
@@ -51,7 +52,7 @@ class RTCIntersectContext(ctypes.Structure):
 class RTCGBBuildStats(ctypes.Structure):
     _fields_ = [("sah", ctypes.c_double), ("build_ms", ctypes.c_double), ("num_nodes", ctypes.c_uint),
                 ("num_leaves", ctypes.c_uint), ("num_prims", ctypes.c_uint), ("depth", ctypes.c_uint),
-                ("ploc_iterations", ctypes.c_uint), ("pad", ctypes.c_uint), ("bvh_bytes", ctypes.c_ulonglong)]
+                ("ploc_iterations", ctypes.c_uint), ("refit", ctypes.c_uint), ("bvh_bytes", ctypes.c_ulonglong)]
 
 
 class RTCGBQueryStats(ctypes.Structure):
@@ -173,13 +174,16 @@ class Scene:
             self.L.rtcSetSceneFlags(self.h, flags)
         device.check("rtcNewScene")
 
-    def add_mesh(self, verts, idx, geom_id=None):
-        """Attaches a triangle mesh using shared buffers (kept alive here)."""
-        verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
-        idx = np.ascontiguousarray(idx, np.uint32).reshape(-1, 3)
+    def add_mesh(self, verts, idx, geom_id=None, quality=None):
+        """Attaches a triangle mesh using shared buffers (kept alive here).
+        quality: RTC_BUILD_QUALITY_* of the geometry (REFIT = 3)."""
+        verts = np.array(verts, np.float32).reshape(-1, 3)
+        idx = np.array(idx, np.uint32).reshape(-1, 3)
         self._keep.append((verts, idx))
         L = self.L
         g = ctypes.c_void_p(L.rtcNewGeometry(self.dev.h, RTC_GEOMETRY_TYPE_TRIANGLE))
+        if quality is not None:
+            L.rtcSetGeometryBuildQuality(g, quality)
         L.rtcSetSharedGeometryBuffer(g, RTC_BUFFER_TYPE_VERTEX, 0, RTC_FORMAT_FLOAT3, _ptr(verts), 0, 12,
                                      verts.shape[0])
         L.rtcSetSharedGeometryBuffer(g, RTC_BUFFER_TYPE_INDEX, 0, RTC_FORMAT_UINT3, _ptr(idx), 0, 12, idx.shape[0])
@@ -191,7 +195,23 @@ class Scene:
             gid = geom_id
         L.rtcReleaseGeometry(g)
         self.dev.check("add_mesh")
+        self._by_id = getattr(self, "_by_id", {})
+        self._by_id[gid] = (verts, idx)
         return gid
+
+    def update_vertices(self, gid, new_verts):
+        """Writes new positions into geometry gid's shared vertex buffer and
+        marks it updated (rtcUpdateGeometryBuffer); takes effect at commit."""
+        verts, _ = self._by_id[gid]
+        verts[:] = np.asarray(new_verts, np.float32).reshape(verts.shape)
+        self.L.rtcUpdateGeometryBuffer(self.L.rtcGetGeometry(self.h, gid), RTC_BUFFER_TYPE_VERTEX, 0)
+        self.dev.check("rtcUpdateGeometryBuffer")
+
+    def update_indices(self, gid, new_idx):
+        _, idx = self._by_id[gid]
+        idx[:] = np.asarray(new_idx, np.uint32).reshape(idx.shape)
+        self.L.rtcUpdateGeometryBuffer(self.L.rtcGetGeometry(self.h, gid), RTC_BUFFER_TYPE_INDEX, 0)
+        self.dev.check("rtcUpdateGeometryBuffer")
 
     def commit(self):
         self.L.rtcCommitScene(self.h)
@@ -207,7 +227,7 @@ class Scene:
         s = RTCGBBuildStats()
         self.L.rtcgbGetSceneBuildStats(self.h, ctypes.byref(s))
         self.dev.check("rtcgbGetSceneBuildStats")
-        return {f: getattr(s, f) for f, _ in s._fields_ if f != "pad"}
+        return {f: getattr(s, f) for f, _ in s._fields_}
 
     def intersect(self, rays, stride=None, count=None):
         """rtcIntersect1M on a host RTCRayHit array (in place)."""

@@ -114,6 +114,18 @@ def gaussian_soup(ntris=4_000_000, seed=11, nclusters=64):
     return verts, idx
 
 
+def displace_soup(verts, frame, seed=14, amplitude=0.002):
+    """Per-frame displacement of a triangle soup: every triangle moves by
+    amplitude * sin(2 pi (frame/60 + x)) along its own random unit normal
+    (x = the triangle centroid's x coordinate).  Returns new float32 vertices."""
+    v = np.asarray(verts, np.float64).reshape(-1, 3, 3)
+    rng = np.random.default_rng(seed)
+    nrm = _unit_vectors(rng, v.shape[0])
+    x = v[:, :, 0].mean(1)
+    off = amplitude * np.sin(2 * math.pi * (frame / 60.0 + x))
+    return (v + (off[:, None] * nrm)[:, None, :]).reshape(-1, 3).astype(np.float32)
+
+
 def triangle_sphere(center=(0.0, 0.0, 0.0), radius=2.0, N=50):
     """UV-sphere tessellation with numPhi=N, numTheta=2N (pole fans)."""
     numPhi, numTheta = N, 2 * N

@@ -20,7 +20,7 @@ typedef struct RTCGBBuildStats {
   unsigned int num_prims;   /* valid triangles in the BVH */
   unsigned int depth;       /* wide levels */
   unsigned int ploc_iterations;
-  unsigned int pad;
+  unsigned int refit;       /* 1 when the last commit refitted the BVH instead of rebuilding */
   unsigned long long bvh_bytes; /* node + triangle record bytes in HBM */
 } RTCGBBuildStats;
 

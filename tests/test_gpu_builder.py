@@ -98,3 +98,44 @@ def test_sah_against_reference_builder(rtc, oracle, name, config, limit):
     assert ratio <= limit
     sc.release()
     device.release()
+
+
+def test_refit_after_displacement(rtc, device, oracle):
+    """RTC_BUILD_QUALITY_REFIT geometry whose vertices move (the animated-soup
+    displacement) is refitted in place; the refitted BVH contains every
+    triangle and its hits equal the oracle's on the displaced mesh."""
+    from parity import assert_clean, compare_closest
+    verts, idx = W.gaussian_soup(60_000, seed=61)
+    rays = W.sphere_rays(200_000, seed=62)
+    sc = rtc.Scene(device)
+    gid = sc.add_mesh(verts, idx, quality=rtc.RTC_BUILD_QUALITY_REFIT)
+    sc.commit()
+    assert sc.build_stats()["refit"] == 0
+    nodes0, _ = sc.bvh()
+    for frame in (1, 7):
+        moved = W.displace_soup(verts, frame)
+        sc.update_vertices(gid, moved)
+        sc.commit()
+        st = sc.build_stats()
+        assert st["refit"] == 1
+        nodes, tris = sc.bvh()
+        assert nodes.shape == nodes0.shape
+        check_structure(nodes, tris, moved, idx)
+        g = rays.copy()
+        sc.intersect(g)
+        so = oracle.OracleScene([(gid, moved, idx)])
+        r = rays.copy()
+        so.intersect(r)
+        assert_clean(compare_closest(so, rays, g, r))
+    # a topology change forces a full build
+    sc.update_indices(gid, idx[::-1].copy())
+    sc.commit()
+    assert sc.build_stats()["refit"] == 0
+    # a vertex that becomes invalid cannot be refitted: the commit rebuilds and drops it
+    bad = W.displace_soup(verts, 3)
+    bad[0] = np.nan
+    sc.update_vertices(gid, bad)
+    sc.commit()
+    st = sc.build_stats()
+    assert st["refit"] == 0 and st["num_prims"] == idx.shape[0] - 1
+    sc.release()
