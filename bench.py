@@ -53,6 +53,13 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--robust", action="store_true", help="RTC_SCENE_FLAG_ROBUST scene (Pluecker test)")
     ap.add_argument("--config", default="", help="extra rtcNewDevice config tokens, e.g. gpu.leaf_max=2")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposer comparison")
+    ap.add_argument("--learned-scale", type=float, default=1.0, help="fraction of the learned workload (tests only)")
+    ap.add_argument("--no-animated", action="store_true", help="skip the animated path-tracing run")
+    ap.add_argument("--animated-scale", type=float, default=1.0, help="fraction of the animated workload (tests only)")
+    ap.add_argument("--frames", type=int, default=64, help="frames of the animated path-tracing run")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes run")
+    ap.add_argument("--batched-scale", type=float, default=1.0, help="fraction of the batched workload (tests only)")
     return ap.parse_args()
 
 
@@ -195,6 +202,308 @@ def run_reference(args, rank, world):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+
+MLP_FLOPS_PER_RAY = 2 * (32 * 64 + 64 * 64 + 64 * 64 + 64 * 4096)  # forward pass of the proposer
+
+
+def run_learned(api, dev, torch, stream, scale, steps, warmup):
+    """Learned proposer vs plain traversal on the ambient-occlusion workload:
+    724x724 heightfield + 300k soup triangles, 1024x1024 primary view, 8
+    cosine-weighted AO rays (tfar 0.05) and 8 diffuse bounce rays per primary
+    hit.  The proposer is trained on ~10M closest-hit records the plain
+    traversal logs for rays drawn with other seeds.  Times include the
+    proposer's inference (the learned calls' kernel time covers inference +
+    seeded traversal)."""
+    from rtcgb import rays as R
+    from rtcgb import workloads as W
+    cells = max(16, int(round(724 * math.sqrt(scale))))
+    res = max(32, int(round(1024 * math.sqrt(scale))))
+    soup = max(1000, int(300_000 * scale))
+    sc = api.Scene(dev)
+    for v, i in W.ao_scene(cells=cells, soup_tris=soup, seed=3):
+        sc.add_mesh(v, i)
+    sc.commit()
+    ntris = sc.build_stats()["num_prims"]
+    prim = W.camera_rays(res, res)
+    sc.intersect(prim)
+    nhit = int((prim["geomID"] != 0xFFFFFFFF).sum())
+    # training log (other seeds than the measured rays): 5 AO + 5 bounce rays per hit
+    ao_t, _ = W.hemisphere_rays(prim, 5, seed=31, tfar=0.05)
+    b_t, _ = W.hemisphere_rays(prim, 5, seed=32)
+    log = torch.from_numpy(np.concatenate([ao_t, b_t]).view(np.uint8)).cuda()
+    nlog = log.numel() // 80
+    del ao_t, b_t
+    sc.intersect_ptr(log.data_ptr(), nlog, 80)
+    prop = api.Proposer(sc, seed=7)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    st = prop.train(log.data_ptr(), epochs=2, batch=16384, lr=5e-3, count=nlog)
+    train_s = time.perf_counter() - t
+    del log
+    ao, _ = W.hemisphere_rays(prim, 8, seed=41, tfar=0.05, record=R.RAY_DTYPE)
+    bounce, _ = W.hemisphere_rays(prim, 8, seed=42)
+
+    def timed(fn, pristine, n, stride):
+        work = torch.empty_like(pristine)
+        ms = []
+        for k in range(warmup + steps):
+            work.copy_(pristine)
+            fn(work.data_ptr(), n, stride)
+            if k >= warmup:
+                ms.append(api.last_query_stats()["kernel_ms"])
+        q = api.last_query_stats()
+        return work, statistics.median(ms), q
+
+    out = {"workload": f"heightfield {cells}x{cells} + {soup} soup triangles ({ntris} tris), {res}x{res} view, "
+                       f"8 AO rays (tfar 0.05) + 8 bounce rays per hit",
+           "train": {"records": int(nlog), "labelled": int(st["samples"]), "epochs": 2, "batch": 16384,
+                     "seconds": train_s, "loss": st["loss"], "top1": st["top1"], "top4": st["top4"],
+                     "treelets": int(st["num_treelets"])}}
+    total_plain = total_learned = 0.0
+    for name, rays, stride, plain_fn, learned_fn in (
+            ("ao", ao, 48, sc.occluded_ptr, prop.occluded_ptr),
+            ("bounce", bounce, 80, sc.intersect_ptr, prop.intersect_ptr)):
+        n = rays.shape[0]
+        pristine = torch.from_numpy(rays.view(np.uint8)).cuda()
+        w_plain, ms_plain, _ = timed(plain_fn, pristine, n, stride)
+        w_learn, ms_learn, q = timed(learned_fn, pristine, n, stride)
+        a = w_plain.cpu().numpy().view(rays.dtype)
+        b = w_learn.cpu().numpy().view(rays.dtype)
+        if stride == 48:
+            mism = int((a.view(np.uint8).reshape(n, 48) != b.view(np.uint8).reshape(n, 48)).any(1).sum())
+            answered = int((a["tfar"] < 0).sum())
+        else:
+            same = R.hits_equal_bits(a, b)
+            tie = (~same) & (a["tfar"].view(np.uint32) == b["tfar"].view(np.uint32))
+            mism = int((~(same | tie)).sum())
+            answered = int((a["geomID"] != 0xFFFFFFFF).sum())
+        # proposer inference alone
+        treelets = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        api.load().rtcgbProposerPredict(prop.h, ctypes_ptr(pristine.data_ptr()), n, stride,
+                                        ctypes_ptr(treelets.data_ptr()))
+        e0.record(stream)
+        api.load().rtcgbProposerPredict(prop.h, ctypes_ptr(pristine.data_ptr()), n, stride,
+                                        ctypes_ptr(treelets.data_ptr()))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        inf_ms = e0.elapsed_time(e1)
+        out[name] = {"rays": n, "plain_Mrays_per_s": n / (ms_plain * 1e-3) / 1e6,
+                     "learned_Mrays_per_s": n / (ms_learn * 1e-3) / 1e6, "speedup": ms_plain / ms_learn,
+                     "mismatches": mism, "answered_by_proposal": int(q["proposal_hits"]),
+                     "hits_or_occluded": answered, "inference_ms": inf_ms,
+                     "mlp_TFLOPs": MLP_FLOPS_PER_RAY * n / (inf_ms * 1e-3) / 1e12}
+        total_plain += ms_plain
+        total_learned += ms_learn
+        del pristine, w_plain, w_learn, treelets
+    out["speedup_all_rays"] = total_plain / total_learned
+    out["mismatches"] = out["ao"]["mismatches"] + out["bounce"]["mismatches"]
+    prop.release()
+    sc.release()
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_animated(api, dev, torch, scale, frames):
+    """Animated path tracing: the 4M-triangle soup moves every frame (0.002 *
+    sin(2 pi (f/60 + x)) along per-triangle random normals), the BVH is refitted
+    and 4-bounce diffuse paths are traced from a 1920x1080 camera with
+    compaction between bounces, each frame one CUDA graph.  Run twice over the
+    same frames: plain traversal only, and adaptive (learned proposer retrained
+    every 8 frames from the frames' own closest-hit logs; the plain graph runs
+    while the proposer's hit rate is below 20%)."""
+    from rtcgb import workloads as W
+    ntris = max(1000, int(4_000_000 * scale))
+    width, height = max(64, int(1920 * math.sqrt(scale))), max(36, int(1080 * math.sqrt(scale)))
+    verts, idx = W.gaussian_soup(ntris, seed=11)
+    dv = torch.from_numpy(verts).cuda()
+    di = torch.from_numpy(idx.view(np.int32)).cuda()
+    sc = api.Scene(dev)
+    gid = sc.add_mesh_device(dv.data_ptr(), verts.shape[0], di.data_ptr(), ntris, quality=api.RTC_BUILD_QUALITY_REFIT)
+    sc.commit()
+    out = {"workload": f"gaussian soup {ntris} tris animated, {width}x{height} camera, 4 diffuse bounces, {frames} frames",
+           "frame": "one CUDA graph: displacement + refit + camera rays + 4 x (trace, shade, compact)"}
+    images = {}
+    for mode in ("plain", "adaptive"):
+        dv.copy_(torch.from_numpy(verts))
+        pt = api.PathTracer(sc, width, height, bounces=4)
+        pt.animate_soup(gid, amplitude=0.002, seed=14)
+        prop = None
+        if mode == "adaptive":
+            prop = api.Proposer(sc, seed=7)
+            pt.set_proposer(prop)
+        pt.render(0)  # captures the graph(s) outside the measured frames
+        rays = ms = 0.0
+        learned_frames, hit_rates, train_s = 0, [], 0.0
+        use_learned = False
+        launches0 = api.launch_count()
+        for f in range(frames):
+            st = pt.render(f, learned=use_learned)
+            rays += st["rays"]
+            ms += st["frame_ms"]
+            if st["errors"]:
+                raise RuntimeError(f"frame {f}: error flags {st['errors']:#x}")
+            if prop is not None:
+                if st["learned"]:
+                    learned_frames += 1
+                    rate = st["proposal_hits"] / max(1, st["rays"])
+                    hit_rates.append(rate)
+                    use_learned = rate >= 0.2
+                if f % 8 == 0:  # online retraining from this frame's log
+                    t = time.perf_counter()
+                    pt.train_proposer(epochs=2, batch=16384, lr=5e-3)
+                    train_s += time.perf_counter() - t
+                    use_learned = True
+        images[mode] = pt.image()
+        out[mode] = {"Mrays_per_s": rays / (ms * 1e-3) / 1e6, "frames_per_s": frames / (ms * 1e-3),
+                     "ms_per_frame": ms / frames, "rays": int(rays), "gpu_launches": int(api.launch_count() - launches0)}
+        if prop is not None:
+            out[mode].update({"learned_frames": learned_frames,
+                              "mean_proposal_hit_rate": float(np.mean(hit_rates)) if hit_rates else None,
+                              "training_s": train_s})
+            prop.release()
+        pt.release()
+    out["speedup"] = out["adaptive"]["Mrays_per_s"] / out["plain"]["Mrays_per_s"]
+    out["identical_last_image"] = bool((images["plain"].view(np.uint32) == images["adaptive"].view(np.uint32)).all())
+    sc.release()
+    del dv, di
+    torch.cuda.empty_cache()
+    return out
+
+
+def _device_rays(torch, n_cam, n_sph, eye, look, seed):
+    """RTCRayHit records on the device: an n_cam-ray pinhole view (60 degrees)
+    and n_sph uniform-sphere rays from the unit cube."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    side = max(1, int(math.isqrt(n_cam)))
+    n_cam = side * side
+    rec = torch.zeros((n_cam + n_sph, 20), dtype=torch.float32, device="cuda")
+    eye_t = torch.tensor(eye, dtype=torch.float32, device="cuda")
+    w = torch.tensor(look, dtype=torch.float32, device="cuda") - eye_t
+    w = w / w.norm()
+    u = torch.linalg.cross(w, torch.tensor([0.0, 0.0, 1.0], device="cuda"))
+    u = u / u.norm()
+    v = torch.linalg.cross(u, w)
+    th = math.tan(math.radians(30.0))
+    px = (torch.arange(side, device="cuda", dtype=torch.float32) + 0.5) / side * 2 - 1
+    sy, sx = torch.meshgrid(-px, px, indexing="ij")
+    d = w + th * (sx.reshape(-1, 1) * u + sy.reshape(-1, 1) * v)
+    rec[:n_cam, 0:3] = eye_t
+    rec[:n_cam, 4:7] = d
+    rec[n_cam:, 0:3] = torch.rand((n_sph, 3), generator=g, device="cuda")
+    ds = torch.randn((n_sph, 3), generator=g, device="cuda")
+    rec[n_cam:, 4:7] = ds / ds.norm(dim=1, keepdim=True)
+    rec[:, 8] = float("inf")
+    ints = rec.view(torch.int32)
+    ints[:, 9] = -1
+    ints[:, 17:20] = -1
+    return rec
+
+
+def run_batched(api, dev_config, torch, scale, steps, warmup):
+    """512 independent scenes (log-uniform 1k-200k triangles, ~20M in total;
+    even scenes noise heightfields of matching grid size, odd scenes Gaussian
+    soups), 32 rays per triangle (half a pinhole view, half uniform-sphere
+    rays), all built by one commit of a batched scene and traced by one
+    persistent launch.  Build parameters come from the autotuner run on a
+    sample of the scenes."""
+    from rtcgb import autotune
+    from rtcgb import rays as R
+    from rtcgb import workloads as W
+    rng = np.random.default_rng(21)
+    nscenes = max(4, int(round(512 * scale)))
+    counts = np.exp(rng.uniform(math.log(1000), math.log(200_000), nscenes)).astype(np.int64)
+    t = time.perf_counter()
+    meshes, kinds = [], []
+    for k, n in enumerate(counts):
+        if k % 2 == 0:
+            cells = max(8, int(round(math.sqrt(n / 2))))
+            meshes.append(W.heightfield(cells, seed=int(rng.integers(1, 10 ** 6))))
+            kinds.append("heightfield")
+        else:
+            meshes.append(W.gaussian_soup(int(n), seed=int(rng.integers(1, 10 ** 6))))
+            kinds.append("soup")
+    gen_s = time.perf_counter() - t
+    tris = np.array([i.shape[0] for _, i in meshes], np.int64)
+    # autotune on 16 scenes with an eighth of their rays (host copies)
+    sample = list(range(0, nscenes, max(1, nscenes // 16)))[:16]
+    s_parts, s_start = [], [0]
+    for k in sample:
+        n = int(32 * tris[k] // 8)
+        eye, look = ((0.5, -0.5, 0.6), (0.5, 0.5, 0.0)) if kinds[k] == "heightfield" else ((0.5, -1.0, 0.5), (0.5, 0.5, 0.5))
+        r = _device_rays(torch, n // 2, n - n // 2, eye, look, 100 + k).cpu().numpy().view(R.RAYHIT_DTYPE).reshape(-1)
+        s_parts.append(r)
+        s_start.append(s_start[-1] + r.shape[0])
+    best, tuning = autotune.tune([meshes[k] for k in sample], np.concatenate(s_parts), np.array(s_start, np.uint32),
+                                 base_config=dev_config)
+    dev = api.Device(autotune.config_string(best, dev_config).encode())
+    sc = api.Scene(dev)
+    sc.set_batched()
+    for v, i in meshes:
+        sc.add_mesh(v, i)
+    t = time.perf_counter()
+    sc.commit()
+    first_commit_s = time.perf_counter() - t
+    builds = []
+    for _ in range(2):
+        sc.commit()
+        builds.append(sc.build_stats()["build_ms"])
+    bst = sc.build_stats()
+    # rays on the device, batch by batch
+    parts, start = [], [0]
+    for k in range(nscenes):
+        n = int(32 * tris[k])
+        eye, look = ((0.5, -0.5, 0.6), (0.5, 0.5, 0.0)) if kinds[k] == "heightfield" else ((0.5, -1.0, 0.5), (0.5, 0.5, 0.5))
+        r = _device_rays(torch, n // 2, n - n // 2, eye, look, 1000 + k)
+        parts.append(r)
+        start.append(start[-1] + r.shape[0])
+    pristine = torch.cat(parts)
+    del parts
+    start = np.array(start, np.uint32)
+    nrays = int(start[-1])
+    work = torch.empty_like(pristine)
+    kms = []
+    for k in range(warmup + steps):
+        work.copy_(pristine)
+        sc.intersect_batched(None, start, ptr=work.data_ptr(), count=nrays)
+        if k >= warmup:
+            kms.append(api.last_query_stats()["kernel_ms"])
+    kernel_ms = statistics.median(kms)
+    out = {"workload": f"{nscenes} scenes ({kinds.count('heightfield')} heightfields, {kinds.count('soup')} soups), "
+                       f"{int(tris.sum())} tris, {nrays} rays (32 per triangle: half pinhole view, half uniform sphere)",
+           "build": {"device_ms": float(statistics.median(builds)), "first_commit_wall_s": first_commit_s,
+                     "Mtris_per_s": float(bst["num_prims"] / (statistics.median(builds) * 1e-3) / 1e6),
+                     "ploc_iterations": bst["ploc_iterations"], "nodes": bst["num_nodes"]},
+           "trace": {"kernel_ms": kernel_ms, "Mrays_per_s": nrays / (kernel_ms * 1e-3) / 1e6, "launches_per_query": 1},
+           "build_plus_trace_ms": float(statistics.median(builds)) + kernel_ms,
+           "autotune": {"chosen": best, "candidates": tuning, "sample_scenes": len(sample)},
+           "generation_s": gen_s}
+    # exact-hit spot check: the first 4096 rays of 4 scenes against the oracle
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_ffi
+    res = work.cpu().numpy().view(R.RAYHIT_DTYPE).reshape(-1)
+    src = pristine.cpu().numpy().view(R.RAYHIT_DTYPE).reshape(-1)
+    same = total = 0
+    for k in (0, 1, nscenes // 2, nscenes - 1):
+        lo, hi = int(start[k]), min(int(start[k]) + 4096, int(start[k + 1]))
+        orc = oracle_ffi.OracleScene([(k, meshes[k][0], meshes[k][1])])
+        ref = src[lo:hi].copy()
+        orc.intersect(ref)
+        same += int(((ref["geomID"] == res["geomID"][lo:hi]) & (ref["primID"] == res["primID"][lo:hi])).sum())
+        total += hi - lo
+        orc.close()
+    out["parity_sample"] = {"rays": total, "identical_ids": same}
+    sc.release()
+    dev.release()
+    del pristine, work
+    torch.cuda.empty_cache()
+    return out
+
+
+def ctypes_ptr(p):
+    import ctypes
+    return ctypes.c_void_p(p)
+
 
 def run_gpu(args, rank, world):
     import torch
@@ -345,8 +654,18 @@ def run_gpu(args, rank, world):
                       "Mtris_per_s": bst["num_prims"] / (build_ms * 1e-3) / 1e6, "sah": bst["sah"],
                       "nodes": bst["num_nodes"], "depth": bst["depth"], "ploc_iterations": bst["ploc_iterations"],
                       "bvh_MB": bst["bvh_bytes"] / 1e6},
-            "learned": None,
+            "learned": None, "animated": None, "batched": None,
         }
+
+    if rank == 0 and not args.no_learned:
+        del pristine, work, sh_pristine, sh_work
+        torch.cuda.empty_cache()
+        line["learned"] = run_learned(api, dev, torch, stream, args.learned_scale, args.steps, args.warmup)
+    if rank == 0 and not args.no_animated:
+        line["animated"] = run_animated(api, dev, torch, args.animated_scale, args.frames)
+    if rank == 0 and not args.no_batched:
+        line["batched"] = run_batched(api, f"gpu.device={local}{',' + args.config if args.config else ''}", torch,
+                                      args.batched_scale, args.steps, args.warmup)
 
     if rank == 0 and not args.no_cpu:
         base, orc, sample = cpu_rate(verts, idx, rays, args.cpu_seconds, robust=args.robust)

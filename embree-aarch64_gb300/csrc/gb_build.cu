@@ -180,9 +180,13 @@ __device__ __forceinline__ uint64_t spread21(uint32_t x) {
   return v;
 }
 
+// Segmented builds put the geometry slot (< kMaxSegments) in the key's top 12
+// bits, so the sort groups every geometry's primitives.
+constexpr uint32_t kMaxSegments = 4096;
+
 __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                 uint32_t n, BoundsAcc* acc, uint64_t* __restrict__ keys,
-                                                uint32_t* __restrict__ vals, int cube) {
+                                                uint32_t* __restrict__ vals, int cube, int segmented) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t key = ~0ull;
   if (i < n) {
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
         x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
         code |= spread21((uint32_t)x) << (2 - d);
       }
-      key = code;
+      key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 51) | (code >> 12) : code;
     }
     keys[i] = key;
     vals[i] = i;
@@ -355,11 +359,12 @@ constexpr int PLOC_SMALL_THREADS = 1024;
 
 // binary nodes: bnlo[k] = (lo.xyz, left), bnhi[k] = (hi.xyz, right);
 // leaves k < N: left = -1, right = primref index
+// Cluster boxes carry their segment in clo.w (0 unless the build is segmented).
 __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                    const uint32_t* __restrict__ sorted, uint32_t n,
                                                    float4* __restrict__ bnlo, float4* __restrict__ bnhi,
                                                    uint32_t* __restrict__ bncnt, uint32_t* __restrict__ cidx,
-                                                   float4* __restrict__ clo, float4* __restrict__ chi) {
+                                                   float4* __restrict__ clo, float4* __restrict__ chi, int segmented) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t p = sorted[i];
@@ -368,13 +373,14 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
   bnhi[i] = make_float4(b.x, b.y, b.z, __uint_as_float(p));
   bncnt[i] = 1;
   cidx[i] = i;
-  clo[i] = make_float4(a.x, a.y, a.z, 0.f);
+  clo[i] = make_float4(a.x, a.y, a.z, segmented ? a.w : __uint_as_float(0u));
   chi[i] = make_float4(b.x, b.y, b.z, 0.f);
 }
 
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict__ clo, const float4* __restrict__ chi,
                                                         uint32_t n, uint32_t* __restrict__ nn) {
   __shared__ float3 s_lo[PLOC_BLOCK + 2 * PLOC_R], s_hi[PLOC_BLOCK + 2 * PLOC_R];
+  __shared__ uint32_t s_seg[PLOC_BLOCK + 2 * PLOC_R];
   const int base = blockIdx.x * PLOC_BLOCK;
   for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
     const int j = base - PLOC_R + k;
@@ -382,22 +388,24 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict
       const float4 a = clo[j], b = chi[j];
       s_lo[k] = make_float3(a.x, a.y, a.z);
       s_hi[k] = make_float3(b.x, b.y, b.z);
+      s_seg[k] = __float_as_uint(a.w);
     }
   }
   __syncthreads();
   const int i = base + threadIdx.x;
   if (i >= (int)n) return;
   const float3 lo = s_lo[threadIdx.x + PLOC_R], hi = s_hi[threadIdx.x + PLOC_R];
+  const uint32_t seg = s_seg[threadIdx.x + PLOC_R];
   unsigned long long best = ~0ull;
 #pragma unroll 4
   for (int o = -PLOC_R; o <= PLOC_R; o++) {
     const int j = i + o;
-    if (o == 0 || j < 0 || j >= (int)n) continue;
+    if (o == 0 || j < 0 || j >= (int)n || s_seg[threadIdx.x + PLOC_R + o] != seg) continue;
     const float a = half_area(f3min(lo, s_lo[threadIdx.x + PLOC_R + o]), f3max(hi, s_hi[threadIdx.x + PLOC_R + o]));
     const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
     best = key < best ? key : best;
   }
-  nn[i] = (n > 1) ? (uint32_t)best : (uint32_t)i;
+  nn[i] = best != ~0ull ? (uint32_t)best : (uint32_t)i;  // no neighbour in the segment: stays alone
 }
 
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_count(const uint32_t* __restrict__ nn, uint32_t n,
@@ -466,7 +474,7 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const float4* __restri
       return;
     }
     const uint32_t l = cidx[i], r = cidx[j];
-    const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), 0.f);
+    const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), a.w);
     const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
     bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
     bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
@@ -489,12 +497,13 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
                                                                   float4* __restrict__ bnhi,
                                                                   uint32_t* __restrict__ bncnt, uint32_t* root_out,
                                                                   uint32_t* iters_out, uint32_t node_cap,
-                                                                  uint32_t* err) {
+                                                                  uint32_t* err, uint32_t nseg) {
   extern __shared__ unsigned char smem[];
   float3* s_lo = reinterpret_cast<float3*>(smem);
   float3* s_hi = s_lo + PLOC_SMALL;
   uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_hi + PLOC_SMALL);
   uint32_t* s_nn = s_idx + PLOC_SMALL;
+  uint32_t* s_seg = s_nn + PLOC_SMALL;
   __shared__ uint32_t s_w[32];
   __shared__ uint32_t s_tot[2];
   constexpr int EPT = PLOC_SMALL / PLOC_SMALL_THREADS;  // elements per thread (contiguous)
@@ -503,12 +512,14 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
     s_lo[k] = make_float3(a.x, a.y, a.z);
     s_hi[k] = make_float3(b.x, b.y, b.z);
     s_idx[k] = cidx[k];
+    s_seg[k] = __float_as_uint(a.w);
   }
   uint32_t n = n0, node_next = node_next0, iters = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // every round merges at least the globally closest pair, so n0 - 1 rounds
-  // always suffice; the bound only guards against a logic error
+  // every round merges at least the closest pair of each segment that still
+  // has two clusters, so n0 - 1 rounds always suffice; the bound only guards
+  // against a logic error.  A round without merges ends the clustering.
   while (n > 1) {
     if (iters >= PLOC_SMALL) {
       if (threadIdx.x == 0) atomicOr(err, kErrBuild);
@@ -518,15 +529,16 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
     // nearest neighbours
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
       const float3 lo = s_lo[i], hi = s_hi[i];
+      const uint32_t seg = s_seg[i];
       unsigned long long best = ~0ull;
       for (int o = -PLOC_R; o <= PLOC_R; o++) {
         const int j = (int)i + o;
-        if (o == 0 || j < 0 || j >= (int)n) continue;
+        if (o == 0 || j < 0 || j >= (int)n || s_seg[j] != seg) continue;
         const float a = half_area(f3min(lo, s_lo[j]), f3max(hi, s_hi[j]));
         const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
         best = key < best ? key : best;
       }
-      s_nn[i] = (uint32_t)best;
+      s_nn[i] = best != ~0ull ? (uint32_t)best : i;
     }
     __syncthreads();
     // flags for this thread's contiguous chunk
@@ -539,7 +551,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
       fs[e] = fm[e] = 0;
       if (i < n) {
         const uint32_t j = s_nn[i];
-        const bool mutual = s_nn[j] == i;
+        const bool mutual = j != i && s_nn[j] == i;
         fm[e] = mutual && i < j;
         fs[e] = !(mutual && j < i);
       }
@@ -571,7 +583,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
     uint32_t ps = excl & 0xFFFFu, pm = excl >> 16;
     // gather outputs into registers
     float3 olo[EPT], ohi[EPT];
-    uint32_t oidx[EPT], opos[EPT];
+    uint32_t oidx[EPT], opos[EPT], oseg[EPT];
 #pragma unroll
     for (int e = 0; e < EPT; e++) {
       const uint32_t i = i0 + e;
@@ -598,6 +610,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
         olo[e] = lo;
         ohi[e] = hi;
         oidx[e] = id;
+        oseg[e] = s_seg[i];
         opos[e] = ps++;
       }
     }
@@ -608,16 +621,21 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
         s_lo[opos[e]] = olo[e];
         s_hi[opos[e]] = ohi[e];
         s_idx[opos[e]] = oidx[e];
+        s_seg[opos[e]] = oseg[e];
       }
     }
-    node_next += s_tot[1];
+    const uint32_t merged = s_tot[1];
+    node_next += merged;
     n = s_tot[0];
     __syncthreads();
+    if (merged == 0) break;
   }
-  if (threadIdx.x == 0) {
-    *root_out = s_idx[0];
-    *iters_out += iters;
+  // one root per segment (nseg == 1: the single tree's root)
+  for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+    const uint32_t seg = nseg > 1 ? s_seg[k] : 0u;
+    if (seg < nseg) root_out[seg] = s_idx[k];
   }
+  if (threadIdx.x == 0) *iters_out += iters;
 }
 
 // ---------------------------------------------------------------------------
@@ -930,7 +948,11 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(dalloc(&keys_b, total, st));
   GB_CHECK(dalloc(&vals_a, total, st));
   GB_CHECK(dalloc(&vals_b, total, st));
-  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube); note_launches(1);
+  const bool segmented = opt.segmented != 0;
+  const uint32_t nseg = segmented ? (uint32_t)ngeoms : 1u;
+  if (segmented && (uint32_t)ngeoms > kMaxSegments) return cudaErrorInvalidValue;
+  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube, segmented ? 1 : 0);
+  note_launches(1);
   GB_CHECK(cudaGetLastError());
   GB_CHECK(cudaMemcpyAsync(&h_acc, acc, sizeof(BoundsAcc), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
@@ -979,13 +1001,16 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(dalloc(&cidx_a, N, st));
   GB_CHECK(dalloc(&cidx_b, N, st));
   GB_CHECK(dalloc(&nn, N, st));
-  k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, bnlo, bnhi, bncnt, cidx_a, clo_a, chi_a); note_launches(1);
+  k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, bnlo, bnhi, bncnt, cidx_a, clo_a, chi_a,
+                                            segmented ? 1 : 0);
+  note_launches(1);
   uint32_t *bsurv, *bmerge, *d_tot, *d_root, *d_iters;
   const uint32_t maxb = cdiv(N, PLOC_BLOCK);
   GB_CHECK(dalloc(&bsurv, maxb, st));
   GB_CHECK(dalloc(&bmerge, maxb, st));
   GB_CHECK(dalloc(&d_tot, 4, st));
-  GB_CHECK(dalloc(&d_root, 1, st));
+  GB_CHECK(dalloc(&d_root, nseg, st));
+  GB_CHECK(cudaMemsetAsync(d_root, 0xFF, sizeof(uint32_t) * nseg, st));
   GB_CHECK(dalloc(&d_iters, 1, st));
   GB_CHECK(cudaMemsetAsync(d_iters, 0, sizeof(uint32_t), st));
   uint32_t n = N, node_next = N, iters = 0;
@@ -1002,9 +1027,14 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     GB_CHECK(cudaGetLastError());
     GB_CHECK(cudaMemcpyAsync(h_tot, d_tot, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GB_CHECK(cudaStreamSynchronize(st));
-    if (h_tot[1] == 0) {  // cannot happen (the globally closest pair is mutual)
-      cudaFreeHost(h_tot);
-      return cudaErrorUnknown;
+    if (h_tot[1] == 0) {
+      // without segments this cannot happen (the globally closest pair is
+      // mutual); with segments it means every segment is down to one cluster
+      if (!segmented || n > PLOC_SMALL) {
+        cudaFreeHost(h_tot);
+        return cudaErrorUnknown;
+      }
+      break;
     }
     node_next += h_tot[1];
     n = h_tot[0];
@@ -1014,18 +1044,28 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     std::swap(cidx_a, cidx_b);
   }
   {
-    const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 2 * sizeof(uint32_t));
+    const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     GB_CHECK(cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(clo_a, chi_a, cidx_a, n, node_next, bnlo, bnhi, bncnt, d_root,
-                                                      d_iters, nnodes_bin, &acc->pad); note_launches(1);
+                                                      d_iters, nnodes_bin, &acc->pad, nseg); note_launches(1);
     GB_CHECK(cudaGetLastError());
   }
-  uint32_t root = 0, small_iters = 0, berr = 0;
-  GB_CHECK(cudaMemcpyAsync(&root, d_root, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  uint32_t small_iters = 0, berr = 0;
+  std::vector<uint32_t> seg_root(nseg, kInvalidID);
+  GB_CHECK(cudaMemcpyAsync(seg_root.data(), d_root, sizeof(uint32_t) * nseg, cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(&small_iters, d_iters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(&berr, &acc->pad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
-  if (berr || root >= nnodes_bin) {
+  // the first collapse level holds one wide root per non-empty segment, in segment order
+  std::vector<uint32_t> root_items;
+  if (segmented) out->roots.assign(nseg, kInvalidID);
+  for (uint32_t s = 0; s < nseg; s++) {
+    if (seg_root[s] == kInvalidID) continue;
+    if (seg_root[s] >= nnodes_bin) berr = 1;
+    if (segmented) out->roots[s] = (uint32_t)root_items.size();
+    root_items.push_back(seg_root[s]);
+  }
+  if (berr || root_items.empty() || (!segmented && root_items.size() != 1)) {
     cudaFreeHost(h_tot);
     return cudaErrorUnknown;
   }
@@ -1054,8 +1094,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(dalloc(&d_leaves, 1, st));
   GB_CHECK(cudaMemsetAsync(d_sah, 0, sizeof(double), st));
   GB_CHECK(cudaMemsetAsync(d_leaves, 0, sizeof(uint32_t), st));
-  GB_CHECK(cudaMemcpyAsync(items_a, &root, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-  uint32_t nitems = 1, level_base = 0, tri_next = 0, depth = 0;
+  GB_CHECK(cudaMemcpyAsync(items_a, root_items.data(), sizeof(uint32_t) * root_items.size(), cudaMemcpyHostToDevice,
+                           st));
+  uint32_t nitems = (uint32_t)root_items.size(), level_base = 0, tri_next = 0, depth = 0;
   std::vector<uint32_t> level_start;
   while (nitems > 0) {
     level_start.push_back(level_base);
@@ -1355,6 +1396,48 @@ cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   stats->depth = bvh->depth;
   stats->refit = 1;
   return cudaSuccess;
+}
+
+cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& bvh, RefitScratch* out,
+                          cudaStream_t st) {
+  *out = RefitScratch{};
+  if (bvh.num_nodes == 0 || bvh.level_start.size() < 2) return cudaErrorInvalidValue;
+  uint32_t nslots = 0;
+  for (int g = 0; g < ngeoms; g++) nslots = std::max(nslots, h_geoms[g].geomID + 1);
+  std::vector<uint32_t> slot_of(std::max(nslots, 1u), kInvalidID);
+  for (int g = 0; g < ngeoms; g++) slot_of[h_geoms[g].geomID] = (uint32_t)g;
+  out->nslots = (uint32_t)slot_of.size();
+  GB_CHECK(cudaMalloc(&out->d_geoms, sizeof(GeomDesc) * std::max(ngeoms, 1)));
+  GB_CHECK(cudaMalloc(&out->d_slot, sizeof(uint32_t) * slot_of.size()));
+  GB_CHECK(cudaMalloc(&out->d_err, sizeof(uint32_t)));
+  GB_CHECK(cudaMalloc(&out->node_box, sizeof(float) * 6 * bvh.num_nodes));
+  GB_CHECK(cudaMalloc(&out->d_sah, sizeof(double)));
+  GB_CHECK(cudaMemcpyAsync(out->d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
+  GB_CHECK(cudaMemcpyAsync(out->d_slot, slot_of.data(), sizeof(uint32_t) * slot_of.size(), cudaMemcpyHostToDevice, st));
+  GB_CHECK(cudaMemsetAsync(out->d_err, 0, sizeof(uint32_t), st));
+  return cudaStreamSynchronize(st);
+}
+
+cudaError_t refit_enqueue(const DeviceBVH& bvh, const RefitScratch& s, cudaStream_t st) {
+  GB_CHECK(cudaMemsetAsync(s.d_sah, 0, sizeof(double), st));
+  k_refit_tris<<<cdiv(bvh.num_tris, 256), 256, 0, st>>>(s.d_geoms, s.d_slot, s.nslots, bvh.tris, bvh.num_tris,
+                                                        bvh.robust, s.d_err);
+  note_launches(1);
+  for (size_t l = bvh.level_start.size() - 1; l-- > 0;) {
+    const uint32_t b = bvh.level_start[l], e = bvh.level_start[l + 1];
+    if (e <= b) continue;
+    k_refit_level<<<cdiv(e - b, 128), 128, 0, st>>>(s.d_geoms, s.d_slot, s.nslots, bvh.tris, bvh.num_tris, bvh.nodes,
+                                                   bvh.num_nodes, s.node_box, b, e, s.d_sah, s.d_err);
+    note_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+void refit_release(RefitScratch* s) {
+  void* ptrs[] = {s->d_geoms, s->d_slot, s->d_err, s->node_box, s->d_sah};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  *s = RefitScratch{};
 }
 
 void free_bvh(DeviceBVH* b) {

@@ -18,6 +18,23 @@ void free_bvh(DeviceBVH* b);
 cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* bvh, BuildStats* stats,
                       bool* fallback);
 
+// Refit split for work captured in CUDA graphs: refit_prepare uploads the
+// geometry table once (synchronous); refit_enqueue only launches the refit
+// kernels on `st` (no allocation, no synchronisation; errors accumulate in
+// d_err until the caller reads it).  The BVH's host-side bounds are not updated.
+struct RefitScratch {
+  GeomDesc* d_geoms = nullptr;
+  uint32_t* d_slot = nullptr;
+  uint32_t nslots = 0;
+  uint32_t* d_err = nullptr;
+  float* node_box = nullptr;
+  double* d_sah = nullptr;
+};
+cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& bvh, RefitScratch* out,
+                          cudaStream_t st);
+cudaError_t refit_enqueue(const DeviceBVH& bvh, const RefitScratch& s, cudaStream_t st);
+void refit_release(RefitScratch* s);
+
 // Stable LSD radix sort of 64-bit keys with 32-bit values (device buffers).
 cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st);
 

@@ -76,6 +76,7 @@ struct DeviceBVH {
   float lo[3] = {0, 0, 0};   // geometry bounds (empty scene: +inf / -inf)
   float hi[3] = {0, 0, 0};
   std::vector<uint32_t> level_start;  // first node of each breadth-first level + end (for refit)
+  std::vector<uint32_t> roots;  // segmented builds: root node of each geometry slot (kInvalidID: empty)
 };
 
 // Builder options (device config keys gpu.leaf_max=1..4, gpu.morton=axis|cube).
@@ -83,6 +84,7 @@ struct BuildOptions {
   int leaf_max = kLeafMaxDefault;
   int morton_cube = 0;  // 1: one Morton scale for all axes (gpu.morton=cube)
   int robust = 0;       // RTC_SCENE_FLAG_ROBUST: triangle records hold v0, v1, v2
+  int segmented = 0;    // one tree per geometry slot (batched scenes), roots at the first level
 };
 
 // Build statistics reported through the extension API.
@@ -99,6 +101,7 @@ struct TraceCounters {
   unsigned long long nodes;
   unsigned long long tris;
   unsigned long long rays;
+  unsigned long long proposal_hits;  // seeded queries: rays answered inside a proposed subtree
 };
 
 // Device-side error flags (bit mask).

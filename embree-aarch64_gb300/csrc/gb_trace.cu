@@ -233,19 +233,29 @@ __device__ __forceinline__ void load_ray(const char* p, TRay& r, float& tfar) {
 // (2) tests its pending triangles -- unless few lanes of the warp have
 // triangle work, in which case the group is pushed and tested later -- and
 // (3) pops the stack when its group is exhausted.
-template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST>
+//
+// SEEDED: the ray's stack starts as [root, seed3, seed2, seed1] with seed0 as
+// the current group, so the proposed subtrees are searched first and the whole
+// tree afterwards.  The answer is the plain traversal's: an any-hit ray that
+// hits inside a proposed subtree is occluded in the whole tree, and a closest
+// hit found there only lowers tfar before the full search, which still tests
+// every triangle whose distance can be the minimum.  `seeding` stays set until
+// the root group is popped; a ray whose final hit was found while it was set
+// counts as a proposal hit.
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED>
 __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
   const Ctx c{P.nodes, P.tris, P.err, P.max_iters, P.num_nodes, P.num_tris};
   const int lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t nrays = P.nrays_ptr ? *P.nrays_ptr : P.nrays;
   uint2 stack[kStackSize];
   int sp = 0;
-  bool active = false, exhausted = false;
+  bool active = false, exhausted = false, seeding = false;
   char* rec = nullptr;
   TRay r;
   float t_best = 0.f, hu = 0.f, hv = 0.f;
-  uint32_t hit_tri = kInvalidID, g_base = 0, g_bits = 0, t_base = 0, t_bits = 0, iters = 0;
-  unsigned long long n_nodes = 0, n_tris = 0, n_rays = 0;
+  uint32_t hit_tri = kInvalidID, seed_tri = kInvalidID, g_base = 0, g_bits = 0, t_base = 0, t_bits = 0, iters = 0;
+  unsigned long long n_nodes = 0, n_tris = 0, n_rays = 0, n_prop = 0;
   for (;;) {
     // ---- refill idle lanes
     const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
@@ -254,26 +264,51 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(P.ray_counter, (unsigned)__popc(idle));
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
-      if (base + __popc(idle) >= P.nrays) exhausted = true;
+      if (base + __popc(idle) >= nrays) exhausted = true;
       if (!active) {
         const uint32_t rid = base + __popc(idle & lt_mask);
-        if (rid < P.nrays) {
+        if (rid < nrays) {
           rec = P.rays + (uint64_t)rid * P.stride;
           float tfar;
           load_ray<ALIGNED>(rec, r, tfar);
           // stream semantics: only tnear <= tfar rays are traced; any-hit also
           // skips already occluded rays (bvh_intersector_stream_filters.cpp:75)
           const bool valid = ANYHIT ? ((r.tnear <= tfar) && !(tfar < 0.0f)) : (r.tnear <= tfar);
-          if (valid) {
+          // batched queries: the ray's batch (binary search) gives its tree's root
+          uint32_t root = 0;
+          if (P.batch_root) {
+            uint32_t lo = 0, hi = P.nbatches;
+            while (hi - lo > 1) {
+              const uint32_t mid = (lo + hi) >> 1;
+              if (__ldg(P.batch_start + mid) <= rid) lo = mid; else hi = mid;
+            }
+            root = __ldg(P.batch_root + lo);
+          }
+          if (valid && root < c.num_nodes) {
             init_ray(r);
             t_best = tfar;
             hit_tri = kInvalidID;
-            g_base = 0;
+            g_base = root;
             g_bits = (1u << (24 + r.oct)) | 1u;  // virtual group: the root as internal slot 0
             t_bits = 0;
             sp = 0;
             iters = 0;
             active = true;
+            if (SEEDED) {
+              // a virtual group (n, root bits) visits node n alone
+              const uint4 s4 = P.seeds[rid];
+              const uint32_t sd[4] = {s4.x, s4.y, s4.z, s4.w};
+              stack[sp++] = make_uint2(g_base, g_bits);
+              seed_tri = kInvalidID;
+              seeding = false;
+              for (int q = 3; q >= 0; q--) {
+                if (sd[q] == 0u || sd[q] >= c.num_nodes) continue;
+                if (seeding) stack[sp++] = make_uint2(g_base, g_bits);
+                g_base = sd[q];
+                seeding = true;
+              }
+              if (!seeding) sp = 0;  // no proposal: plain traversal from the root
+            }
             if (COUNT) n_rays++;
           }
         }
@@ -327,6 +362,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
         if (pluecker(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org,
                      r.dir, r.tnear, t_best, U, V, UVW, t)) {
           hit_tri = ti;
+          if (SEEDED && seeding) seed_tri = ti;
           if (ANYHIT) { done = true; t_bits = 0; break; }
           // PlueckerHitM::finalize: u,v = U,V * rcp(UVW), 0 when |UVW| < 1e-18
           const float rcp = fabsf(UVW) < kMinRcpInput ? 0.0f : __frcp_rn(UVW);
@@ -339,6 +375,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
         if (moeller(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org, r.dir,
                     r.tnear, t_best, U, V, T, absDen)) {
           hit_tri = ti;
+          if (SEEDED && seeding) seed_tri = ti;
           if (ANYHIT) { done = true; t_bits = 0; break; }
           const float rcp = __frcp_rn(absDen);
           t_best = __fmul_rn(T, rcp);
@@ -353,12 +390,14 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
         const uint2 e = stack[--sp];
         if (e.x & kTriGroup) { t_base = e.x & ~kTriGroup; t_bits = e.y; g_bits = 0; }
         else { g_base = e.x; g_bits = e.y; }
+        if (SEEDED && sp == 0) seeding = false;  // the root group: proposals are done
       } else {
         done = true;
       }
     }
     if (active && done) {
       active = false;
+      if (SEEDED && hit_tri != kInvalidID && hit_tri == seed_tri) n_prop++;
       if (hit_tri != kInvalidID) {
         if (ANYHIT) {
           *reinterpret_cast<float*>(rec + 32) = -INFINITY;
@@ -383,6 +422,11 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
       }
     }
   }
+  if (SEEDED) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n_prop += __shfl_xor_sync(0xFFFFFFFFu, n_prop, o);
+    if (lane == 0 && n_prop) atomicAdd(&P.counters->proposal_hits, n_prop);
+  }
   if (COUNT) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -398,14 +442,14 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
   }
 }
 
-template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST>
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED = false>
 static cudaError_t launch_one(const TraceParams& P, cudaStream_t st) {
   static int blocks_per_sm = -1, num_sms = 0;
   if (blocks_per_sm < 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED, ROBUST>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED>,
                                                   TRACE_THREADS, 0);
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
@@ -413,12 +457,17 @@ static cudaError_t launch_one(const TraceParams& P, cudaStream_t st) {
   uint64_t grid = (uint64_t)num_sms * blocks_per_sm;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
-  k_trace<ANYHIT, COUNT, ALIGNED, ROBUST><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
+  k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
   return cudaGetLastError();
 }
 
 template <bool ANYHIT, bool COUNT>
 static cudaError_t launch_variant(const TraceParams& P, bool aligned, cudaStream_t st) {
+  // seeded queries: 16-byte aligned records of non-robust scenes (checked by the caller)
+  if (P.seeds) {
+    if (!aligned || P.robust) return cudaErrorInvalidValue;
+    return launch_one<ANYHIT, COUNT, true, false, true>(P, st);
+  }
   if (P.robust) return aligned ? launch_one<ANYHIT, COUNT, true, true>(P, st) : launch_one<ANYHIT, COUNT, false, true>(P, st);
   return aligned ? launch_one<ANYHIT, COUNT, true, false>(P, st) : launch_one<ANYHIT, COUNT, false, false>(P, st);
 }

@@ -12,11 +12,17 @@ struct TraceParams {
   uint32_t nrays;
   unsigned int* ray_counter;  // zeroed before launch; persistent warps fetch rays from it
   unsigned int* err;          // error flags (kErr*)
-  TraceCounters* counters;    // counting variant only
+  TraceCounters* counters;    // counting variant; proposal_hits also in the seeded variant
   uint32_t max_iters;         // per-ray loop bound
   uint32_t num_nodes;         // bounds of the node and triangle arrays
   uint32_t num_tris;
   int robust;                 // Pluecker test on (v0, v1, v2) records
+  const unsigned int* nrays_ptr;  // optional: the ray count is read from device memory
+  const uint4* seeds;         // optional: per ray up to four subtree roots (node indices,
+                              // kInvalidID = none) traversed before the root
+  const uint32_t* batch_start;  // optional (segmented BVHs): rays [batch_start[b], batch_start[b+1])
+  const uint32_t* batch_root;   //   start at node batch_root[b] (kInvalidID: the batch hits nothing)
+  uint32_t nbatches;
 };
 
 // Launches the persistent closest-hit (anyhit = false) or any-hit kernel.

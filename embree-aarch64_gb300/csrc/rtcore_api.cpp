@@ -23,6 +23,7 @@
 #include <cstring>
 #include <exception>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <set>
 #include <string>
@@ -34,6 +35,8 @@
 #include "gb_build.h"
 #include "gb_common.h"
 #include "gb_launch.h"
+#include "gb_learned.h"
+#include "gb_paths.h"
 #include "gb_trace.h"
 
 namespace {
@@ -352,6 +355,19 @@ struct ThreadCtx {
       cuda_ok(cudaEventCreateWithFlags(&ev_tr[i], cudaEventDisableTiming), "event");
     }
   }
+  uint4* seeds = nullptr;   // learned queries: per-ray proposals
+  size_t seeds_cap = 0;
+  uint4* seed_buffer(size_t n) {
+    if (n > seeds_cap) {
+      if (seeds) cudaFree(seeds);
+      seeds = nullptr;
+      seeds_cap = 0;
+      const size_t want = std::max(n, seeds_cap * 2);
+      cuda_ok(cudaMalloc((void**)&seeds, want * sizeof(uint4)), "cudaMalloc proposals");
+      seeds_cap = want;
+    }
+    return seeds;
+  }
   char* buffer(size_t bytes) {
     if (bytes > cap) {
       if (dbuf) cudaFree(dbuf);
@@ -365,6 +381,7 @@ struct ThreadCtx {
   }
   ~ThreadCtx() {
     if (dbuf) cudaFree(dbuf);
+    if (seeds) cudaFree(seeds);
     if (dscratch) cudaFree(dscratch);
     if (hscratch) cudaFreeHost(hscratch);
     if (own) cudaStreamDestroy(own);
@@ -409,11 +426,17 @@ struct Scene : RefCounted {
   };
   std::vector<SigEntry> built_sig;
   bool built_robust = false;
+  uint64_t build_serial = 0;  // counts full builds (a refit keeps the BVH's structure)
+  std::vector<gb::GeomDesc> descs;  // geometry table of the committed BVH (device buffers)
+  bool batched = false;             // rtcgbSetSceneBatched: one tree per geometry
+  uint32_t* d_roots = nullptr;      // batched BVH: root node per geometry ID (device)
+  uint32_t nroots = 0;
 
   explicit Scene(Device* d) : device(d) { device->inc(); }
   ~Scene() override {
     for (Geometry* g : geoms)
       if (g) g->dec();
+    if (d_roots) cudaFree(d_roots);
     gb::free_bvh(&bvh);
     device->dec();
   }
@@ -492,6 +515,7 @@ struct Scene : RefCounted {
       cuda_ok(gb::refit_bvh(descs.data(), (int)descs.size(), st, &bvh, &bs, &fallback), "rtcCommitScene (refit)");
       if (!fallback) {
         stats = bs;
+        this->descs = descs;
         if (progress) progress(progress_ptr, 1.0);
         return;
       }
@@ -503,9 +527,25 @@ struct Scene : RefCounted {
     gb::BuildStats bs;
     gb::BuildOptions opt = device->build_opt;
     opt.robust = robust;
+    opt.segmented = batched ? 1 : 0;
     cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, opt, &bvh, &bs), "rtcCommitScene");
+    if (d_roots) cudaFree(d_roots);
+    d_roots = nullptr;
+    nroots = 0;
+    if (batched) {
+      // root of every geometry ID (descs are in slot order; bvh.roots is per slot)
+      std::vector<uint32_t> by_id(geoms.size(), gb::kInvalidID);
+      for (size_t k = 0; k < descs.size() && k < bvh.roots.size(); k++) by_id[descs[k].geomID] = bvh.roots[k];
+      nroots = (uint32_t)by_id.size();
+      cuda_ok(cudaMalloc((void**)&d_roots, std::max<size_t>(1, by_id.size()) * sizeof(uint32_t)), "cudaMalloc roots");
+      cuda_ok(cudaMemcpyAsync(d_roots, by_id.data(), by_id.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+              "roots");
+      cuda_ok(cudaStreamSynchronize(st), "roots");
+    }
     stats = bs;
     committed = true;
+    build_serial++;
+    this->descs = descs;
     built_sig = sig;
     built_robust = robust;
     if (progress) progress(progress_ptr, 1.0);
@@ -519,10 +559,37 @@ struct Scene : RefCounted {
 };
 
 // ---------------------------------------------------------------------------
+// learned proposer
+// ---------------------------------------------------------------------------
+
+struct ProposerObj : RefCounted {
+  Scene* scene;
+  uint64_t build_serial;
+  gb::Proposer net;
+  std::vector<uint32_t> roots, record_treelet;
+  std::mutex mtx;
+  explicit ProposerObj(Scene* s) : scene(s), build_serial(s->build_serial) { scene->inc(); }
+  ~ProposerObj() override {
+    scene->device->set_current();
+    net.release();
+    scene->dec();
+  }
+  // usable for queries on the scene as currently built
+  bool current() const { return scene->committed && build_serial == scene->build_serial && !scene->bvh.robust; }
+};
+
+// ---------------------------------------------------------------------------
 // queries
 // ---------------------------------------------------------------------------
 
-void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit, size_t recsize) {
+// Batched queries on a segmented BVH: rays [start[b], start[b+1]) query geometry b.
+struct BatchArgs {
+  const uint32_t* start = nullptr;  // caller's array (host or device), nbatches + 1 entries
+  uint32_t nbatches = 0;
+};
+
+void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit, size_t recsize,
+               ProposerObj* prop = nullptr, const BatchArgs* batch = nullptr) {
   VERIFY_HANDLE(scene);
   if (!scene->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
   if (M == 0) return;
@@ -533,6 +600,15 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   c.last = RTCGBQueryStats{};
   const gb::DeviceBVH& bvh = scene->bvh;
   if (bvh.num_nodes == 0) return;  // empty scene: nothing is hit
+  if (scene->batched != (batch != nullptr))
+    fail(RTC_ERROR_INVALID_OPERATION, scene->batched ? "batched scene: use rtcgbIntersect1MBatched / rtcgbOccluded1MBatched"
+                                                     : "not a batched scene (rtcgbSetSceneBatched)");
+  if (prop && scene->batched) fail(RTC_ERROR_INVALID_OPERATION, "the proposer does not support batched scenes");
+  if (prop && prop->scene != scene) fail(RTC_ERROR_INVALID_ARGUMENT, "proposer belongs to another scene");
+  // seeded traversal needs 16-byte aligned records; otherwise the plain one runs
+  if (prop && (!prop->current() || (stride % 16) != 0)) prop = nullptr;
+  std::unique_lock<std::mutex> prop_lock;
+  if (prop) prop_lock = std::unique_lock<std::mutex>(prop->mtx);
   Device* dev = scene->device;
   dev->set_current();
   c.ensure(dev->cuda_device);
@@ -555,14 +631,46 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   P.num_nodes = bvh.num_nodes;
   P.num_tris = bvh.num_tris;
   P.robust = bvh.robust;
+  // batched: the batch boundaries on the device, validated on the host
+  std::unique_ptr<uint32_t, void (*)(uint32_t*)> d_start(nullptr, [](uint32_t* p) { if (p) cudaFree(p); });
+  if (batch) {
+    if (!batch->start || batch->nbatches == 0 || batch->nbatches > scene->nroots)
+      fail(RTC_ERROR_INVALID_ARGUMENT, "invalid batches");
+    std::vector<uint32_t> hs(batch->nbatches + 1);
+    cuda_ok(cudaMemcpy(hs.data(), batch->start, hs.size() * sizeof(uint32_t), cudaMemcpyDefault), "batches");
+    if (hs[0] != 0 || hs.back() != M) fail(RTC_ERROR_INVALID_ARGUMENT, "batches must cover the rays exactly");
+    for (size_t b = 1; b < hs.size(); b++)
+      if (hs[b] < hs[b - 1]) fail(RTC_ERROR_INVALID_ARGUMENT, "batch boundaries must not decrease");
+    uint32_t* p = nullptr;
+    cuda_ok(cudaMalloc((void**)&p, hs.size() * sizeof(uint32_t)), "cudaMalloc batches");
+    d_start.reset(p);
+    cuda_ok(cudaMemcpyAsync(p, hs.data(), hs.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st), "batches");
+    P.batch_start = p;
+    P.batch_root = scene->d_roots;
+    P.nbatches = batch->nbatches;
+  }
   cuda_ok(cudaEventRecord(c.e0, st), "event");
   cuda_ok(cudaMemsetAsync(c.dscratch, 0, 64, st), "memset");
   unsigned launches = 1;
   const uint32_t kChunk = 1u << 21;  // rays per pipeline stage
+  // learned queries: proposals for every ray, then the seeded traversal
+  auto propose = [&](gb::TraceParams& Pq) {
+    if (!prop) return;
+    uint4* seeds = c.seed_buffer(Pq.nrays);
+    cuda_ok(prop->net.predict(Pq.rays, stride, Pq.nrays, seeds, nullptr, st), "proposer inference");
+    Pq.seeds = seeds;
+    Pq.max_iters = 8 * bvh.num_nodes + 64;  // proposed subtrees are searched again by the full search
+    launches++;
+  };
+  if (prop && ((uintptr_t)rays % 16) != 0 && (on_device || direct)) {
+    prop = nullptr;
+    prop_lock = std::unique_lock<std::mutex>();
+  }
   if (on_device || direct) {
     P.rays = (char*)rays;
     P.nrays = M;
     cuda_ok(cudaEventRecord(c.e1, st), "event");
+    propose(P);
     cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
     launches++;
     cuda_ok(cudaEventRecord(c.e2, st), "event");
@@ -570,7 +678,7 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
       c.last.h2d_bytes = (unsigned long long)M * 48;                     // ray records read by the kernel
       c.last.d2h_bytes = (unsigned long long)M * (anyhit ? 4 : 36);      // at most tfar (+ hit) written
     }
-  } else if (dev->host_mode >= 1 && M > kChunk) {
+  } else if (dev->host_mode >= 1 && M > kChunk && !prop && !batch) {
     // chunked pipeline: H2D of chunk i+1 and D2H of chunk i-1 overlap the trace of chunk i
     c.ensure_pipeline();
     char* d_rays = c.buffer(span);
@@ -610,6 +718,7 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
     P.rays = d_rays;
     P.nrays = M;
     cuda_ok(cudaEventRecord(c.e1, st), "event");
+    propose(P);
     cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
     launches++;
     cuda_ok(cudaEventRecord(c.e2, st), "event");
@@ -626,12 +735,13 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   cudaEventElapsedTime(&t_ms, c.e0, c.e3);
   c.last.kernel_ms = k_ms;
   c.last.total_ms = t_ms;
+  const gb::TraceCounters* tc = reinterpret_cast<const gb::TraceCounters*>(c.hscratch + 2);
   if (c.counting) {
-    const gb::TraceCounters* tc = reinterpret_cast<const gb::TraceCounters*>(c.hscratch + 2);
     c.last.nodes = tc->nodes;
     c.last.tris = tc->tris;
     c.last.rays = tc->rays;
   }
+  if (prop) c.last.proposal_hits = tc->proposal_hits;
   const unsigned err = c.hscratch[1];
   if (err & gb::kErrStackOverflow) fail(RTC_ERROR_UNKNOWN, "traversal stack overflow");
   if (err & gb::kErrIterationLimit) fail(RTC_ERROR_UNKNOWN, "traversal iteration limit reached");
@@ -648,6 +758,119 @@ void run_query_pointers(Scene* scene, Rec** recs, unsigned M, bool anyhit) {
   for (unsigned i = 0; i < M; i++) tmp[i] = *recs[i];
   run_query(scene, tmp.data(), M, sizeof(Rec), anyhit, sizeof(Rec));
   for (unsigned i = 0; i < M; i++) *recs[i] = tmp[i];
+}
+
+// SOA layouts (packets RTCRayHit4/8/16, RTCRayHitN streams, RTCRayHitNp pointer streams).
+// Field numbering follows the SOA order of include/embree3/rtcore_ray.h:222-248: ray fields
+// 0..11, hit fields 12..19 (Ng_x, Ng_y, Ng_z, u, v, primID, geomID, instID[0]).
+enum SoaField {
+  kOrgX, kOrgY, kOrgZ, kTnear, kDirX, kDirY, kDirZ, kTime, kTfar, kMask, kId, kFlags,
+  kNgX, kNgY, kNgZ, kU, kV, kPrimID, kGeomID, kInstID, kNumSoaFields
+};
+
+// The lanes are gathered into packed AOS records, traced by the stream path and scattered
+// back.  Lane selection is the reference's: valid[i] == -1 for packets
+// (kernels/bvh/bvh_intersector_hybrid.cpp:131, 623) and tnear <= tfar for every layout
+// (kernels/common/ray.h:622-627, 922-927); a missing tnear reads as 0, a missing
+// time as 0, missing mask/id/flags as all ones (ray.h:938-980).  A closest-hit lane is
+// written only when it hit something, an occlusion lane only when it is occluded
+// (ray.h:903-911, 988-1010), and null Ng/instID pointers are skipped.
+template <typename Addr>
+void run_query_soa(Scene* scene, size_t count, const int* valid, bool anyhit, Addr addr) {
+  VERIFY_HANDLE(scene);
+  if (count == 0) return;
+  if (count > 0xffffffffull) fail(RTC_ERROR_INVALID_ARGUMENT, "too many rays");
+  auto f32 = [&](int f, size_t i, float dflt) {
+    const float* p = (const float*)addr(f, i);
+    return p ? *p : dflt;
+  };
+  auto u32 = [&](int f, size_t i, unsigned dflt) {
+    const unsigned* p = (const unsigned*)addr(f, i);
+    return p ? *p : dflt;
+  };
+  std::vector<uint32_t> lane;
+  lane.reserve(count);
+  for (size_t i = 0; i < count; i++) {
+    if (valid && valid[i] != -1) continue;
+    if (!(f32(kTnear, i, 0.0f) <= f32(kTfar, i, 0.0f))) continue;
+    lane.push_back((uint32_t)i);
+  }
+  if (lane.empty()) return;
+  const unsigned M = (unsigned)lane.size();
+  auto load_ray = [&](RTCRay& r, size_t i) {
+    r.org_x = f32(kOrgX, i, 0.0f); r.org_y = f32(kOrgY, i, 0.0f); r.org_z = f32(kOrgZ, i, 0.0f);
+    r.tnear = f32(kTnear, i, 0.0f);
+    r.dir_x = f32(kDirX, i, 0.0f); r.dir_y = f32(kDirY, i, 0.0f); r.dir_z = f32(kDirZ, i, 0.0f);
+    r.time = f32(kTime, i, 0.0f);
+    r.tfar = f32(kTfar, i, 0.0f);
+    r.mask = u32(kMask, i, 0xffffffffu); r.id = u32(kId, i, 0xffffffffu); r.flags = u32(kFlags, i, 0xffffffffu);
+  };
+  if (anyhit) {
+    std::vector<RTCRay> tmp(M);
+    for (unsigned j = 0; j < M; j++) load_ray(tmp[j], lane[j]);
+    run_query(scene, tmp.data(), M, sizeof(RTCRay), true, sizeof(RTCRay));
+    for (unsigned j = 0; j < M; j++)
+      if (tmp[j].tfar < 0.0f) *(float*)addr(kTfar, lane[j]) = tmp[j].tfar;
+    return;
+  }
+  std::vector<RTCRayHit> tmp(M);
+  for (unsigned j = 0; j < M; j++) {
+    load_ray(tmp[j].ray, lane[j]);
+    tmp[j].hit.geomID = RTC_INVALID_GEOMETRY_ID;
+    tmp[j].hit.primID = RTC_INVALID_GEOMETRY_ID;
+    tmp[j].hit.instID[0] = RTC_INVALID_GEOMETRY_ID;
+  }
+  run_query(scene, tmp.data(), M, sizeof(RTCRayHit), false, sizeof(RTCRayHit));
+  for (unsigned j = 0; j < M; j++) {
+    const RTCRayHit& h = tmp[j];
+    if (h.hit.geomID == RTC_INVALID_GEOMETRY_ID) continue;
+    const size_t i = lane[j];
+    const float fv[6] = {h.ray.tfar, h.hit.Ng_x, h.hit.Ng_y, h.hit.Ng_z, h.hit.u, h.hit.v};
+    const int ff[6] = {kTfar, kNgX, kNgY, kNgZ, kU, kV};
+    for (int k = 0; k < 6; k++)
+      if (float* p = (float*)addr(ff[k], i)) *p = fv[k];
+    const unsigned uv[3] = {h.hit.primID, h.hit.geomID, h.hit.instID[0]};
+    const int uf[3] = {kPrimID, kGeomID, kInstID};
+    for (int k = 0; k < 3; k++)
+      if (unsigned* p = (unsigned*)addr(uf[k], i)) *p = uv[k];
+  }
+}
+
+// packets of K lanes / NM streams: field f of lane i of packet p sits at
+// base + p * stride + (f * K + i) * 4 (rtcore_ray.h:222-248)
+void run_query_packets(Scene* scene, void* base, unsigned K, size_t packets, size_t stride, const int* valid,
+                       bool anyhit) {
+  if (!base) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  if (is_device_pointer(base)) fail(RTC_ERROR_INVALID_ARGUMENT, "ray packets must be in host memory");
+  if (packets > 1 && stride < (size_t)(anyhit ? 12 : 20) * K * 4)
+    fail(RTC_ERROR_INVALID_ARGUMENT, "byteStride smaller than one ray packet");
+  char* b = (char*)base;
+  run_query_soa(scene, (size_t)K * packets, valid, anyhit, [=](int f, size_t r) -> void* {
+    const size_t p = r / K, i = r % K;
+    return b + p * stride + ((size_t)f * K + i) * 4;
+  });
+}
+
+// pointer-SOA streams (rtcore_ray.h:170-213); optional fields may be null
+void run_query_pointer_soa(Scene* scene, const RTCRayHitNp* rh, const RTCRayNp* ray, unsigned N, bool anyhit) {
+  if (!rh && !ray) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  if (N == 0) return;
+  const RTCRayNp& r = rh ? rh->ray : *ray;
+  void* fld[kNumSoaFields] = {r.org_x, r.org_y, r.org_z, r.tnear, r.dir_x, r.dir_y, r.dir_z, r.time,
+                              r.tfar,  r.mask,  r.id,    r.flags};
+  if (rh) {
+    const RTCHitNp& h = rh->hit;
+    void* hf[8] = {h.Ng_x, h.Ng_y, h.Ng_z, h.u, h.v, h.primID, h.geomID, h.instID[0]};
+    for (int k = 0; k < 8; k++) fld[kNgX + k] = hf[k];
+    if (!h.u || !h.v || !h.primID || !h.geomID) fail(RTC_ERROR_INVALID_ARGUMENT, "missing hit arrays");
+  }
+  if (!r.org_x || !r.org_y || !r.org_z || !r.dir_x || !r.dir_y || !r.dir_z || !r.tfar)
+    fail(RTC_ERROR_INVALID_ARGUMENT, "missing ray arrays");
+  for (int k = 0; k < kNumSoaFields; k++)
+    if (fld[k] && is_device_pointer(fld[k])) fail(RTC_ERROR_INVALID_ARGUMENT, "ray arrays must be in host memory");
+  run_query_soa(scene, N, nullptr, anyhit, [&](int f, size_t i) -> void* {
+    return fld[f] ? (char*)fld[f] + i * 4 : nullptr;
+  });
 }
 
 }  // namespace
@@ -1207,6 +1430,76 @@ RTC_API void rtcOccluded1Mp(RTCScene hs, struct RTCIntersectContext* ctx, struct
   API_END(s ? s->device : nullptr)
 }
 
+#define GB_PACKET_QUERY(NAME, REC, K, ANYHIT)                                                     \
+  RTC_API void NAME(const int* valid, RTCScene hs, struct RTCIntersectContext* ctx, struct REC* r) { \
+    Scene* s = (Scene*)hs;                                                                         \
+    API_BEGIN                                                                                      \
+    (void)ctx;                                                                                     \
+    VERIFY_HANDLE(hs);                                                                             \
+    if (!valid) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid valid mask");                            \
+    run_query_packets(s, r, K, 1, sizeof(struct REC), valid, ANYHIT);                              \
+    API_END(s ? s->device : nullptr)                                                               \
+  }
+GB_PACKET_QUERY(rtcIntersect4, RTCRayHit4, 4, false)
+GB_PACKET_QUERY(rtcIntersect8, RTCRayHit8, 8, false)
+GB_PACKET_QUERY(rtcIntersect16, RTCRayHit16, 16, false)
+GB_PACKET_QUERY(rtcOccluded4, RTCRay4, 4, true)
+GB_PACKET_QUERY(rtcOccluded8, RTCRay8, 8, true)
+GB_PACKET_QUERY(rtcOccluded16, RTCRay16, 16, true)
+#undef GB_PACKET_QUERY
+
+RTC_API void rtcIntersectNM(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRayHitN* rayhit, unsigned int N,
+                            unsigned int M, size_t byteStride) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  VERIFY_HANDLE(hs);
+  // rtcore.cpp:672-686: N == 1 is an AOS stream of RTCRayHit records
+  if (N == 1) {
+    if (M == 1 && rayhit && !(((RTCRayHit*)rayhit)->ray.tnear <= ((RTCRayHit*)rayhit)->ray.tfar)) return;
+    run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit));
+  } else if (N != 0 && M != 0) {
+    run_query_packets(s, rayhit, N, M, byteStride, nullptr, false);
+  }
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcIntersectNp(RTCScene hs, struct RTCIntersectContext* ctx, const struct RTCRayHitNp* rayhit,
+                            unsigned int N) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  VERIFY_HANDLE(hs);
+  if (!rayhit) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  run_query_pointer_soa(s, rayhit, nullptr, N, false);
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcOccludedNM(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRayN* ray, unsigned int N,
+                           unsigned int M, size_t byteStride) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  VERIFY_HANDLE(hs);
+  if (N == 1) {
+    if (M == 1 && ray && !(((RTCRay*)ray)->tnear <= ((RTCRay*)ray)->tfar)) return;
+    run_query(s, ray, M, byteStride, true, sizeof(RTCRay));
+  } else if (N != 0 && M != 0) {
+    run_query_packets(s, ray, N, M, byteStride, nullptr, true);
+  }
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcOccludedNp(RTCScene hs, struct RTCIntersectContext* ctx, const struct RTCRayNp* ray, unsigned int N) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  (void)ctx;
+  VERIFY_HANDLE(hs);
+  if (!ray) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  run_query_pointer_soa(s, nullptr, ray, N, true);
+  API_END(s ? s->device : nullptr)
+}
+
 // ---- extensions
 
 RTC_API void rtcgbGetSceneBuildStats(RTCScene hs, RTCGBBuildStats* out) {
@@ -1312,6 +1605,430 @@ RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, 
   cudaFree(dk);
   cudaFree(dv);
   return rc;
+}
+
+// ---- learned proposer
+
+namespace {
+// Device view of a caller buffer: device-accessible memory is used in place,
+// host memory is staged in a temporary device allocation.
+struct DevSpan {
+  char* d = nullptr;
+  void* host = nullptr;
+  size_t bytes = 0;
+  bool owned = false;
+  DevSpan(const void* p, size_t n, cudaStream_t st, bool copy_in) {
+    const cudaMemoryType mt = pointer_type(p);
+    if (mt == cudaMemoryTypeDevice || mt == cudaMemoryTypeManaged) {
+      d = (char*)p;
+      return;
+    }
+    cuda_ok(cudaMalloc((void**)&d, std::max<size_t>(n, 16)), "cudaMalloc staging");
+    owned = true;
+    bytes = n;
+    host = const_cast<void*>(p);
+    if (copy_in) cuda_ok(cudaMemcpyAsync(d, p, n, cudaMemcpyHostToDevice, st), "H2D");
+  }
+  void copy_out(cudaStream_t st) {
+    if (owned) cuda_ok(cudaMemcpyAsync(host, d, bytes, cudaMemcpyDeviceToHost, st), "D2H");
+  }
+  ~DevSpan() {
+    if (owned) cudaFree(d);
+  }
+};
+
+cudaStream_t proposer_stream(ProposerObj* p) {
+  Device* dev = p->scene->device;
+  dev->set_current();
+  t_ctx.ensure(dev->cuda_device);
+  return t_ctx.stream();
+}
+}  // namespace
+
+RTC_API RTCGBProposer rtcgbNewProposer(RTCScene hs, unsigned int seed) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  std::lock_guard<std::mutex> lk(s->mtx);
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  if (s->batched) fail(RTC_ERROR_INVALID_OPERATION, "the proposer does not support batched scenes");
+  s->device->set_current();
+  t_ctx.ensure(s->device->cuda_device);
+  cudaStream_t st = t_ctx.stream();
+  ProposerObj* p = new ProposerObj(s);
+  try {
+    std::vector<uint32_t> prim, geom;
+    cuda_ok(gb::choose_treelets(s->bvh, st, &p->roots, &p->record_treelet, &prim, &geom), "treelet cut");
+    // primitive numbering of the labels: geometry slots in ID order
+    std::vector<uint32_t> prefix(s->geoms.size(), gb::kInvalidID);
+    uint64_t total = 0;
+    for (size_t id = 0; id < s->geoms.size(); id++) {
+      const Geometry* g = s->geoms[id];
+      if (!g || !g->indices.ptr) continue;
+      prefix[id] = (uint32_t)total;
+      total += g->indices.num;
+    }
+    std::vector<uint32_t> prim_treelet((size_t)total, gb::kInvalidID);
+    for (size_t r = 0; r < prim.size(); r++) {
+      if (geom[r] >= prefix.size() || prefix[geom[r]] == gb::kInvalidID) continue;
+      const uint64_t k = (uint64_t)prefix[geom[r]] + prim[r];
+      if (k < total) prim_treelet[k] = p->record_treelet[r];
+    }
+    gb::GridSpec grid{};
+    for (int a = 0; a < 3; a++) {
+      const float lo = s->bvh.lo[a], ext = s->bvh.hi[a] - s->bvh.lo[a];
+      const bool ok = std::isfinite(lo) && std::isfinite(ext) && ext > 0.0f;
+      grid.lo[a] = ok ? lo : 0.0f;
+      grid.scale[a] = ok ? 1.0f / ext : 1.0f;
+    }
+    cuda_ok(p->net.init(p->roots, prim_treelet, prefix, grid, seed, st), "proposer initialisation");
+  } catch (...) {
+    p->dec();
+    throw;
+  }
+  return (RTCGBProposer)p;
+  API_END(s ? s->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcgbRetainProposer(RTCGBProposer hp) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  p->inc();
+  API_END(nullptr)
+}
+
+RTC_API void rtcgbReleaseProposer(RTCGBProposer hp) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  p->dec();
+  API_END(nullptr)
+}
+
+RTC_API void rtcgbProposerTrain(RTCGBProposer hp, const struct RTCRayHit* records, unsigned int M, size_t byteStride,
+                                unsigned int epochs, unsigned int batch, float learning_rate) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (M == 0) return;
+  if (!records || byteStride < sizeof(RTCRayHit) || (byteStride % 4)) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid records");
+  if (!(learning_rate > 0.0f)) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid learning rate");
+  cudaStream_t st = proposer_stream(p);
+  std::lock_guard<std::mutex> lk(p->mtx);
+  DevSpan recs(records, (size_t)(M - 1) * byteStride + sizeof(RTCRayHit), st, true);
+  cuda_ok(p->net.train(recs.d, byteStride, M, epochs, batch, learning_rate, st), "proposer training");
+  cuda_ok(cudaStreamSynchronize(st), "proposer training");
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API void rtcgbProposerPredict(RTCGBProposer hp, const struct RTCRay* rays, unsigned int M, size_t byteStride,
+                                  unsigned int* treelets) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (M == 0) return;
+  if (!rays || !treelets || byteStride < sizeof(RTCRay) || (byteStride % 4)) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  cudaStream_t st = proposer_stream(p);
+  std::lock_guard<std::mutex> lk(p->mtx);
+  DevSpan in(rays, (size_t)(M - 1) * byteStride + sizeof(RTCRay), st, true);
+  DevSpan out(treelets, (size_t)M * 16, st, false);
+  cuda_ok(p->net.predict(in.d, byteStride, M, nullptr, (uint32_t*)out.d, st), "proposer inference");
+  out.copy_out(st);
+  cuda_ok(cudaStreamSynchronize(st), "proposer inference");
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API void rtcgbProposerGetStats(RTCGBProposer hp, RTCGBProposerStats* out) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (!out) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  RTCGBProposerStats r{};
+  r.num_treelets = p->net.num_treelets;
+  r.samples = p->net.stats.samples;
+  r.steps = p->net.stats.steps;
+  r.loss = p->net.stats.loss;
+  r.top1 = p->net.stats.top1;
+  r.top4 = p->net.stats.top4;
+  *out = r;
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API size_t rtcgbProposerParamCount(void) { return gb::kNumParams; }
+
+RTC_API void rtcgbProposerGetParams(RTCGBProposer hp, float* params) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (!params) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  cudaStream_t st = proposer_stream(p);
+  std::lock_guard<std::mutex> lk(p->mtx);
+  cuda_ok(p->net.get_params(params, st), "proposer parameters");
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API void rtcgbProposerSetParams(RTCGBProposer hp, const float* params) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (!params) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  cudaStream_t st = proposer_stream(p);
+  std::lock_guard<std::mutex> lk(p->mtx);
+  cuda_ok(p->net.set_params(params, st), "proposer parameters");
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API float rtcgbProposerGradients(RTCGBProposer hp, const struct RTCRay* rays, unsigned int B, size_t byteStride,
+                                     const int* labels, float* grads) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (B == 0 || !rays || !labels || !grads || byteStride < sizeof(RTCRay) || (byteStride % 4))
+    fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  cudaStream_t st = proposer_stream(p);
+  std::lock_guard<std::mutex> lk(p->mtx);
+  DevSpan in(rays, (size_t)(B - 1) * byteStride + sizeof(RTCRay), st, true);
+  DevSpan lab(labels, (size_t)B * 4, st, true);
+  DevSpan g(grads, gb::kNumParams * sizeof(float), st, false);
+  float loss = 0.0f;
+  cuda_ok(p->net.gradients(in.d, byteStride, (const int32_t*)lab.d, B, (float*)g.d, &loss, st), "proposer gradients");
+  g.copy_out(st);
+  cuda_ok(cudaStreamSynchronize(st), "proposer gradients");
+  return loss;
+  API_END(p ? p->scene->device : nullptr)
+  return NAN;
+}
+
+RTC_API unsigned int rtcgbProposerGetTreelets(RTCGBProposer hp, unsigned int* roots, unsigned int* record_treelet,
+                                              unsigned int max_records) {
+  ProposerObj* p = (ProposerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (roots)
+    for (unsigned i = 0; i < (unsigned)gb::kTreelets; i++) roots[i] = i < p->roots.size() ? p->roots[i] : gb::kInvalidID;
+  if (record_treelet)
+    for (unsigned i = 0; i < max_records && i < p->record_treelet.size(); i++) record_treelet[i] = p->record_treelet[i];
+  return (unsigned)p->roots.size();
+  API_END(p ? p->scene->device : nullptr)
+  return 0;
+}
+
+RTC_API void rtcgbIntersect1MLearned(RTCScene hs, RTCGBProposer hp, struct RTCRayHit* rayhit, unsigned int M,
+                                     size_t byteStride) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit), (ProposerObj*)hp);
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcgbOccluded1MLearned(RTCScene hs, RTCGBProposer hp, struct RTCRay* ray, unsigned int M,
+                                    size_t byteStride) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  run_query(s, ray, M, byteStride, true, sizeof(RTCRay), (ProposerObj*)hp);
+  API_END(s ? s->device : nullptr)
+}
+
+// ---- animated path tracing
+
+namespace {
+struct PathTracerObj : RefCounted {
+  Scene* scene;
+  uint64_t build_serial;
+  gb::PathTracer pt;
+  gb::RefitScratch refit{};
+  ProposerObj* prop = nullptr;
+  explicit PathTracerObj(Scene* s) : scene(s), build_serial(s->build_serial) { scene->inc(); }
+  ~PathTracerObj() override {
+    scene->device->set_current();
+    pt.release();
+    gb::refit_release(&refit);
+    if (prop) prop->dec();
+    scene->dec();
+  }
+  cudaStream_t stream() {
+    scene->device->set_current();
+    t_ctx.ensure(scene->device->cuda_device);
+    return t_ctx.stream();
+  }
+};
+}  // namespace
+
+RTC_API RTCGBPathTracer rtcgbNewPathTracer(RTCScene hs, unsigned int width, unsigned int height,
+                                           unsigned int bounces, const float* camera) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!camera || width == 0 || height == 0 || bounces == 0 || bounces > (unsigned)gb::kMaxBounces)
+    fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  std::lock_guard<std::mutex> lk(s->mtx);
+  if (!s->committed || s->bvh.num_nodes == 0) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed or empty");
+  if (s->bvh.robust || s->batched)
+    fail(RTC_ERROR_INVALID_OPERATION, "robust and batched scenes are not supported by the path tracer");
+  PathTracerObj* p = new PathTracerObj(s);
+  try {
+    gb::CameraSpec cam{};
+    for (int a = 0; a < 3; a++) {
+      cam.eye[a] = camera[a];
+      cam.look[a] = camera[3 + a];
+      cam.up[a] = camera[6 + a];
+    }
+    cam.fov_deg = camera[9];
+    cuda_ok(p->pt.init(&s->bvh, width, height, bounces, cam, p->stream()), "path tracer");
+  } catch (...) {
+    p->dec();
+    throw;
+  }
+  return (RTCGBPathTracer)p;
+  API_END(s ? s->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcgbRetainPathTracer(RTCGBPathTracer hp) {
+  PathTracerObj* p = (PathTracerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  p->inc();
+  API_END(nullptr)
+}
+
+RTC_API void rtcgbReleasePathTracer(RTCGBPathTracer hp) {
+  PathTracerObj* p = (PathTracerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  p->dec();
+  API_END(nullptr)
+}
+
+RTC_API void rtcgbPathTracerAnimateSoup(RTCGBPathTracer hp, unsigned int geomID, float amplitude, unsigned int seed) {
+  PathTracerObj* p = (PathTracerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  Scene* s = p->scene;
+  std::lock_guard<std::mutex> lk(s->mtx);
+  if (geomID >= s->geoms.size() || !s->geoms[geomID]) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid geometry ID");
+  const gb::GeomDesc* d = nullptr;
+  for (const gb::GeomDesc& x : s->descs)
+    if (x.geomID == geomID) d = &x;
+  if (!d) fail(RTC_ERROR_INVALID_ARGUMENT, "geometry is not part of the committed BVH");
+  const Geometry* g = s->geoms[geomID];
+  if (!is_device_pointer(g->vertices.ptr) || (const char*)g->vertices.ptr != d->verts)
+    fail(RTC_ERROR_INVALID_OPERATION, "the animated geometry needs a shared vertex buffer in device memory");
+  cudaStream_t st = p->stream();
+  gb::refit_release(&p->refit);
+  cuda_ok(gb::refit_prepare(s->descs.data(), (int)s->descs.size(), s->bvh, &p->refit, st), "refit setup");
+  gb::SoupAnimation a{};
+  a.verts = (float*)d->verts;
+  a.vstride = d->vstride;
+  a.idx = d->idx;
+  a.istride = d->istride;
+  a.ntris = d->ntris;
+  a.nverts = d->nverts;
+  a.amplitude = amplitude;
+  a.seed = seed;
+  cuda_ok(p->pt.animate(a, &p->refit, st), "animation setup");
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API void rtcgbPathTracerSetProposer(RTCGBPathTracer hp, RTCGBProposer hprop) {
+  PathTracerObj* p = (PathTracerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  ProposerObj* q = (ProposerObj*)hprop;
+  if (q && q->scene != p->scene) fail(RTC_ERROR_INVALID_ARGUMENT, "proposer belongs to another scene");
+  if (q) q->inc();
+  if (p->prop) p->prop->dec();
+  p->prop = q;
+  p->pt.set_proposer(q ? &q->net : nullptr);
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API void rtcgbPathTracerRenderFrame(RTCGBPathTracer hp, unsigned int frame, int learned, RTCGBFrameStats* out) {
+  PathTracerObj* p = (PathTracerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  Scene* s = p->scene;
+  if (!s->committed || s->build_serial != p->build_serial)
+    fail(RTC_ERROR_INVALID_OPERATION, "the scene was rebuilt since the path tracer was made");
+  const bool use = learned && p->prop && p->prop->current();
+  std::unique_lock<std::mutex> plk;
+  if (use) plk = std::unique_lock<std::mutex>(p->prop->mtx);
+  gb::FrameStats fs;
+  cuda_ok(p->pt.render(frame, use, p->stream(), &fs), "frame");
+  if (out) {
+    RTCGBFrameStats r{};
+    r.frame_ms = fs.frame_ms;
+    r.rays = fs.rays;
+    r.proposal_hits = fs.proposal_hits;
+    for (int b = 0; b < gb::kMaxBounces; b++) r.rays_per_bounce[b] = fs.rays_per_bounce[b];
+    r.learned = fs.learned;
+    r.errors = fs.errors;
+    *out = r;
+  }
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API void rtcgbPathTracerTrainProposer(RTCGBPathTracer hp, unsigned int epochs, unsigned int batch, float lr) {
+  PathTracerObj* p = (PathTracerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (!p->prop) fail(RTC_ERROR_INVALID_OPERATION, "no proposer attached");
+  if (!(lr > 0.0f)) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid learning rate");
+  std::lock_guard<std::mutex> lk(p->prop->mtx);
+  cudaStream_t st = p->stream();
+  cuda_ok(p->prop->net.train(p->pt.log_records(), 80, p->pt.log_count(), epochs, batch, lr, st), "proposer training");
+  cuda_ok(cudaStreamSynchronize(st), "proposer training");
+  API_END(p ? p->scene->device : nullptr)
+}
+
+RTC_API void rtcgbPathTracerGetImage(RTCGBPathTracer hp, float* rgb) {
+  PathTracerObj* p = (PathTracerObj*)hp;
+  API_BEGIN
+  VERIFY_HANDLE(hp);
+  if (!rgb) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  cuda_ok(p->pt.image(rgb, p->stream()), "image");
+  API_END(p ? p->scene->device : nullptr)
+}
+
+// ---- batched scenes
+
+RTC_API void rtcgbSetSceneBatched(RTCScene hs, int enable) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  std::lock_guard<std::mutex> lk(s->mtx);
+  s->batched = enable != 0;
+  s->committed = false;  // takes effect at the next commit
+  s->built_sig.clear();
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcgbIntersect1MBatched(RTCScene hs, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride,
+                                     const unsigned int* batch_start, unsigned int num_batches) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  BatchArgs b;
+  b.start = batch_start;
+  b.nbatches = num_batches;
+  run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit), nullptr, &b);
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API void rtcgbOccluded1MBatched(RTCScene hs, struct RTCRay* ray, unsigned int M, size_t byteStride,
+                                    const unsigned int* batch_start, unsigned int num_batches) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  BatchArgs b;
+  b.start = batch_start;
+  b.nbatches = num_batches;
+  run_query(s, ray, M, byteStride, true, sizeof(RTCRay), nullptr, &b);
+  API_END(s ? s->device : nullptr)
 }
 
 }  // extern "C"

@@ -36,8 +36,14 @@ rtcSetGeometryOccludedFilterFunction rtcSetGeometryUserData rtcGetGeometryUserDa
 rtcRetainScene rtcReleaseScene rtcAttachGeometry rtcAttachGeometryByID rtcDetachGeometry rtcGetGeometry
 rtcCommitScene rtcJoinCommitScene rtcSetSceneProgressMonitorFunction rtcSetSceneBuildQuality rtcSetSceneFlags
 rtcGetSceneFlags rtcGetSceneBounds rtcGetSceneLinearBounds rtcIntersect1 rtcIntersect1M rtcIntersect1Mp
-rtcOccluded1 rtcOccluded1M rtcOccluded1Mp rtcgbGetSceneBuildStats rtcgbGetLastQueryStats rtcgbSetQueryCounting
-rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs rtcgbIntersect1MNoAlloc rtcgbGetDeviceHostAccess""".split()
+rtcOccluded1 rtcOccluded1M rtcOccluded1Mp rtcIntersect4 rtcIntersect8 rtcIntersect16 rtcIntersectNM
+rtcIntersectNp rtcOccluded4 rtcOccluded8 rtcOccluded16 rtcOccludedNM rtcOccludedNp rtcgbGetSceneBuildStats rtcgbGetLastQueryStats rtcgbSetQueryCounting
+rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs rtcgbIntersect1MNoAlloc rtcgbGetDeviceHostAccess
+rtcgbNewProposer rtcgbRetainProposer rtcgbReleaseProposer rtcgbProposerTrain rtcgbProposerPredict rtcgbProposerGetStats
+rtcgbProposerParamCount rtcgbProposerGetParams rtcgbProposerSetParams rtcgbProposerGradients rtcgbProposerGetTreelets
+rtcgbIntersect1MLearned rtcgbOccluded1MLearned rtcgbNewPathTracer rtcgbRetainPathTracer rtcgbReleasePathTracer
+rtcgbPathTracerAnimateSoup rtcgbPathTracerSetProposer rtcgbPathTracerRenderFrame rtcgbPathTracerTrainProposer
+rtcgbPathTracerGetImage rtcgbSetSceneBatched rtcgbIntersect1MBatched rtcgbOccluded1MBatched""".split()
 
 
 class RTCBounds(ctypes.Structure):
@@ -58,7 +64,18 @@ class RTCGBBuildStats(ctypes.Structure):
 class RTCGBQueryStats(ctypes.Structure):
     _fields_ = [("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("rays", ctypes.c_ulonglong),
                 ("nodes", ctypes.c_ulonglong), ("tris", ctypes.c_ulonglong), ("h2d_bytes", ctypes.c_ulonglong),
-                ("d2h_bytes", ctypes.c_ulonglong)]
+                ("d2h_bytes", ctypes.c_ulonglong), ("proposal_hits", ctypes.c_ulonglong)]
+
+
+class RTCGBFrameStats(ctypes.Structure):
+    _fields_ = [("frame_ms", ctypes.c_double), ("rays", ctypes.c_ulonglong), ("proposal_hits", ctypes.c_ulonglong),
+                ("rays_per_bounce", ctypes.c_uint * 8), ("learned", ctypes.c_uint), ("errors", ctypes.c_uint)]
+
+
+class RTCGBProposerStats(ctypes.Structure):
+    _fields_ = [("num_treelets", ctypes.c_uint), ("samples", ctypes.c_uint), ("steps", ctypes.c_uint),
+                ("reserved", ctypes.c_uint), ("loss", ctypes.c_double), ("top1", ctypes.c_double),
+                ("top4", ctypes.c_double)]
 
 
 ERROR_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p)
@@ -113,6 +130,11 @@ def load(build=True):
         "rtcIntersect1Mp": (None, [vp, vp, vp, u]),
         "rtcOccluded1": (None, [vp, vp, vp]), "rtcOccluded1M": (None, [vp, vp, vp, u, sz]),
         "rtcOccluded1Mp": (None, [vp, vp, vp, u]),
+        "rtcIntersect4": (None, [vp, vp, vp, vp]), "rtcIntersect8": (None, [vp, vp, vp, vp]),
+        "rtcIntersect16": (None, [vp, vp, vp, vp]), "rtcOccluded4": (None, [vp, vp, vp, vp]),
+        "rtcOccluded8": (None, [vp, vp, vp, vp]), "rtcOccluded16": (None, [vp, vp, vp, vp]),
+        "rtcIntersectNM": (None, [vp, vp, vp, u, u, sz]), "rtcOccludedNM": (None, [vp, vp, vp, u, u, sz]),
+        "rtcIntersectNp": (None, [vp, vp, vp, u]), "rtcOccludedNp": (None, [vp, vp, vp, u]),
         "rtcgbGetSceneBuildStats": (None, [vp, ctypes.POINTER(RTCGBBuildStats)]),
         "rtcgbGetLastQueryStats": (None, [ctypes.POINTER(RTCGBQueryStats)]),
         "rtcgbSetQueryCounting": (None, [i]),
@@ -122,6 +144,27 @@ def load(build=True):
         "rtcgbRadixSortPairs": (i, [vp, vp, u]),
         "rtcgbIntersect1MNoAlloc": (None, [vp, vp, u, sz, vp]),
         "rtcgbGetDeviceHostAccess": (i, [vp]),
+        "rtcgbNewProposer": (vp, [vp, u]), "rtcgbRetainProposer": (None, [vp]),
+        "rtcgbReleaseProposer": (None, [vp]),
+        "rtcgbProposerTrain": (None, [vp, vp, u, sz, u, u, ctypes.c_float]),
+        "rtcgbProposerPredict": (None, [vp, vp, u, sz, vp]),
+        "rtcgbProposerGetStats": (None, [vp, ctypes.POINTER(RTCGBProposerStats)]),
+        "rtcgbProposerParamCount": (sz, []),
+        "rtcgbProposerGetParams": (None, [vp, vp]), "rtcgbProposerSetParams": (None, [vp, vp]),
+        "rtcgbProposerGradients": (ctypes.c_float, [vp, vp, u, sz, vp, vp]),
+        "rtcgbProposerGetTreelets": (u, [vp, vp, vp, u]),
+        "rtcgbIntersect1MLearned": (None, [vp, vp, vp, u, sz]),
+        "rtcgbOccluded1MLearned": (None, [vp, vp, vp, u, sz]),
+        "rtcgbNewPathTracer": (vp, [vp, u, u, u, ctypes.POINTER(ctypes.c_float)]),
+        "rtcgbRetainPathTracer": (None, [vp]), "rtcgbReleasePathTracer": (None, [vp]),
+        "rtcgbPathTracerAnimateSoup": (None, [vp, u, ctypes.c_float, u]),
+        "rtcgbPathTracerSetProposer": (None, [vp, vp]),
+        "rtcgbPathTracerRenderFrame": (None, [vp, u, i, ctypes.POINTER(RTCGBFrameStats)]),
+        "rtcgbPathTracerTrainProposer": (None, [vp, u, u, ctypes.c_float]),
+        "rtcgbPathTracerGetImage": (None, [vp, vp]),
+        "rtcgbSetSceneBatched": (None, [vp, i]),
+        "rtcgbIntersect1MBatched": (None, [vp, vp, u, sz, vp, u]),
+        "rtcgbOccluded1MBatched": (None, [vp, vp, u, sz, vp, u]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -199,6 +242,23 @@ class Scene:
         self._by_id[gid] = (verts, idx)
         return gid
 
+    def add_mesh_device(self, verts_ptr, nverts, idx_ptr, ntris, quality=None):
+        """Attaches a triangle mesh whose FLOAT3 / UINT3 buffers are CUDA device
+        memory (used in place by the builder, the refit and the path tracer)."""
+        L = self.L
+        g = ctypes.c_void_p(L.rtcNewGeometry(self.dev.h, RTC_GEOMETRY_TYPE_TRIANGLE))
+        if quality is not None:
+            L.rtcSetGeometryBuildQuality(g, quality)
+        L.rtcSetSharedGeometryBuffer(g, RTC_BUFFER_TYPE_VERTEX, 0, RTC_FORMAT_FLOAT3, ctypes.c_void_p(verts_ptr), 0,
+                                     12, nverts)
+        L.rtcSetSharedGeometryBuffer(g, RTC_BUFFER_TYPE_INDEX, 0, RTC_FORMAT_UINT3, ctypes.c_void_p(idx_ptr), 0, 12,
+                                     ntris)
+        L.rtcCommitGeometry(g)
+        gid = L.rtcAttachGeometry(self.h, g)
+        L.rtcReleaseGeometry(g)
+        self.dev.check("add_mesh_device")
+        return gid
+
     def update_vertices(self, gid, new_verts):
         """Writes new positions into geometry gid's shared vertex buffer and
         marks it updated (rtcUpdateGeometryBuffer); takes effect at commit."""
@@ -256,6 +316,33 @@ class Scene:
         self.L.rtcOccluded1M(self.h, ctypes.byref(ctx), ctypes.c_void_p(ptr), n, stride)
         self.dev.check("rtcOccluded1M")
 
+    def set_batched(self, on=True):
+        """One BVH per geometry; query with intersect_batched / occluded_batched."""
+        self.L.rtcgbSetSceneBatched(self.h, 1 if on else 0)
+        self.dev.check("rtcgbSetSceneBatched")
+
+    def intersect_batched(self, rays, batch_start, ptr=None, count=None):
+        """rays [batch_start[b], batch_start[b+1]) query geometry b (host array, or a
+        device pointer `ptr` with `count` rays)."""
+        bs = np.ascontiguousarray(batch_start, np.uint32)
+        if ptr is None:
+            self.L.rtcgbIntersect1MBatched(self.h, _ptr(rays), rays.shape[0], rays.dtype.itemsize, _ptr(bs),
+                                           bs.shape[0] - 1)
+        else:
+            self.L.rtcgbIntersect1MBatched(self.h, ctypes.c_void_p(ptr), count, 80, _ptr(bs), bs.shape[0] - 1)
+        self.dev.check("rtcgbIntersect1MBatched")
+        return rays
+
+    def occluded_batched(self, rays, batch_start, ptr=None, count=None):
+        bs = np.ascontiguousarray(batch_start, np.uint32)
+        if ptr is None:
+            self.L.rtcgbOccluded1MBatched(self.h, _ptr(rays), rays.shape[0], rays.dtype.itemsize, _ptr(bs),
+                                          bs.shape[0] - 1)
+        else:
+            self.L.rtcgbOccluded1MBatched(self.h, ctypes.c_void_p(ptr), count, 48, _ptr(bs), bs.shape[0] - 1)
+        self.dev.check("rtcgbOccluded1MBatched")
+        return rays
+
     def bvh(self):
         """Copies the committed BVH: (nodes uint8 [n,80], tris float32 [m,12])."""
         nt = ctypes.c_uint()
@@ -299,3 +386,127 @@ def radix_sort_pairs(keys, values):
 
 def set_thread_stream(stream_ptr):
     load().rtcgbSetThreadStream(ctypes.c_void_p(stream_ptr) if stream_ptr else None)
+
+
+class Proposer:
+    """Learned hit proposer of a committed scene (rtcgbNewProposer)."""
+
+    def __init__(self, scene, seed=1):
+        self.scene = scene
+        self.L = scene.L
+        self.h = ctypes.c_void_p(self.L.rtcgbNewProposer(scene.h, seed))
+        scene.dev.check("rtcgbNewProposer")
+
+    def train(self, records, epochs=1, batch=16384, lr=5e-3, count=None, stride=80):
+        """records: host RTCRayHit array, or an int device pointer (then count is required)."""
+        if isinstance(records, int):
+            ptr, n = ctypes.c_void_p(records), count
+        else:
+            ptr, n = _ptr(records), records.shape[0] if count is None else count
+        self.L.rtcgbProposerTrain(self.h, ptr, n, stride, epochs, batch, lr)
+        self.scene.dev.check("rtcgbProposerTrain")
+        return self.stats()
+
+    def predict(self, rays):
+        out = np.zeros((rays.shape[0], 4), np.uint32)
+        self.L.rtcgbProposerPredict(self.h, _ptr(rays), rays.shape[0], rays.dtype.itemsize, _ptr(out))
+        self.scene.dev.check("rtcgbProposerPredict")
+        return out
+
+    def stats(self):
+        s = RTCGBProposerStats()
+        self.L.rtcgbProposerGetStats(self.h, ctypes.byref(s))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def params(self):
+        p = np.zeros(self.L.rtcgbProposerParamCount(), np.float32)
+        self.L.rtcgbProposerGetParams(self.h, _ptr(p))
+        self.scene.dev.check("rtcgbProposerGetParams")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.shape[0] == self.L.rtcgbProposerParamCount()
+        self.L.rtcgbProposerSetParams(self.h, _ptr(p))
+        self.scene.dev.check("rtcgbProposerSetParams")
+
+    def gradients(self, rays, labels):
+        labels = np.ascontiguousarray(labels, np.int32)
+        g = np.zeros(self.L.rtcgbProposerParamCount(), np.float32)
+        loss = self.L.rtcgbProposerGradients(self.h, _ptr(rays), rays.shape[0], rays.dtype.itemsize,
+                                             _ptr(labels), _ptr(g))
+        self.scene.dev.check("rtcgbProposerGradients")
+        return loss, g
+
+    def treelets(self, num_records):
+        roots = np.zeros(4096, np.uint32)
+        rec = np.zeros(max(num_records, 1), np.uint32)
+        n = self.L.rtcgbProposerGetTreelets(self.h, _ptr(roots), _ptr(rec), num_records)
+        return roots[:n], rec[:num_records]
+
+    def intersect(self, rays):
+        self.L.rtcgbIntersect1MLearned(self.scene.h, self.h, _ptr(rays), rays.shape[0], rays.dtype.itemsize)
+        self.scene.dev.check("rtcgbIntersect1MLearned")
+        return rays
+
+    def occluded(self, rays):
+        self.L.rtcgbOccluded1MLearned(self.scene.h, self.h, _ptr(rays), rays.shape[0], rays.dtype.itemsize)
+        self.scene.dev.check("rtcgbOccluded1MLearned")
+        return rays
+
+    def intersect_ptr(self, ptr, n, stride=80):
+        self.L.rtcgbIntersect1MLearned(self.scene.h, self.h, ctypes.c_void_p(ptr), n, stride)
+        self.scene.dev.check("rtcgbIntersect1MLearned")
+
+    def occluded_ptr(self, ptr, n, stride=48):
+        self.L.rtcgbOccluded1MLearned(self.scene.h, self.h, ctypes.c_void_p(ptr), n, stride)
+        self.scene.dev.check("rtcgbOccluded1MLearned")
+
+    def release(self):
+        if self.h:
+            self.L.rtcgbReleaseProposer(self.h)
+            self.h = None
+
+
+class PathTracer:
+    """Wavefront diffuse path tracer whose frames run as CUDA graphs."""
+
+    def __init__(self, scene, width, height, bounces=4, eye=(0.5, -1.2, 0.5), look=(0.5, 0.5, 0.5), up=(0, 0, 1),
+                 fov=50.0):
+        self.scene = scene
+        self.L = scene.L
+        self.width, self.height = width, height
+        cam = (ctypes.c_float * 10)(*eye, *look, *up, fov)
+        self.h = ctypes.c_void_p(self.L.rtcgbNewPathTracer(scene.h, width, height, bounces, cam))
+        scene.dev.check("rtcgbNewPathTracer")
+
+    def animate_soup(self, geom_id, amplitude=0.002, seed=14):
+        self.L.rtcgbPathTracerAnimateSoup(self.h, geom_id, amplitude, seed)
+        self.scene.dev.check("rtcgbPathTracerAnimateSoup")
+
+    def set_proposer(self, proposer):
+        self.L.rtcgbPathTracerSetProposer(self.h, proposer.h if proposer is not None else None)
+        self.scene.dev.check("rtcgbPathTracerSetProposer")
+
+    def render(self, frame, learned=False):
+        st = RTCGBFrameStats()
+        self.L.rtcgbPathTracerRenderFrame(self.h, frame, 1 if learned else 0, ctypes.byref(st))
+        self.scene.dev.check("rtcgbPathTracerRenderFrame")
+        out = {f: getattr(st, f) for f, _ in st._fields_}
+        out["rays_per_bounce"] = list(st.rays_per_bounce)
+        return out
+
+    def train_proposer(self, epochs=1, batch=16384, lr=5e-3):
+        self.L.rtcgbPathTracerTrainProposer(self.h, epochs, batch, lr)
+        self.scene.dev.check("rtcgbPathTracerTrainProposer")
+
+    def image(self):
+        img = np.zeros((self.height, self.width, 3), np.float32)
+        self.L.rtcgbPathTracerGetImage(self.h, _ptr(img))
+        self.scene.dev.check("rtcgbPathTracerGetImage")
+        return img
+
+    def release(self):
+        if self.h:
+            self.L.rtcgbReleasePathTracer(self.h)
+            self.h = None

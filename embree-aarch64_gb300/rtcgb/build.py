@@ -18,7 +18,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librtcore_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gb_build.cu", "gb_trace.cu", "rtcore_api.cpp"]
+SOURCES = ["gb_build.cu", "gb_trace.cu", "gb_learned.cu", "gb_paths.cu", "rtcore_api.cpp"]
 
 
 def _nvcc():

@@ -57,3 +57,27 @@ def hits_equal_bits(a, b, fields=("tfar", "Ng_x", "Ng_y", "Ng_z", "u", "v", "pri
     for f in fields:
         ok &= a[f].view(np.uint32) == b[f].view(np.uint32)
     return ok
+
+
+def to_soa(records, K, stride_words=None):
+    """Packs AOS records (RAYHIT_DTYPE or RAY_DTYPE) into packets of K lanes in the SOA
+    layout of RTCRayHit4/8/16 and RTCRayHitN (include/embree3/rtcore_ray.h:222-248):
+    field f of lane i of packet p is the uint32 at p * stride_words + f * K + i.
+    Lanes past the end of `records` are zero.  Returns a (packets, stride_words) uint32 array."""
+    nf = records.dtype.itemsize // 4
+    n = records.shape[0]
+    P = (n + K - 1) // K
+    stride_words = stride_words or nf * K
+    words = np.zeros((P * K, nf), np.uint32)
+    words[:n] = np.ascontiguousarray(records).view(np.uint32).reshape(n, nf)
+    out = np.zeros((P, stride_words), np.uint32)
+    out[:, :nf * K] = words.reshape(P, K, nf).transpose(0, 2, 1).reshape(P, nf * K)
+    return out
+
+
+def from_soa(packets, K, n, dtype):
+    """Inverse of to_soa for the first n lanes."""
+    nf = dtype.itemsize // 4
+    P = packets.shape[0]
+    words = packets[:, :nf * K].reshape(P, nf, K).transpose(0, 2, 1).reshape(P * K, nf)[:n]
+    return np.ascontiguousarray(words).view(dtype).reshape(n)

@@ -25,7 +25,7 @@ import math
 
 import numpy as np
 
-from .rays import make_rayhits, make_rays
+from .rays import RAYHIT_DTYPE, make_rayhits, make_rays
 
 
 # --------------------------------------------------------------------------
@@ -234,6 +234,48 @@ def shadow_rays(hits, seed=13, eps=1e-4):
     rays["tnear"] = np.where(hit, np.float32(eps), np.float32(np.inf))
     rays["tfar"] = np.where(hit, (0.999 * dist).astype(np.float32), np.float32(0.0))
     return rays, light
+
+
+def ao_scene(cells=724, soup_tris=300_000, seed=3):
+    """Heightfield (value noise seed 1, amplitude 0.1) plus a Gaussian-mixture
+    soup: [(verts, idx) of the heightfield, (verts, idx) of the soup]."""
+    return [heightfield(cells), gaussian_soup(soup_tris, seed=seed)]
+
+
+def hemisphere_rays(hits, per_hit=8, seed=21, tnear=1e-4, tfar=np.inf, record=RAYHIT_DTYPE):
+    """Cosine-weighted rays about the geometric normal (facing the incoming
+    ray) of every hit of `hits` (RTCRayHit after a closest-hit query):
+    `per_hit` rays per hit, in hit order.  Ambient-occlusion rays use a short
+    tfar, diffuse bounce rays tfar = inf.  Returns (rays, index of the hit of
+    each ray)."""
+    rng = np.random.default_rng(seed)
+    hit = np.nonzero(hits["geomID"] != 0xFFFFFFFF)[0]
+    h = hits[hit]
+    o = np.stack([h["org_x"], h["org_y"], h["org_z"]], -1).astype(np.float64)
+    d = np.stack([h["dir_x"], h["dir_y"], h["dir_z"]], -1).astype(np.float64)
+    p = o + d * h["tfar"].astype(np.float64)[:, None]
+    nrm = np.stack([h["Ng_x"], h["Ng_y"], h["Ng_z"]], -1).astype(np.float64)
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
+    nrm *= np.where((nrm * d).sum(1) > 0, -1.0, 1.0)[:, None]
+    # orthonormal basis (Duff et al. 2017, "Building an orthonormal basis, revisited")
+    sgn = np.where(nrm[:, 2] >= 0, 1.0, -1.0)
+    a = -1.0 / (sgn + nrm[:, 2])
+    b = nrm[:, 0] * nrm[:, 1] * a
+    t1 = np.stack([1.0 + sgn * nrm[:, 0] ** 2 * a, sgn * b, -sgn * nrm[:, 0]], -1)
+    t2 = np.stack([b, sgn + nrm[:, 1] ** 2 * a, -nrm[:, 1]], -1)
+    n = hit.shape[0] * per_hit
+    src = np.repeat(np.arange(hit.shape[0]), per_hit)
+    u1, u2 = rng.random(n), rng.random(n)
+    r, phi = np.sqrt(u1), 2.0 * np.pi * u2
+    lx, ly, lz = r * np.cos(phi), r * np.sin(phi), np.sqrt(np.maximum(0.0, 1.0 - u1))
+    dirs = t1[src] * lx[:, None] + t2[src] * ly[:, None] + nrm[src] * lz[:, None]
+    rays = make_rayhits(p[src], dirs, tnear, tfar)
+    if record is not RAYHIT_DTYPE:
+        out = np.zeros(n, record)
+        for name in record.names:
+            out[name] = rays[name]
+        rays = out
+    return rays, hit[src]
 
 
 def config_workload(name, scale=1.0):

@@ -162,6 +162,47 @@ struct RTCRayHit {
   struct RTCHit hit;
 };
 
+/* Packets of K rays in SOA layout (rtcore_ray.h:51-230): every ray field is
+   an array of K values, then every hit field. */
+#define RTCGB_DECLARE_PACKET(K, A)                                                                   \
+  struct RTC_ALIGN(A) RTCRay##K {                                                                    \
+    float org_x[K], org_y[K], org_z[K], tnear[K];                                                    \
+    float dir_x[K], dir_y[K], dir_z[K], time[K];                                                     \
+    float tfar[K];                                                                                   \
+    unsigned int mask[K], id[K], flags[K];                                                           \
+  };                                                                                                 \
+  struct RTC_ALIGN(A) RTCHit##K {                                                                    \
+    float Ng_x[K], Ng_y[K], Ng_z[K], u[K], v[K];                                                     \
+    unsigned int primID[K], geomID[K];                                                               \
+    unsigned int instID[RTC_MAX_INSTANCE_LEVEL_COUNT][K];                                            \
+  };                                                                                                 \
+  struct RTCRayHit##K {                                                                              \
+    struct RTCRay##K ray;                                                                            \
+    struct RTCHit##K hit;                                                                            \
+  };
+RTCGB_DECLARE_PACKET(4, 16)
+RTCGB_DECLARE_PACKET(8, 32)
+RTCGB_DECLARE_PACKET(16, 64)
+#undef RTCGB_DECLARE_PACKET
+
+/* Streams of N rays in pointer-SOA layout (rtcore_ray.h:170-207). */
+struct RTCRayNp {
+  float* org_x; float* org_y; float* org_z; float* tnear;
+  float* dir_x; float* dir_y; float* dir_z; float* time;
+  float* tfar;
+  unsigned int* mask; unsigned int* id; unsigned int* flags;
+};
+struct RTCHitNp {
+  float* Ng_x; float* Ng_y; float* Ng_z; float* u; float* v;
+  unsigned int* primID; unsigned int* geomID;
+  unsigned int* instID[RTC_MAX_INSTANCE_LEVEL_COUNT];
+};
+struct RTCRayHitNp {
+  struct RTCRayNp ray;
+  struct RTCHitNp hit;
+};
+struct RTCRayHitN;  /* packets of runtime size N (SOA, rtcore_ray.h:209-230) */
+
 /* ---------------------------------------------------------------------- */
 /* Device (include/embree3/rtcore_device.h)                                */
 /* ---------------------------------------------------------------------- */
@@ -386,6 +427,28 @@ RTC_API void rtcIntersect1(RTCScene scene, struct RTCIntersectContext* context, 
 RTC_API void rtcIntersect1M(RTCScene scene, struct RTCIntersectContext* context, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride);
 /* replaces include/embree3/rtcore_scene.h:111 / kernels/common/rtcore.cpp:626 (array of pointers) */
 RTC_API void rtcIntersect1Mp(RTCScene scene, struct RTCIntersectContext* context, struct RTCRayHit** rayhit, unsigned int M);
+/* replaces include/embree3/rtcore_scene.h:99 / kernels/common/rtcore.cpp:498: lanes with
+   valid[i] == -1 are traced (through the stream path); other lanes untouched */
+RTC_API void rtcIntersect4(const int* valid, RTCScene scene, struct RTCIntersectContext* context, struct RTCRayHit4* rayhit);
+/* replaces include/embree3/rtcore_scene.h:102 / kernels/common/rtcore.cpp:529 */
+RTC_API void rtcIntersect8(const int* valid, RTCScene scene, struct RTCIntersectContext* context, struct RTCRayHit8* rayhit);
+/* replaces include/embree3/rtcore_scene.h:105 / kernels/common/rtcore.cpp:562 */
+RTC_API void rtcIntersect16(const int* valid, RTCScene scene, struct RTCIntersectContext* context, struct RTCRayHit16* rayhit);
+/* replaces include/embree3/rtcore_scene.h:114 / kernels/common/rtcore.cpp:657: M packets of
+   N SOA rays, byteStride apart (N == 1: AOS records) */
+RTC_API void rtcIntersectNM(RTCScene scene, struct RTCIntersectContext* context, struct RTCRayHitN* rayhit, unsigned int N, unsigned int M, size_t byteStride);
+/* replaces include/embree3/rtcore_scene.h:117 / kernels/common/rtcore.cpp:695 */
+RTC_API void rtcIntersectNp(RTCScene scene, struct RTCIntersectContext* context, const struct RTCRayHitNp* rayhit, unsigned int N);
+/* replaces include/embree3/rtcore_scene.h:123 / kernels/common/rtcore.cpp:749 */
+RTC_API void rtcOccluded4(const int* valid, RTCScene scene, struct RTCIntersectContext* context, struct RTCRay4* ray);
+/* replaces include/embree3/rtcore_scene.h:126 / kernels/common/rtcore.cpp:780 */
+RTC_API void rtcOccluded8(const int* valid, RTCScene scene, struct RTCIntersectContext* context, struct RTCRay8* ray);
+/* replaces include/embree3/rtcore_scene.h:129 / kernels/common/rtcore.cpp:814 */
+RTC_API void rtcOccluded16(const int* valid, RTCScene scene, struct RTCIntersectContext* context, struct RTCRay16* ray);
+/* replaces include/embree3/rtcore_scene.h:138 / kernels/common/rtcore.cpp:907 */
+RTC_API void rtcOccludedNM(RTCScene scene, struct RTCIntersectContext* context, struct RTCRayN* ray, unsigned int N, unsigned int M, size_t byteStride);
+/* replaces include/embree3/rtcore_scene.h:141 / kernels/common/rtcore.cpp:946 */
+RTC_API void rtcOccludedNp(RTCScene scene, struct RTCIntersectContext* context, const struct RTCRayNp* ray, unsigned int N);
 /* replaces include/embree3/rtcore_scene.h:120 / kernels/common/rtcore.cpp:733 */
 RTC_API void rtcOccluded1(RTCScene scene, struct RTCIntersectContext* context, struct RTCRay* ray);
 /* replaces include/embree3/rtcore_scene.h:132 / kernels/common/rtcore.cpp:848: any hit; occluded rays get

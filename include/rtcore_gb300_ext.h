@@ -32,6 +32,7 @@ typedef struct RTCGBQueryStats {
   unsigned long long tris;       /* triangle tests (counting mode only) */
   unsigned long long h2d_bytes;  /* bytes copied host->device by the call */
   unsigned long long d2h_bytes;  /* bytes copied device->host by the call */
+  unsigned long long proposal_hits; /* learned queries: rays answered inside a proposed treelet */
 } RTCGBQueryStats;
 
 /* Statistics of the scene's last commit. */
@@ -91,5 +92,132 @@ RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, 
 #define RTCGB_NOALLOC_STAGING_BYTES 33554432u
 RTC_API void rtcgbIntersect1MNoAlloc(RTCScene scene, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride,
                                      void* cuda_stream);
+
+/* ---- Learned hit proposer (no counterpart in the reference) ----------------
+
+   A proposer belongs to one committed scene.  It cuts the scene's BVH into up
+   to 4096 treelets (subtrees) and learns, from closest-hit records the plain
+   traversal produced, which treelets a ray hits: a hash-grid encoding of the
+   ray origin and direction feeds a 32-64-64-64-4096 MLP (BF16 tensor cores,
+   FP32 accumulation), trained on the GPU with the library's own forward,
+   backward and Adam kernels.  The learned queries search the four proposed
+   treelets before the whole tree, so their results are those of
+   rtcIntersect1M / rtcOccluded1M; a good proposal ends an occlusion ray early
+   or lowers a closest-hit ray's tfar before the full search.  After a full
+   rebuild of the scene (a refit keeps the treelets) the learned queries run
+   the plain traversal until a new proposer is made.  Rays, records, labels
+   and outputs may be in host or device memory. */
+typedef struct RTCGBProposerTy* RTCGBProposer;
+
+typedef struct RTCGBProposerStats {
+  unsigned int num_treelets;  /* treelets of the cut (<= 4096) */
+  unsigned int samples;       /* labelled records of the last training call */
+  unsigned int steps;         /* Adam steps taken */
+  unsigned int reserved;
+  double loss;                /* mean cross-entropy of the last epoch */
+  double top1, top4;          /* share of the last epoch's records whose treelet ranked first / in the top 4 */
+} RTCGBProposerStats;
+
+RTC_API RTCGBProposer rtcgbNewProposer(RTCScene scene, unsigned int seed);
+RTC_API void rtcgbRetainProposer(RTCGBProposer proposer);
+RTC_API void rtcgbReleaseProposer(RTCGBProposer proposer);
+
+/* Trains on M RTCRayHit records after a closest-hit query (records without a
+   hit are skipped): `epochs` passes in shuffled batches of `batch` records,
+   Adam with the given learning rate. */
+RTC_API void rtcgbProposerTrain(RTCGBProposer proposer, const struct RTCRayHit* records, unsigned int M,
+                                size_t byteStride, unsigned int epochs, unsigned int batch, float learning_rate);
+
+/* Top-4 treelet indices (4 per ray, best first; 0xFFFFFFFF when fewer exist). */
+RTC_API void rtcgbProposerPredict(RTCGBProposer proposer, const struct RTCRay* rays, unsigned int M,
+                                  size_t byteStride, unsigned int* treelets);
+
+RTC_API void rtcgbProposerGetStats(RTCGBProposer proposer, RTCGBProposerStats* out);
+
+/* Parameter vector (FP32): hash table (16 x 2^18 x 2), then per layer the
+   weights [out][in] and the biases of the 32-64-64-64-4096 MLP. */
+RTC_API size_t rtcgbProposerParamCount(void);
+RTC_API void rtcgbProposerGetParams(RTCGBProposer proposer, float* params);
+RTC_API void rtcgbProposerSetParams(RTCGBProposer proposer, const float* params);
+
+/* Mean softmax cross-entropy of B rays with the given treelet labels (-1:
+   ignored, counted in the mean) and its gradient with respect to every
+   parameter (rtcgbProposerParamCount() floats).  Returns the loss. */
+RTC_API float rtcgbProposerGradients(RTCGBProposer proposer, const struct RTCRay* rays, unsigned int B,
+                                     size_t byteStride, const int* labels, float* grads);
+
+/* The cut: root node of each treelet (up to 4096 entries, 0xFFFFFFFF after
+   the last) and the treelet of each triangle record of the BVH (max_records
+   entries; 0xFFFFFFFF for triangles held above the cut).  Returns the number
+   of treelets. */
+RTC_API unsigned int rtcgbProposerGetTreelets(RTCGBProposer proposer, unsigned int* roots,
+                                              unsigned int* record_treelet, unsigned int max_records);
+
+/* rtcIntersect1M / rtcOccluded1M with the proposer's treelets searched first
+   (records 16-byte aligned with a stride that is a multiple of 16; otherwise,
+   and for robust scenes, the plain traversal runs). */
+RTC_API void rtcgbIntersect1MLearned(RTCScene scene, RTCGBProposer proposer, struct RTCRayHit* rayhit,
+                                     unsigned int M, size_t byteStride);
+RTC_API void rtcgbOccluded1MLearned(RTCScene scene, RTCGBProposer proposer, struct RTCRay* ray, unsigned int M,
+                                    size_t byteStride);
+
+/* ---- Animated diffuse path tracing (no counterpart in the reference) --------
+
+   A wavefront path tracer over a committed (non-robust) scene: per frame the
+   camera rays, then per bounce a closest-hit traversal of the live rays, a
+   cosine-weighted diffuse bounce (albedo 0.75, sky light on a miss) and the
+   compaction of the surviving paths.  Each frame runs as one CUDA graph
+   (captured on first use, one graph per mode) whose launches read their ray
+   counts from device memory.  With rtcgbPathTracerAnimateSoup each frame first
+   moves the soup's triangles by amplitude * sin(2 pi (frame / 60 + x)) along a
+   random per-triangle normal (x: the triangle centroid's rest x coordinate)
+   and refits the BVH inside the same graph.  Learned frames search the
+   attached proposer's treelets first (same hits).  The scene must not be
+   committed while a path tracer renders; after a full rebuild make a new one. */
+typedef struct RTCGBPathTracerTy* RTCGBPathTracer;
+
+typedef struct RTCGBFrameStats {
+  double frame_ms;                  /* device time of the frame's graph */
+  unsigned long long rays;          /* rays traced over all bounces */
+  unsigned long long proposal_hits; /* learned frames: rays answered inside a proposed treelet */
+  unsigned int rays_per_bounce[8];
+  unsigned int learned;             /* 1 when the frame ran the learned graph */
+  unsigned int errors;              /* traversal error bits; 0x100: a refit met an invalid vertex */
+} RTCGBFrameStats;
+
+/* camera: eye xyz, look-at xyz, up xyz, vertical field of view in degrees; bounces 1..8 */
+RTC_API RTCGBPathTracer rtcgbNewPathTracer(RTCScene scene, unsigned int width, unsigned int height,
+                                           unsigned int bounces, const float* camera);
+RTC_API void rtcgbRetainPathTracer(RTCGBPathTracer tracer);
+RTC_API void rtcgbReleasePathTracer(RTCGBPathTracer tracer);
+/* The geometry must be a triangle soup whose shared vertex buffer is device memory. */
+RTC_API void rtcgbPathTracerAnimateSoup(RTCGBPathTracer tracer, unsigned int geomID, float amplitude,
+                                        unsigned int seed);
+RTC_API void rtcgbPathTracerSetProposer(RTCGBPathTracer tracer, RTCGBProposer proposer);
+/* Renders frame `frame` (learned != 0: with the proposer when it is current). */
+RTC_API void rtcgbPathTracerRenderFrame(RTCGBPathTracer tracer, unsigned int frame, int learned,
+                                        RTCGBFrameStats* stats);
+/* Trains the attached proposer on the last frame's first diffuse bounce (closest-hit records). */
+RTC_API void rtcgbPathTracerTrainProposer(RTCGBPathTracer tracer, unsigned int epochs, unsigned int batch,
+                                          float learning_rate);
+/* Radiance of the last frame, width * height * 3 floats (row-major, rgb). */
+RTC_API void rtcgbPathTracerGetImage(RTCGBPathTracer tracer, float* rgb);
+
+/* ---- Batched scenes (no counterpart in the reference) ----------------------
+
+   A batched scene holds many independent scenes, one per geometry: its commit
+   builds all their BVHs in one pass (one sort with the geometry ID in the key's
+   top bits, one agglomerative clustering whose merges stay inside a geometry,
+   one collapse; the work does not grow with the number of scenes), and one
+   persistent traversal launch answers the rays of all of them.  Rays
+   [batch_start[b], batch_start[b+1]) query geometry ID b only; hits report
+   geomID b.  batch_start has num_batches + 1 entries (host or device memory),
+   batch_start[0] = 0 and batch_start[num_batches] = M.  rtcIntersect1M and the
+   learned queries are not available on batched scenes. */
+RTC_API void rtcgbSetSceneBatched(RTCScene scene, int enable);
+RTC_API void rtcgbIntersect1MBatched(RTCScene scene, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride,
+                                     const unsigned int* batch_start, unsigned int num_batches);
+RTC_API void rtcgbOccluded1MBatched(RTCScene scene, struct RTCRay* ray, unsigned int M, size_t byteStride,
+                                    const unsigned int* batch_start, unsigned int num_batches);
 
 #endif

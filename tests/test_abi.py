@@ -97,3 +97,39 @@ def test_drop_in_include_path(tmp_path):
         }
     """))
     subprocess.run(["g++", "-c", "-Wall", "-I", INC, str(src), "-o", str(tmp_path / "prog.o")], check=True)
+
+
+PACKET_C = textwrap.dedent("""
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "rtcore_gb300.h"
+    int main(void) {
+      printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",
+             sizeof(struct RTCRayHit4), sizeof(struct RTCRayHit8), sizeof(struct RTCRayHit16),
+             sizeof(struct RTCRay4), sizeof(struct RTCRay8), sizeof(struct RTCRay16),
+             offsetof(struct RTCRayHit8, hit), offsetof(struct RTCRay16, tfar),
+             offsetof(struct RTCHit8, geomID), _Alignof(struct RTCRay4), _Alignof(struct RTCRay8),
+             _Alignof(struct RTCRay16));
+      printf("%zu %zu %zu\\n", sizeof(struct RTCRayNp), sizeof(struct RTCHitNp), offsetof(struct RTCRayHitNp, hit));
+      return 0;
+    }
+""")
+
+
+def test_packet_layouts(tmp_path):
+    """RTCRayHit4/8/16 and the pointer-SOA structs have the reference's SOA layout
+    (include/embree3/rtcore_ray.h:51-213): 20 fields of K lanes, 12 for rays."""
+    src = tmp_path / "packets.c"
+    src.write_text(PACKET_C)
+    exe = tmp_path / "packets"
+    subprocess.run(["gcc", "-Wall", "-Werror", "-I", INC, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    assert list(map(int, out[0].split())) == [320, 640, 1280, 192, 384, 768, 384, 512, 192, 16, 32, 64]
+    assert list(map(int, out[1].split())) == [96, 64, 96]
+    # the numpy SOA packing used by the tests follows the same layout
+    rh = R.make_rayhits(np.arange(15, dtype=np.float32).reshape(5, 3), np.ones((5, 3), np.float32))
+    soa = R.to_soa(rh, 4)
+    assert soa.shape == (2, 20 * 4)
+    assert soa.view(np.float32)[0, 2 * 4 + 1] == rh["org_z"][1]
+    back = R.from_soa(soa, 4, 5, R.RAYHIT_DTYPE)
+    assert (back.view(np.uint8) == rh.view(np.uint8)).all()

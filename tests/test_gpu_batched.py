@@ -1,0 +1,116 @@
+"""Batched scenes (rtcgbSetSceneBatched): many independent scenes built in one
+segmented pass and queried in one launch, each batch of rays against its own
+geometry only, checked against one oracle scene per batch."""
+import numpy as np
+import pytest
+
+from parity import assert_clean, compare_closest, compare_occluded
+from rtcgb import rays as R
+from rtcgb import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes(seed, n):
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        if k % 2 == 0:
+            out.append(W.heightfield(int(rng.integers(8, 60)), seed=int(rng.integers(1, 1000))))
+        else:
+            out.append(W.gaussian_soup(int(rng.integers(1000, 30000)), seed=int(rng.integers(1, 1000))))
+    return out
+
+
+def _rays_for(meshes, per_tri, seed):
+    """Half camera rays, half uniform-sphere rays per scene; returns (rays, start)."""
+    rng = np.random.default_rng(seed)
+    parts, start = [], [0]
+    for v, i in meshes:
+        n = max(64, per_tri * i.shape[0] // 8)
+        side = max(4, int(np.sqrt(n // 2)))
+        cam = W.camera_rays(side, side)
+        sph = W.sphere_rays(n // 2, seed=int(rng.integers(1, 10 ** 6)))
+        r = np.concatenate([cam, sph])
+        parts.append(r)
+        start.append(start[-1] + r.shape[0])
+    return np.concatenate(parts), np.array(start, np.uint32)
+
+
+def test_batched_closest_and_occluded_match_oracle(rtc, device, oracle):
+    meshes = _scenes(3, 7)
+    sc = rtc.Scene(device)
+    sc.set_batched()
+    for v, i in meshes:
+        sc.add_mesh(v, i)
+    sc.commit()
+    rays, start = _rays_for(meshes, 2, 5)
+    gpu = rays.copy()
+    sc.intersect_batched(gpu, start)
+    sh = np.zeros(rays.shape[0], R.RAY_DTYPE)
+    for name in R.RAY_DTYPE.names:
+        sh[name] = rays[name]
+    sh["tfar"] = 0.3
+    gsh = sh.copy()
+    sc.occluded_batched(gsh, start)
+    for b, (v, i) in enumerate(meshes):
+        lo, hi = start[b], start[b + 1]
+        orc = oracle.OracleScene([(b, v, i)])
+        ref = rays[lo:hi].copy()
+        orc.intersect(ref)
+        g = gpu[lo:hi]
+        assert set(np.unique(g["geomID"])) <= {b, 0xFFFFFFFF}
+        assert (g["geomID"] == b).sum() > 0
+        assert_clean(compare_closest(orc, rays[lo:hi], g, ref))
+        rs = sh[lo:hi].copy()
+        orc.occluded(rs)
+        assert_clean(compare_occluded(orc, sh[lo:hi], gsh[lo:hi], rs))
+    sc.release()
+
+
+def test_batched_empty_batch_and_errors(rtc, device):
+    sc = rtc.Scene(device)
+    sc.set_batched()
+    v, i = W.heightfield(16)
+    sc.add_mesh(v, i)
+    bad = v.copy()
+    bad[:] = np.nan  # every triangle invalid: this batch has no tree
+    sc.add_mesh(bad, i)
+    sc.add_mesh(*W.gaussian_soup(2000, seed=2))
+    sc.commit()
+    rays = W.camera_rays(32, 32)
+    start = np.array([0, 400, 700, rays.shape[0]], np.uint32)
+    out = rays.copy()
+    sc.intersect_batched(out, start)
+    assert (out["geomID"][400:700] == 0xFFFFFFFF).all()
+    assert (out["geomID"][:400] == 0).sum() > 0
+    L = rtc.load()
+    with pytest.raises(rtc.RTCError):
+        sc.intersect_batched(rays.copy(), np.array([0, 10, 20], np.uint32))  # does not cover M
+    with pytest.raises(rtc.RTCError):
+        sc.intersect(rays.copy())  # plain query on a batched scene
+    L.rtcGetDeviceError(device.h)
+    sc.release()
+
+
+def test_batched_refit(rtc, device, oracle):
+    meshes = [W.gaussian_soup(5000, seed=s) for s in (1, 2, 3)]
+    sc = rtc.Scene(device)
+    sc.set_batched()
+    gids = [sc.add_mesh(v, i, quality=rtc.RTC_BUILD_QUALITY_REFIT) for v, i in meshes]
+    sc.commit()
+    moved = [W.displace_soup(v, 9, seed=4, amplitude=0.01) for v, _ in meshes]
+    for g, mv in zip(gids, moved):
+        sc.update_vertices(g, mv)
+    sc.commit()
+    assert sc.build_stats()["refit"] == 1
+    rays = W.sphere_rays(9000, seed=8)
+    start = np.array([0, 3000, 6000, 9000], np.uint32)
+    gpu = rays.copy()
+    sc.intersect_batched(gpu, start)
+    for b in range(3):
+        orc = oracle.OracleScene([(b, moved[b], meshes[b][1])])
+        ref = rays[start[b]:start[b + 1]].copy()
+        orc.intersect(ref)
+        assert_clean(compare_closest(orc, rays[start[b]:start[b + 1]], gpu[start[b]:start[b + 1]], ref))
+    sc.release()
