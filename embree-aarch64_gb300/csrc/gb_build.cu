@@ -119,6 +119,15 @@ __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ g
     const int gs = find_geom(geoms, ngeoms, gi);
     const GeomDesc g = geoms[gs];
     const uint32_t j = gi - g.prim_offset;
+    if (g.kind == 1) {
+      const InstBox bx = reinterpret_cast<const InstBox*>(g.verts)[j];
+      if (vtx_ok(bx.lo[0], bx.lo[1], bx.lo[2]) && vtx_ok(bx.hi[0], bx.hi[1], bx.hi[2]) && bx.lo[0] <= bx.hi[0] &&
+          bx.lo[1] <= bx.hi[1] && bx.lo[2] <= bx.hi[2]) {
+        ok = true;
+        lo = make_float3(bx.lo[0], bx.lo[1], bx.lo[2]);
+        hi = make_float3(bx.hi[0], bx.hi[1], bx.hi[2]);
+      }
+    } else {
     const uint3 t = load_tri(g, j);
     if (t.x < g.nverts && t.y < g.nverts && t.z < g.nverts) {
       const float3 a = load_vtx(g, t.x), b = load_vtx(g, t.y), c = load_vtx(g, t.z);
@@ -127,6 +136,7 @@ __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ g
         lo = f3min(f3min(a, b), c);
         hi = f3max(f3max(a, b), c);
       }
+    }
     }
     plo[gi] = make_float4(lo.x, lo.y, lo.z, __uint_as_float((uint32_t)gs));
     phi[gi] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(j));
@@ -740,6 +750,13 @@ __device__ __forceinline__ void write_tri(const GeomDesc* __restrict__ geoms, co
   const uint32_t gs = __float_as_uint(plo[prim].w);
   const uint32_t j = __float_as_uint(phi[prim].w);
   const GeomDesc g = geoms[gs];
+  if (g.kind == 1) {  // instance leaf
+    const InstBox bx = reinterpret_cast<const InstBox*>(g.verts)[j];
+    dst->a = make_float4(0.f, 0.f, 0.f, __uint_as_float(bx.inst));
+    dst->b = make_float4(0.f, 0.f, 0.f, __uint_as_float(bx.geomID));
+    dst->c = make_float4(0.f, 0.f, 0.f, __uint_as_float(kInstanceLeaf));
+    return;
+  }
   const uint3 t = load_tri(g, j);
   const float3 p0 = load_vtx(g, t.x), p1 = load_vtx(g, t.y), p2 = load_vtx(g, t.z);
   // Triangle4: e1 = v0 - v1, e2 = v2 - v0 (triangle.h:40-41); Triangle4v of
@@ -1170,6 +1187,27 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
 
 // Sorts (key, value) pairs with the builder's radix sort (all 8 digits,
 // constant digits skipped).  Device pointers; results in keys/vals.
+cudaError_t sort_pairs_passes(uint64_t* keys, uint32_t* vals, uint64_t* kb, uint32_t* vb, uint32_t* hist, uint32_t n,
+                              int passes, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (passes < 0 || passes > 8 || (passes & 1)) return cudaErrorInvalidValue;
+  const uint32_t nb = cdiv(n, RS_TILE);
+  uint64_t* ka = keys;
+  uint32_t* va = vals;
+  for (int pass = 0; pass < passes; pass++) {
+    const int shift = 8 * pass;
+    k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, shift, hist, nb);
+    k_scan_excl<<<1, 1024, 0, st>>>(hist, 256 * nb, nullptr);
+    k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
+    note_launches(3);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  return cudaGetLastError();
+}
+
+uint32_t sort_hist_entries(uint32_t n) { return 256u * cdiv(n, RS_TILE); }
+
 cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   uint64_t* kb = nullptr;

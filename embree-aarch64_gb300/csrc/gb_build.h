@@ -37,5 +37,10 @@ void refit_release(RefitScratch* s);
 
 // Stable LSD radix sort of 64-bit keys with 32-bit values (device buffers).
 cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st);
+// The low 8 * passes bits only (passes even), with caller scratch (kb, vb: n
+// entries; hist: sort_hist_entries(n)); no allocation, no synchronisation.
+cudaError_t sort_pairs_passes(uint64_t* keys, uint32_t* vals, uint64_t* kb, uint32_t* vb, uint32_t* hist, uint32_t n,
+                              int passes, cudaStream_t st);
+uint32_t sort_hist_entries(uint32_t n);
 
 }  // namespace gb

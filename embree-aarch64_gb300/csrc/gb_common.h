@@ -54,6 +54,7 @@ struct alignas(16) TriRecord {
 static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
 
 // One geometry as the builder sees it (device pointers, byte strides).
+// kind 1 (instances): `verts` points to `ntris` InstBox records, one primitive each.
 struct GeomDesc {
   const char* verts;
   const char* idx;
@@ -63,7 +64,34 @@ struct GeomDesc {
   uint32_t ntris;
   uint32_t geomID;     // user-visible geometry ID
   uint32_t prim_offset; // exclusive prefix of ntris over the scene's geometries
+  uint32_t kind = 0;    // 0: triangle mesh, 1: instances
+  uint32_t pad = 0;
 };
+
+// World-space box of one instance (builder input of kind-1 geometries).
+struct InstBox {
+  float lo[3];
+  float hi[3];
+  uint32_t inst;    // index into the scene's InstDesc table
+  uint32_t geomID;  // the instance geometry's ID
+};
+
+// One instance as the traversal sees it: the instanced scene's BVH and the
+// world-to-local transform (columns vx, vy, vz, p).
+struct alignas(16) InstDesc {
+  const WideNode* nodes;
+  const TriRecord* tris;
+  uint32_t num_nodes;
+  uint32_t num_tris;
+  uint32_t geomID;
+  uint32_t pad;
+  float w2l[12];
+};
+static_assert(sizeof(InstDesc) == 80, "InstDesc is 80 bytes");
+
+// Instance leaf record: a triangle-record slot whose c.w holds kInstanceLeaf;
+// a.w = index into the InstDesc table, b.w = the instance's geometry ID.
+constexpr uint32_t kInstanceLeaf = 1u;
 
 // A committed BVH in device memory.
 struct DeviceBVH {

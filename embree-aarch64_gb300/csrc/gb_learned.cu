@@ -619,6 +619,301 @@ __global__ void __launch_bounds__(kPW * 32, 2)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05).  One CTA per SM
+// (16 warps, 128 rays per tile) owns all 512 TMEM columns: two 128x256 FP32
+// accumulators.  In the epilogue warp w reads TMEM lanes 32 (w % 4) .. +31
+// (its rows) and the column quarter w / 4 of each chunk; the four partial
+// top-4 lists of a row are merged through shared memory at the end of the tile.  The 4096x64 output
+// weights are kept in global memory in the UMMA canonical K-major layout
+// (8x16-byte core matrices; LBO 128 B along K, SBO 1024 B along rows), so each
+// 256-treelet chunk is one contiguous 32 KB block that a single bulk copy
+// (cp.async.bulk, completion on an mbarrier) brings into one of two shared
+// stages.  One thread issues the four K=16 MMAs of a chunk and commits them to
+// an mbarrier; meanwhile all threads read the previous chunk's accumulators
+// with tcgen05.ld and keep their row's running top 4.  Every wait on an
+// mbarrier is bounded; on a timeout the kernel sets kErrIterationLimit and
+// stops.
+// ---------------------------------------------------------------------------
+
+constexpr int kTcThreads = 512;
+constexpr int kTcRays = 128;                       // UMMA M
+constexpr int kTcN = 256;                          // UMMA N: treelets per chunk
+constexpr int kTcChunks = kTreelets / kTcN;        // 16
+constexpr uint32_t kTcChunkBytes = kTcN * kHidden * 2;
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kSpinLimit = 1u << 22;
+// kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A and
+// B (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                            ((uint32_t)(kTcRays >> 4) << 24);
+
+struct TcSmem {
+  uint16_t w4[2][kTcN * kHidden];   // streamed output weights (UMMA layout)
+  uint16_t a[kTcRays * kHidden];    // last hidden layer of the tile (UMMA layout)
+  uint16_t x[kTcRays * kLdX];
+  uint16_t h[kTcRays * kLdH];
+  uint16_t w1[kHidden * kLdX];
+  uint16_t w2[kHidden * kLdH];
+  uint16_t w3[kHidden * kLdH];
+  float b[3][kHidden];
+  float b4[kTreelets];
+  float mv[kTcRays][4][4];          // partial top-4 per row and column quarter
+  int mi[kTcRays][4][4];
+  unsigned long long tma_bar[2];
+  unsigned long long mma_bar[2];
+  uint32_t tmem_base;
+  uint32_t fail;
+};
+static_assert(offsetof(TcSmem, a) % 1024 == 0, "operand tiles start on 1 KB boundaries");
+static_assert(offsetof(TcSmem, tma_bar) % 8 == 0, "mbarrier alignment");
+
+// element offset of (row, k) in the UMMA K-major core-matrix layout (64 columns)
+__device__ __forceinline__ uint32_t umma_off(uint32_t row, uint32_t k) {
+  return (row >> 3) * 512 + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t umma_desc(const void* smem) {
+  constexpr uint64_t kLbo = 128, kSbo = 1024;
+  return (uint64_t)((smem_u32(smem) >> 4) & 0x3FFFu) | (((kLbo >> 4) & 0x3FFFu) << 16) |
+         (((kSbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity) {
+  const uint32_t a = smem_u32(b);
+  for (uint32_t i = 0; i < kSpinLimit; i++) {
+    uint32_t ok = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+// The streamed weights in the UMMA layout: chunk c (treelets 256c..256c+255)
+// is a contiguous block; refreshed whenever the BF16 mirror changes.
+__global__ void k_permute_w4(const uint16_t* __restrict__ Pb, uint16_t* __restrict__ w4p) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // one 16-byte row piece per thread
+  if (i >= kTreelets * (kHidden / 8)) return;
+  const uint32_t n = i / (kHidden / 8), kc = i % (kHidden / 8);
+  const uint32_t c = n / kTcN, r = n % kTcN;
+  const uint4 v = *reinterpret_cast<const uint4*>(Pb + kOffW4 + (size_t)n * kHidden + kc * 8);
+  *reinterpret_cast<uint4*>(w4p + (size_t)c * kTcN * kHidden + umma_off(r, kc * 8)) = v;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_propose_tc(const char* rays, uint64_t stride, uint32_t M, const uint32_t* d_count, GridSpec grid,
+                 const uint16_t* __restrict__ Pb, const float* __restrict__ P, const uint16_t* __restrict__ W4p,
+                 const uint32_t* __restrict__ node_of_treelet, int ntl, uint4* seeds, uint32_t* treelets,
+                 uint32_t* err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+  TcSmem& S = *reinterpret_cast<TcSmem*>(tc_smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  const bool leader = tid == 0;
+  for (int i = tid; i < kHidden * kIn / 2; i += kTcThreads) {
+    const int o = (2 * i) / kIn, k = (2 * i) % kIn;
+    *reinterpret_cast<uint32_t*>(S.w1 + o * kLdX + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW1)[i];
+  }
+  for (int i = tid; i < kHidden * kHidden / 2; i += kTcThreads) {
+    const int o = (2 * i) / kHidden, k = (2 * i) % kHidden;
+    *reinterpret_cast<uint32_t*>(S.w2 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW2)[i];
+    *reinterpret_cast<uint32_t*>(S.w3 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW3)[i];
+  }
+  for (int i = tid; i < 3 * kHidden; i += kTcThreads) {
+    const size_t off = i < kHidden ? kOffB1 : (i < 2 * kHidden ? kOffB2 : kOffB3);
+    S.b[i / kHidden][i % kHidden] = P[off + i % kHidden];
+  }
+  for (int i = tid; i < kTreelets; i += kTcThreads) S.b4[i] = i < ntl ? P[kOffB4 + i] : -INFINITY;
+  if (leader) {
+    mbar_init(&S.tma_bar[0], 1);
+    mbar_init(&S.tma_bar[1], 1);
+    mbar_init(&S.mma_bar[0], 1);
+    mbar_init(&S.mma_bar[1], 1);
+    S.fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&S.tmem_base)),
+                 "n"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem_base;
+  if (d_count) M = min(M, *d_count);
+  const uint32_t ntiles = (M + kTcRays - 1) / kTcRays;
+  uint32_t tma_par[2] = {0, 0}, mma_par[2] = {0, 0};
+  uint32_t tma_pending[2] = {0, 0};  // leader: copies issued and not yet waited for
+  if (leader && blockIdx.x < ntiles) {
+    bulk_load(S.w4[0], W4p, kTcChunkBytes, &S.tma_bar[0]);
+    bulk_load(S.w4[1], W4p + (size_t)kTcN * kHidden, kTcChunkBytes, &S.tma_bar[1]);
+    tma_pending[0] = tma_pending[1] = 1;
+  }
+  bool failed = false;
+  for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+    const uint32_t r0 = tile * kTcRays;
+    const bool next_tile = tile + gridDim.x < ntiles;
+    for (int it = tid; it < kTcRays * kLevels; it += kTcThreads) {
+      const int rr = it / kLevels, l = it % kLevels;
+      const uint32_t rid = r0 + rr;
+      const uint32_t pk = rid < M ? encode_level(Pb, rays + (uint64_t)rid * stride, grid, l) : 0u;
+      *reinterpret_cast<uint32_t*>(S.x + rr * kLdX + 2 * l) = pk;
+    }
+    __syncthreads();
+    // hidden layers: warps 0..7 own 16 rows each
+    if (warp < kTcRays / 16) {
+      const int row0 = warp * 16;
+      uint16_t* hrow = S.h + row0 * kLdH;
+      hidden_layer<kIn, kLdX>(S.x + row0 * kLdX, S.w1, kLdX, S.b[0], hrow, g, t);
+      __syncwarp();
+      hidden_layer<kHidden, kLdH>(hrow, S.w2, kLdH, S.b[1], hrow, g, t);
+      __syncwarp();
+      hidden_layer<kHidden, kLdH>(hrow, S.w3, kLdH, S.b[2], hrow, g, t);
+    }
+    __syncthreads();
+    // rows into the A operand (8 pieces of 16 bytes per row)
+    for (int it = tid; it < kTcRays * (kHidden / 8); it += kTcThreads) {
+      const int r = it >> 3, kc = it & 7;
+      *reinterpret_cast<uint4*>(S.a + umma_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(S.h + r * kLdH + kc * 8);
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    const uint64_t adesc0 = umma_desc(S.a);
+    auto issue = [&](int c) {  // leader: MMAs of chunk c into accumulator c & 1
+      const int s = c & 1;
+      if (!mbar_wait(&S.tma_bar[s], tma_par[s])) return false;
+      tma_par[s] ^= 1;
+      tma_pending[s] = 0;
+      tc_fence_after();
+      const uint64_t bdesc0 = umma_desc(S.w4[s]);
+#pragma unroll
+      for (int ks = 0; ks < kHidden / 16; ks++)  // +256 B per K step: two core matrices
+        umma_bf16(tmem + (uint32_t)s * kTcN, adesc0 + (uint64_t)(ks * 16), bdesc0 + (uint64_t)(ks * 16), ks > 0);
+      umma_commit(&S.mma_bar[s]);
+      return true;
+    };
+    if (leader && !issue(0)) S.fail = 1;
+    float v[4];
+    int ix[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) { v[q] = -INFINITY; ix[q] = -1; }
+    for (int c = 0; c < kTcChunks; c++) {
+      const int s = c & 1;
+      if (leader && !S.fail && c + 1 < kTcChunks && !issue(c + 1)) S.fail = 1;
+      if (!mbar_wait(&S.mma_bar[s], mma_par[s])) S.fail = 1;
+      mma_par[s] ^= 1;
+      tc_fence_after();
+      if (leader && !S.fail) {  // stage s is free: the next chunk that uses it
+        if (c + 2 < kTcChunks) {
+          bulk_load(S.w4[s], W4p + (size_t)(c + 2) * kTcN * kHidden, kTcChunkBytes, &S.tma_bar[s]);
+          tma_pending[s] = 1;
+        } else if (next_tile) {
+          bulk_load(S.w4[s], W4p + (size_t)(c + 2 - kTcChunks) * kTcN * kHidden, kTcChunkBytes, &S.tma_bar[s]);
+          tma_pending[s] = 1;
+        }
+      }
+      const int quarter = warp >> 2;
+      const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)s * kTcN + (uint32_t)quarter * 64;
+#pragma unroll 1
+      for (int j = 0; j < 2; j++) {
+        uint32_t acc[32];
+        tmem_ld32(taddr + (uint32_t)(j * 32), acc);
+        const int col0 = c * kTcN + quarter * 64 + j * 32;
+#pragma unroll
+        for (int q = 0; q < 32; q++) top4_insert(v, ix, __fadd_rn(__uint_as_float(acc[q]), S.b4[col0 + q]), col0 + q);
+      }
+      tc_fence_before();
+      __syncthreads();
+      if (S.fail) {
+        failed = true;
+        break;
+      }
+    }
+    if (failed) break;
+    {  // merge the four column quarters of each row (ties to the lower column)
+      const int row = (warp & 3) * 32 + lane, quarter = warp >> 2;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        S.mv[row][quarter][q] = v[q];
+        S.mi[row][quarter][q] = ix[q];
+      }
+    }
+    __syncthreads();
+    if (tid < kTcRays) {
+      float bv[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+      int bi[4] = {-1, -1, -1, -1};
+      for (int qq = 0; qq < 4; qq++)
+        for (int q = 0; q < 4; q++) {
+          const float x = S.mv[tid][qq][q];
+          const int i = S.mi[tid][qq][q];
+          if (i < 0) continue;
+          // insert (x, i) ordered by value desc, column asc
+          int pos = 4;
+          while (pos > 0 && (x > bv[pos - 1] || (x == bv[pos - 1] && (unsigned)i < (unsigned)bi[pos - 1]))) pos--;
+          if (pos < 4) {
+            for (int m = 3; m > pos; m--) { bv[m] = bv[m - 1]; bi[m] = bi[m - 1]; }
+            bv[pos] = x;
+            bi[pos] = i;
+          }
+        }
+      const uint32_t rid = r0 + tid;
+      if (rid < M) {
+        auto node = [&](int tl) { return tl >= 0 ? __ldg(node_of_treelet + tl) : kInvalidID; };
+        if (seeds) seeds[rid] = make_uint4(node(bi[0]), node(bi[1]), node(bi[2]), node(bi[3]));
+        if (treelets)
+          reinterpret_cast<uint4*>(treelets)[rid] = make_uint4((uint32_t)bi[0], (uint32_t)bi[1], (uint32_t)bi[2], (uint32_t)bi[3]);
+      }
+    }
+  }
+  if (failed && leader) {
+    atomicOr(err, kErrIterationLimit);
+    // let copies still in flight land before the shared memory is released
+    for (int s = 0; s < 2; s++)
+      if (tma_pending[s]) mbar_wait(&S.tma_bar[s], tma_par[s]);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(kTmemCols) : "memory");
+}
+
 inline unsigned blocks_for(uint64_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
 
 int num_sms() {
@@ -664,6 +959,10 @@ cudaError_t Proposer::init(const std::vector<uint32_t>& node_of_treelet, const s
   GB_TRY(cudaMalloc(&prim_treelet_, std::max<size_t>(1, num_prims) * sizeof(uint32_t)));
   GB_TRY(cudaMalloc(&geom_prefix_, std::max<size_t>(1, num_geom_ids_) * sizeof(uint32_t)));
   GB_TRY(cudaMalloc(&acc_, 16 * sizeof(float)));
+  GB_TRY(cudaMalloc(&W4p_, (size_t)kTreelets * kHidden * sizeof(uint16_t)));
+  GB_TRY(cudaMalloc(&err_, sizeof(uint32_t)));
+  GB_TRY(cudaMemsetAsync(err_, 0, sizeof(uint32_t), st));
+  GB_TRY(cudaFuncSetAttribute(k_propose_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem)));
   std::vector<uint32_t> nodes(kTreelets, kInvalidID);
   std::copy(node_of_treelet.begin(), node_of_treelet.begin() + num_treelets, nodes.begin());
   GB_TRY(cudaMemcpyAsync(node_of_treelet_, nodes.data(), kTreelets * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
@@ -678,18 +977,26 @@ cudaError_t Proposer::init(const std::vector<uint32_t>& node_of_treelet, const s
   k_init_params<<<blocks, 256, 0, st>>>(P_, seed);
   k_to_bf16<<<blocks, 256, 0, st>>>(P_, Pb_, kNumParams);
   note_launches(2);
+  GB_TRY(refresh_w4(st));
   GB_TRY(cudaGetLastError());
   return cudaStreamSynchronize(st);
 }
 
+cudaError_t Proposer::refresh_w4(cudaStream_t st) {
+  k_permute_w4<<<blocks_for((uint64_t)kTreelets * (kHidden / 8), 256), 256, 0, st>>>(Pb_, W4p_);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
 void Proposer::release() {
   void* ptrs[] = {P_, Pb_, G_, m_, v_, node_of_treelet_, prim_treelet_, geom_prefix_, acc_, X0_, H1_, H2_, H3_,
-                  dZ4_, dZ_, Z_, Z4_, dH_, dX0_};
+                  dZ4_, dZ_, Z_, Z4_, dH_, dX0_, W4p_, err_};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   P_ = G_ = m_ = v_ = acc_ = Z_ = Z4_ = dH_ = dX0_ = nullptr;
   Pb_ = X0_ = H1_ = H2_ = H3_ = dZ4_ = dZ_ = nullptr;
-  node_of_treelet_ = prim_treelet_ = geom_prefix_ = nullptr;
+  node_of_treelet_ = prim_treelet_ = geom_prefix_ = err_ = nullptr;
+  W4p_ = nullptr;
   cap_ = 0;
 }
 
@@ -816,12 +1123,21 @@ cudaError_t Proposer::train(const char* records, uint64_t stride, uint32_t M, ui
       stats.top4 = acc[2] / acc[3];
     }
   }
+  if ((err = refresh_w4(st)) != cudaSuccess) return fail(err);
   return fail(cudaGetLastError());
 }
 
 cudaError_t Proposer::predict(const char* rays, uint64_t stride, uint32_t M, uint4* seeds, uint32_t* treelets,
-                              cudaStream_t st, const uint32_t* d_count) {
+                              cudaStream_t st, const uint32_t* d_count, uint32_t* err) {
   if (M == 0) return cudaSuccess;
+  if (!use_mma_sync) {
+    const uint32_t grid_n = std::min<uint32_t>((M + kTcRays - 1) / kTcRays, (uint32_t)num_sms());
+    k_propose_tc<<<grid_n, kTcThreads, sizeof(TcSmem), st>>>(rays, stride, M, d_count, grid, Pb_, P_, W4p_,
+                                                             node_of_treelet_, (int)num_treelets, seeds, treelets,
+                                                             err ? err : err_);
+    note_launches(1);
+    return cudaGetLastError();
+  }
   const uint32_t ntiles = (M + kPRays - 1) / kPRays;
   const uint32_t grid_n = std::min<uint32_t>(ntiles, (uint32_t)num_sms() * 2);
   k_propose<<<grid_n, kPW * 32, sizeof(PropSmem), st>>>(rays, stride, M, d_count, grid, Pb_, P_, node_of_treelet_,
@@ -851,6 +1167,7 @@ cudaError_t Proposer::set_params(const float* host, cudaStream_t st) {
   GB_TRY(cudaMemcpyAsync(P_, host, kNumParams * sizeof(float), cudaMemcpyDefault, st));
   k_to_bf16<<<(unsigned)num_sms() * 8, 256, 0, st>>>(P_, Pb_, kNumParams);
   note_launches(1);
+  GB_TRY(refresh_w4(st));
   GB_TRY(cudaGetLastError());
   return cudaStreamSynchronize(st);
 }

@@ -81,8 +81,9 @@ class Proposer {
   // Top-4 proposals for M rays (RTCRay prefix of each record): node indices for
   // a seeded traversal (seeds, optional) and treelet indices (treelets, 4 per ray, optional).
   // d_count (optional, device): the number of rays is min(*d_count, M), read by the kernel.
+  // err (optional, device): receives kErrIterationLimit if the tensor-core kernel timed out.
   cudaError_t predict(const char* rays, uint64_t stride, uint32_t M, uint4* seeds, uint32_t* treelets,
-                      cudaStream_t st, const uint32_t* d_count = nullptr);
+                      cudaStream_t st, const uint32_t* d_count = nullptr, uint32_t* err = nullptr);
   // Loss and gradients of one batch (rays + labels in device memory); grads
   // receives kNumParams floats (device).
   cudaError_t gradients(const char* rays, uint64_t stride, const int32_t* labels, uint32_t B, float* grads,
@@ -93,6 +94,7 @@ class Proposer {
 
   uint32_t num_treelets = 0;
   uint32_t num_prims = 0;
+  bool use_mma_sync = false;  // inference on mma.sync instead of tcgen05 (device key gpu.proposer=mma)
   GridSpec grid{};
   TrainStats stats;
 
@@ -111,6 +113,9 @@ class Proposer {
   uint32_t* geom_prefix_ = nullptr;
   uint32_t num_geom_ids_ = 0;
   float* acc_ = nullptr;       // device accumulators: loss sum, top1 count, top4 count, labelled count
+  uint16_t* W4p_ = nullptr;    // output weights in the tensor cores' shared-memory layout
+  uint32_t* err_ = nullptr;    // error word of inference calls without one
+  cudaError_t refresh_w4(cudaStream_t st);
 
   // batch scratch
   uint32_t cap_ = 0;

@@ -255,7 +255,7 @@ struct FrameBody {
       P.robust = bvh->robust;
       GB_TRY(cudaMemsetAsync(scratch, 0, sizeof(uint32_t), st));
       if (learned && prop) {
-        GB_TRY(prop->predict(rays[cur], 80, n, seeds, nullptr, st, counts + b));
+        GB_TRY(prop->predict(rays[cur], 80, n, seeds, nullptr, st, counts + b, scratch + 1));
         nk++;
         P.seeds = seeds;
         P.max_iters = 8 * bvh->num_nodes + 64;

@@ -22,7 +22,9 @@
 
 #include <mutex>
 
+#include "gb_build.h"
 #include "gb_common.h"
+#include "gb_launch.h"
 #include "gb_trace.h"
 
 namespace gb {
@@ -242,9 +244,32 @@ __device__ __forceinline__ void load_ray(const char* p, TRay& r, float& tfar) {
 // every triangle whose distance can be the minimum.  `seeding` stays set until
 // the root group is popped; a ray whose final hit was found while it was set
 // counts as a proposal hit.
-template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED>
+//
+// INST: the scene holds instance leaves (kInstanceLeaf records).  Reaching one,
+// the lane pushes the rest of its triangle group and a marker, switches to the
+// instanced scene's BVH and transforms its ray into the instance's space the
+// way the reference does (kernels/geometry/instance_intersector.cpp:56-69,
+// xfmPoint / xfmVector of common/math/affinespace.h:102-103).  The ray
+// parameter t is the same in both spaces (affine map, direction not
+// renormalised), so tfar carries over.  Popping the marker reloads the world
+// ray from its record.  Instances inside instances are skipped (one instance
+// level, RTC_MAX_INSTANCE_LEVEL_COUNT = 1).
+constexpr uint32_t kInstMarker = 0xFFFFFFFFu;  // stack entry (kInstMarker, 0)
+
+__device__ __forceinline__ void to_instance(const float* __restrict__ m, TRay& r) {
+  const float3 o = r.org, d = r.dir;
+  r.org = make_float3(__fmaf_rn(o.x, m[0], __fmaf_rn(o.y, m[3], __fmaf_rn(o.z, m[6], m[9]))),
+                      __fmaf_rn(o.x, m[1], __fmaf_rn(o.y, m[4], __fmaf_rn(o.z, m[7], m[10]))),
+                      __fmaf_rn(o.x, m[2], __fmaf_rn(o.y, m[5], __fmaf_rn(o.z, m[8], m[11]))));
+  r.dir = make_float3(__fmaf_rn(d.x, m[0], __fmaf_rn(d.y, m[3], __fmul_rn(d.z, m[6]))),
+                      __fmaf_rn(d.x, m[1], __fmaf_rn(d.y, m[4], __fmul_rn(d.z, m[7]))),
+                      __fmaf_rn(d.x, m[2], __fmaf_rn(d.y, m[5], __fmul_rn(d.z, m[8]))));
+}
+
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED, bool INST = false>
 __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
-  const Ctx c{P.nodes, P.tris, P.err, P.max_iters, P.num_nodes, P.num_tris};
+  Ctx c{P.nodes, P.tris, P.err, P.max_iters, P.num_nodes, P.num_tris};
+  uint32_t cur_inst = kInvalidID, hit_inst = kInvalidID;  // INST: instance being traversed / of the hit
   const int lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t nrays = P.nrays_ptr ? *P.nrays_ptr : P.nrays;
@@ -266,8 +291,9 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
       if (base + __popc(idle) >= nrays) exhausted = true;
       if (!active) {
-        const uint32_t rid = base + __popc(idle & lt_mask);
+        uint32_t rid = base + __popc(idle & lt_mask);
         if (rid < nrays) {
+          if (P.order) rid = __ldg(P.order + rid);  // the record this fetch slot traces
           rec = P.rays + (uint64_t)rid * P.stride;
           float tfar;
           load_ray<ALIGNED>(rec, r, tfar);
@@ -283,6 +309,14 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
               if (__ldg(P.batch_start + mid) <= rid) lo = mid; else hi = mid;
             }
             root = __ldg(P.batch_root + lo);
+          }
+          if (INST) {  // a ray that ended inside an instance left the lane in its space
+            c.nodes = P.nodes;
+            c.tris = P.tris;
+            c.num_nodes = P.num_nodes;
+            c.num_tris = P.num_tris;
+            cur_inst = kInvalidID;
+            hit_inst = kInvalidID;
           }
           if (valid && root < c.num_nodes) {
             init_ray(r);
@@ -356,12 +390,38 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
       if (ti >= c.num_tris) { atomicOr(c.err, kErrBuild); active = false; break; }
       const float4* tp = reinterpret_cast<const float4*>(c.tris + ti);
       const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
+      if (INST && __float_as_uint(d.w) == kInstanceLeaf) {
+        const uint32_t ii = __float_as_uint(a.w);
+        if (cur_inst != kInvalidID) continue;  // nested instance: not traversed
+        if (ii >= P.ninsts) { atomicOr(c.err, kErrBuild); active = false; break; }
+        const InstDesc* in = P.insts + ii;
+        const uint32_t bn = in->num_nodes;
+        if (bn == 0) continue;  // empty instanced scene
+        if (sp + 3 > kStackSize) { atomicOr(c.err, kErrStackOverflow); active = false; break; }
+        // the node group of this visit (its hit internal children) and the rest of this
+        // leaf group resume after the instance
+        if (g_bits & 0xFF000000u) stack[sp++] = make_uint2(g_base, g_bits);
+        if (t_bits) stack[sp++] = make_uint2(t_base | kTriGroup, t_bits);
+        stack[sp++] = make_uint2(kInstMarker, 0u);
+        t_bits = 0;
+        cur_inst = ii;
+        c.nodes = in->nodes;
+        c.tris = in->tris;
+        c.num_nodes = bn;
+        c.num_tris = in->num_tris;
+        to_instance(in->w2l, r);
+        init_ray(r);
+        g_base = 0;
+        g_bits = (1u << (24 + r.oct)) | 1u;
+        break;
+      }
       if (COUNT) n_tris++;
       if (ROBUST) {
         float U, V, UVW, t;
         if (pluecker(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org,
                      r.dir, r.tnear, t_best, U, V, UVW, t)) {
           hit_tri = ti;
+          if (INST) hit_inst = cur_inst;
           if (SEEDED && seeding) seed_tri = ti;
           if (ANYHIT) { done = true; t_bits = 0; break; }
           // PlueckerHitM::finalize: u,v = U,V * rcp(UVW), 0 when |UVW| < 1e-18
@@ -375,6 +435,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
         if (moeller(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(d.x, d.y, d.z), r.org, r.dir,
                     r.tnear, t_best, U, V, T, absDen)) {
           hit_tri = ti;
+          if (INST) hit_inst = cur_inst;
           if (SEEDED && seeding) seed_tri = ti;
           if (ANYHIT) { done = true; t_bits = 0; break; }
           const float rcp = __frcp_rn(absDen);
@@ -388,7 +449,19 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
     if (active && !done && t_bits == 0 && !(g_bits & 0xFF000000u)) {
       if (sp > 0) {
         const uint2 e = stack[--sp];
-        if (e.x & kTriGroup) { t_base = e.x & ~kTriGroup; t_bits = e.y; g_bits = 0; }
+        if (INST && e.x == kInstMarker && e.y == 0u) {
+          // leaving the instance: world ray and top-level BVH again
+          float unused_tfar;
+          load_ray<ALIGNED>(rec, r, unused_tfar);
+          init_ray(r);
+          c.nodes = P.nodes;
+          c.tris = P.tris;
+          c.num_nodes = P.num_nodes;
+          c.num_tris = P.num_tris;
+          cur_inst = kInvalidID;
+          g_bits = 0;
+          t_bits = 0;
+        } else if (e.x & kTriGroup) { t_base = e.x & ~kTriGroup; t_bits = e.y; g_bits = 0; }
         else { g_base = e.x; g_bits = e.y; }
         if (SEEDED && sp == 0) seeding = false;  // the root group: proposals are done
       } else {
@@ -402,7 +475,9 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
         if (ANYHIT) {
           *reinterpret_cast<float*>(rec + 32) = -INFINITY;
         } else {
-          const float4* tp = reinterpret_cast<const float4*>(c.tris + hit_tri);
+          const TriRecord* htris = (INST && hit_inst != kInvalidID) ? P.insts[hit_inst].tris : P.tris;
+          const uint32_t inst_id = (INST && hit_inst != kInvalidID) ? P.insts[hit_inst].geomID : kInvalidID;
+          const float4* tp = reinterpret_cast<const float4*>(htris + hit_tri);
           const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
           const float3 Ng = ROBUST ? pluecker_normal(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
                                                      make_float3(d.x, d.y, d.z), r.org)
@@ -411,12 +486,12 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
           if (ALIGNED) {
             *reinterpret_cast<float4*>(rec + 48) = make_float4(Ng.x, Ng.y, Ng.z, hu);
             *reinterpret_cast<uint4*>(rec + 64) =
-                make_uint4(__float_as_uint(hv), __float_as_uint(a.w), __float_as_uint(b.w), kInvalidID);
+                make_uint4(__float_as_uint(hv), __float_as_uint(a.w), __float_as_uint(b.w), inst_id);
           } else {
             float* f = reinterpret_cast<float*>(rec + 48);
             f[0] = Ng.x; f[1] = Ng.y; f[2] = Ng.z; f[3] = hu; f[4] = hv;
             uint32_t* w = reinterpret_cast<uint32_t*>(rec + 68);
-            w[0] = __float_as_uint(a.w); w[1] = __float_as_uint(b.w); w[2] = kInvalidID;
+            w[0] = __float_as_uint(a.w); w[1] = __float_as_uint(b.w); w[2] = inst_id;
           }
         }
       }
@@ -442,14 +517,14 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(TraceParams P) {
   }
 }
 
-template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED = false>
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED = false, bool INST = false>
 static cudaError_t launch_one(const TraceParams& P, cudaStream_t st) {
   static int blocks_per_sm = -1, num_sms = 0;
   if (blocks_per_sm < 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED, INST>,
                                                   TRACE_THREADS, 0);
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
@@ -457,12 +532,18 @@ static cudaError_t launch_one(const TraceParams& P, cudaStream_t st) {
   uint64_t grid = (uint64_t)num_sms * blocks_per_sm;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
-  k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
+  k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED, INST><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
   return cudaGetLastError();
 }
 
 template <bool ANYHIT, bool COUNT>
 static cudaError_t launch_variant(const TraceParams& P, bool aligned, cudaStream_t st) {
+  // scenes with instances (non-robust, no proposals or batches: checked by the caller)
+  if (P.insts) {
+    if (P.robust || P.seeds || P.batch_root) return cudaErrorInvalidValue;
+    return aligned ? launch_one<ANYHIT, COUNT, true, false, false, true>(P, st)
+                   : launch_one<ANYHIT, COUNT, false, false, false, true>(P, st);
+  }
   // seeded queries: 16-byte aligned records of non-robust scenes (checked by the caller)
   if (P.seeds) {
     if (!aligned || P.robust) return cudaErrorInvalidValue;
@@ -476,6 +557,49 @@ cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStre
   const bool aligned = ((uintptr_t)P.rays % 16 == 0) && (P.stride % 16 == 0);
   if (anyhit) return count ? launch_variant<true, true>(P, aligned, st) : launch_variant<true, false>(P, aligned, st);
   return count ? launch_variant<false, true>(P, aligned, st) : launch_variant<false, false>(P, aligned, st);
+}
+
+// ---------------------------------------------------------------------------
+// Ray reordering
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint64_t spread15(uint32_t x) {
+  uint64_t v = x & 0x7FFFu;
+  v = (v | (v << 16)) & 0x00FF0000FFull;
+  v = (v | (v << 8)) & 0x0F00F00F00Full;
+  v = (v | (v << 4)) & 0xC30C30C30C3ull;
+  v = (v | (v << 2)) & 0x249249249249ull;
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_ray_keys(const char* __restrict__ rays, uint64_t stride, uint32_t M,
+                                                  float lx, float ly, float lz, float sx, float sy, float sz,
+                                                  uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M) return;
+  const float* f = reinterpret_cast<const float*>(rays + (uint64_t)i * stride);
+  const float o[3] = {(f[0] - lx) * sx, (f[1] - ly) * sy, (f[2] - lz) * sz};
+  uint64_t code = 0;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float q = fminf(fmaxf(o[a] * 32768.0f, 0.0f), 32767.0f);  // NaN -> 0
+    code |= spread15((uint32_t)q) << (2 - a);
+  }
+  const uint64_t oct = (f[4] < 0.0f ? 1u : 0u) | (f[5] < 0.0f ? 2u : 0u) | (f[6] < 0.0f ? 4u : 0u);
+  keys[i] = (oct << 45) | code;
+  vals[i] = i;
+}
+
+cudaError_t order_rays(const char* rays, uint64_t stride, uint32_t M, const float lo[3], const float hi[3],
+                       uint64_t* keys, uint32_t* vals, uint64_t* kb, uint32_t* vb, uint32_t* hist, cudaStream_t st) {
+  float s[3];
+  for (int a = 0; a < 3; a++) {
+    const float ext = hi[a] - lo[a];
+    s[a] = (ext > 0.0f && ext < INFINITY) ? 1.0f / ext : 0.0f;
+  }
+  k_ray_keys<<<(M + 255) / 256, 256, 0, st>>>(rays, stride, M, lo[0], lo[1], lo[2], s[0], s[1], s[2], keys, vals);
+  note_launches(1);
+  return sort_pairs_passes(keys, vals, kb, vb, hist, M, 6, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -20,6 +20,9 @@ struct TraceParams {
   const unsigned int* nrays_ptr;  // optional: the ray count is read from device memory
   const uint4* seeds;         // optional: per ray up to four subtree roots (node indices,
                               // kInvalidID = none) traversed before the root
+  const uint32_t* order;      // optional: the i-th fetched ray is record order[i] (ray reordering)
+  const InstDesc* insts;      // optional: instance table of a scene with instance leaves
+  uint32_t ninsts;
   const uint32_t* batch_start;  // optional (segmented BVHs): rays [batch_start[b], batch_start[b+1])
   const uint32_t* batch_root;   //   start at node batch_root[b] (kInvalidID: the batch hits nothing)
   uint32_t nbatches;
@@ -27,6 +30,14 @@ struct TraceParams {
 
 // Launches the persistent closest-hit (anyhit = false) or any-hit kernel.
 cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStream_t st);
+
+// Ray reordering: writes, for M records, keys = direction octant (3 bits) over a
+// 45-bit Morton code of the origin in the box lo..hi (15 bits per axis) and
+// vals = record index, then sorts them (6 digit passes) so that vals becomes a
+// fetch order in which neighbouring rays start close together and point into
+// the same octant.  Scratch: kb/vb (M entries), hist (sort_hist_entries(M)).
+cudaError_t order_rays(const char* rays, uint64_t stride, uint32_t M, const float lo[3], const float hi[3],
+                       uint64_t* keys, uint32_t* vals, uint64_t* kb, uint32_t* vb, uint32_t* hist, cudaStream_t st);
 
 // Size of the staging area for host-resident rays in the no-allocation query.
 constexpr uint64_t kNoAllocStagingBytes = 32ull << 20;

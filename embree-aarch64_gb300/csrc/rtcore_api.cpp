@@ -88,6 +88,8 @@ struct Device : RefCounted {
   // GB300 the kernel reaches host memory over NVLink-C2C at the pace it
   // consumes rays, so no copy phase is exposed.
   int host_mode = 2;
+  bool proposer_mma = false;  // gpu.proposer=mma: proposer inference on mma.sync instead of tcgen05
+  int reorder = 0;            // gpu.reorder=1: streams of >= 65536 rays are traced in octant + origin-Morton order
   int pageable_access = 0;     // cudaDevAttrPageableMemoryAccess
   int host_ptr_registered = 0; // cudaDevAttrCanUseHostPointerForRegisteredMem
   std::mutex mtx;
@@ -104,7 +106,8 @@ struct Device : RefCounted {
   }
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
-  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.host_rays; the CPU tasking and ISA keys
+  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.host_rays, gpu.proposer, gpu.reorder;
+  // the CPU tasking and ISA keys
   // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
   void parse(const char* cfg) {
     std::string s(cfg);
@@ -126,6 +129,8 @@ struct Device : RefCounted {
         else if (k == "gpu.leaf_max") build_opt.leaf_max = atoi(v.c_str());
         else if (k == "gpu.morton") build_opt.morton_cube = (v == "cube");
         else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
+        else if (k == "gpu.proposer") proposer_mma = (v == "mma");
+        else if (k == "gpu.reorder") reorder = atoi(v.c_str());
       }
       i = j + 1;
     }
@@ -233,6 +238,48 @@ bool is_device_pointer(const void* p) {
   return t == cudaMemoryTypeDevice || t == cudaMemoryTypeManaged;
 }
 
+struct Scene;
+void release_scene_ref(Scene* s);
+
+// Affine maps of instances, columns vx, vy, vz, p (the reference's
+// AffineSpace3fa).  Fused multiply-adds where the reference's SSE/AVX2 code
+// fuses them (madd chains of linearspace3.h / affinespace.h); this file is
+// compiled with -ffp-contract=off so nothing else is fused.
+namespace xf {
+inline float dot3(const float* a, const float* b) { return std::fma(a[0], b[0], std::fma(a[1], b[1], a[2] * b[2])); }
+inline void cross3(const float* a, const float* b, float* o) {
+  o[0] = std::fma(a[1], b[2], -(a[2] * b[1]));
+  o[1] = std::fma(a[2], b[0], -(a[0] * b[2]));
+  o[2] = std::fma(a[0], b[1], -(a[1] * b[0]));
+}
+// world-to-local: rcp(AffineSpace3fa) = (adjoint / det, -(inverse * p))
+// (common/math/affinespace.h:83, common/math/linearspace3.h:44-50), with the
+// correctly rounded 1/det.  Returns false for a singular or non-finite map.
+inline bool invert(const float* m, float* out) {
+  const float *vx = m, *vy = m + 3, *vz = m + 6, *p = m + 9;
+  float c0[3], c1[3], c2[3];
+  cross3(vy, vz, c0);
+  cross3(vz, vx, c1);
+  cross3(vx, vy, c2);
+  const float det = dot3(vx, c0);
+  if (!(det != 0.0f) || !std::isfinite(det)) return false;
+  const float r = 1.0f / det;
+  for (int j = 0; j < 3; j++) {  // transposed adjoint: column j = (c0[j], c1[j], c2[j])
+    out[3 * j + 0] = c0[j] * r;
+    out[3 * j + 1] = c1[j] * r;
+    out[3 * j + 2] = c2[j] * r;
+  }
+  for (int c = 0; c < 3; c++) out[9 + c] = -std::fma(p[0], out[c], std::fma(p[1], out[3 + c], p[2] * out[6 + c]));
+  for (int k = 0; k < 12; k++)
+    if (!std::isfinite(out[k])) return false;
+  return true;
+}
+// xfmPoint (affinespace.h:102): madd chains ending in the translation
+inline void xfm_point(const float* m, const float* q, float* o) {
+  for (int c = 0; c < 3; c++) o[c] = std::fma(q[0], m[c], std::fma(q[1], m[3 + c], std::fma(q[2], m[6 + c], m[9 + c])));
+}
+}  // namespace xf
+
 struct Geometry : RefCounted {
   Device* device;
   RTCGeometryType type;
@@ -247,11 +294,15 @@ struct Geometry : RefCounted {
   char* d_verts = nullptr;
   char* d_idx = nullptr;
   size_t cap_verts = 0, cap_idx = 0;
+  // instances: the instanced scene (retained) and the local-to-world map
+  Scene* inst_scene = nullptr;
+  float l2w[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
 
   Geometry(Device* d, RTCGeometryType t) : device(d), type(t) { device->inc(); }
   ~Geometry() override {
     if (d_verts) cudaFree(d_verts);
     if (d_idx) cudaFree(d_idx);
+    if (inst_scene) release_scene_ref(inst_scene);
     device->dec();
   }
 
@@ -355,6 +406,19 @@ struct ThreadCtx {
       cuda_ok(cudaEventCreateWithFlags(&ev_tr[i], cudaEventDisableTiming), "event");
     }
   }
+  char* obuf = nullptr;     // ray reordering: keys, values and sort scratch
+  size_t ocap = 0;
+  char* order_buffer(size_t bytes) {
+    if (bytes > ocap) {
+      if (obuf) cudaFree(obuf);
+      obuf = nullptr;
+      ocap = 0;
+      const size_t want = std::max(bytes, ocap * 2);
+      cuda_ok(cudaMalloc((void**)&obuf, want), "cudaMalloc ray order");
+      ocap = want;
+    }
+    return obuf;
+  }
   uint4* seeds = nullptr;   // learned queries: per-ray proposals
   size_t seeds_cap = 0;
   uint4* seed_buffer(size_t n) {
@@ -382,6 +446,7 @@ struct ThreadCtx {
   ~ThreadCtx() {
     if (dbuf) cudaFree(dbuf);
     if (seeds) cudaFree(seeds);
+    if (obuf) cudaFree(obuf);
     if (dscratch) cudaFree(dscratch);
     if (hscratch) cudaFreeHost(hscratch);
     if (own) cudaStreamDestroy(own);
@@ -431,11 +496,20 @@ struct Scene : RefCounted {
   bool batched = false;             // rtcgbSetSceneBatched: one tree per geometry
   uint32_t* d_roots = nullptr;      // batched BVH: root node per geometry ID (device)
   uint32_t nroots = 0;
+  uint64_t commit_serial = 0;       // counts commits (builds and refits)
+  // instances of the committed BVH: device table, and the instanced scenes it
+  // reads (retained) with their commit serials at this scene's commit
+  gb::InstDesc* d_insts = nullptr;
+  uint32_t ninsts = 0;
+  uint64_t inst_nodes = 0;          // nodes of all instanced BVHs (iteration bound)
+  std::vector<std::pair<Scene*, uint64_t>> inst_refs;
 
   explicit Scene(Device* d) : device(d) { device->inc(); }
+  void drop_instances();
   ~Scene() override {
     for (Geometry* g : geoms)
       if (g) g->dec();
+    drop_instances();
     if (d_roots) cudaFree(d_roots);
     gb::free_bvh(&bvh);
     device->dec();
@@ -482,6 +556,52 @@ struct Scene : RefCounted {
     if (progress && !progress(progress_ptr, 0.0)) fail(RTC_ERROR_CANCELLED, "progress monitor forced termination");
     std::vector<gb::GeomDesc> descs;
     uint64_t total = 0;
+    // instances: world boxes for the builder, the traversal's table, the scenes they read
+    std::vector<gb::InstBox> iboxes;
+    std::vector<gb::InstDesc> idescs;
+    std::vector<std::pair<Scene*, uint64_t>> irefs;
+    uint64_t inodes = 0;
+    const bool robust_now = (flags & RTC_SCENE_FLAG_ROBUST) != 0;
+    for (unsigned id = 0; id < geoms.size(); id++) {
+      Geometry* g = geoms[id];
+      if (!g || !g->enabled || g->type != RTC_GEOMETRY_TYPE_INSTANCE || !g->inst_scene) continue;
+      if (batched) fail(RTC_ERROR_INVALID_OPERATION, "batched scenes hold triangle meshes only");
+      if (robust_now) fail(RTC_ERROR_INVALID_OPERATION, "instances in robust scenes are not supported");
+      Scene* is = g->inst_scene;
+      if (is == this) fail(RTC_ERROR_INVALID_OPERATION, "a scene cannot instance itself");
+      if (!is->committed) fail(RTC_ERROR_INVALID_OPERATION, "instanced scene not committed");
+      if (is->bvh.robust || is->batched) fail(RTC_ERROR_INVALID_OPERATION, "instanced scene must be a plain triangle scene");
+      irefs.push_back({is, is->commit_serial});
+      if (is->bvh.num_nodes == 0) continue;  // empty scene: nothing to hit
+      gb::InstDesc in{};
+      if (!xf::invert(g->l2w, in.w2l)) continue;  // singular transform: the instance is never hit
+      in.nodes = is->bvh.nodes;
+      in.tris = is->bvh.tris;
+      in.num_nodes = is->bvh.num_nodes;
+      in.num_tris = is->bvh.num_tris;
+      in.geomID = id;
+      // xfmBounds (affinespace.h:105-118) of the instanced scene's box, widened
+      // by a few ulps of its magnitude so that rounding never culls a hit
+      gb::InstBox b{};
+      for (int a = 0; a < 3; a++) { b.lo[a] = INFINITY; b.hi[a] = -INFINITY; }
+      for (int k = 0; k < 8; k++) {
+        const float q[3] = {(k & 1) ? is->bvh.hi[0] : is->bvh.lo[0], (k & 2) ? is->bvh.hi[1] : is->bvh.lo[1],
+                            (k & 4) ? is->bvh.hi[2] : is->bvh.lo[2]};
+        float w[3];
+        xf::xfm_point(g->l2w, q, w);
+        for (int a = 0; a < 3; a++) { b.lo[a] = std::min(b.lo[a], w[a]); b.hi[a] = std::max(b.hi[a], w[a]); }
+      }
+      for (int a = 0; a < 3; a++) {
+        const float mag = std::max(std::fabs(b.lo[a]), std::fabs(b.hi[a])) + (b.hi[a] - b.lo[a]);
+        b.lo[a] -= 4e-6f * mag;
+        b.hi[a] += 4e-6f * mag;
+      }
+      b.inst = (uint32_t)idescs.size();
+      b.geomID = id;
+      iboxes.push_back(b);
+      idescs.push_back(in);
+      inodes += in.num_nodes;
+    }
     for (unsigned id = 0; id < geoms.size(); id++) {
       Geometry* g = geoms[id];
       if (!g || !g->enabled || g->type != RTC_GEOMETRY_TYPE_TRIANGLE) continue;
@@ -498,10 +618,31 @@ struct Scene : RefCounted {
       total += d.ntris;
       descs.push_back(d);
     }
+    // all instances as one kind-1 geometry of box primitives
+    gb::InstBox* d_boxes = nullptr;
+    std::unique_ptr<gb::InstBox, void (*)(gb::InstBox*)> boxes_guard(nullptr, [](gb::InstBox* q) { if (q) cudaFree(q); });
+    if (!iboxes.empty()) {
+      cuda_ok(cudaMalloc((void**)&d_boxes, iboxes.size() * sizeof(gb::InstBox)), "cudaMalloc instances");
+      boxes_guard.reset(d_boxes);
+      cuda_ok(cudaMemcpyAsync(d_boxes, iboxes.data(), iboxes.size() * sizeof(gb::InstBox), cudaMemcpyHostToDevice, st),
+              "instances");
+      gb::GeomDesc d{};
+      d.verts = (const char*)d_boxes;
+      d.ntris = (uint32_t)iboxes.size();
+      d.geomID = gb::kInvalidID;
+      d.prim_offset = (uint32_t)total;
+      d.kind = 1;
+      total += d.ntris;
+      descs.push_back(d);
+    }
     if (total >= 0x7FFFFFFFull) fail(RTC_ERROR_INVALID_OPERATION, "too many primitives");
     std::vector<SigEntry> sig;
     bool all_refit = !descs.empty();
     for (const gb::GeomDesc& d : descs) {
+      if (d.kind != 0) {  // scenes with instances are always rebuilt
+        all_refit = false;
+        continue;
+      }
       const Geometry* g = geoms[d.geomID];
       sig.push_back(SigEntry{d.geomID, g, g->topo_version, d.ntris, d.nverts});
       all_refit &= g->quality == RTC_BUILD_QUALITY_REFIT;
@@ -516,6 +657,7 @@ struct Scene : RefCounted {
       if (!fallback) {
         stats = bs;
         this->descs = descs;
+        commit_serial++;
         if (progress) progress(progress_ptr, 1.0);
         return;
       }
@@ -545,7 +687,19 @@ struct Scene : RefCounted {
     stats = bs;
     committed = true;
     build_serial++;
+    commit_serial++;
     this->descs = descs;
+    drop_instances();
+    if (!idescs.empty()) {
+      cuda_ok(cudaMalloc((void**)&d_insts, idescs.size() * sizeof(gb::InstDesc)), "cudaMalloc instance table");
+      cuda_ok(cudaMemcpyAsync(d_insts, idescs.data(), idescs.size() * sizeof(gb::InstDesc), cudaMemcpyHostToDevice, st),
+              "instance table");
+      cuda_ok(cudaStreamSynchronize(st), "instance table");
+      ninsts = (uint32_t)idescs.size();
+      inst_nodes = inodes;
+    }
+    for (auto& r : irefs) r.first->inc();
+    inst_refs = irefs;
     built_sig = sig;
     built_robust = robust;
     if (progress) progress(progress_ptr, 1.0);
@@ -557,6 +711,17 @@ struct Scene : RefCounted {
               bs.num_nodes, bs.depth, bs.sah, bs.build_ms);
   }
 };
+
+void Scene::drop_instances() {
+  if (d_insts) cudaFree(d_insts);
+  d_insts = nullptr;
+  ninsts = 0;
+  inst_nodes = 0;
+  for (auto& r : inst_refs) r.first->dec();
+  inst_refs.clear();
+}
+
+void release_scene_ref(Scene* s) { s->dec(); }
 
 // ---------------------------------------------------------------------------
 // learned proposer
@@ -604,6 +769,11 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
     fail(RTC_ERROR_INVALID_OPERATION, scene->batched ? "batched scene: use rtcgbIntersect1MBatched / rtcgbOccluded1MBatched"
                                                      : "not a batched scene (rtcgbSetSceneBatched)");
   if (prop && scene->batched) fail(RTC_ERROR_INVALID_OPERATION, "the proposer does not support batched scenes");
+  if (prop && scene->ninsts) fail(RTC_ERROR_INVALID_OPERATION, "the proposer does not support scenes with instances");
+  // the BVHs the instance leaves point to must be those of this scene's commit
+  for (const auto& r : scene->inst_refs)
+    if (!r.first->committed || r.first->commit_serial != r.second)
+      fail(RTC_ERROR_INVALID_OPERATION, "an instanced scene changed: commit the instancing scene again");
   if (prop && prop->scene != scene) fail(RTC_ERROR_INVALID_ARGUMENT, "proposer belongs to another scene");
   // seeded traversal needs 16-byte aligned records; otherwise the plain one runs
   if (prop && (!prop->current() || (stride % 16) != 0)) prop = nullptr;
@@ -628,6 +798,11 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   P.err = c.dscratch + 1;
   P.counters = reinterpret_cast<gb::TraceCounters*>(c.dscratch + 2);
   P.max_iters = 4 * bvh.num_nodes + 64;  // node visits, triangle phases and pops per ray
+  if (scene->ninsts) {
+    P.insts = scene->d_insts;
+    P.ninsts = scene->ninsts;
+    P.max_iters = (uint32_t)std::min<uint64_t>(0x7FFFFFFFull, 4 * ((uint64_t)bvh.num_nodes + scene->inst_nodes) + 64);
+  }
   P.num_nodes = bvh.num_nodes;
   P.num_tris = bvh.num_tris;
   P.robust = bvh.robust;
@@ -653,11 +828,26 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   cuda_ok(cudaMemsetAsync(c.dscratch, 0, 64, st), "memset");
   unsigned launches = 1;
   const uint32_t kChunk = 1u << 21;  // rays per pipeline stage
+  // ray reordering (gpu.reorder=1): fetch order by direction octant and origin Morton code
+  auto reorder = [&](gb::TraceParams& Pq) {
+    if (!dev->reorder || Pq.nrays < (1u << 16)) return;
+    const size_t n = Pq.nrays, hist = gb::sort_hist_entries(Pq.nrays);
+    char* b = c.order_buffer(n * 24 + hist * 4 + 64);
+    uint64_t* keys = reinterpret_cast<uint64_t*>(b);
+    uint64_t* kb = keys + n;
+    uint32_t* vals = reinterpret_cast<uint32_t*>(kb + n);
+    uint32_t* vb = vals + n;
+    uint32_t* h = vb + n;
+    cuda_ok(gb::order_rays(Pq.rays, stride, Pq.nrays, bvh.lo, bvh.hi, keys, vals, kb, vb, h, st), "ray order");
+    Pq.order = vals;
+    launches += 19;
+  };
   // learned queries: proposals for every ray, then the seeded traversal
   auto propose = [&](gb::TraceParams& Pq) {
     if (!prop) return;
     uint4* seeds = c.seed_buffer(Pq.nrays);
-    cuda_ok(prop->net.predict(Pq.rays, stride, Pq.nrays, seeds, nullptr, st), "proposer inference");
+    cuda_ok(prop->net.predict(Pq.rays, stride, Pq.nrays, seeds, nullptr, st, nullptr, c.dscratch + 1),
+            "proposer inference");
     Pq.seeds = seeds;
     Pq.max_iters = 8 * bvh.num_nodes + 64;  // proposed subtrees are searched again by the full search
     launches++;
@@ -670,6 +860,7 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
     P.rays = (char*)rays;
     P.nrays = M;
     cuda_ok(cudaEventRecord(c.e1, st), "event");
+    reorder(P);
     propose(P);
     cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
     launches++;
@@ -718,6 +909,7 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
     P.rays = d_rays;
     P.nrays = M;
     cuda_ok(cudaEventRecord(c.e1, st), "event");
+    reorder(P);
     propose(P);
     cuda_ok(gb::launch_trace(P, anyhit, c.counting, st), "traversal launch");
     launches++;
@@ -1038,7 +1230,8 @@ RTC_API RTCGeometry rtcNewGeometry(RTCDevice hdevice, enum RTCGeometryType type)
   Device* d = (Device*)hdevice;
   API_BEGIN
   VERIFY_HANDLE(hdevice);
-  if (type != RTC_GEOMETRY_TYPE_TRIANGLE) fail(RTC_ERROR_UNKNOWN, "geometry type is not supported");
+  if (type != RTC_GEOMETRY_TYPE_TRIANGLE && type != RTC_GEOMETRY_TYPE_INSTANCE)
+    fail(RTC_ERROR_UNKNOWN, "geometry type is not supported");
   return (RTCGeometry) new Geometry(d, type);
   API_END(d)
   return nullptr;
@@ -1194,6 +1387,72 @@ RTC_API void rtcSetGeometryOccludedFilterFunction(RTCGeometry hg, RTCFilterFunct
   API_BEGIN
   VERIFY_HANDLE(hg);
   if (filter) fail(RTC_ERROR_INVALID_OPERATION, "filter functions are not supported by the GPU path");
+  API_END(g ? g->device : nullptr)
+}
+
+// ---- instances (kernels/common/rtcore.cpp:996-1135, scene_instance.cpp)
+
+RTC_API void rtcSetGeometryInstancedScene(RTCGeometry hg, RTCScene hs) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  VERIFY_HANDLE(hs);
+  if (g->type != RTC_GEOMETRY_TYPE_INSTANCE) fail(RTC_ERROR_INVALID_OPERATION, "operation not supported for this geometry");
+  Scene* s = (Scene*)hs;
+  s->inc();
+  if (g->inst_scene) g->inst_scene->dec();
+  g->inst_scene = s;
+  API_END(g ? g->device : nullptr)
+}
+
+// loadTransform / storeTransform (rtcore.cpp:1010-1069): 3x4 row-major, 3x4
+// column-major and 4x4 column-major layouts
+RTC_API void rtcSetGeometryTransform(RTCGeometry hg, unsigned int timeStep, enum RTCFormat format, const void* xfm) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  VERIFY_HANDLE(hg);
+  VERIFY_HANDLE(xfm);
+  if (g->type != RTC_GEOMETRY_TYPE_INSTANCE) fail(RTC_ERROR_INVALID_OPERATION, "operation not supported for this geometry");
+  if (timeStep >= g->time_steps) fail(RTC_ERROR_INVALID_OPERATION, "invalid timestep");
+  const float* m = (const float*)xfm;
+  float t[12];
+  if (format == RTC_FORMAT_FLOAT3X4_ROW_MAJOR) {
+    for (int c = 0; c < 4; c++)
+      for (int r = 0; r < 3; r++) t[3 * c + r] = m[4 * r + c];
+  } else if (format == RTC_FORMAT_FLOAT3X4_COLUMN_MAJOR) {
+    for (int k = 0; k < 12; k++) t[k] = m[k];
+  } else if (format == RTC_FORMAT_FLOAT4X4_COLUMN_MAJOR) {
+    for (int c = 0; c < 4; c++)
+      for (int r = 0; r < 3; r++) t[3 * c + r] = m[4 * c + r];
+  } else {
+    fail(RTC_ERROR_INVALID_OPERATION, "invalid matrix format");
+  }
+  std::memcpy(g->l2w, t, sizeof(t));
+  API_END(g ? g->device : nullptr)
+}
+
+RTC_API void rtcGetGeometryTransform(RTCGeometry hg, float time, enum RTCFormat format, void* xfm) {
+  Geometry* g = (Geometry*)hg;
+  API_BEGIN
+  (void)time;
+  VERIFY_HANDLE(hg);
+  VERIFY_HANDLE(xfm);
+  if (g->type != RTC_GEOMETRY_TYPE_INSTANCE) fail(RTC_ERROR_INVALID_OPERATION, "operation not supported for this geometry");
+  float* m = (float*)xfm;
+  const float* t = g->l2w;
+  if (format == RTC_FORMAT_FLOAT3X4_ROW_MAJOR) {
+    for (int c = 0; c < 4; c++)
+      for (int r = 0; r < 3; r++) m[4 * r + c] = t[3 * c + r];
+  } else if (format == RTC_FORMAT_FLOAT3X4_COLUMN_MAJOR) {
+    for (int k = 0; k < 12; k++) m[k] = t[k];
+  } else if (format == RTC_FORMAT_FLOAT4X4_COLUMN_MAJOR) {
+    for (int c = 0; c < 4; c++) {
+      for (int r = 0; r < 3; r++) m[4 * c + r] = t[3 * c + r];
+      m[4 * c + 3] = c == 3 ? 1.0f : 0.0f;
+    }
+  } else {
+    fail(RTC_ERROR_INVALID_OPERATION, "invalid matrix format");
+  }
   API_END(g ? g->device : nullptr)
 }
 
@@ -1681,6 +1940,7 @@ RTC_API RTCGBProposer rtcgbNewProposer(RTCScene hs, unsigned int seed) {
       grid.lo[a] = ok ? lo : 0.0f;
       grid.scale[a] = ok ? 1.0f / ext : 1.0f;
     }
+    p->net.use_mma_sync = s->device->proposer_mma;
     cuda_ok(p->net.init(p->roots, prim_treelet, prefix, grid, seed, st), "proposer initialisation");
   } catch (...) {
     p->dec();

@@ -21,6 +21,10 @@ RTC_FORMAT_FLOAT3 = 0x9003
 RTC_INVALID_GEOMETRY_ID = 0xFFFFFFFF
 RTC_SCENE_FLAG_ROBUST = 1 << 2
 RTC_BUILD_QUALITY_REFIT = 3
+RTC_GEOMETRY_TYPE_INSTANCE = 121
+RTC_FORMAT_FLOAT3X4_ROW_MAJOR = 0x9134
+RTC_FORMAT_FLOAT3X4_COLUMN_MAJOR = 0x9234
+RTC_FORMAT_FLOAT4X4_COLUMN_MAJOR = 0x9244
 
 ERRORS = {0: "NONE", 1: "UNKNOWN", 2: "INVALID_ARGUMENT", 3: "INVALID_OPERATION", 4: "OUT_OF_MEMORY",
           5: "UNSUPPORTED_CPU", 6: "CANCELLED"}
@@ -43,7 +47,8 @@ rtcgbNewProposer rtcgbRetainProposer rtcgbReleaseProposer rtcgbProposerTrain rtc
 rtcgbProposerParamCount rtcgbProposerGetParams rtcgbProposerSetParams rtcgbProposerGradients rtcgbProposerGetTreelets
 rtcgbIntersect1MLearned rtcgbOccluded1MLearned rtcgbNewPathTracer rtcgbRetainPathTracer rtcgbReleasePathTracer
 rtcgbPathTracerAnimateSoup rtcgbPathTracerSetProposer rtcgbPathTracerRenderFrame rtcgbPathTracerTrainProposer
-rtcgbPathTracerGetImage rtcgbSetSceneBatched rtcgbIntersect1MBatched rtcgbOccluded1MBatched""".split()
+rtcgbPathTracerGetImage rtcgbSetSceneBatched rtcgbIntersect1MBatched rtcgbOccluded1MBatched
+rtcSetGeometryInstancedScene rtcSetGeometryTransform rtcGetGeometryTransform""".split()
 
 
 class RTCBounds(ctypes.Structure):
@@ -163,6 +168,9 @@ def load(build=True):
         "rtcgbPathTracerTrainProposer": (None, [vp, u, u, ctypes.c_float]),
         "rtcgbPathTracerGetImage": (None, [vp, vp]),
         "rtcgbSetSceneBatched": (None, [vp, i]),
+        "rtcSetGeometryInstancedScene": (None, [vp, vp]),
+        "rtcSetGeometryTransform": (None, [vp, u, i, vp]),
+        "rtcGetGeometryTransform": (None, [vp, ctypes.c_float, i, vp]),
         "rtcgbIntersect1MBatched": (None, [vp, vp, u, sz, vp, u]),
         "rtcgbOccluded1MBatched": (None, [vp, vp, u, sz, vp, u]),
     }
@@ -257,6 +265,24 @@ class Scene:
         gid = L.rtcAttachGeometry(self.h, g)
         L.rtcReleaseGeometry(g)
         self.dev.check("add_mesh_device")
+        return gid
+
+    def add_instance(self, scene, xfm, geom_id=None, fmt=RTC_FORMAT_FLOAT3X4_COLUMN_MAJOR):
+        """Attaches an instance of `scene` with the local-to-world map xfm (12 or 16
+        floats in the given format)."""
+        L = self.L
+        g = ctypes.c_void_p(L.rtcNewGeometry(self.dev.h, RTC_GEOMETRY_TYPE_INSTANCE))
+        L.rtcSetGeometryInstancedScene(g, scene.h)
+        m = np.ascontiguousarray(xfm, np.float32).ravel()
+        L.rtcSetGeometryTransform(g, 0, fmt, _ptr(m))
+        L.rtcCommitGeometry(g)
+        if geom_id is None:
+            gid = L.rtcAttachGeometry(self.h, g)
+        else:
+            L.rtcAttachGeometryByID(self.h, g, geom_id)
+            gid = geom_id
+        L.rtcReleaseGeometry(g)
+        self.dev.check("add_instance")
         return gid
 
     def update_vertices(self, gid, new_verts):

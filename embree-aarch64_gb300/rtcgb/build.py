@@ -29,7 +29,7 @@ def _nvcc():
 
 
 def _flags():
-    return ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+    return ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
             "-I", INC, "-I", CSRC] + ARCH
 
 

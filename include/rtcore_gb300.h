@@ -369,6 +369,15 @@ RTC_API void rtcUpdateGeometryBuffer(RTCGeometry geometry, enum RTCBufferType ty
 RTC_API void rtcSetGeometryIntersectFilterFunction(RTCGeometry geometry, RTCFilterFunctionN filter);
 /* replaces include/embree3/rtcore_geometry.h:193 / kernels/common/rtcore.cpp:1674 (same restriction as above) */
 RTC_API void rtcSetGeometryOccludedFilterFunction(RTCGeometry geometry, RTCFilterFunctionN filter);
+/* replaces include/embree3/rtcore_geometry.h:224 / kernels/common/rtcore.cpp:996: the scene an
+   RTC_GEOMETRY_TYPE_INSTANCE geometry instances (one instance level) */
+RTC_API void rtcSetGeometryInstancedScene(RTCGeometry geometry, RTCScene scene);
+/* replaces include/embree3/rtcore_geometry.h:227 / kernels/common/rtcore.cpp:1071: local-to-world
+   map (RTC_FORMAT_FLOAT3X4_ROW_MAJOR, _FLOAT3X4_COLUMN_MAJOR or _FLOAT4X4_COLUMN_MAJOR) */
+RTC_API void rtcSetGeometryTransform(RTCGeometry geometry, unsigned int timeStep, enum RTCFormat format, const void* xfm);
+/* replaces include/embree3/rtcore_geometry.h:233 / kernels/common/rtcore.cpp:1117 */
+RTC_API void rtcGetGeometryTransform(RTCGeometry geometry, float time, enum RTCFormat format, void* xfm);
+
 /* replaces include/embree3/rtcore_geometry.h:196 / kernels/common/rtcore.cpp:1543 */
 RTC_API void rtcSetGeometryUserData(RTCGeometry geometry, void* ptr);
 /* replaces include/embree3/rtcore_geometry.h:199 / kernels/common/rtcore.cpp:1553 */

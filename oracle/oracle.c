@@ -1035,6 +1035,107 @@ void orc_occluded1M(const OracleScene* s, void* rays, unsigned M, size_t stride,
   run_stream(s, rays, M, stride, nthreads, 1);
 }
 
+/* ---- instances (RTC_GEOMETRY_TYPE_INSTANCE, one level) ----------------------
+   kernels/geometry/instance_intersector.cpp:56-97: the ray is moved into the
+   instance's space (xfmPoint / xfmVector, common/math/affinespace.h:102-103,
+   madd chains), traced in the instanced scene with the current tfar, and its
+   world origin and direction are restored; the hit keeps the instanced
+   scene's geomID / primID / object-space Ng and gets instID = the instance's
+   geometry ID.  The world-to-local map is rcp(AffineSpace3fa)
+   (affinespace.h:83, linearspace3.h:44-50: transposed adjoint / det,
+   -(inverse * p)) with the correctly rounded 1/det. */
+
+static int orc_invert(const float* m, float* o) {
+  const v3 vx = {m[0], m[1], m[2]}, vy = {m[3], m[4], m[5]}, vz = {m[6], m[7], m[8]};
+  const v3 c0 = cross3(vy, vz), c1 = cross3(vz, vx), c2 = cross3(vx, vy);
+  const float det = dot3(vx, c0);
+  if (!(det != 0.0f) || !isfinite(det)) return 0;
+  const float r = 1.0f / det;
+  const float c[3][3] = {{c0.x, c0.y, c0.z}, {c1.x, c1.y, c1.z}, {c2.x, c2.y, c2.z}};
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) o[3 * j + i] = c[i][j] * r;
+  for (int k = 0; k < 3; k++)
+    o[9 + k] = -fmaf(m[9], o[k], fmaf(m[10], o[3 + k], m[11] * o[6 + k]));
+  for (int k = 0; k < 12; k++)
+    if (!isfinite(o[k])) return 0;
+  return 1;
+}
+
+static void to_instance(const float* w, const char* rec, char* tmp) {
+  float f[12];
+  memcpy(f, rec, sizeof(f));
+  float o[3], d[3];
+  for (int c = 0; c < 3; c++) {
+    o[c] = fmaf(f[0], w[c], fmaf(f[1], w[3 + c], fmaf(f[2], w[6 + c], w[9 + c])));
+    d[c] = fmaf(f[4], w[c], fmaf(f[5], w[3 + c], f[6] * w[6 + c]));
+  }
+  memcpy(tmp, rec, 80);
+  memcpy(tmp + 0, o, 12);
+  memcpy(tmp + 16, d, 12);
+}
+
+void orc_intersect_instanced(const OracleScene* top, unsigned ninst, const OracleScene* const* scenes,
+                             const float* l2w, const unsigned* inst_geomIDs, void* rays, unsigned M, size_t stride) {
+  float* w2l = (float*)malloc(sizeof(float) * 12 * (ninst ? ninst : 1));
+  int* ok = (int*)malloc(sizeof(int) * (ninst ? ninst : 1));
+  for (unsigned k = 0; k < ninst; k++) ok[k] = orc_invert(l2w + 12 * k, w2l + 12 * k);
+  OCount cnt = {0, 0, 0};
+  for (unsigned i = 0; i < M; i++) {
+    char* rec = (char*)rays + (size_t)i * stride;
+    ORay r;
+    load_ray(rec, &r);
+    if (!(r.tnear <= r.tfar)) continue;
+    if (top) trace_closest(top, rec, &cnt);
+    for (unsigned k = 0; k < ninst; k++) {
+      if (!ok[k] || scenes[k]->root == EMPTY_REF) continue;
+      char tmp[80];
+      to_instance(w2l + 12 * k, rec, tmp);
+      const uint32_t none = 0xFFFFFFFFu;
+      memcpy(tmp + 72, &none, 4);
+      trace_closest(scenes[k], tmp, &cnt);
+      uint32_t g;
+      memcpy(&g, tmp + 72, 4);
+      if (g == none) continue;
+      memcpy(rec + 32, tmp + 32, 4);        /* tfar */
+      memcpy(rec + 48, tmp + 48, 28);       /* Ng, u, v, primID, geomID */
+      memcpy(rec + 76, &inst_geomIDs[k], 4); /* instID[0] */
+    }
+  }
+  free(w2l);
+  free(ok);
+}
+
+void orc_occluded_instanced(const OracleScene* top, unsigned ninst, const OracleScene* const* scenes,
+                            const float* l2w, void* rays, unsigned M, size_t stride) {
+  float* w2l = (float*)malloc(sizeof(float) * 12 * (ninst ? ninst : 1));
+  int* ok = (int*)malloc(sizeof(int) * (ninst ? ninst : 1));
+  for (unsigned k = 0; k < ninst; k++) ok[k] = orc_invert(l2w + 12 * k, w2l + 12 * k);
+  OCount cnt = {0, 0, 0};
+  for (unsigned i = 0; i < M; i++) {
+    char* rec = (char*)rays + (size_t)i * stride;
+    ORay r;
+    load_ray(rec, &r);
+    if (r.tnear > r.tfar || r.tfar < 0.0f || !(r.tnear <= r.tfar)) continue;
+    if (top) trace_occluded(top, rec, &cnt);
+    float tf;
+    memcpy(&tf, rec + 32, 4);
+    for (unsigned k = 0; k < ninst && !(tf < 0.0f); k++) {
+      if (!ok[k] || scenes[k]->root == EMPTY_REF) continue;
+      char tmp[80];
+      to_instance(w2l + 12 * k, rec, tmp);
+      trace_occluded(scenes[k], tmp, &cnt);
+      float t2;
+      memcpy(&t2, tmp + 32, 4);
+      if (t2 < 0.0f) {
+        memcpy(rec + 32, &t2, 4);
+        tf = t2;
+      }
+    }
+  }
+  free(w2l);
+  free(ok);
+}
+
 /* ------------------------------------------------------------------------ */
 /* brute force                                                              */
 /* ------------------------------------------------------------------------ */

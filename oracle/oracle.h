@@ -125,6 +125,15 @@ int orc_moeller1(const float v0[3], const float v1[3], const float v2[3],
 int orc_pluecker1(const float v0[3], const float v1[3], const float v2[3], const float org[3], const float dir[3],
                   float tnear, float tfar, float out_tuv[3], float out_Ng[3]);
 
+/* Scenes with instances: rays against the top scene's own triangles (top may
+   be NULL) and `ninst` instances of committed scenes with local-to-world maps
+   l2w (12 floats each, columns vx, vy, vz, p).  Closest hits of instances
+   report instID = inst_geomIDs[k].  RTCRayHit / RTCRay records, byte stride. */
+void orc_intersect_instanced(const OracleScene* top, unsigned ninst, const OracleScene* const* scenes,
+                             const float* l2w, const unsigned* inst_geomIDs, void* rays, unsigned M, size_t stride);
+void orc_occluded_instanced(const OracleScene* top, unsigned ninst, const OracleScene* const* scenes,
+                            const float* l2w, void* rays, unsigned M, size_t stride);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,8 @@ def lib():
         L.orc_scene_set_robust.argtypes = [vp, i]
         L.orc_pluecker1.argtypes = [ctypes.POINTER(f)] * 5 + [f, f] + [ctypes.POINTER(f)] * 2
         L.orc_pluecker1.restype = i
+        L.orc_intersect_instanced.argtypes = [vp, u, vp, vp, vp, vp, u, sz]
+        L.orc_occluded_instanced.argtypes = [vp, u, vp, vp, vp, u, sz]
         _lib = L
     return _lib
 
@@ -148,3 +150,19 @@ def moeller1(v0, v1, v2, org, d, tnear=0.0, tfar=float("inf")):
     out4, tuv, ng = (ctypes.c_float * 4)(), f3(), f3()
     ok = lib().orc_moeller1(f3(*v0), f3(*v1), f3(*v2), f3(*org), f3(*d), tnear, tfar, out4, tuv, ng)
     return bool(ok), tuple(out4), tuple(tuv), tuple(ng)
+
+
+def instanced(top, instances, rays, anyhit=False):
+    """Rays (in place) against `top` (an OracleScene or None) and instances
+    [(OracleScene, l2w 12 floats column-major, instance geomID)]."""
+    n = len(instances)
+    scenes = (ctypes.c_void_p * max(n, 1))(*[inst[0]._h.value for inst in instances])
+    l2w = np.ascontiguousarray(np.array([inst[1] for inst in instances], np.float32).reshape(-1))
+    gids = np.ascontiguousarray(np.array([inst[2] for inst in instances], np.uint32))
+    th = top._h if top is not None else None
+    stride = rays.dtype.itemsize
+    if anyhit:
+        lib().orc_occluded_instanced(th, n, scenes, _ptr(l2w), _ptr(rays), rays.shape[0], stride)
+    else:
+        lib().orc_intersect_instanced(th, n, scenes, _ptr(l2w), _ptr(gids), _ptr(rays), rays.shape[0], stride)
+    return rays

@@ -183,3 +183,26 @@ def test_learned_queries_fall_back_after_rebuild(rtc, device):
     assert (a.view(np.uint8) == b.view(np.uint8)).all()
     assert rtc.last_query_stats()["proposal_hits"] == 0
     prop.release()
+
+
+def test_tensor_core_inference_matches_mma_sync(rtc, small_scene):
+    """The tcgen05 inference kernel (default) and the mma.sync one (device key
+    gpu.proposer=mma) propose the same treelets up to FP32 accumulation-order ties."""
+    dev_mma = rtc.Device(b"gpu.proposer=mma")
+    sc2 = rtc.Scene(dev_mma)
+    sc2.add_mesh(*W.heightfield(48))
+    sc2.add_mesh(*W.gaussian_soup(20000, seed=3))
+    sc2.commit()
+    params = PO.random_params(seed=13)
+    a = rtc.Proposer(small_scene, seed=1)
+    b = rtc.Proposer(sc2, seed=1)
+    a.set_params(params)
+    b.set_params(params)
+    rays = _random_rays(5000, 14)
+    ta, tb = a.predict(rays), b.predict(rays)
+    same = (np.sort(ta, 1) == np.sort(tb, 1)).all(1)
+    assert same.mean() > 0.99, same.mean()
+    a.release()
+    b.release()
+    sc2.release()
+    dev_mma.release()

@@ -138,6 +138,31 @@ def test_soup_parity(rtc, device, oracle):
     assert rep2["occluded"] > 1000
 
 
+def test_reordered_rays_parity(rtc, oracle):
+    """gpu.reorder=1: the traversal fetches rays in direction-octant + origin-Morton
+    order; every ray's result is still the oracle's (device and host rays)."""
+    dev = rtc.Device(b"gpu.reorder=1")
+    verts, idx = W.gaussian_soup(200_000, seed=31)
+    sg = rtc.Scene(dev)
+    sg.add_mesh(verts, idx)
+    sg.commit()
+    so = oracle.OracleScene([(0, verts, idx)])
+    rays = W.sphere_rays(300_000, seed=32)
+    g, r = rays.copy(), rays.copy()
+    sg.intersect(g)
+    so.intersect(r)
+    rep = compare_closest(so, rays, g, r)
+    assert_clean(rep)
+    assert rep["hits"] > 5000
+    shadow, _ = W.shadow_rays(r, seed=33)
+    sgo, soo = shadow.copy(), shadow.copy()
+    sg.occluded(sgo)
+    so.occluded(soo)
+    assert_clean(compare_occluded(so, shadow, sgo, soo, sg))
+    sg.release()
+    dev.release()
+
+
 def test_multi_geometry_ids(rtc, device, oracle):
     """Several meshes with explicit geometry IDs; disabled and detached
     geometry is excluded from the next commit."""
