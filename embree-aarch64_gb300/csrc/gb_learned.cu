@@ -621,26 +621,33 @@ __global__ void __launch_bounds__(kPW * 32, 2)
 
 // ---------------------------------------------------------------------------
 // Inference on the 5th-generation tensor cores (tcgen05).  One CTA per SM
-// (16 warps, 128 rays per tile) owns all 512 TMEM columns: two 128x256 FP32
-// accumulators.  In the epilogue warp w reads TMEM lanes 32 (w % 4) .. +31
-// (its rows) and the column quarter w / 4 of each chunk; the four partial
-// top-4 lists of a row are merged through shared memory at the end of the tile.  The 4096x64 output
-// weights are kept in global memory in the UMMA canonical K-major layout
-// (8x16-byte core matrices; LBO 128 B along K, SBO 1024 B along rows), so each
-// 256-treelet chunk is one contiguous 32 KB block that a single bulk copy
-// (cp.async.bulk, completion on an mbarrier) brings into one of two shared
-// stages.  One thread issues the four K=16 MMAs of a chunk and commits them to
-// an mbarrier; meanwhile all threads read the previous chunk's accumulators
-// with tcgen05.ld and keep their row's running top 4.  Every wait on an
-// mbarrier is bounded; on a timeout the kernel sets kErrIterationLimit and
-// stops.
+// holds all 512 TMEM columns: two 128x256 FP32 accumulators.  Warps 0-15
+// encode the rays, run the hidden layers and scan the accumulators; warp 16
+// (the producer) streams the output weights and issues the MMAs.  Hand-offs
+// are mbarriers, never CTA-wide barriers:
+//   tma_bar[s]  stage s holds a weight chunk (bulk copy complete)
+//   mma_bar[b]  accumulator b holds a chunk's logits (tcgen05.commit)
+//   epi_bar[b]  accumulator b has been read by all 16 scanning warps
+//   a_bar       the tile's last hidden layer is in the A operand
+// The output weights live in global memory in the UMMA canonical K-major
+// layout with K = 80: the 64 weights, then the bias split into two BF16 parts
+// (hi, lo) that the A operand multiplies by ones, so the MMA adds the bias;
+// unused treelets carry a -inf bias.  Each 256-treelet chunk (40 KB) is one
+// contiguous block for one bulk copy.  In the scan, warp w reads TMEM lanes
+// 32 (w % 4) .. +31 (its rows) and the column quarter w / 4 of each chunk; the
+// four partial top-4 lists of a row are merged through shared memory at the
+// end of the tile.  Every mbarrier wait is bounded; on a timeout the kernel
+// sets kErrIterationLimit and stops.
 // ---------------------------------------------------------------------------
 
-constexpr int kTcThreads = 512;
-constexpr int kTcRays = 128;                       // UMMA M
-constexpr int kTcN = 256;                          // UMMA N: treelets per chunk
-constexpr int kTcChunks = kTreelets / kTcN;        // 16
-constexpr uint32_t kTcChunkBytes = kTcN * kHidden * 2;
+constexpr int kTcScanWarps = 16;
+constexpr int kTcScanThreads = kTcScanWarps * 32;
+constexpr int kTcThreads = kTcScanThreads + 32;     // + the producer warp
+constexpr int kTcRays = 128;                        // UMMA M
+constexpr int kTcN = 256;                           // UMMA N: treelets per chunk
+constexpr int kTcK = kHidden + 16;                  // 64 weights + bias (hi, lo) + zero padding
+constexpr int kTcChunks = kTreelets / kTcN;         // 16
+constexpr uint32_t kTcChunkBytes = kTcN * kTcK * 2; // 40 KB
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kSpinLimit = 1u << 22;
 // kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A and
@@ -649,34 +656,36 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTc
                             ((uint32_t)(kTcRays >> 4) << 24);
 
 struct TcSmem {
-  uint16_t w4[2][kTcN * kHidden];   // streamed output weights (UMMA layout)
-  uint16_t a[kTcRays * kHidden];    // last hidden layer of the tile (UMMA layout)
+  uint16_t w4[2][kTcN * kTcK];      // streamed output weights + bias (UMMA layout)
+  uint16_t a[kTcRays * kTcK];       // last hidden layer of the tile + ones (UMMA layout)
   uint16_t x[kTcRays * kLdX];
   uint16_t h[kTcRays * kLdH];
   uint16_t w1[kHidden * kLdX];
   uint16_t w2[kHidden * kLdH];
   uint16_t w3[kHidden * kLdH];
   float b[3][kHidden];
-  float b4[kTreelets];
   float mv[kTcRays][4][4];          // partial top-4 per row and column quarter
   int mi[kTcRays][4][4];
   unsigned long long tma_bar[2];
   unsigned long long mma_bar[2];
+  unsigned long long epi_bar[2];
+  unsigned long long a_bar;
   uint32_t tmem_base;
   uint32_t fail;
 };
 static_assert(offsetof(TcSmem, a) % 1024 == 0, "operand tiles start on 1 KB boundaries");
 static_assert(offsetof(TcSmem, tma_bar) % 8 == 0, "mbarrier alignment");
 
-// element offset of (row, k) in the UMMA K-major core-matrix layout (64 columns)
+// element offset of (row, k) in the UMMA K-major core-matrix layout (K = 80:
+// ten 8x8 core matrices per 8-row group, 128 B apart along K, 1280 B along rows)
 __device__ __forceinline__ uint32_t umma_off(uint32_t row, uint32_t k) {
-  return (row >> 3) * 512 + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
+  return (row >> 3) * (kTcK * 8) + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ uint64_t umma_desc(const void* smem) {
-  constexpr uint64_t kLbo = 128, kSbo = 1024;
+  constexpr uint64_t kLbo = 128, kSbo = kTcK * 16;
   return (uint64_t)((smem_u32(smem) >> 4) & 0x3FFFu) | (((kLbo >> 4) & 0x3FFFu) << 16) |
          (((kSbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
@@ -696,6 +705,9 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity
     if (ok) return true;
   }
   return false;
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(b)) : "memory");
 }
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
@@ -717,56 +729,84 @@ __device__ __forceinline__ void umma_commit(unsigned long long* bar) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// two 32-column loads, one wait
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+// barrier among the scanning warps only (the producer warp does not take part)
+__device__ __forceinline__ void scan_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(kTcScanThreads) : "memory"); }
+
+__device__ __forceinline__ uint16_t bf16_bits(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
 
 // The streamed weights in the UMMA layout: chunk c (treelets 256c..256c+255)
-// is a contiguous block; refreshed whenever the BF16 mirror changes.
-__global__ void k_permute_w4(const uint16_t* __restrict__ Pb, uint16_t* __restrict__ w4p) {
+// is a contiguous block; k 64 / 65 hold the bias as BF16 hi + lo parts, k 66-79
+// are zero.  Refreshed whenever the BF16 mirror changes.
+__global__ void k_permute_w4(const uint16_t* __restrict__ Pb, const float* __restrict__ P, int ntl,
+                             uint16_t* __restrict__ w4p) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // one 16-byte row piece per thread
-  if (i >= kTreelets * (kHidden / 8)) return;
-  const uint32_t n = i / (kHidden / 8), kc = i % (kHidden / 8);
+  if (i >= kTreelets * (kTcK / 8)) return;
+  const uint32_t n = i / (kTcK / 8), kc = i % (kTcK / 8);
   const uint32_t c = n / kTcN, r = n % kTcN;
-  const uint4 v = *reinterpret_cast<const uint4*>(Pb + kOffW4 + (size_t)n * kHidden + kc * 8);
-  *reinterpret_cast<uint4*>(w4p + (size_t)c * kTcN * kHidden + umma_off(r, kc * 8)) = v;
+  uint4 v;
+  if (kc < kHidden / 8) {
+    v = *reinterpret_cast<const uint4*>(Pb + kOffW4 + (size_t)n * kHidden + kc * 8);
+  } else if (kc == kHidden / 8) {
+    const float b = P[kOffB4 + n];
+    uint32_t hi = bf16_bits(-INFINITY), lo = 0;
+    if ((int)n < ntl) {
+      hi = bf16_bits(b);
+      lo = bf16_bits(b - __uint_as_float(hi << 16));
+    }
+    v = make_uint4(hi | (lo << 16), 0u, 0u, 0u);
+  } else {
+    v = make_uint4(0u, 0u, 0u, 0u);
+  }
+  *reinterpret_cast<uint4*>(w4p + (size_t)c * kTcN * kTcK + umma_off(r, kc * 8)) = v;
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_propose_tc(const char* rays, uint64_t stride, uint32_t M, const uint32_t* d_count, GridSpec grid,
                  const uint16_t* __restrict__ Pb, const float* __restrict__ P, const uint16_t* __restrict__ W4p,
-                 const uint32_t* __restrict__ node_of_treelet, int ntl, uint4* seeds, uint32_t* treelets,
-                 uint32_t* err) {
+                 const uint32_t* __restrict__ node_of_treelet, uint4* seeds, uint32_t* treelets, uint32_t* err) {
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   TcSmem& S = *reinterpret_cast<TcSmem*>(tc_smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-  const bool leader = tid == 0;
-  for (int i = tid; i < kHidden * kIn / 2; i += kTcThreads) {
-    const int o = (2 * i) / kIn, k = (2 * i) % kIn;
-    *reinterpret_cast<uint32_t*>(S.w1 + o * kLdX + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW1)[i];
-  }
-  for (int i = tid; i < kHidden * kHidden / 2; i += kTcThreads) {
-    const int o = (2 * i) / kHidden, k = (2 * i) % kHidden;
-    *reinterpret_cast<uint32_t*>(S.w2 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW2)[i];
-    *reinterpret_cast<uint32_t*>(S.w3 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW3)[i];
-  }
-  for (int i = tid; i < 3 * kHidden; i += kTcThreads) {
-    const size_t off = i < kHidden ? kOffB1 : (i < 2 * kHidden ? kOffB2 : kOffB3);
-    S.b[i / kHidden][i % kHidden] = P[off + i % kHidden];
-  }
-  for (int i = tid; i < kTreelets; i += kTcThreads) S.b4[i] = i < ntl ? P[kOffB4 + i] : -INFINITY;
-  if (leader) {
-    mbar_init(&S.tma_bar[0], 1);
-    mbar_init(&S.tma_bar[1], 1);
-    mbar_init(&S.mma_bar[0], 1);
-    mbar_init(&S.mma_bar[1], 1);
-    S.fail = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  if (warp == 0) {
+  const bool producer = warp == kTcScanWarps;
+  if (!producer) {
+    for (int i = tid; i < kHidden * kIn / 2; i += kTcScanThreads) {
+      const int o = (2 * i) / kIn, k = (2 * i) % kIn;
+      *reinterpret_cast<uint32_t*>(S.w1 + o * kLdX + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW1)[i];
+    }
+    for (int i = tid; i < kHidden * kHidden / 2; i += kTcScanThreads) {
+      const int o = (2 * i) / kHidden, k = (2 * i) % kHidden;
+      *reinterpret_cast<uint32_t*>(S.w2 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW2)[i];
+      *reinterpret_cast<uint32_t*>(S.w3 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW3)[i];
+    }
+    for (int i = tid; i < 3 * kHidden; i += kTcScanThreads) {
+      const size_t off = i < kHidden ? kOffB1 : (i < 2 * kHidden ? kOffB2 : kOffB3);
+      S.b[i / kHidden][i % kHidden] = P[off + i % kHidden];
+    }
+    // the A operand's bias columns: ones at k 64 and 65, zeros up to 79
+    for (int r = tid; r < kTcRays; r += kTcScanThreads) {
+      const uint32_t one = 0x3F80u;  // 1.0 in BF16
+      *reinterpret_cast<uint4*>(S.a + umma_off(r, kHidden)) = make_uint4(one | (one << 16), 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(S.a + umma_off(r, kHidden + 8)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+  } else {
+    if (lane == 0) {
+      for (int b = 0; b < 2; b++) {
+        mbar_init(&S.tma_bar[b], 1);
+        mbar_init(&S.mma_bar[b], 1);
+        mbar_init(&S.epi_bar[b], kTcScanWarps);
+      }
+      mbar_init(&S.a_bar, 1);
+      S.fail = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncwarp();
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&S.tmem_base)),
                  "n"(kTmemCols)
                  : "memory");
@@ -778,140 +818,158 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t tmem = S.tmem_base;
   if (d_count) M = min(M, *d_count);
   const uint32_t ntiles = (M + kTcRays - 1) / kTcRays;
-  uint32_t tma_par[2] = {0, 0}, mma_par[2] = {0, 0};
-  uint32_t tma_pending[2] = {0, 0};  // leader: copies issued and not yet waited for
-  if (leader && blockIdx.x < ntiles) {
-    bulk_load(S.w4[0], W4p, kTcChunkBytes, &S.tma_bar[0]);
-    bulk_load(S.w4[1], W4p + (size_t)kTcN * kHidden, kTcChunkBytes, &S.tma_bar[1]);
-    tma_pending[0] = tma_pending[1] = 1;
-  }
-  bool failed = false;
-  for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-    const uint32_t r0 = tile * kTcRays;
-    const bool next_tile = tile + gridDim.x < ntiles;
-    for (int it = tid; it < kTcRays * kLevels; it += kTcThreads) {
-      const int rr = it / kLevels, l = it % kLevels;
-      const uint32_t rid = r0 + rr;
-      const uint32_t pk = rid < M ? encode_level(Pb, rays + (uint64_t)rid * stride, grid, l) : 0u;
-      *reinterpret_cast<uint32_t*>(S.x + rr * kLdX + 2 * l) = pk;
-    }
-    __syncthreads();
-    // hidden layers: warps 0..7 own 16 rows each
-    if (warp < kTcRays / 16) {
-      const int row0 = warp * 16;
-      uint16_t* hrow = S.h + row0 * kLdH;
-      hidden_layer<kIn, kLdX>(S.x + row0 * kLdX, S.w1, kLdX, S.b[0], hrow, g, t);
-      __syncwarp();
-      hidden_layer<kHidden, kLdH>(hrow, S.w2, kLdH, S.b[1], hrow, g, t);
-      __syncwarp();
-      hidden_layer<kHidden, kLdH>(hrow, S.w3, kLdH, S.b[2], hrow, g, t);
-    }
-    __syncthreads();
-    // rows into the A operand (8 pieces of 16 bytes per row)
-    for (int it = tid; it < kTcRays * (kHidden / 8); it += kTcThreads) {
-      const int r = it >> 3, kc = it & 7;
-      *reinterpret_cast<uint4*>(S.a + umma_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(S.h + r * kLdH + kc * 8);
-    }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();
-    const uint64_t adesc0 = umma_desc(S.a);
-    auto issue = [&](int c) {  // leader: MMAs of chunk c into accumulator c & 1
-      const int s = c & 1;
-      if (!mbar_wait(&S.tma_bar[s], tma_par[s])) return false;
-      tma_par[s] ^= 1;
-      tma_pending[s] = 0;
-      tc_fence_after();
-      const uint64_t bdesc0 = umma_desc(S.w4[s]);
+  const uint32_t my_tiles = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
+  const uint32_t total_chunks = my_tiles * kTcChunks;
+
+  if (producer) {
+    if (lane == 0 && total_chunks > 0) {
+      bool ok = true;
+      bulk_load(S.w4[0], W4p, kTcChunkBytes, &S.tma_bar[0]);
+      if (total_chunks > 1) bulk_load(S.w4[1], W4p + (size_t)kTcN * kTcK, kTcChunkBytes, &S.tma_bar[1]);
+      const uint64_t adesc0 = umma_desc(S.a);
+      for (uint32_t gc = 0; gc < total_chunks && ok; gc++) {
+        const uint32_t c = gc % kTcChunks, s = gc & 1u, par = (gc >> 1) & 1u;
+        if (c == 0) ok = mbar_wait(&S.a_bar, (gc / kTcChunks) & 1u);           // A operand of this tile
+        if (ok) ok = mbar_wait(&S.tma_bar[s], par);                            // weights of chunk gc
+        if (ok && gc >= 2) ok = mbar_wait(&S.epi_bar[s], ((gc - 2) >> 1) & 1u); // accumulator s read
+        if (!ok) break;
+        tc_fence_after();
+        const uint64_t bdesc0 = umma_desc(S.w4[s]);
 #pragma unroll
-      for (int ks = 0; ks < kHidden / 16; ks++)  // +256 B per K step: two core matrices
-        umma_bf16(tmem + (uint32_t)s * kTcN, adesc0 + (uint64_t)(ks * 16), bdesc0 + (uint64_t)(ks * 16), ks > 0);
-      umma_commit(&S.mma_bar[s]);
-      return true;
-    };
-    if (leader && !issue(0)) S.fail = 1;
-    float v[4];
-    int ix[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) { v[q] = -INFINITY; ix[q] = -1; }
-    for (int c = 0; c < kTcChunks; c++) {
-      const int s = c & 1;
-      if (leader && !S.fail && c + 1 < kTcChunks && !issue(c + 1)) S.fail = 1;
-      if (!mbar_wait(&S.mma_bar[s], mma_par[s])) S.fail = 1;
-      mma_par[s] ^= 1;
-      tc_fence_after();
-      if (leader && !S.fail) {  // stage s is free: the next chunk that uses it
-        if (c + 2 < kTcChunks) {
-          bulk_load(S.w4[s], W4p + (size_t)(c + 2) * kTcN * kHidden, kTcChunkBytes, &S.tma_bar[s]);
-          tma_pending[s] = 1;
-        } else if (next_tile) {
-          bulk_load(S.w4[s], W4p + (size_t)(c + 2 - kTcChunks) * kTcN * kHidden, kTcChunkBytes, &S.tma_bar[s]);
-          tma_pending[s] = 1;
+        for (int ks = 0; ks < kTcK / 16; ks++)  // +256 B per K step: two core matrices
+          umma_bf16(tmem + s * kTcN, adesc0 + (uint64_t)(ks * 16), bdesc0 + (uint64_t)(ks * 16), ks > 0);
+        umma_commit(&S.mma_bar[s]);
+        // stage (gc - 1) & 1 is free once chunk gc - 1's MMAs are done: next copy into it
+        if (gc >= 1 && gc + 1 < total_chunks) {
+          if (!(ok = mbar_wait(&S.mma_bar[(gc - 1) & 1u], ((gc - 1) >> 1) & 1u))) break;
+          bulk_load(S.w4[(gc + 1) & 1u], W4p + (size_t)((gc + 1) % kTcChunks) * kTcN * kTcK, kTcChunkBytes,
+                    &S.tma_bar[(gc + 1) & 1u]);
         }
       }
-      const int quarter = warp >> 2;
-      const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)s * kTcN + (uint32_t)quarter * 64;
-#pragma unroll 1
-      for (int j = 0; j < 2; j++) {
-        uint32_t acc[32];
-        tmem_ld32(taddr + (uint32_t)(j * 32), acc);
-        const int col0 = c * kTcN + quarter * 64 + j * 32;
-#pragma unroll
-        for (int q = 0; q < 32; q++) top4_insert(v, ix, __fadd_rn(__uint_as_float(acc[q]), S.b4[col0 + q]), col0 + q);
+      if (!ok) {
+        *(volatile uint32_t*)&S.fail = 1u;
+        atomicOr(err, kErrIterationLimit);
       }
-      tc_fence_before();
-      __syncthreads();
-      if (S.fail) {
-        failed = true;
+    }
+    __syncwarp();
+  } else {
+    uint32_t gc = 0;
+    for (uint32_t k = 0; k < my_tiles; k++) {
+      const uint32_t tile = blockIdx.x + k * gridDim.x;
+      const uint32_t r0 = tile * kTcRays;
+      for (int it = tid; it < kTcRays * kLevels; it += kTcScanThreads) {
+        const int rr = it / kLevels, l = it % kLevels;
+        const uint32_t rid = r0 + rr;
+        const uint32_t pk = rid < M ? encode_level(Pb, rays + (uint64_t)rid * stride, grid, l) : 0u;
+        *reinterpret_cast<uint32_t*>(S.x + rr * kLdX + 2 * l) = pk;
+      }
+      scan_sync();
+      if (warp < kTcRays / 16) {
+        const int row0 = warp * 16;
+        uint16_t* hrow = S.h + row0 * kLdH;
+        hidden_layer<kIn, kLdX>(S.x + row0 * kLdX, S.w1, kLdX, S.b[0], hrow, g, t);
+        __syncwarp();
+        hidden_layer<kHidden, kLdH>(hrow, S.w2, kLdH, S.b[1], hrow, g, t);
+        __syncwarp();
+        hidden_layer<kHidden, kLdH>(hrow, S.w3, kLdH, S.b[2], hrow, g, t);
+      }
+      scan_sync();
+      for (int it = tid; it < kTcRays * (kHidden / 8); it += kTcScanThreads) {
+        const int r = it >> 3, kc = it & 7;
+        *reinterpret_cast<uint4*>(S.a + umma_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(S.h + r * kLdH + kc * 8);
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      scan_sync();
+      if (tid == 0) mbar_arrive(&S.a_bar);
+      float v[4];
+      int ix[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) { v[q] = -INFINITY; ix[q] = -1; }
+      const int quarter = warp >> 2;
+      bool ok = true;
+      for (int c = 0; c < kTcChunks; c++, gc++) {
+        const uint32_t s = gc & 1u;
+        if (!mbar_wait(&S.mma_bar[s], (gc >> 1) & 1u)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + s * kTcN + (uint32_t)quarter * 64;
+        uint32_t acc0[32], acc1[32];
+        tmem_ld32(taddr, acc0);
+        tmem_ld32(taddr + 32, acc1);
+        tmem_wait_ld();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S.epi_bar[s]);  // this warp is done with accumulator s
+        const int col0 = c * kTcN + quarter * 64;
+        float m0 = __uint_as_float(acc0[0]), m1 = __uint_as_float(acc1[0]);
+#pragma unroll
+        for (int q = 1; q < 32; q++) {
+          m0 = fmaxf(m0, __uint_as_float(acc0[q]));
+          m1 = fmaxf(m1, __uint_as_float(acc1[q]));
+        }
+        if (m0 > v[3]) {
+#pragma unroll
+          for (int q = 0; q < 32; q++) top4_insert(v, ix, __uint_as_float(acc0[q]), col0 + q);
+        }
+        if (m1 > v[3]) {
+#pragma unroll
+          for (int q = 0; q < 32; q++) top4_insert(v, ix, __uint_as_float(acc1[q]), col0 + 32 + q);
+        }
+      }
+      // the failure decision is taken by all scanning warps together, after a
+      // barrier they all reach (a warp that timed out left its chunk loop early)
+      volatile uint32_t* fail_flag = &S.fail;
+      if (!ok) *fail_flag = 1u;
+      scan_sync();
+      if (*fail_flag) {
+        if (tid == 0) atomicOr(err, kErrIterationLimit);
         break;
       }
-    }
-    if (failed) break;
-    {  // merge the four column quarters of each row (ties to the lower column)
-      const int row = (warp & 3) * 32 + lane, quarter = warp >> 2;
+      {  // merge the four column quarters of each row (ties to the lower column)
+        const int row = (warp & 3) * 32 + lane;
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        S.mv[row][quarter][q] = v[q];
-        S.mi[row][quarter][q] = ix[q];
-      }
-    }
-    __syncthreads();
-    if (tid < kTcRays) {
-      float bv[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
-      int bi[4] = {-1, -1, -1, -1};
-      for (int qq = 0; qq < 4; qq++)
         for (int q = 0; q < 4; q++) {
-          const float x = S.mv[tid][qq][q];
-          const int i = S.mi[tid][qq][q];
-          if (i < 0) continue;
-          // insert (x, i) ordered by value desc, column asc
-          int pos = 4;
-          while (pos > 0 && (x > bv[pos - 1] || (x == bv[pos - 1] && (unsigned)i < (unsigned)bi[pos - 1]))) pos--;
-          if (pos < 4) {
-            for (int m = 3; m > pos; m--) { bv[m] = bv[m - 1]; bi[m] = bi[m - 1]; }
-            bv[pos] = x;
-            bi[pos] = i;
-          }
+          S.mv[row][quarter][q] = v[q];
+          S.mi[row][quarter][q] = ix[q];
         }
-      const uint32_t rid = r0 + tid;
-      if (rid < M) {
-        auto node = [&](int tl) { return tl >= 0 ? __ldg(node_of_treelet + tl) : kInvalidID; };
-        if (seeds) seeds[rid] = make_uint4(node(bi[0]), node(bi[1]), node(bi[2]), node(bi[3]));
-        if (treelets)
-          reinterpret_cast<uint4*>(treelets)[rid] = make_uint4((uint32_t)bi[0], (uint32_t)bi[1], (uint32_t)bi[2], (uint32_t)bi[3]);
+      }
+      scan_sync();
+      if (tid < kTcRays) {
+        float bv[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        int bi[4] = {-1, -1, -1, -1};
+        for (int qq = 0; qq < 4; qq++)
+          for (int q = 0; q < 4; q++) {
+            const float x = S.mv[tid][qq][q];
+            const int i = S.mi[tid][qq][q];
+            if (i < 0) continue;
+            int pos = 4;
+            while (pos > 0 && (x > bv[pos - 1] || (x == bv[pos - 1] && (unsigned)i < (unsigned)bi[pos - 1]))) pos--;
+            if (pos < 4) {
+              for (int m = 3; m > pos; m--) { bv[m] = bv[m - 1]; bi[m] = bi[m - 1]; }
+              bv[pos] = x;
+              bi[pos] = i;
+            }
+          }
+        const uint32_t rid = r0 + tid;
+        if (rid < M) {
+          auto node = [&](int tl) { return tl >= 0 ? __ldg(node_of_treelet + tl) : kInvalidID; };
+          if (seeds) seeds[rid] = make_uint4(node(bi[0]), node(bi[1]), node(bi[2]), node(bi[3]));
+          if (treelets)
+            reinterpret_cast<uint4*>(treelets)[rid] =
+                make_uint4((uint32_t)bi[0], (uint32_t)bi[1], (uint32_t)bi[2], (uint32_t)bi[3]);
+        }
       }
     }
-  }
-  if (failed && leader) {
-    atomicOr(err, kErrIterationLimit);
-    // let copies still in flight land before the shared memory is released
-    for (int s = 0; s < 2; s++)
-      if (tma_pending[s]) mbar_wait(&S.tma_bar[s], tma_par[s]);
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0)
+  if (producer) {
+    // bulk copies still in flight after a failure land before the CTA ends
+    if (lane == 0 && *(volatile uint32_t*)&S.fail)
+      for (int s = 0; s < 2; s++) mbar_wait(&S.tma_bar[s], 0), mbar_wait(&S.tma_bar[s], 1);
+    __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(kTmemCols) : "memory");
+  }
 }
 
 inline unsigned blocks_for(uint64_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
@@ -959,7 +1017,7 @@ cudaError_t Proposer::init(const std::vector<uint32_t>& node_of_treelet, const s
   GB_TRY(cudaMalloc(&prim_treelet_, std::max<size_t>(1, num_prims) * sizeof(uint32_t)));
   GB_TRY(cudaMalloc(&geom_prefix_, std::max<size_t>(1, num_geom_ids_) * sizeof(uint32_t)));
   GB_TRY(cudaMalloc(&acc_, 16 * sizeof(float)));
-  GB_TRY(cudaMalloc(&W4p_, (size_t)kTreelets * kHidden * sizeof(uint16_t)));
+  GB_TRY(cudaMalloc(&W4p_, (size_t)kTreelets * kTcK * sizeof(uint16_t)));
   GB_TRY(cudaMalloc(&err_, sizeof(uint32_t)));
   GB_TRY(cudaMemsetAsync(err_, 0, sizeof(uint32_t), st));
   GB_TRY(cudaFuncSetAttribute(k_propose_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem)));
@@ -983,7 +1041,7 @@ cudaError_t Proposer::init(const std::vector<uint32_t>& node_of_treelet, const s
 }
 
 cudaError_t Proposer::refresh_w4(cudaStream_t st) {
-  k_permute_w4<<<blocks_for((uint64_t)kTreelets * (kHidden / 8), 256), 256, 0, st>>>(Pb_, W4p_);
+  k_permute_w4<<<blocks_for((uint64_t)kTreelets * (kTcK / 8), 256), 256, 0, st>>>(Pb_, P_, (int)num_treelets, W4p_);
   note_launches(1);
   return cudaGetLastError();
 }
@@ -1133,8 +1191,7 @@ cudaError_t Proposer::predict(const char* rays, uint64_t stride, uint32_t M, uin
   if (!use_mma_sync) {
     const uint32_t grid_n = std::min<uint32_t>((M + kTcRays - 1) / kTcRays, (uint32_t)num_sms());
     k_propose_tc<<<grid_n, kTcThreads, sizeof(TcSmem), st>>>(rays, stride, M, d_count, grid, Pb_, P_, W4p_,
-                                                             node_of_treelet_, (int)num_treelets, seeds, treelets,
-                                                             err ? err : err_);
+                                                             node_of_treelet_, seeds, treelets, err ? err : err_);
     note_launches(1);
     return cudaGetLastError();
   }
