@@ -649,31 +649,26 @@ constexpr int kTcK = kHidden + 16;                  // 64 weights + bias (hi, lo
 constexpr int kTcChunks = kTreelets / kTcN;         // 16
 constexpr uint32_t kTcChunkBytes = kTcN * kTcK * 2; // 40 KB
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr uint32_t kTcStages = 2;                   // weight chunks in flight
 // kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A and
 // B (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
                             ((uint32_t)(kTcRays >> 4) << 24);
 
 struct TcSmem {
-  uint16_t w4[2][kTcN * kTcK];      // streamed output weights + bias (UMMA layout)
-  uint16_t a[kTcRays * kTcK];       // last hidden layer of the tile + ones (UMMA layout)
-  uint16_t x[kTcRays * kLdX];
-  uint16_t h[kTcRays * kLdH];
-  uint16_t w1[kHidden * kLdX];
-  uint16_t w2[kHidden * kLdH];
-  uint16_t w3[kHidden * kLdH];
-  float b[3][kHidden];
+  uint16_t w4[kTcStages][kTcN * kTcK];  // streamed output weights + bias (UMMA layout)
+  uint16_t a[2][kTcRays * kTcK];    // last hidden layers of two tiles + ones (UMMA layout)
   float mv[kTcRays][4][4];          // partial top-4 per row and column quarter
   int mi[kTcRays][4][4];
-  unsigned long long tma_bar[2];
+  unsigned long long tma_bar[kTcStages];
+  unsigned long long a_bar[2];
   unsigned long long mma_bar[2];
   unsigned long long epi_bar[2];
-  unsigned long long a_bar;
   uint32_t tmem_base;
   uint32_t fail;
 };
 static_assert(offsetof(TcSmem, a) % 1024 == 0, "operand tiles start on 1 KB boundaries");
+constexpr uint32_t kTcTileBytes = kTcRays * kTcK * 2;  // one A tile, 20 KB
 static_assert(offsetof(TcSmem, tma_bar) % 8 == 0, "mbarrier alignment");
 
 // element offset of (row, k) in the UMMA K-major core-matrix layout (K = 80:
@@ -693,9 +688,19 @@ __device__ __forceinline__ uint64_t umma_desc(const void* smem) {
 __device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
 }
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+// Waits for the phase with the given parity; gives up after kWaitNs of wall
+// time (a try_wait may itself suspend for a while, so the bound is on time,
+// not on the number of tries).
+constexpr uint64_t kWaitNs = 2000000000ull;
 __device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity) {
   const uint32_t a = smem_u32(b);
-  for (uint32_t i = 0; i < kSpinLimit; i++) {
+  uint64_t t0 = 0;
+  for (uint32_t i = 0;; i++) {
     uint32_t ok = 0;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -703,8 +708,9 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity
         : "r"(a), "r"(parity)
         : "memory");
     if (ok) return true;
+    if (i == 0) t0 = global_ns();
+    else if ((i & 63) == 0 && global_ns() - t0 > kWaitNs) return false;
   }
-  return false;
 }
 __device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(b)) : "memory");
@@ -767,42 +773,89 @@ __global__ void k_permute_w4(const uint16_t* __restrict__ Pb, const float* __res
   *reinterpret_cast<uint4*>(w4p + (size_t)c * kTcN * kTcK + umma_off(r, kc * 8)) = v;
 }
 
+// Encoder and hidden layers for tiles of 128 rays (8 warps, 16 rows each):
+// each tile's last hidden layer is written, with the bias ones, in the UMMA
+// layout k_propose_tc bulk-copies (tile t at H + t * kTcRays * kTcK).
+struct HidSmem {
+  uint16_t x[kTcRays * kLdX];
+  uint16_t h[kTcRays * kLdH];
+  uint16_t w1[kHidden * kLdX];
+  uint16_t w2[kHidden * kLdH];
+  uint16_t w3[kHidden * kLdH];
+  float b[3][kHidden];
+};
+
+__global__ void __launch_bounds__(256) k_propose_hidden(const char* rays, uint64_t stride, uint32_t M,
+                                                        const uint32_t* d_count, GridSpec grid,
+                                                        const uint16_t* __restrict__ Pb, const float* __restrict__ P,
+                                                        uint16_t* __restrict__ H) {
+  extern __shared__ __align__(16) unsigned char hid_smem_raw[];
+  HidSmem& S = *reinterpret_cast<HidSmem*>(hid_smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  for (int i = tid; i < kHidden * kIn / 2; i += 256) {
+    const int o = (2 * i) / kIn, k = (2 * i) % kIn;
+    *reinterpret_cast<uint32_t*>(S.w1 + o * kLdX + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW1)[i];
+  }
+  for (int i = tid; i < kHidden * kHidden / 2; i += 256) {
+    const int o = (2 * i) / kHidden, k = (2 * i) % kHidden;
+    *reinterpret_cast<uint32_t*>(S.w2 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW2)[i];
+    *reinterpret_cast<uint32_t*>(S.w3 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW3)[i];
+  }
+  for (int i = tid; i < 3 * kHidden; i += 256) {
+    const size_t off = i < kHidden ? kOffB1 : (i < 2 * kHidden ? kOffB2 : kOffB3);
+    S.b[i / kHidden][i % kHidden] = P[off + i % kHidden];
+  }
+  __syncthreads();
+  if (d_count) M = min(M, *d_count);
+  const uint32_t ntiles = (M + kTcRays - 1) / kTcRays;
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t r0 = tile * kTcRays;
+    for (int it = tid; it < kTcRays * kLevels; it += 256) {
+      const int rr = it / kLevels, l = it % kLevels;
+      const uint32_t rid = r0 + rr;
+      const uint32_t pk = rid < M ? encode_level(Pb, rays + (uint64_t)rid * stride, grid, l) : 0u;
+      *reinterpret_cast<uint32_t*>(S.x + rr * kLdX + 2 * l) = pk;
+    }
+    __syncthreads();
+    {
+      const int row0 = warp * 16;
+      uint16_t* hrow = S.h + row0 * kLdH;
+      hidden_layer<kIn, kLdX>(S.x + row0 * kLdX, S.w1, kLdX, S.b[0], hrow, g, t);
+      __syncwarp();
+      hidden_layer<kHidden, kLdH>(hrow, S.w2, kLdH, S.b[1], hrow, g, t);
+      __syncwarp();
+      hidden_layer<kHidden, kLdH>(hrow, S.w3, kLdH, S.b[2], hrow, g, t);
+    }
+    __syncthreads();
+    // 16-byte pieces in memory order: row group, K core matrix, row within the group
+    uint4* dst = reinterpret_cast<uint4*>(H + (size_t)tile * kTcRays * kTcK);
+    for (int pc = tid; pc < kTcRays * (kTcK / 8); pc += 256) {
+      const int grp = pc / (kTcK), rem = pc % (kTcK), kc = rem >> 3, r = grp * 8 + (rem & 7);
+      uint4 v;
+      if (kc < kHidden / 8) v = *reinterpret_cast<const uint4*>(S.h + r * kLdH + kc * 8);
+      else if (kc == kHidden / 8) v = make_uint4(0x3F803F80u, 0u, 0u, 0u);  // 1.0, 1.0 in BF16
+      else v = make_uint4(0u, 0u, 0u, 0u);
+      dst[pc] = v;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_propose_tc(const char* rays, uint64_t stride, uint32_t M, const uint32_t* d_count, GridSpec grid,
-                 const uint16_t* __restrict__ Pb, const float* __restrict__ P, const uint16_t* __restrict__ W4p,
-                 const uint32_t* __restrict__ node_of_treelet, uint4* seeds, uint32_t* treelets, uint32_t* err) {
+    k_propose_tc(uint32_t M, const uint32_t* d_count, const uint16_t* __restrict__ H,
+                 const uint16_t* __restrict__ W4p, const uint32_t* __restrict__ node_of_treelet, uint4* seeds,
+                 uint32_t* treelets, uint32_t* err) {
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   TcSmem& S = *reinterpret_cast<TcSmem*>(tc_smem_raw);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool producer = warp == kTcScanWarps;
-  if (!producer) {
-    for (int i = tid; i < kHidden * kIn / 2; i += kTcScanThreads) {
-      const int o = (2 * i) / kIn, k = (2 * i) % kIn;
-      *reinterpret_cast<uint32_t*>(S.w1 + o * kLdX + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW1)[i];
-    }
-    for (int i = tid; i < kHidden * kHidden / 2; i += kTcScanThreads) {
-      const int o = (2 * i) / kHidden, k = (2 * i) % kHidden;
-      *reinterpret_cast<uint32_t*>(S.w2 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW2)[i];
-      *reinterpret_cast<uint32_t*>(S.w3 + o * kLdH + k) = reinterpret_cast<const uint32_t*>(Pb + kOffW3)[i];
-    }
-    for (int i = tid; i < 3 * kHidden; i += kTcScanThreads) {
-      const size_t off = i < kHidden ? kOffB1 : (i < 2 * kHidden ? kOffB2 : kOffB3);
-      S.b[i / kHidden][i % kHidden] = P[off + i % kHidden];
-    }
-    // the A operand's bias columns: ones at k 64 and 65, zeros up to 79
-    for (int r = tid; r < kTcRays; r += kTcScanThreads) {
-      const uint32_t one = 0x3F80u;  // 1.0 in BF16
-      *reinterpret_cast<uint4*>(S.a + umma_off(r, kHidden)) = make_uint4(one | (one << 16), 0u, 0u, 0u);
-      *reinterpret_cast<uint4*>(S.a + umma_off(r, kHidden + 8)) = make_uint4(0u, 0u, 0u, 0u);
-    }
-  } else {
+  if (producer) {
     if (lane == 0) {
+      for (uint32_t b = 0; b < kTcStages; b++) mbar_init(&S.tma_bar[b], 1);
       for (int b = 0; b < 2; b++) {
-        mbar_init(&S.tma_bar[b], 1);
+        mbar_init(&S.a_bar[b], 1);
         mbar_init(&S.mma_bar[b], 1);
         mbar_init(&S.epi_bar[b], kTcScanWarps);
       }
-      mbar_init(&S.a_bar, 1);
       S.fail = 0;
       asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
@@ -820,30 +873,51 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t ntiles = (M + kTcRays - 1) / kTcRays;
   const uint32_t my_tiles = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
   const uint32_t total_chunks = my_tiles * kTcChunks;
+  auto tile_src = [&](uint32_t k) { return H + (size_t)(blockIdx.x + k * gridDim.x) * kTcRays * kTcK; };
 
+  // phases started on each barrier by the producer (bulk copies and MMA
+  // commits): after a failure the producer waits for the last one of each, so
+  // that no copy or MMA is in flight when the CTA frees its shared memory and TMEM
+  uint32_t n_w[kTcStages], n_a[2] = {0u, 0u}, n_m[2] = {0u, 0u};
+  for (uint32_t q = 0; q < kTcStages; q++) n_w[q] = 0u;
   if (producer) {
     if (lane == 0 && total_chunks > 0) {
       bool ok = true;
-      bulk_load(S.w4[0], W4p, kTcChunkBytes, &S.tma_bar[0]);
-      if (total_chunks > 1) bulk_load(S.w4[1], W4p + (size_t)kTcN * kTcK, kTcChunkBytes, &S.tma_bar[1]);
-      const uint64_t adesc0 = umma_desc(S.a);
+      bulk_load(S.a[0], tile_src(0), kTcTileBytes, &S.a_bar[0]);
+      n_a[0]++;
+      if (my_tiles > 1) bulk_load(S.a[1], tile_src(1), kTcTileBytes, &S.a_bar[1]), n_a[1]++;
+      for (uint32_t q = 0; q < kTcStages && q < total_chunks; q++) {
+        bulk_load(S.w4[q], W4p + (size_t)(q % kTcChunks) * kTcN * kTcK, kTcChunkBytes, &S.tma_bar[q]);
+        n_w[q]++;
+      }
       for (uint32_t gc = 0; gc < total_chunks && ok; gc++) {
-        const uint32_t c = gc % kTcChunks, s = gc & 1u, par = (gc >> 1) & 1u;
-        if (c == 0) ok = mbar_wait(&S.a_bar, (gc / kTcChunks) & 1u);           // A operand of this tile
-        if (ok) ok = mbar_wait(&S.tma_bar[s], par);                            // weights of chunk gc
-        if (ok && gc >= 2) ok = mbar_wait(&S.epi_bar[s], ((gc - 2) >> 1) & 1u); // accumulator s read
+        const uint32_t k = gc / kTcChunks, c = gc % kTcChunks, s = gc & 1u, ab = k & 1u;
+        const uint32_t ws = gc % kTcStages;
+        if (c == 0) ok = mbar_wait(&S.a_bar[ab], (k >> 1) & 1u);                       // A operand of tile k
+        if (ok) ok = mbar_wait(&S.tma_bar[ws], (gc / kTcStages) & 1u);                 // weights of chunk gc
+        if (ok && gc >= 2) ok = mbar_wait(&S.epi_bar[s], ((gc - 2) >> 1) & 1u);         // accumulator s read
         if (!ok) break;
         tc_fence_after();
-        const uint64_t bdesc0 = umma_desc(S.w4[s]);
+        const uint64_t adesc0 = umma_desc(S.a[ab]), bdesc0 = umma_desc(S.w4[ws]);
 #pragma unroll
         for (int ks = 0; ks < kTcK / 16; ks++)  // +256 B per K step: two core matrices
           umma_bf16(tmem + s * kTcN, adesc0 + (uint64_t)(ks * 16), bdesc0 + (uint64_t)(ks * 16), ks > 0);
         umma_commit(&S.mma_bar[s]);
-        // stage (gc - 1) & 1 is free once chunk gc - 1's MMAs are done: next copy into it
-        if (gc >= 1 && gc + 1 < total_chunks) {
+        n_m[s]++;
+        // stage (gc - 1) % kTcStages is free once chunk gc - 1's MMAs are done: it
+        // takes chunk gc - 1 + kTcStages
+        if (gc >= 1 && gc - 1 + kTcStages < total_chunks) {
           if (!(ok = mbar_wait(&S.mma_bar[(gc - 1) & 1u], ((gc - 1) >> 1) & 1u))) break;
-          bulk_load(S.w4[(gc + 1) & 1u], W4p + (size_t)((gc + 1) % kTcChunks) * kTcN * kTcK, kTcChunkBytes,
-                    &S.tma_bar[(gc + 1) & 1u]);
+          const uint32_t nc = gc - 1 + kTcStages;
+          bulk_load(S.w4[nc % kTcStages], W4p + (size_t)(nc % kTcChunks) * kTcN * kTcK, kTcChunkBytes,
+                    &S.tma_bar[nc % kTcStages]);
+          n_w[nc % kTcStages]++;
+        }
+        // after the last MMA of tile k, its A buffer takes tile k + 2
+        if (c == kTcChunks - 1 && k + 2 < my_tiles) {
+          if (!(ok = mbar_wait(&S.mma_bar[s], (gc >> 1) & 1u))) break;
+          bulk_load(S.a[ab], tile_src(k + 2), kTcTileBytes, &S.a_bar[ab]);
+          n_a[ab]++;
         }
       }
       if (!ok) {
@@ -854,38 +928,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncwarp();
   } else {
     uint32_t gc = 0;
+    const int quarter = warp >> 2;
     for (uint32_t k = 0; k < my_tiles; k++) {
       const uint32_t tile = blockIdx.x + k * gridDim.x;
-      const uint32_t r0 = tile * kTcRays;
-      for (int it = tid; it < kTcRays * kLevels; it += kTcScanThreads) {
-        const int rr = it / kLevels, l = it % kLevels;
-        const uint32_t rid = r0 + rr;
-        const uint32_t pk = rid < M ? encode_level(Pb, rays + (uint64_t)rid * stride, grid, l) : 0u;
-        *reinterpret_cast<uint32_t*>(S.x + rr * kLdX + 2 * l) = pk;
-      }
-      scan_sync();
-      if (warp < kTcRays / 16) {
-        const int row0 = warp * 16;
-        uint16_t* hrow = S.h + row0 * kLdH;
-        hidden_layer<kIn, kLdX>(S.x + row0 * kLdX, S.w1, kLdX, S.b[0], hrow, g, t);
-        __syncwarp();
-        hidden_layer<kHidden, kLdH>(hrow, S.w2, kLdH, S.b[1], hrow, g, t);
-        __syncwarp();
-        hidden_layer<kHidden, kLdH>(hrow, S.w3, kLdH, S.b[2], hrow, g, t);
-      }
-      scan_sync();
-      for (int it = tid; it < kTcRays * (kHidden / 8); it += kTcScanThreads) {
-        const int r = it >> 3, kc = it & 7;
-        *reinterpret_cast<uint4*>(S.a + umma_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(S.h + r * kLdH + kc * 8);
-      }
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      scan_sync();
-      if (tid == 0) mbar_arrive(&S.a_bar);
       float v[4];
       int ix[4];
 #pragma unroll
       for (int q = 0; q < 4; q++) { v[q] = -INFINITY; ix[q] = -1; }
-      const int quarter = warp >> 2;
       bool ok = true;
       for (int c = 0; c < kTcChunks; c++, gc++) {
         const uint32_t s = gc & 1u;
@@ -919,11 +968,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // barrier they all reach (a warp that timed out left its chunk loop early)
       volatile uint32_t* fail_flag = &S.fail;
       if (!ok) *fail_flag = 1u;
-      scan_sync();
-      if (*fail_flag) {
-        if (tid == 0) atomicOr(err, kErrIterationLimit);
-        break;
-      }
       {  // merge the four column quarters of each row (ties to the lower column)
         const int row = (warp & 3) * 32 + lane;
 #pragma unroll
@@ -933,6 +977,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
       }
       scan_sync();
+      if (*fail_flag) {
+        if (tid == 0) atomicOr(err, kErrIterationLimit);
+        break;
+      }
       if (tid < kTcRays) {
         float bv[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
         int bi[4] = {-1, -1, -1, -1};
@@ -949,7 +997,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               bi[pos] = i;
             }
           }
-        const uint32_t rid = r0 + tid;
+        const uint32_t rid = tile * kTcRays + tid;
         if (rid < M) {
           auto node = [&](int tl) { return tl >= 0 ? __ldg(node_of_treelet + tl) : kInvalidID; };
           if (seeds) seeds[rid] = make_uint4(node(bi[0]), node(bi[1]), node(bi[2]), node(bi[3]));
@@ -958,15 +1006,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 make_uint4((uint32_t)bi[0], (uint32_t)bi[1], (uint32_t)bi[2], (uint32_t)bi[3]);
         }
       }
+      scan_sync();  // S.mv is written again by the next tile
     }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (producer) {
-    // bulk copies still in flight after a failure land before the CTA ends
-    if (lane == 0 && *(volatile uint32_t*)&S.fail)
-      for (int s = 0; s < 2; s++) mbar_wait(&S.tma_bar[s], 0), mbar_wait(&S.tma_bar[s], 1);
+    // after a failure, copies and MMAs still in flight complete before the CTA
+    // ends (each wait is bounded; phase n - 1 is the last one started)
+    if (lane == 0 && *(volatile uint32_t*)&S.fail) {
+      for (uint32_t q = 0; q < kTcStages; q++)
+        if (n_w[q]) mbar_wait(&S.tma_bar[q], (n_w[q] - 1u) & 1u);
+      for (int q = 0; q < 2; q++) {
+        if (n_a[q]) mbar_wait(&S.a_bar[q], (n_a[q] - 1u) & 1u);
+        if (n_m[q]) mbar_wait(&S.mma_bar[q], (n_m[q] - 1u) & 1u);
+      }
+    }
     __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(kTmemCols) : "memory");
   }
@@ -1021,6 +1077,7 @@ cudaError_t Proposer::init(const std::vector<uint32_t>& node_of_treelet, const s
   GB_TRY(cudaMalloc(&err_, sizeof(uint32_t)));
   GB_TRY(cudaMemsetAsync(err_, 0, sizeof(uint32_t), st));
   GB_TRY(cudaFuncSetAttribute(k_propose_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem)));
+  GB_TRY(cudaFuncSetAttribute(k_propose_hidden, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(HidSmem)));
   std::vector<uint32_t> nodes(kTreelets, kInvalidID);
   std::copy(node_of_treelet.begin(), node_of_treelet.begin() + num_treelets, nodes.begin());
   GB_TRY(cudaMemcpyAsync(node_of_treelet_, nodes.data(), kTreelets * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
@@ -1048,13 +1105,14 @@ cudaError_t Proposer::refresh_w4(cudaStream_t st) {
 
 void Proposer::release() {
   void* ptrs[] = {P_, Pb_, G_, m_, v_, node_of_treelet_, prim_treelet_, geom_prefix_, acc_, X0_, H1_, H2_, H3_,
-                  dZ4_, dZ_, Z_, Z4_, dH_, dX0_, W4p_, err_};
+                  dZ4_, dZ_, Z_, Z4_, dH_, dX0_, W4p_, err_, H_};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   P_ = G_ = m_ = v_ = acc_ = Z_ = Z4_ = dH_ = dX0_ = nullptr;
   Pb_ = X0_ = H1_ = H2_ = H3_ = dZ4_ = dZ_ = nullptr;
   node_of_treelet_ = prim_treelet_ = geom_prefix_ = err_ = nullptr;
-  W4p_ = nullptr;
+  W4p_ = H_ = nullptr;
+  hcap_ = 0;
   cap_ = 0;
 }
 
@@ -1189,10 +1247,19 @@ cudaError_t Proposer::predict(const char* rays, uint64_t stride, uint32_t M, uin
                               cudaStream_t st, const uint32_t* d_count, uint32_t* err) {
   if (M == 0) return cudaSuccess;
   if (!use_mma_sync) {
-    const uint32_t grid_n = std::min<uint32_t>((M + kTcRays - 1) / kTcRays, (uint32_t)num_sms());
-    k_propose_tc<<<grid_n, kTcThreads, sizeof(TcSmem), st>>>(rays, stride, M, d_count, grid, Pb_, P_, W4p_,
-                                                             node_of_treelet_, seeds, treelets, err ? err : err_);
-    note_launches(1);
+    const uint32_t ntiles = (M + kTcRays - 1) / kTcRays;
+    if ((size_t)ntiles * kTcRays * kTcK > hcap_) {
+      if (H_) cudaFree(H_);
+      H_ = nullptr;
+      hcap_ = 0;
+      GB_TRY(cudaMalloc(&H_, (size_t)ntiles * kTcTileBytes));
+      hcap_ = (size_t)ntiles * kTcRays * kTcK;
+    }
+    k_propose_hidden<<<std::min<uint32_t>(ntiles, (uint32_t)num_sms() * 4), 256, sizeof(HidSmem), st>>>(
+        rays, stride, M, d_count, grid, Pb_, P_, H_);
+    k_propose_tc<<<std::min<uint32_t>(ntiles, (uint32_t)num_sms()), kTcThreads, sizeof(TcSmem), st>>>(
+        M, d_count, H_, W4p_, node_of_treelet_, seeds, treelets, err ? err : err_);
+    note_launches(2);
     return cudaGetLastError();
   }
   const uint32_t ntiles = (M + kPRays - 1) / kPRays;

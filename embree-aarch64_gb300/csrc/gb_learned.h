@@ -114,6 +114,8 @@ class Proposer {
   uint32_t num_geom_ids_ = 0;
   float* acc_ = nullptr;       // device accumulators: loss sum, top1 count, top4 count, labelled count
   uint16_t* W4p_ = nullptr;    // output weights in the tensor cores' shared-memory layout
+  uint16_t* H_ = nullptr;      // inference: last hidden layer of every tile (same layout)
+  size_t hcap_ = 0;
   uint32_t* err_ = nullptr;    // error word of inference calls without one
   cudaError_t refresh_w4(cudaStream_t st);
 

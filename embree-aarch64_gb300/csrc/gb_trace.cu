@@ -207,8 +207,8 @@ struct Ctx {
   uint32_t num_tris;
 };
 
-constexpr int kRefillIdle = 8;      // a warp fetches new rays once this many lanes are idle
-constexpr int kPostponePct = 20;    // triangle work waits while fewer active lanes have it
+constexpr int kRefillIdle = 4;      // a warp fetches new rays once this many lanes are idle
+constexpr int kPostponePct = 10;    // triangle work waits while fewer active lanes have it
 constexpr uint32_t kTriGroup = 0x80000000u;  // stack entry flag: triangle group
 
 template <bool ALIGNED>

@@ -1994,9 +1994,15 @@ RTC_API void rtcgbProposerPredict(RTCGBProposer hp, const struct RTCRay* rays, u
   std::lock_guard<std::mutex> lk(p->mtx);
   DevSpan in(rays, (size_t)(M - 1) * byteStride + sizeof(RTCRay), st, true);
   DevSpan out(treelets, (size_t)M * 16, st, false);
-  cuda_ok(p->net.predict(in.d, byteStride, M, nullptr, (uint32_t*)out.d, st), "proposer inference");
+  t_ctx.ensure(p->scene->device->cuda_device);
+  cuda_ok(cudaMemsetAsync(t_ctx.dscratch + 1, 0, sizeof(uint32_t), st), "memset");
+  cuda_ok(p->net.predict(in.d, byteStride, M, nullptr, (uint32_t*)out.d, st, nullptr, t_ctx.dscratch + 1),
+          "proposer inference");
   out.copy_out(st);
+  uint32_t perr = 0;
+  cuda_ok(cudaMemcpyAsync(&perr, t_ctx.dscratch + 1, sizeof(perr), cudaMemcpyDeviceToHost, st), "status");
   cuda_ok(cudaStreamSynchronize(st), "proposer inference");
+  if (perr) fail(RTC_ERROR_UNKNOWN, "proposer inference timed out");
   API_END(p ? p->scene->device : nullptr)
 }
 
