@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--animated-scale", type=float, default=1.0, help="fraction of the animated workload (tests only)")
     ap.add_argument("--frames", type=int, default=64, help="frames of the animated path-tracing run")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes run")
+    ap.add_argument("--no-heightfield", action="store_true", help="skip the heightfield-view run")
     ap.add_argument("--batched-scale", type=float, default=1.0, help="fraction of the batched workload (tests only)")
     return ap.parse_args()
 
@@ -144,6 +145,23 @@ def peaks():
         return 6800.0, "fallback 6.8 TB/s"
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The maximum of a per-rank float over all ranks (the slowest rank sets
+    the job's time); x itself without a process group."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, seconds):
+    """Whole-job rate in millions of units per second: every rank processed
+    units_per_rank units (weak scaling) in at most `seconds`."""
+    return world * units_per_rank / seconds / 1e6
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (the oracle port of the reference path)
 # ---------------------------------------------------------------------------
@@ -206,7 +224,7 @@ def run_reference(args, rank, world):
 MLP_FLOPS_PER_RAY = 2 * (32 * 64 + 64 * 64 + 64 * 64 + 64 * 4096)  # forward pass of the proposer
 
 
-def run_learned(api, dev, torch, stream, scale, steps, warmup):
+def run_learned(api, dev, torch, stream, scale, steps, warmup, cpu_seconds):
     """Learned proposer vs plain traversal on the ambient-occlusion workload:
     724x724 heightfield + 300k soup triangles, 1024x1024 primary view, 8
     cosine-weighted AO rays (tfar 0.05) and 8 diffuse bounce rays per primary
@@ -300,6 +318,23 @@ def run_learned(api, dev, torch, stream, scale, steps, warmup):
     out["mismatches"] = out["ao"]["mismatches"] + out["bounce"]["mismatches"]
     prop.release()
     sc.release()
+    if cpu_seconds > 0:  # the oracle on the same two ray sets, all host threads
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle_ffi
+        orc = oracle_ffi.OracleScene([(g, v, i) for g, (v, i) in
+                                      enumerate(W.ao_scene(cells=cells, soup_tris=soup, seed=3))])
+        cpu = {}
+        for name, rays, shadow in (("ao", ao, True), ("bounce", bounce, False)):
+            r, _, _ = cpu_rate(None, None, rays, cpu_seconds / 2, shadow=shadow, orc=orc)
+            cpu[name] = r["value"]
+        orc.close()
+        cores = os.cpu_count() or 1
+        out["cpu_baseline"] = {"value": (ao.shape[0] + bounce.shape[0]) / (ao.shape[0] / cpu["ao"] / 1e6 +
+                                                                           bounce.shape[0] / cpu["bounce"] / 1e6) / 1e6,
+                               "unit": "Mrays/s", "cores": cores, "kind": "port",
+                               "ao_Mrays_per_s": cpu["ao"], "bounce_Mrays_per_s": cpu["bounce"],
+                               "sample": f"leading rays of the AO and bounce sets (~{cpu_seconds / 2:.0f} s each), "
+                                         f"all {cores} host threads"}
     torch.cuda.empty_cache()
     return out
 
@@ -400,7 +435,124 @@ def _device_rays(torch, n_cam, n_sph, eye, look, seed):
     return rec
 
 
-def run_batched(api, dev_config, torch, scale, steps, warmup):
+def flush_l2(torch, buf):
+    """Writes a buffer larger than the 129 MB L2 so the next launch starts cold."""
+    buf.fill_(0)
+
+
+def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds):
+    """The heightfield view: a 256x256-cell value-noise heightfield (131,072
+    triangles), 1024x1024 pinhole primary rays through rtcIntersect1M, then
+    shadow rays from the hits through rtcOccluded1M.  The rays (80 MB) fit in
+    L2, so a 256 MB buffer is written between timed launches.  Every ray is
+    compared with the oracle, which is also timed as the CPU baseline."""
+    from rtcgb import rays as R
+    from rtcgb import workloads as W
+    verts, idx = W.heightfield(256)
+    rays = W.camera_rays(1024, 1024)
+    n = rays.shape[0]
+    sc = api.Scene(dev)
+    sc.add_mesh(verts, idx)
+    t = time.perf_counter()
+    sc.commit()
+    first_s = time.perf_counter() - t
+    builds = []
+    for _ in range(3):
+        sc.commit()
+        builds.append(sc.build_stats()["build_ms"])
+    bst = sc.build_stats()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    pristine = torch.from_numpy(rays.view(np.uint8)).cuda()
+    work = torch.empty_like(pristine)
+    kms = []
+    for k in range(warmup + steps):
+        work.copy_(pristine)
+        flush_l2(torch, flush)
+        sc.intersect_ptr(work.data_ptr(), n, 80)
+        if k >= warmup:
+            kms.append(api.last_query_stats()["kernel_ms"])
+    out_rays = work.cpu().numpy().view(R.RAYHIT_DTYPE)
+    shadow, _ = W.shadow_rays(out_rays, seed=13)
+    active = int(np.sum(shadow["tnear"] <= shadow["tfar"]))
+    sh_pristine = torch.from_numpy(shadow.view(np.uint8)).cuda()
+    sh_work = torch.empty_like(sh_pristine)
+    sms = []
+    for k in range(warmup + steps):
+        sh_work.copy_(sh_pristine)
+        flush_l2(torch, flush)
+        sc.occluded_ptr(sh_work.data_ptr(), n, 48)
+        if k >= warmup:
+            sms.append(api.last_query_stats()["kernel_ms"])
+    sh_out = sh_work.cpu().numpy().view(R.RAY_DTYPE)
+    # end to end through the public call on pinned host memory
+    host = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory()
+    src = torch.from_numpy(rays.view(np.uint8))
+    e2e = []
+    for k in range(warmup + steps):
+        host.copy_(src)
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sc.intersect_ptr(host.data_ptr(), n, 80)
+        if k >= warmup:
+            e2e.append(time.perf_counter() - t)
+    kernel_ms, sh_ms = statistics.median(kms), statistics.median(sms)
+    out = {"workload": f"value-noise heightfield 256x256 cells ({idx.shape[0]} tris), 1024x1024 pinhole closest-hit "
+                       "rays + shadow rays from the hits",
+           "l2": "rays fit in L2: a 256 MB buffer is written before every timed launch",
+           "build": {"device_ms": float(statistics.median(builds)), "first_commit_wall_ms": first_s * 1e3,
+                     "Mtris_per_s": float(bst["num_prims"] / (statistics.median(builds) * 1e-3) / 1e6),
+                     "sah": bst["sah"], "sah_exact_boxes": bst["sah_exact"]},
+           "closest": {"kernel_ms": kernel_ms, "Mrays_per_s": n / (kernel_ms * 1e-3) / 1e6,
+                       "hit_rate": float(np.mean(out_rays["geomID"] != 0xFFFFFFFF))},
+           "shadow": {"kernel_ms": sh_ms, "Mrays_per_s": active / (sh_ms * 1e-3) / 1e6, "active_rays": active},
+           "e2e": {"Mrays_per_s": n / statistics.median(e2e) / 1e6, "h2d_bytes_per_step": n * 80,
+                   "d2h_bytes_per_step": n * 36, "host_buffer": "pinned"}}
+    del pristine, work, sh_pristine, sh_work, flush, host
+    torch.cuda.empty_cache()
+    sc.release()
+    if cpu_seconds > 0:
+        base, orc, sample = cpu_rate(verts, idx, rays, cpu_seconds)
+        orc.intersect(rays)  # every ray (the sample may be shorter)
+        sh_ref = shadow.copy()
+        orc.occluded(sh_ref)
+        st = orc.stats()
+        orc.close()
+        same = R.hits_equal_bits(out_rays, rays)
+        out["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        out["build"]["sah_reference_builder"] = st.sah
+        out["build"]["sah_ratio"] = bst["sah"] / st.sah
+        out["build"]["sah_ratio_exact_boxes"] = bst["sah_exact"] / st.sah
+        out["parity"] = {"rays": n, "identical_hits": int(same.sum()),
+                         "identical_ids": int(((out_rays["geomID"] == rays["geomID"]) &
+                                               (out_rays["primID"] == rays["primID"])).sum()),
+                         "shadow_rays": n, "identical_occlusion": int(((sh_out["tfar"] < 0) == (sh_ref["tfar"] < 0)).sum())}
+    return out
+
+
+def fp32_order_tie(mesh, ray, a, b, oracle_ffi):
+    """True when both reported triangles pass the reference's single-triangle
+    FP32 test for the ray and their distances are at most 2 ulps apart: the
+    ray crosses their shared edge, and the answer depends on which triangle is
+    tested first, because the test accepts T <= absDen * tfar before dividing
+    (triangle_intersector_moeller.h:62-104), so the first accepted hit's tfar
+    still admits a hit one ulp farther."""
+    v, idx = mesh
+    o = (float(ray["org_x"]), float(ray["org_y"]), float(ray["org_z"]))
+    d = (float(ray["dir_x"]), float(ray["dir_y"]), float(ray["dir_z"]))
+    ts = []
+    for h in (a, b):
+        if int(h["geomID"]) == 0xFFFFFFFF:
+            return False
+        t = idx[int(h["primID"])]
+        ok, _, tuv, _ = oracle_ffi.moeller1(v[t[0]], v[t[1]], v[t[2]], o, d, float(ray["tnear"]), float(ray["tfar"]))
+        if not ok:
+            return False
+        ts.append(np.float32(tuv[0]))
+    return abs(int(ts[0].view(np.int32)) - int(ts[1].view(np.int32))) <= 2
+
+
+def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
     """512 independent scenes (log-uniform 1k-200k triangles, ~20M in total;
     even scenes noise heightfields of matching grid size, odd scenes Gaussian
     soups), 32 rays per triangle (half a pinhole view, half uniform-sphere
@@ -478,21 +630,58 @@ def run_batched(api, dev_config, torch, scale, steps, warmup):
            "build_plus_trace_ms": float(statistics.median(builds)) + kernel_ms,
            "autotune": {"chosen": best, "candidates": tuning, "sample_scenes": len(sample)},
            "generation_s": gen_s}
-    # exact-hit spot check: the first 4096 rays of 4 scenes against the oracle
+    # CPU baseline and exact-hit check: the oracle builds and traces whole
+    # scenes one after another (every 8th scene, then the rest, until the time
+    # budget is spent), every ray of each compared with the GPU's result
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle_ffi
     res = work.cpu().numpy().view(R.RAYHIT_DTYPE).reshape(-1)
     src = pristine.cpu().numpy().view(R.RAYHIT_DTYPE).reshape(-1)
-    same = total = 0
-    for k in (0, 1, nscenes // 2, nscenes - 1):
-        lo, hi = int(start[k]), min(int(start[k]) + 4096, int(start[k + 1]))
+    same = ties = total = done_tris = 0
+    verdicts = {}
+    build_s = trace_s = 0.0
+    order = list(range(0, nscenes, 8)) + [k for k in range(nscenes) if k % 8]
+    scenes_done = 0
+    for k in order:
+        if build_s + trace_s > cpu_seconds and scenes_done >= 2:
+            break
+        lo, hi = int(start[k]), int(start[k + 1])
+        t = time.perf_counter()
         orc = oracle_ffi.OracleScene([(k, meshes[k][0], meshes[k][1])])
+        build_s += time.perf_counter() - t
         ref = src[lo:hi].copy()
+        t = time.perf_counter()
         orc.intersect(ref)
-        same += int(((ref["geomID"] == res["geomID"][lo:hi]) & (ref["primID"] == res["primID"][lo:hi])).sum())
+        trace_s += time.perf_counter() - t
+        ids = (ref["geomID"] == res["geomID"][lo:hi]) & (ref["primID"] == res["primID"][lo:hi])
+        same += int(ids.sum())
+        # different triangles at the same distance (shared edges): ties of the visiting order
+        tie = ~ids & (ref["tfar"].view(np.uint32) == res["tfar"][lo:hi].view(np.uint32))
+        ties += int(tie.sum())
+        # the other differences go to the FP64 adjudicator (near tie, grazing, or which side is right)
+        for j in np.nonzero(~ids & ~tie)[0][:2000]:
+            g = res[lo + j]
+            code = orc.adjudicate(src[lo + j], (g["geomID"], g["primID"], g["tfar"]),
+                                  (ref["geomID"][j], ref["primID"][j], ref["tfar"][j]))
+            if code != 1 and fp32_order_tie(meshes[k], src[lo + j], g, ref[j], oracle_ffi):
+                code = 5
+            verdicts[code] = verdicts.get(code, 0) + 1
         total += hi - lo
+        done_tris += int(tris[k])
+        scenes_done += 1
         orc.close()
-    out["parity_sample"] = {"rays": total, "identical_ids": same}
+    cores = os.cpu_count() or 1
+    names = {0: "real_mismatch", 1: "near_tie_fp64", 2: "grazing", 3: "gpu_right_fp64", 4: "oracle_right_fp64",
+             5: "fp32_order_tie"}
+    out["parity_sample"] = {"scenes": scenes_done, "rays": total, "identical_ids": same, "equal_t_ties": ties,
+                            "differing_not_tie": total - same - ties,
+                            "fp64_adjudicated": {names[k]: v for k, v in sorted(verdicts.items())}}
+    out["cpu_baseline"] = {"value": total / (build_s + trace_s) / 1e6, "unit": "Mrays/s (build + trace)",
+                           "cores": cores, "kind": "port",
+                           "sample": f"{scenes_done} whole scenes ({done_tris} tris, {total} rays), built one after "
+                                     f"another by the single-threaded oracle builder and traced on {cores} threads",
+                           "build_Mtris_per_s": done_tris / build_s / 1e6, "trace_Mrays_per_s": total / trace_s / 1e6}
+    out["gpu_build_plus_trace_Mrays_per_s"] = nrays / ((float(statistics.median(builds)) + kernel_ms) * 1e-3) / 1e6
     sc.release()
     dev.release()
     del pristine, work
@@ -564,14 +753,11 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     launches = api.launch_count() - launches0
     clk = clocks.stop()
-    total_ms = ev0.elapsed_time(ev1)
+    total_ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     ms_per_step = total_ms / args.steps
-    value = world * nrays / (ms_per_step * 1e-3) / 1e6
+    value = job_rate(nrays, world, ms_per_step * 1e-3)
     kernel_ms = statistics.mean(kms)
 
     # counting run (untimed): traversal work for the algorithmic byte model
@@ -618,12 +804,8 @@ def run_gpu(args, rank, world):
             if k >= args.warmup:
                 times.append(dt)
         q = api.last_query_stats()
-        e2e_s = statistics.median(times)
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * nrays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(q["h2d_bytes"]),
+        e2e_s = max_over_ranks(statistics.median(times), dist, "cuda")
+        e2e = {"value": job_rate(nrays, world, e2e_s), "unit": "Mrays/s", "h2d_bytes_per_step": int(q["h2d_bytes"]),
                "d2h_bytes_per_step": int(q["d2h_bytes"]), "ms_per_step": e2e_s * 1e3,
                "host_buffer": "pinned", "host_access": int(api.load().rtcgbGetDeviceHostAccess(dev.h)),
                "path": "rtcIntersect1M on host memory (" + (args.config or "gpu.host_rays default") + ")"}
@@ -652,20 +834,26 @@ def run_gpu(args, rank, world):
                        "occluded_rate": float(np.mean(sh_work.cpu().numpy().view(R.RAY_DTYPE)["tfar"] == -np.inf))},
             "build": {"device_ms": build_ms, "wall_ms": build_wall_ms, "first_commit_wall_ms": build_wall * 1e3,
                       "Mtris_per_s": bst["num_prims"] / (build_ms * 1e-3) / 1e6, "sah": bst["sah"],
+                      "sah_exact_boxes": bst["sah_exact"],
                       "nodes": bst["num_nodes"], "depth": bst["depth"], "ploc_iterations": bst["ploc_iterations"],
                       "bvh_MB": bst["bvh_bytes"] / 1e6},
-            "learned": None, "animated": None, "batched": None,
+            "learned": None, "animated": None, "batched": None, "heightfield": None,
         }
 
     if rank == 0 and not args.no_learned:
         del pristine, work, sh_pristine, sh_work
         torch.cuda.empty_cache()
-        line["learned"] = run_learned(api, dev, torch, stream, args.learned_scale, args.steps, args.warmup)
+        line["learned"] = run_learned(api, dev, torch, stream, args.learned_scale, args.steps, args.warmup,
+                                      0.0 if args.no_cpu else min(6.0, args.cpu_seconds))
     if rank == 0 and not args.no_animated:
         line["animated"] = run_animated(api, dev, torch, args.animated_scale, args.frames)
     if rank == 0 and not args.no_batched:
         line["batched"] = run_batched(api, f"gpu.device={local}{',' + args.config if args.config else ''}", torch,
-                                      args.batched_scale, args.steps, args.warmup)
+                                      args.batched_scale, args.steps, args.warmup,
+                                      0.0 if args.no_cpu else min(8.0, args.cpu_seconds))
+    if rank == 0 and not args.no_heightfield:
+        line["heightfield"] = run_heightfield(api, dev, torch, stream, args.steps, args.warmup,
+                                              0.0 if args.no_cpu else min(3.0, args.cpu_seconds))
 
     if rank == 0 and not args.no_cpu:
         base, orc, sample = cpu_rate(verts, idx, rays, args.cpu_seconds, robust=args.robust)
@@ -673,6 +861,7 @@ def run_gpu(args, rank, world):
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["build"]["sah_reference_builder"] = st.sah
         line["build"]["sah_ratio"] = bst["sah"] / st.sah
+        line["build"]["sah_ratio_exact_boxes"] = bst["sah_exact"] / st.sah
         line["build"]["reference_builder_s_1thread"] = base["build_s"]
         # exact-hit check of the sampled rays against the oracle
         n = sample.shape[0]

@@ -205,14 +205,18 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
       const float lo[3] = {ord2f(acc->clo[0]), ord2f(acc->clo[1]), ord2f(acc->clo[2])};
       const float hi[3] = {ord2f(acc->chi[0]), ord2f(acc->chi[1]), ord2f(acc->chi[2])};
       const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
-      // cube: one scale for all axes (the centroid box's largest extent) keeps
-      // the scene's aspect ratio, so flat scenes are ordered mostly in-plane;
-      // otherwise every axis is scaled to its own extent
+      // one scale for all axes (the centroid box's largest extent) keeps the
+      // scene's aspect ratio, so flat scenes (heightfields) are ordered mostly
+      // in-plane, which lowers their SAH; per-axis scales trace faster on
+      // volumetric scenes.  cube: 0 per-axis, 1 one scale, 2 one scale when
+      // the centroid box is flat
       const float emax = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+      const float emin = fminf(fminf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+      const bool one_scale = cube == 1 || (cube == 2 && emin < 0.5f * emax);
       uint64_t code = 0;
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        const float ext = cube ? emax : hi[d] - lo[d];
+        const float ext = one_scale ? emax : hi[d] - lo[d];
         float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
         x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
         code |= spread21((uint32_t)x) << (2 - d);
@@ -258,53 +262,85 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* __restri
   hist[threadIdx.x * nblocks + blockIdx.x] = s_h[threadIdx.x];
 }
 
-// Exclusive scan of a uint32 array by a single block of 1024 threads.
-// Optionally writes the total to *total.
-__global__ void __launch_bounds__(1024) k_scan_excl(uint32_t* __restrict__ a, uint32_t n, uint32_t* total) {
-  __shared__ uint32_t s_w[32];
-  __shared__ uint32_t s_carry;
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
+// Exclusive scans of uint32 arrays.  One tile is 1024 threads x 8 consecutive
+// elements.  Small arrays are scanned by one CTA; larger ones by
+// reduce-then-scan over many CTAs (tile sums, a one-CTA scan of the sums, then
+// each tile scanned again from its offset), which reads the array twice and
+// writes it once.
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER = 8;
+constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_PER;
+
+// Scans a[base, base + SCAN_TILE) in place, offset by carry; every thread gets
+// the tile's total.  All threads of the CTA must call it.
+__device__ __forceinline__ uint32_t scan_tile(uint32_t* __restrict__ a, uint32_t n, uint32_t base, uint32_t carry,
+                                              uint32_t* s_w) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int PER = 8;
-  for (uint32_t base = 0; base < n; base += 1024 * PER) {
-    uint32_t v[PER];
-    uint32_t sum = 0;
-    const uint32_t i0 = base + threadIdx.x * PER;
+  uint32_t v[SCAN_PER];
+  uint32_t sum = 0;
+  const uint32_t i0 = base + threadIdx.x * SCAN_PER;
 #pragma unroll
-    for (int k = 0; k < PER; k++) {
-      v[k] = (i0 + k < n) ? a[i0 + k] : 0u;
-      sum += v[k];
-    }
-    uint32_t x = sum;
+  for (int k = 0; k < SCAN_PER; k++) {
+    v[k] = (i0 + k < n) ? a[i0 + k] : 0u;
+    sum += v[k];
+  }
+  uint32_t x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = s_w[lane];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-      if (lane >= o) x += y;
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
     }
-    if (lane == 31) s_w[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t w = s_w[lane];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
-        if (lane >= o) w += y;
-      }
-      s_w[lane] = w;
-    }
-    __syncthreads();
-    uint32_t excl = s_carry + (warp ? s_w[warp - 1] : 0u) + (x - sum);
-#pragma unroll
-    for (int k = 0; k < PER; k++) {
-      if (i0 + k < n) a[i0 + k] = excl;
-      excl += v[k];
-    }
-    __syncthreads();
-    if (threadIdx.x == 1023) s_carry = excl;
-    __syncthreads();
+    s_w[lane] = w;
   }
-  if (total && threadIdx.x == 0) *total = s_carry;
+  __syncthreads();
+  uint32_t excl = carry + (warp ? s_w[warp - 1] : 0u) + (x - sum);
+#pragma unroll
+  for (int k = 0; k < SCAN_PER; k++) {
+    if (i0 + k < n) a[i0 + k] = excl;
+    excl += v[k];
+  }
+  const uint32_t tile_total = s_w[31];
+  __syncthreads();  // s_w is reused by the next call
+  return tile_total;
+}
+
+// One CTA of 1024 threads over the whole array; optionally writes the total.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_excl(uint32_t* __restrict__ a, uint32_t n, uint32_t* total) {
+  __shared__ uint32_t s_w[32];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < n; base += SCAN_TILE) carry += scan_tile(a, n, base, carry, s_w);
+  if (total && threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(const uint32_t* __restrict__ a, uint32_t n,
+                                                                 uint32_t* __restrict__ sums) {
+  __shared__ uint32_t s_w[32];
+  const uint32_t i0 = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER; k++) sum += (i0 + k < n) ? a[i0 + k] : 0u;
+  sum = __reduce_add_sync(0xFFFFFFFFu, sum);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, s_w[threadIdx.x]);
+    if (threadIdx.x == 0) sums[blockIdx.x] = w;
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(uint32_t* __restrict__ a, uint32_t n,
+                                                             const uint32_t* __restrict__ offs) {
+  __shared__ uint32_t s_w[32];
+  scan_tile(a, n, blockIdx.x * SCAN_TILE, offs[blockIdx.x], s_w);
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin,
@@ -387,11 +423,17 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
   chi[i] = make_float4(b.x, b.y, b.z, 0.f);
 }
 
+// PLOC rounds run back to back without the host: the cluster count and the
+// next binary node index live in device memory (ploc_state[0], [1]); grids are
+// sized for an upper bound of the count, and CTAs past the count have no work.
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict__ clo, const float4* __restrict__ chi,
-                                                        uint32_t n, uint32_t* __restrict__ nn) {
+                                                        const uint32_t* __restrict__ ploc_state,
+                                                        uint32_t* __restrict__ nn) {
   __shared__ float3 s_lo[PLOC_BLOCK + 2 * PLOC_R], s_hi[PLOC_BLOCK + 2 * PLOC_R];
   __shared__ uint32_t s_seg[PLOC_BLOCK + 2 * PLOC_R];
+  const uint32_t n = ploc_state[0];
   const int base = blockIdx.x * PLOC_BLOCK;
+  if ((uint32_t)base >= n) return;
   for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
     const int j = base - PLOC_R + k;
     if (j >= 0 && j < (int)n) {
@@ -418,8 +460,10 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict
   nn[i] = best != ~0ull ? (uint32_t)best : (uint32_t)i;  // no neighbour in the segment: stays alone
 }
 
-__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_count(const uint32_t* __restrict__ nn, uint32_t n,
+__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_count(const uint32_t* __restrict__ nn,
+                                                           const uint32_t* __restrict__ ploc_state,
                                                            uint32_t* __restrict__ bsurv, uint32_t* __restrict__ bmerge) {
+  const uint32_t n = ploc_state[0];  // CTAs past it write zero counts
   const uint32_t i = blockIdx.x * PLOC_BLOCK + threadIdx.x;
   int surv = 0, merge = 0;
   if (i < n) {
@@ -450,14 +494,17 @@ __device__ __forceinline__ uint32_t block_excl_scan_flag(int flag, uint32_t* s_w
 
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const float4* __restrict__ clo, const float4* __restrict__ chi,
                                                           const uint32_t* __restrict__ cidx,
-                                                          const uint32_t* __restrict__ nn, uint32_t n,
+                                                          const uint32_t* __restrict__ nn,
+                                                          const uint32_t* __restrict__ ploc_state,
                                                           const uint32_t* __restrict__ bsurv_off,
-                                                          const uint32_t* __restrict__ bmerge_off, uint32_t node_next,
+                                                          const uint32_t* __restrict__ bmerge_off,
                                                           float4* __restrict__ bnlo, float4* __restrict__ bnhi,
                                                           uint32_t* __restrict__ bncnt, float4* __restrict__ olo,
                                                           float4* __restrict__ ohi, uint32_t* __restrict__ oidx,
                                                           uint32_t node_cap, uint32_t* err) {
   __shared__ uint32_t s_w[PLOC_BLOCK / 32];
+  const uint32_t n = ploc_state[0], node_next = ploc_state[1];
+  if (blockIdx.x * PLOC_BLOCK >= n) return;
   const uint32_t i = blockIdx.x * PLOC_BLOCK + threadIdx.x;
   int surv = 0, merge = 0;
   uint32_t j = 0;
@@ -496,6 +543,16 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const float4* __restri
     olo[pos] = a;
     ohi[pos] = b;
     oidx[pos] = cidx[i];
+  }
+}
+
+// After a round: the survivors are the new clusters, the merges took the next
+// binary node indices; ploc_state[2] counts the rounds that merged anything.
+__global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ ploc_state) {
+  if (threadIdx.x == 0) {
+    ploc_state[0] = tot[0];
+    ploc_state[1] += tot[1];
+    ploc_state[2] += tot[1] > 0 ? 1u : 0u;
   }
 }
 
@@ -652,6 +709,32 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
 // 5. collapse to 8-wide quantised nodes
 // ---------------------------------------------------------------------------
 
+// Adds the per-thread values a, b to acc[0], acc[1] with one atomic each per
+// CTA; every thread of the CTA calls it (blockDim.x a multiple of 32).
+__device__ __forceinline__ void block_add2(double a, double b, double* acc) {
+  __shared__ double s_a[32], s_b[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xFFFFFFFFu, a, o);
+    b += __shfl_down_sync(0xFFFFFFFFu, b, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    s_a[warp] = a;
+    s_b[warp] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int w = 0; w < nw; w++) {
+      ta += s_a[w];
+      tb += s_b[w];
+    }
+    if (ta != 0.0) atomicAdd(acc + 0, ta);
+    if (tb != 0.0) atomicAdd(acc + 1, tb);
+  }
+}
+
 struct BinTree {
   const float4* lo;
   const float4* hi;
@@ -659,6 +742,7 @@ struct BinTree {
   uint32_t nleaves;
   uint32_t leaf_max;  // subtrees of at most this many triangles may become leaves
   uint32_t robust;    // write raw vertices into triangle records
+  const uint2* choice;  // SAH-optimal collapse decisions (k_collapse_dp); null: greedy collapse
 };
 
 __device__ __forceinline__ bool bt_leaf(const BinTree& t, uint32_t k) { return k < t.nleaves; }
@@ -673,12 +757,139 @@ __device__ __forceinline__ float3 bt_hi(const BinTree& t, uint32_t k) {
   return make_float3(a.x, a.y, a.z);
 }
 
+// ---- SAH-optimal collapse (dynamic programming over the binary tree, after
+// Ylitie, Karras and Laine, "Efficient incoherent ray traversal on GPUs
+// through compressed wide BVHs", HPG 2017).  cost(n, i) is the least SAH cost
+// of the subtree of binary node n when it may take up to i child slots of a
+// wide node: i = 1 is n itself as one child (a leaf when it holds at most
+// leaf_max triangles -- then its cost is area x Triangle4 blocks -- else a wide
+// node of its own: area + D(n, 8)); i > 1 is min(cost(n, i - 1), D(n, i)) with
+// D(n, i) = min over k of cost(left, k) + cost(right, i - k).  The costs are
+// the SAH statistic's terms (bvh_statistics.cpp:10-160), so the tree minimises
+// the reported SAH for the given binary tree and leaf size.
+//
+// choice[n] packs the decisions: byte 0 = argmin k of D(n, 8) (the split of a
+// wide node made from n); byte i - 1 (i = 2..8) = the k of D(n, i) when it beat
+// cost(n, i - 1), else 0.  The pass runs bottom-up from the primitives: each
+// thread climbs through parent links, and at every node only the second child
+// to arrive (atomic counter) goes on, so every node is computed once, after
+// both children.
+
+__global__ void __launch_bounds__(256) k_bin_parents(const float4* __restrict__ bnlo, const float4* __restrict__ bnhi,
+                                                     uint32_t first, uint32_t end, uint32_t* __restrict__ parent) {
+  const uint32_t k = first + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end) return;
+  parent[__float_as_uint(bnlo[k].w)] = k;
+  parent[__float_as_uint(bnhi[k].w)] = k;
+}
+
+__device__ __forceinline__ void dp_store(float4* cost, uint2* choice, uint32_t n, const float c[8], uint2 ch) {
+  __stcg(cost + 2 * (size_t)n, make_float4(c[0], c[1], c[2], c[3]));
+  __stcg(cost + 2 * (size_t)n + 1, make_float4(c[4], c[5], c[6], c[7]));
+  __stcg(choice + n, ch);
+}
+
+__global__ void __launch_bounds__(256) k_collapse_dp(BinTree t, const uint32_t* __restrict__ parent, uint32_t nnodes,
+                                                     uint32_t* __restrict__ arrivals, float4* __restrict__ cost,
+                                                     uint2* __restrict__ choice) {
+  uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= t.nleaves) return;
+  {  // a primitive: one triangle, one block, whatever the number of slots
+    const float A = half_area(bt_lo(t, n), bt_hi(t, n));
+    const float c[8] = {A, A, A, A, A, A, A, A};
+    dp_store(cost, choice, n, c, make_uint2(0u, 0u));
+  }
+  for (uint32_t guard = 0; guard < nnodes; guard++) {
+    __threadfence();  // this node's costs before the arrival count
+    const uint32_t p = parent[n];
+    if (p == kInvalidID || p >= nnodes) return;
+    if (atomicAdd(arrivals + p, 1u) == 0u) return;  // the sibling is not done: it continues
+    __threadfence();
+    n = p;
+    const uint32_t l = bt_left(t, n), r = bt_right(t, n);
+    float cl[8], cr[8];
+    {
+      const float4 a = __ldcg(cost + 2 * (size_t)l), b = __ldcg(cost + 2 * (size_t)l + 1);
+      const float4 e = __ldcg(cost + 2 * (size_t)r), f = __ldcg(cost + 2 * (size_t)r + 1);
+      cl[0] = a.x; cl[1] = a.y; cl[2] = a.z; cl[3] = a.w; cl[4] = b.x; cl[5] = b.y; cl[6] = b.z; cl[7] = b.w;
+      cr[0] = e.x; cr[1] = e.y; cr[2] = e.z; cr[3] = e.w; cr[4] = f.x; cr[5] = f.y; cr[6] = f.z; cr[7] = f.w;
+    }
+    float D[9];
+    uint32_t K[9];
+#pragma unroll
+    for (int i = 2; i <= 8; i++) {
+      D[i] = INFINITY;
+      K[i] = 1;
+#pragma unroll
+      for (int k = 1; k < i; k++) {
+        const float v = cl[k - 1] + cr[i - k - 1];
+        if (v < D[i]) {
+          D[i] = v;
+          K[i] = (uint32_t)k;
+        }
+      }
+    }
+    const float A = half_area(bt_lo(t, n), bt_hi(t, n));
+    const uint32_t cnt = t.cnt[n];
+    const float c_int = A + D[8];
+    const float c_leaf = cnt <= t.leaf_max ? A * (float)((cnt + 3) / 4) : INFINITY;
+    float c[8];
+    c[0] = fminf(c_leaf, c_int);
+    uint32_t b[8];
+    b[0] = K[8];
+#pragma unroll
+    for (int i = 2; i <= 8; i++) {
+      const bool split = D[i] < c[i - 2];
+      c[i - 1] = split ? D[i] : c[i - 2];
+      b[i - 1] = split ? K[i] : 0u;
+    }
+    dp_store(cost, choice, n, c,
+             make_uint2(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24), b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24)));
+  }
+}
+
+__device__ __forceinline__ uint32_t dp_choice(const BinTree& t, uint32_t n, int i) {
+  const uint2 c = t.choice[n];
+  const uint32_t w = i - 1 < 4 ? c.x : c.y;
+  return (w >> (8 * ((i - 1) & 3))) & 0xFFu;
+}
+
+// Children of the wide node made from binary node b by the recorded DP splits.
+__device__ int gather_children_dp(const BinTree& t, uint32_t b, uint32_t kids[8]) {
+  uint32_t sn[8];
+  int si[8];
+  int sp = 0, nk = 0;
+  const uint32_t k8 = dp_choice(t, b, 1);  // byte 0: split of D(b, 8)
+  sn[sp] = bt_left(t, b);
+  si[sp++] = (int)k8;
+  sn[sp] = bt_right(t, b);
+  si[sp++] = 8 - (int)k8;
+  while (sp > 0) {
+    const uint32_t n = sn[--sp];
+    int i = si[sp];
+    while (i > 1 && (bt_leaf(t, n) || dp_choice(t, n, i) == 0)) i--;
+    // the slots of the pending entries and the emitted children sum to at most
+    // 8, so a split always fits; the capacity test only guards the stack
+    if (i <= 1 || nk + sp + 2 > 8) {
+      if (nk < 8) kids[nk++] = n;
+      continue;
+    }
+    const int k = (int)dp_choice(t, n, i);
+    sn[sp] = bt_left(t, n);
+    si[sp++] = k;
+    sn[sp] = bt_right(t, n);
+    si[sp++] = i - k;
+  }
+  return nk;
+}
+
 // Chooses up to 8 children for the wide node that replaces binary node b.
 __device__ int gather_children(const BinTree& t, uint32_t b, uint32_t kids[8]) {
   if (bt_leaf(t, b)) {
     kids[0] = b;
     return 1;
   }
+  if (t.choice) return gather_children_dp(t, b, kids);
   kids[0] = bt_left(t, b);
   kids[1] = bt_right(t, b);
   int nk = 2;
@@ -768,18 +979,15 @@ __device__ __forceinline__ void write_tri(const GeomDesc* __restrict__ geoms, co
   dst->c = make_float4(e2.x, e2.y, e2.z, 0.f);
 }
 
-__global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc* __restrict__ geoms,
-                                                       const float4* __restrict__ plo, const float4* __restrict__ phi,
-                                                       const uint32_t* __restrict__ kids_in, uint32_t nitems,
-                                                       const uint32_t* __restrict__ off_int,
-                                                       const uint32_t* __restrict__ off_tri, uint32_t level_base,
-                                                       uint32_t next_base, uint32_t tri_next,
-                                                       WideNode* __restrict__ nodes, TriRecord* __restrict__ tris,
-                                                       uint32_t* __restrict__ next_items, double* sah_acc,
-                                                       uint32_t* leaf_count, uint32_t node_cap, uint32_t tri_cap,
-                                                       uint32_t* err) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nitems) return;
+// Writes wide node k of the level and the triangle records of its leaves;
+// adds the node's SAH terms and leaf count to sah_out / nleaf_out.
+__device__ __forceinline__ void collapse_emit_node(
+    const BinTree& t, const GeomDesc* __restrict__ geoms, const float4* __restrict__ plo,
+    const float4* __restrict__ phi, const uint32_t* __restrict__ kids_in, uint32_t k,
+    const uint32_t* __restrict__ off_int, const uint32_t* __restrict__ off_tri, uint32_t level_base,
+    uint32_t next_base, uint32_t tri_next, WideNode* __restrict__ nodes, TriRecord* __restrict__ tris,
+    uint32_t* __restrict__ next_items, uint32_t node_cap, uint32_t tri_cap, uint32_t* err, double& sah_out,
+    double& sahx_out, uint32_t& nleaf_out) {
   uint32_t kids[8];
   int nk = 0;
   for (int i = 0; i < 8; i++) {
@@ -840,7 +1048,7 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
   node.child_base = next_base + off_int[k];
   node.tri_base = tri_next + off_tri[k];
   uint32_t int_rank = 0, tri_off = 0;
-  double sah = 0.0;
+  double sah = 0.0, sahx = 0.0;  // on the decoded (quantised) and on the exact boxes
   uint32_t nleaf = 0;
   for (int s = 0; s < 8; s++) {
     const int i = kid_at[s];
@@ -864,6 +1072,7 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
     const float3 dlo = make_float3(__fmaf_rd(qlx, sx, ulo.x), __fmaf_rd(qly, sy, ulo.y), __fmaf_rd(qlz, sz, ulo.z));
     const float3 dhi = make_float3(__fmaf_ru(qhx, sx, ulo.x), __fmaf_ru(qhy, sy, ulo.y), __fmaf_ru(qhz, sz, ulo.z));
     const double A = (double)fmaxf(0.f, half_area(dlo, dhi));
+    const double Ax = (double)fmaxf(0.f, half_area(a, b));
     const uint32_t cnt = t.cnt[c];
     if (cnt > t.leaf_max) {
       node.meta[s] = (uint8_t)(0x80u | (uint32_t)s);
@@ -875,6 +1084,7 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
       next_items[off_int[k] + int_rank] = c;
       int_rank++;
       sah += A;  // inner node term
+      sahx += Ax;
     } else {
       node.meta[s] = (uint8_t)(0x80u | ((cnt - 1u) << 5) | tri_off);
       // collect the subtree's primitives (<= leaf_max) in depth-first order
@@ -902,6 +1112,7 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
       }
       tri_off += cnt;
       sah += A * (double)((cnt + 3) / 4);  // leaf term: area x Triangle4 blocks
+      sahx += Ax * (double)((cnt + 3) / 4);
       nleaf++;
     }
   }
@@ -910,8 +1121,30 @@ __global__ void __launch_bounds__(128) k_collapse_emit(BinTree t, const GeomDesc
     return;
   }
   nodes[level_base + k] = node;
-  atomicAdd(sah_acc, sah);
-  atomicAdd(leaf_count, nleaf);
+  sah_out = sah;
+  sahx_out = sahx;
+  nleaf_out = nleaf;
+}
+
+constexpr int COLLAPSE_THREADS = 128;
+
+// One wide node per thread; the SAH sums and the leaf count are reduced per
+// CTA first (one atomic per CTA instead of one per node).
+__global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
+    BinTree t, const GeomDesc* __restrict__ geoms, const float4* __restrict__ plo, const float4* __restrict__ phi,
+    const uint32_t* __restrict__ kids_in, uint32_t nitems, const uint32_t* __restrict__ off_int,
+    const uint32_t* __restrict__ off_tri, uint32_t level_base, uint32_t next_base, uint32_t tri_next,
+    WideNode* __restrict__ nodes, TriRecord* __restrict__ tris, uint32_t* __restrict__ next_items, double* sah_acc,
+    uint32_t* leaf_count, uint32_t node_cap, uint32_t tri_cap, uint32_t* err) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  double sah = 0.0, sahx = 0.0;
+  uint32_t nleaf = 0;
+  if (k < nitems)
+    collapse_emit_node(t, geoms, plo, phi, kids_in, k, off_int, off_tri, level_base, next_base, tri_next, nodes, tris,
+                       next_items, node_cap, tri_cap, err, sah, sahx, nleaf);
+  nleaf = __reduce_add_sync(0xFFFFFFFFu, nleaf);
+  if ((threadIdx.x & 31) == 0 && nleaf) atomicAdd(leaf_count, nleaf);
+  block_add2(sah, sahx, sah_acc);
 }
 
 // ---------------------------------------------------------------------------
@@ -924,6 +1157,24 @@ static cudaError_t dalloc(T** p, size_t count, cudaStream_t st) {
 }
 
 static inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+// Entries of tile-sum scratch that scan_excl needs for n elements.
+static inline uint32_t scan_scratch(uint32_t n) { return cdiv(n, SCAN_TILE) + 1; }
+
+// Exclusive scan of a[0, n) in place (total to *total when non-null); sums
+// holds scan_scratch(n) entries.
+static void scan_excl(uint32_t* a, uint32_t n, uint32_t* total, uint32_t* sums, cudaStream_t st) {
+  if (n <= 2 * SCAN_TILE) {
+    k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(a, n, total);
+    note_launches(1);
+    return;
+  }
+  const uint32_t nt = cdiv(n, SCAN_TILE);
+  k_scan_tile_sums<<<nt, SCAN_THREADS, 0, st>>>(a, n, sums);
+  k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(sums, nt, total);
+  k_scan_tiles<<<nt, SCAN_THREADS, 0, st>>>(a, n, sums);
+  note_launches(3);
+}
 
 cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, const BuildOptions& opt, DeviceBVH* out,
                       BuildStats* stats) {
@@ -987,13 +1238,13 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   {
     const uint32_t nb = cdiv(total, RS_TILE);
     uint32_t* hist = nullptr;
-    GB_CHECK(dalloc(&hist, (size_t)256 * nb, st));
+    GB_CHECK(dalloc(&hist, (size_t)sort_hist_entries(total), st));
     for (int pass = 0; pass < 8; pass++) {
       const int shift = 8 * pass;
       const uint64_t a = (h_acc.kand >> shift) & 0xFF, o = (h_acc.kor >> shift) & 0xFF;
       if (a == o) continue;  // digit constant over all keys
       k_rs_hist<<<nb, RS_THREADS, 0, st>>>(keys_a, total, shift, hist, nb); note_launches(1);
-      k_scan_excl<<<1, 1024, 0, st>>>(hist, 256 * nb, nullptr); note_launches(1);
+      scan_excl(hist, 256 * nb, nullptr, hist + 256 * nb, st);
       k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(keys_a, vals_a, keys_b, vals_b, total, shift, hist, nb); note_launches(1);
       std::swap(keys_a, keys_b);
       std::swap(vals_a, vals_b);
@@ -1025,41 +1276,59 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   const uint32_t maxb = cdiv(N, PLOC_BLOCK);
   GB_CHECK(dalloc(&bsurv, maxb, st));
   GB_CHECK(dalloc(&bmerge, maxb, st));
+  uint32_t* scan_sums = nullptr;  // tile sums of the PLOC and collapse scans
+  GB_CHECK(dalloc(&scan_sums, scan_scratch(std::max(maxb, N)), st));
   GB_CHECK(dalloc(&d_tot, 4, st));
   GB_CHECK(dalloc(&d_root, nseg, st));
   GB_CHECK(cudaMemsetAsync(d_root, 0xFF, sizeof(uint32_t) * nseg, st));
   GB_CHECK(dalloc(&d_iters, 1, st));
   GB_CHECK(cudaMemsetAsync(d_iters, 0, sizeof(uint32_t), st));
-  uint32_t n = N, node_next = N, iters = 0;
+  // rounds in batches of kPlocBatch between host reads of the state; the
+  // count only shrinks, so the count read last bounds the grids of a batch
+  // (a batch may run a few rounds past PLOC_SMALL: they are ordinary rounds)
+  constexpr int kPlocBatch = 4;
+  uint32_t* ploc_state = nullptr;
+  GB_CHECK(dalloc(&ploc_state, 4, st));
   uint32_t* h_tot = nullptr;
   GB_CHECK(cudaMallocHost((void**)&h_tot, 4 * sizeof(uint32_t)));
+  h_tot[0] = N;
+  h_tot[1] = N;
+  h_tot[2] = 0;
+  h_tot[3] = 0;
+  GB_CHECK(cudaMemcpyAsync(ploc_state, h_tot, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  uint32_t n = N;
   while (n > PLOC_SMALL) {
     const uint32_t nb = cdiv(n, PLOC_BLOCK);
-    k_ploc_nn<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, n, nn); note_launches(1);
-    k_ploc_count<<<nb, PLOC_BLOCK, 0, st>>>(nn, n, bsurv, bmerge); note_launches(1);
-    k_scan_excl<<<1, 1024, 0, st>>>(bsurv, nb, d_tot + 0); note_launches(1);
-    k_scan_excl<<<1, 1024, 0, st>>>(bmerge, nb, d_tot + 1); note_launches(1);
-    k_ploc_emit<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, cidx_a, nn, n, bsurv, bmerge, node_next, bnlo, bnhi, bncnt,
-                                           clo_b, chi_b, cidx_b, nnodes_bin, &acc->pad); note_launches(1);
+    for (int b = 0; b < kPlocBatch; b++) {
+      k_ploc_nn<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn);
+      k_ploc_count<<<nb, PLOC_BLOCK, 0, st>>>(nn, ploc_state, bsurv, bmerge);
+      note_launches(2);
+      scan_excl(bsurv, nb, d_tot + 0, scan_sums, st);
+      scan_excl(bmerge, nb, d_tot + 1, scan_sums, st);
+      k_ploc_emit<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, cidx_a, nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt,
+                                             clo_b, chi_b, cidx_b, nnodes_bin, &acc->pad);
+      k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state);
+      note_launches(2);
+      std::swap(clo_a, clo_b);
+      std::swap(chi_a, chi_b);
+      std::swap(cidx_a, cidx_b);
+    }
     GB_CHECK(cudaGetLastError());
-    GB_CHECK(cudaMemcpyAsync(h_tot, d_tot, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GB_CHECK(cudaMemcpyAsync(h_tot, ploc_state, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GB_CHECK(cudaStreamSynchronize(st));
-    if (h_tot[1] == 0) {
-      // without segments this cannot happen (the globally closest pair is
-      // mutual); with segments it means every segment is down to one cluster
+    if (h_tot[0] == n) {
+      // no merge in a whole batch: without segments this cannot happen (the
+      // globally closest pair is mutual); with segments it means every
+      // segment is down to one cluster
       if (!segmented || n > PLOC_SMALL) {
         cudaFreeHost(h_tot);
         return cudaErrorUnknown;
       }
       break;
     }
-    node_next += h_tot[1];
     n = h_tot[0];
-    iters++;
-    std::swap(clo_a, clo_b);
-    std::swap(chi_a, chi_b);
-    std::swap(cidx_a, cidx_b);
   }
+  const uint32_t node_next = h_tot[1], iters = h_tot[2];
   {
     const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     GB_CHECK(cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1089,11 +1358,34 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   stats->ploc_iterations = iters + small_iters;
   cudaFreeAsync(clo_b, st); cudaFreeAsync(chi_b, st); cudaFreeAsync(cidx_b, st);
   cudaFreeAsync(clo_a, st); cudaFreeAsync(chi_a, st); cudaFreeAsync(cidx_a, st);
-  cudaFreeAsync(nn, st); cudaFreeAsync(bsurv, st); cudaFreeAsync(bmerge, st);
+  cudaFreeAsync(nn, st); cudaFreeAsync(bsurv, st); cudaFreeAsync(bmerge, st); cudaFreeAsync(ploc_state, st);
 
   // ---- collapse, level by level (breadth-first node order)
   BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(opt.leaf_max, 1), kLeafMaxLimit),
-             (uint32_t)(opt.robust != 0)};
+             (uint32_t)(opt.robust != 0), nullptr};
+  uint2* d_choice = nullptr;
+  if (opt.collapse == 1) {  // SAH-optimal collapse decisions
+    const uint32_t nbin = 2 * N - (uint32_t)root_items.size();  // binary nodes of all trees
+    uint32_t *parent = nullptr, *arrivals = nullptr;
+    float4* cost = nullptr;
+    GB_CHECK(dalloc(&parent, nbin, st));
+    GB_CHECK(dalloc(&arrivals, nbin, st));
+    GB_CHECK(dalloc(&cost, 2 * (size_t)nbin, st));
+    GB_CHECK(dalloc(&d_choice, nbin, st));
+    GB_CHECK(cudaMemsetAsync(parent, 0xFF, sizeof(uint32_t) * nbin, st));
+    GB_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * nbin, st));
+    if (nbin > N) {
+      k_bin_parents<<<cdiv(nbin - N, 256), 256, 0, st>>>(bnlo, bnhi, N, nbin, parent);
+      note_launches(1);
+    }
+    k_collapse_dp<<<cdiv(N, 256), 256, 0, st>>>(bt, parent, nbin, arrivals, cost, d_choice);
+    note_launches(1);
+    GB_CHECK(cudaGetLastError());
+    cudaFreeAsync(parent, st);
+    cudaFreeAsync(arrivals, st);
+    cudaFreeAsync(cost, st);
+    bt.choice = d_choice;
+  }
   WideNode* wnodes = nullptr;
   TriRecord* wtris = nullptr;
   const uint32_t maxw = N;  // wide internal nodes <= binary internal nodes + 1
@@ -1107,9 +1399,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(dalloc(&ntri, maxw, st));
   double* d_sah = nullptr;
   uint32_t* d_leaves = nullptr;
-  GB_CHECK(dalloc(&d_sah, 1, st));
+  GB_CHECK(dalloc(&d_sah, 2, st));  // quantised, exact
   GB_CHECK(dalloc(&d_leaves, 1, st));
-  GB_CHECK(cudaMemsetAsync(d_sah, 0, sizeof(double), st));
+  GB_CHECK(cudaMemsetAsync(d_sah, 0, 2 * sizeof(double), st));
   GB_CHECK(cudaMemsetAsync(d_leaves, 0, sizeof(uint32_t), st));
   GB_CHECK(cudaMemcpyAsync(items_a, root_items.data(), sizeof(uint32_t) * root_items.size(), cudaMemcpyHostToDevice,
                            st));
@@ -1119,8 +1411,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     level_start.push_back(level_base);
     const uint32_t nb = cdiv(nitems, 128);
     k_collapse_count<<<nb, 128, 0, st>>>(bt, items_a, nitems, kids, nint, ntri); note_launches(1);
-    k_scan_excl<<<1, 1024, 0, st>>>(nint, nitems, d_tot + 0); note_launches(1);
-    k_scan_excl<<<1, 1024, 0, st>>>(ntri, nitems, d_tot + 1); note_launches(1);
+    scan_excl(nint, nitems, d_tot + 0, scan_sums, st);
+    scan_excl(ntri, nitems, d_tot + 1, scan_sums, st);
     const uint32_t next_base = level_base + nitems;
     k_collapse_emit<<<nb, 128, 0, st>>>(bt, d_geoms, plo, phi, kids, nitems, nint, ntri, level_base, next_base,
                                         tri_next, wnodes, wtris, items_b, d_sah, d_leaves, maxw, N, &acc->pad); note_launches(1);
@@ -1141,9 +1433,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     cudaFreeHost(h_tot);
     return cudaErrorUnknown;
   }
-  double sah_sum = 0;
+  double sah_sum[2] = {0.0, 0.0};
   uint32_t nleaves = 0;
-  GB_CHECK(cudaMemcpyAsync(&sah_sum, d_sah, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(sah_sum, d_sah, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(&nleaves, d_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
 
   // exact-size outputs
@@ -1161,7 +1453,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   cudaFreeAsync(wnodes, st); cudaFreeAsync(wtris, st);
   cudaFreeAsync(items_a, st); cudaFreeAsync(items_b, st); cudaFreeAsync(kids, st);
   cudaFreeAsync(nint, st); cudaFreeAsync(ntri, st); cudaFreeAsync(d_sah, st); cudaFreeAsync(d_leaves, st);
-  cudaFreeAsync(d_tot, st); cudaFreeAsync(d_root, st); cudaFreeAsync(d_iters, st);
+  if (d_choice) cudaFreeAsync(d_choice, st);
+  cudaFreeAsync(d_tot, st); cudaFreeAsync(d_root, st); cudaFreeAsync(d_iters, st); cudaFreeAsync(scan_sums, st);
   cudaFreeAsync(bnlo, st); cudaFreeAsync(bnhi, st); cudaFreeAsync(bncnt, st);
   cudaFreeAsync(plo, st); cudaFreeAsync(phi, st); cudaFreeAsync(acc, st); cudaFreeAsync(d_geoms, st);
   cudaFreeAsync(keys_a, st); cudaFreeAsync(keys_b, st); cudaFreeAsync(vals_a, st); cudaFreeAsync(vals_b, st);
@@ -1176,7 +1469,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   // SAH relative to the root box (bvh_statistics.cpp: root node counts once)
   const float gx = out->hi[0] - out->lo[0], gy = out->hi[1] - out->lo[1], gz = out->hi[2] - out->lo[2];
   const double Aroot = std::max(0.0, (double)(gx * (gy + gz) + gy * gz));
-  stats->sah = Aroot > 0 ? (Aroot + sah_sum) / Aroot : 0.0;
+  stats->sah = Aroot > 0 ? (Aroot + sah_sum[0]) / Aroot : 0.0;
+  stats->sah_exact = Aroot > 0 ? (Aroot + sah_sum[1]) / Aroot : 0.0;
   stats->build_ms = ms;
   stats->num_nodes = num_nodes;
   stats->num_leaves = nleaves;
@@ -1197,16 +1491,17 @@ cudaError_t sort_pairs_passes(uint64_t* keys, uint32_t* vals, uint64_t* kb, uint
   for (int pass = 0; pass < passes; pass++) {
     const int shift = 8 * pass;
     k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, shift, hist, nb);
-    k_scan_excl<<<1, 1024, 0, st>>>(hist, 256 * nb, nullptr);
+    scan_excl(hist, 256 * nb, nullptr, hist + 256 * nb, st);
     k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
-    note_launches(3);
+    note_launches(2);
     std::swap(ka, kb);
     std::swap(va, vb);
   }
   return cudaGetLastError();
 }
 
-uint32_t sort_hist_entries(uint32_t n) { return 256u * cdiv(n, RS_TILE); }
+// digit histograms of all tiles, then the scan's tile sums
+uint32_t sort_hist_entries(uint32_t n) { return 256u * cdiv(n, RS_TILE) + scan_scratch(256u * cdiv(n, RS_TILE)); }
 
 cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
@@ -1216,15 +1511,15 @@ cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t 
   const uint32_t nb = cdiv(n, RS_TILE);
   GB_CHECK(dalloc(&kb, n, st));
   GB_CHECK(dalloc(&vb, n, st));
-  GB_CHECK(dalloc(&hist, (size_t)256 * nb, st));
+  GB_CHECK(dalloc(&hist, (size_t)sort_hist_entries(n), st));
   uint64_t* ka = keys;
   uint32_t* va = vals;
   for (int pass = 0; pass < 8; pass++) {
     const int shift = 8 * pass;
     k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, shift, hist, nb);
-    k_scan_excl<<<1, 1024, 0, st>>>(hist, 256 * nb, nullptr);
+    scan_excl(hist, 256 * nb, nullptr, hist + 256 * nb, st);
     k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
-    note_launches(3);
+    note_launches(2);
     std::swap(ka, kb);
     std::swap(va, vb);
   }
@@ -1286,14 +1581,14 @@ __global__ void __launch_bounds__(256) k_refit_tris(const GeomDesc* __restrict__
   tris[i] = rec;
 }
 
-__global__ void __launch_bounds__(128) k_refit_level(const GeomDesc* __restrict__ geoms,
-                                                     const uint32_t* __restrict__ slot_of, uint32_t nslots,
-                                                     const TriRecord* __restrict__ tris, uint32_t num_tris,
-                                                     WideNode* __restrict__ nodes, uint32_t num_nodes,
-                                                     float* __restrict__ node_box, uint32_t begin, uint32_t end,
-                                                     double* sah_acc, uint32_t* err) {
-  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= end || k >= num_nodes) return;
+// Refits wide node k from its children's boxes (inner children: node_box of the
+// level below; leaf children: their triangles' current vertices); returns the
+// node's SAH terms on the decoded and on the exact boxes.
+__device__ __forceinline__ void refit_node(const GeomDesc* __restrict__ geoms, const uint32_t* __restrict__ slot_of,
+                                           uint32_t nslots, const TriRecord* __restrict__ tris, uint32_t num_tris,
+                                           WideNode* __restrict__ nodes, uint32_t num_nodes,
+                                           float* __restrict__ node_box, uint32_t k, uint32_t* err, double& sah_out,
+                                           double& sahx_out) {
   WideNode node = nodes[k];
   float3 clo[8], chi[8];
   float3 ulo = make_float3(INFINITY, INFINITY, INFINITY), uhi = make_float3(-INFINITY, -INFINITY, -INFINITY);
@@ -1338,10 +1633,11 @@ __global__ void __launch_bounds__(128) k_refit_level(const GeomDesc* __restrict_
   node.ex = (uint8_t)Ex;
   node.ey = (uint8_t)Ey;
   node.ez = (uint8_t)Ez;
-  double sah = 0.0;
+  double sah = 0.0, sahx = 0.0;
   for (int s = 0; s < 8; s++) {
     if (node.meta[s] == 0) continue;
     const float3 a = clo[s], b = chi[s];
+    sahx += (double)fmaxf(0.f, half_area(a, b));
     const float qlx = fminf(fmaxf(floorf(__fsub_rd(a.x, ulo.x) * ix), 0.f), 255.f);
     const float qly = fminf(fmaxf(floorf(__fsub_rd(a.y, ulo.y) * iy), 0.f), 255.f);
     const float qlz = fminf(fmaxf(floorf(__fsub_rd(a.z, ulo.z) * iz), 0.f), 255.f);
@@ -1357,7 +1653,22 @@ __global__ void __launch_bounds__(128) k_refit_level(const GeomDesc* __restrict_
   nodes[k] = node;
   node_box[6 * (size_t)k + 0] = ulo.x; node_box[6 * (size_t)k + 1] = ulo.y; node_box[6 * (size_t)k + 2] = ulo.z;
   node_box[6 * (size_t)k + 3] = uhi.x; node_box[6 * (size_t)k + 4] = uhi.y; node_box[6 * (size_t)k + 5] = uhi.z;
-  atomicAdd(sah_acc, sah);
+  sah_out = sah;
+  sahx_out = sahx;
+}
+
+// One node of the level [begin, end) per thread; SAH sums reduced per CTA.
+__global__ void __launch_bounds__(128) k_refit_level(const GeomDesc* __restrict__ geoms,
+                                                     const uint32_t* __restrict__ slot_of, uint32_t nslots,
+                                                     const TriRecord* __restrict__ tris, uint32_t num_tris,
+                                                     WideNode* __restrict__ nodes, uint32_t num_nodes,
+                                                     float* __restrict__ node_box, uint32_t begin, uint32_t end,
+                                                     double* sah_acc, uint32_t* err) {
+  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  double sah = 0.0, sahx = 0.0;
+  if (k < end && k < num_nodes)
+    refit_node(geoms, slot_of, nslots, tris, num_tris, nodes, num_nodes, node_box, k, err, sah, sahx);
+  block_add2(sah, sahx, sah_acc);
 }
 
 cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* bvh, BuildStats* stats,
@@ -1383,11 +1694,11 @@ cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   GB_CHECK(dalloc(&d_slot, slot_of.size(), st));
   GB_CHECK(dalloc(&d_err, 1, st));
   GB_CHECK(dalloc(&node_box, (size_t)6 * bvh->num_nodes, st));
-  GB_CHECK(dalloc(&d_sah, 1, st));
+  GB_CHECK(dalloc(&d_sah, 2, st));
   GB_CHECK(cudaMemcpyAsync(d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
   GB_CHECK(cudaMemcpyAsync(d_slot, slot_of.data(), sizeof(uint32_t) * slot_of.size(), cudaMemcpyHostToDevice, st));
   GB_CHECK(cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st));
-  GB_CHECK(cudaMemsetAsync(d_sah, 0, sizeof(double), st));
+  GB_CHECK(cudaMemsetAsync(d_sah, 0, 2 * sizeof(double), st));
   k_refit_tris<<<cdiv(bvh->num_tris, 256), 256, 0, st>>>(d_geoms, d_slot, (uint32_t)slot_of.size(), bvh->tris,
                                                          bvh->num_tris, bvh->robust, d_err);
   note_launches(1);
@@ -1402,10 +1713,10 @@ cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   GB_CHECK(cudaGetLastError());
   uint32_t err = 0;
   float root[6];
-  double sah_sum = 0;
+  double sah_sum[2] = {0.0, 0.0};
   GB_CHECK(cudaMemcpyAsync(&err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(root, node_box, sizeof(root), cudaMemcpyDeviceToHost, st));
-  GB_CHECK(cudaMemcpyAsync(&sah_sum, d_sah, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(sah_sum, d_sah, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaEventRecord(ev1, st));
   cudaFreeAsync(d_geoms, st);
   cudaFreeAsync(d_slot, st);
@@ -1427,7 +1738,8 @@ cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   }
   const float gx = bvh->hi[0] - bvh->lo[0], gy = bvh->hi[1] - bvh->lo[1], gz = bvh->hi[2] - bvh->lo[2];
   const double Aroot = std::max(0.0, (double)(gx * (gy + gz) + gy * gz));
-  stats->sah = Aroot > 0 ? (Aroot + sah_sum) / Aroot : 0.0;
+  stats->sah = Aroot > 0 ? (Aroot + sah_sum[0]) / Aroot : 0.0;
+  stats->sah_exact = Aroot > 0 ? (Aroot + sah_sum[1]) / Aroot : 0.0;
   stats->build_ms = ms;
   stats->num_nodes = bvh->num_nodes;
   stats->num_prims = bvh->num_tris;
@@ -1449,7 +1761,7 @@ cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& 
   GB_CHECK(cudaMalloc(&out->d_slot, sizeof(uint32_t) * slot_of.size()));
   GB_CHECK(cudaMalloc(&out->d_err, sizeof(uint32_t)));
   GB_CHECK(cudaMalloc(&out->node_box, sizeof(float) * 6 * bvh.num_nodes));
-  GB_CHECK(cudaMalloc(&out->d_sah, sizeof(double)));
+  GB_CHECK(cudaMalloc(&out->d_sah, 2 * sizeof(double)));
   GB_CHECK(cudaMemcpyAsync(out->d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
   GB_CHECK(cudaMemcpyAsync(out->d_slot, slot_of.data(), sizeof(uint32_t) * slot_of.size(), cudaMemcpyHostToDevice, st));
   GB_CHECK(cudaMemsetAsync(out->d_err, 0, sizeof(uint32_t), st));
@@ -1457,7 +1769,7 @@ cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& 
 }
 
 cudaError_t refit_enqueue(const DeviceBVH& bvh, const RefitScratch& s, cudaStream_t st) {
-  GB_CHECK(cudaMemsetAsync(s.d_sah, 0, sizeof(double), st));
+  GB_CHECK(cudaMemsetAsync(s.d_sah, 0, 2 * sizeof(double), st));
   k_refit_tris<<<cdiv(bvh.num_tris, 256), 256, 0, st>>>(s.d_geoms, s.d_slot, s.nslots, bvh.tris, bvh.num_tris,
                                                         bvh.robust, s.d_err);
   note_launches(1);

@@ -110,14 +110,19 @@ struct DeviceBVH {
 // Builder options (device config keys gpu.leaf_max=1..4, gpu.morton=axis|cube).
 struct BuildOptions {
   int leaf_max = kLeafMaxDefault;
-  int morton_cube = 0;  // 1: one Morton scale for all axes (gpu.morton=cube)
+  // Morton scaling: 0 per-axis scales (gpu.morton=axis), 1 one scale for all
+  // axes (gpu.morton=cube), 2 cube when the centroid box is flat (its smallest
+  // extent below half its largest), per-axis otherwise (gpu.morton=auto)
+  int morton_cube = 2;
   int robust = 0;       // RTC_SCENE_FLAG_ROBUST: triangle records hold v0, v1, v2
   int segmented = 0;    // one tree per geometry slot (batched scenes), roots at the first level
+  int collapse = 1;     // binary -> 8-wide: 1 SAH-optimal (gpu.collapse=sah), 0 greedy (gpu.collapse=greedy)
 };
 
 // Build statistics reported through the extension API.
 struct BuildStats {
   double sah = 0;            // bvh_statistics.cpp semantics on the decoded boxes
+  double sah_exact = 0;      // the same on the exact (unquantised) child boxes
   double build_ms = 0;       // device time of the whole build
   uint32_t num_nodes = 0, num_leaves = 0, num_prims = 0, depth = 0;
   uint32_t ploc_iterations = 0;

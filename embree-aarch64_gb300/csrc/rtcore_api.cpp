@@ -106,7 +106,8 @@ struct Device : RefCounted {
   }
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
-  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.host_rays, gpu.proposer, gpu.reorder;
+  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.collapse, gpu.host_rays, gpu.proposer,
+  // gpu.reorder;
   // the CPU tasking and ISA keys
   // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
   void parse(const char* cfg) {
@@ -127,7 +128,8 @@ struct Device : RefCounted {
         else if (k == "benchmark") benchmark = atoi(v.c_str());
         else if (k == "gpu.device") cuda_device = atoi(v.c_str());
         else if (k == "gpu.leaf_max") build_opt.leaf_max = atoi(v.c_str());
-        else if (k == "gpu.morton") build_opt.morton_cube = (v == "cube");
+        else if (k == "gpu.morton") build_opt.morton_cube = v == "cube" ? 1 : v == "axis" ? 0 : 2;
+        else if (k == "gpu.collapse") build_opt.collapse = v == "greedy" ? 0 : 1;
         else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
         else if (k == "gpu.proposer") proposer_mma = (v == "mma");
         else if (k == "gpu.reorder") reorder = atoi(v.c_str());
@@ -382,9 +384,12 @@ struct ThreadCtx {
   RTCGBQueryStats last{};
   int device = -1;
 
+  // The thread's own stream is a blocking stream: it is ordered after work the
+  // caller issued on the legacy default stream (for example the copy that
+  // filled a device ray buffer), as a synchronous query must be.
   cudaStream_t stream() {
     if (user_set) return user;
-    if (!own) cuda_ok(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!own) cuda_ok(cudaStreamCreateWithFlags(&own, cudaStreamDefault), "cudaStreamCreate");
     return own;
   }
   void ensure(int dev) {
@@ -1769,6 +1774,7 @@ RTC_API void rtcgbGetSceneBuildStats(RTCScene hs, RTCGBBuildStats* out) {
   if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
   memset(out, 0, sizeof(*out));
   out->sah = s->stats.sah;
+  out->sah_exact = s->stats.sah_exact;
   out->build_ms = s->stats.build_ms;
   out->num_nodes = s->stats.num_nodes;
   out->num_leaves = s->stats.num_leaves;

@@ -63,7 +63,8 @@ class RTCIntersectContext(ctypes.Structure):
 class RTCGBBuildStats(ctypes.Structure):
     _fields_ = [("sah", ctypes.c_double), ("build_ms", ctypes.c_double), ("num_nodes", ctypes.c_uint),
                 ("num_leaves", ctypes.c_uint), ("num_prims", ctypes.c_uint), ("depth", ctypes.c_uint),
-                ("ploc_iterations", ctypes.c_uint), ("refit", ctypes.c_uint), ("bvh_bytes", ctypes.c_ulonglong)]
+                ("ploc_iterations", ctypes.c_uint), ("refit", ctypes.c_uint), ("bvh_bytes", ctypes.c_ulonglong),
+                ("sah_exact", ctypes.c_double)]
 
 
 class RTCGBQueryStats(ctypes.Structure):

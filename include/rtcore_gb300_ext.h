@@ -13,15 +13,17 @@
 #include "rtcore_gb300.h"
 
 typedef struct RTCGBBuildStats {
-  double sah;               /* SAH cost with the reference's bvh_statistics semantics */
+  double sah;               /* SAH cost with the reference's bvh_statistics semantics, on the
+                               quantised child boxes traversal sees */
   double build_ms;          /* device time of the build (CUDA events) */
   unsigned int num_nodes;   /* 8-wide nodes */
-  unsigned int num_leaves;  /* leaf children (<= 3 triangles each) */
+  unsigned int num_leaves;  /* leaf children (<= 4 triangles each) */
   unsigned int num_prims;   /* valid triangles in the BVH */
   unsigned int depth;       /* wide levels */
   unsigned int ploc_iterations;
   unsigned int refit;       /* 1 when the last commit refitted the BVH instead of rebuilding */
   unsigned long long bvh_bytes; /* node + triangle record bytes in HBM */
+  double sah_exact;         /* the same SAH on the exact (unquantised) child boxes */
 } RTCGBBuildStats;
 
 typedef struct RTCGBQueryStats {

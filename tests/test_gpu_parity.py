@@ -293,7 +293,9 @@ def test_full_size_soup_sample(rtc, device, oracle):
 
 def test_radix_sort_bit_exact_vs_host_stable_sort(rtc):
     rng = np.random.default_rng(5)
-    for n in (1, 1000, 4097, 300_000):
+    # 300k and 2M keys: the digit histograms (256 per 4096-key tile) take the
+    # multi-CTA scan (3 and 16 scan tiles)
+    for n in (1, 1000, 4097, 300_000, 2_000_000):
         keys = rng.integers(0, 1 << 20, n, dtype=np.uint64) << np.uint64(rng.integers(0, 40))
         keys[rng.random(n) < 0.1] = np.uint64(0xFFFFFFFFFFFFFFFF)
         vals = np.arange(n, dtype=np.uint32)
