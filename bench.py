@@ -145,6 +145,24 @@ def peaks():
         return 6800.0, "fallback 6.8 TB/s"
 
 
+TRAFFIC_SUMMARY = os.path.join("profiles", "trace_closest_soup4M.md")
+
+
+def profiled_traffic():
+    """DRAM bytes (read + written) per launch of the closest-hit traversal on
+    the 4M-soup / 16M-ray workload, from the committed ncu summary of that
+    kernel and workload (its `traffic_bytes_per_launch = N` line); None
+    without it."""
+    try:
+        with open(os.path.join(REPO, TRAFFIC_SUMMARY)) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch"):
+                    return int(line.split("=")[1].strip().replace(",", ""))
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def max_over_ranks(x, dist=None, device="cpu"):
     """The maximum of a per-rank float over all ranks (the slowest rank sets
     the job's time); x itself without a process group."""
@@ -810,6 +828,9 @@ def run_gpu(args, rank, world):
                "host_buffer": "pinned", "host_access": int(api.load().rtcgbGetDeviceHostAccess(dev.h)),
                "path": "rtcIntersect1M on host memory (" + (args.config or "gpu.host_rays default") + ")"}
 
+    # DRAM traffic of the same kernel on the same workload (ncu), when this is that workload
+    traffic = profiled_traffic() if (args.workload == "soup" and args.scale == 1.0 and not args.robust
+                                     and not args.config) else None
     line = None
     if rank == 0:
         line = {
@@ -822,7 +843,9 @@ def run_gpu(args, rank, world):
                        "inputs smaller than L2"},
             "clocks": clk, "e2e": e2e, "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "traffic_source": TRAFFIC_SUMMARY + " (ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                           "same kernel and workload)" if traffic else None,
                          "kernel": "k_trace<closest> (gb_trace.cu)", "kernel_ms": kernel_ms,
                          "bytes_per_launch": alg_bytes, "compulsory_GBps": compulsory,
                          "nodes_per_ray": cnt["nodes"] / max(1, cnt["rays"]),

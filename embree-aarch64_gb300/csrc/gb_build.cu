@@ -398,7 +398,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __res
 // 4. PLOC
 // ---------------------------------------------------------------------------
 
-constexpr int PLOC_R = 16;
+// PLOC's search radius (clusters on each side in Morton order) is a template
+// parameter of the nearest-neighbour kernel; gpu.ploc_radius picks 1, 2, 4, 8
+// or 16.  Measured on a GB300, radius 1 gave the lowest SAH on heightfields,
+// the fastest traversal and the fastest build (a wider window made the
+// clusters' merges less local: the 4M soup went from 1033 to 889 Mrays/s
+// closest between radius 1 and 16).
+constexpr int PLOC_R_MAX = 16;
 constexpr int PLOC_BLOCK = 256;
 constexpr uint32_t PLOC_SMALL = 4096;   // finish on one CTA below this many clusters
 constexpr int PLOC_SMALL_THREADS = 1024;
@@ -426,6 +432,7 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
 // PLOC rounds run back to back without the host: the cluster count and the
 // next binary node index live in device memory (ploc_state[0], [1]); grids are
 // sized for an upper bound of the count, and CTAs past the count have no work.
+template <int PLOC_R>
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict__ clo, const float4* __restrict__ chi,
                                                         const uint32_t* __restrict__ ploc_state,
                                                         uint32_t* __restrict__ nn) {
@@ -564,7 +571,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
                                                                   float4* __restrict__ bnhi,
                                                                   uint32_t* __restrict__ bncnt, uint32_t* root_out,
                                                                   uint32_t* iters_out, uint32_t node_cap,
-                                                                  uint32_t* err, uint32_t nseg) {
+                                                                  uint32_t* err, uint32_t nseg, int radius) {
   extern __shared__ unsigned char smem[];
   float3* s_lo = reinterpret_cast<float3*>(smem);
   float3* s_hi = s_lo + PLOC_SMALL;
@@ -598,7 +605,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
       const float3 lo = s_lo[i], hi = s_hi[i];
       const uint32_t seg = s_seg[i];
       unsigned long long best = ~0ull;
-      for (int o = -PLOC_R; o <= PLOC_R; o++) {
+      for (int o = -radius; o <= radius; o++) {
         const int j = (int)i + o;
         if (o == 0 || j < 0 || j >= (int)n || s_seg[j] != seg) continue;
         const float a = half_area(f3min(lo, s_lo[j]), f3max(hi, s_hi[j]));
@@ -1296,11 +1303,20 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   h_tot[2] = 0;
   h_tot[3] = 0;
   GB_CHECK(cudaMemcpyAsync(ploc_state, h_tot, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  const int radius = opt.ploc_radius == 1 || opt.ploc_radius == 2 || opt.ploc_radius == 4 || opt.ploc_radius == 8
+                         ? opt.ploc_radius
+                         : PLOC_R_MAX;
   uint32_t n = N;
   while (n > PLOC_SMALL) {
     const uint32_t nb = cdiv(n, PLOC_BLOCK);
     for (int b = 0; b < kPlocBatch; b++) {
-      k_ploc_nn<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn);
+      switch (radius) {
+        case 1: k_ploc_nn<1><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
+        case 2: k_ploc_nn<2><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
+        case 4: k_ploc_nn<4><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
+        case 8: k_ploc_nn<8><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
+        default: k_ploc_nn<PLOC_R_MAX><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
+      }
       k_ploc_count<<<nb, PLOC_BLOCK, 0, st>>>(nn, ploc_state, bsurv, bmerge);
       note_launches(2);
       scan_excl(bsurv, nb, d_tot + 0, scan_sums, st);
@@ -1333,7 +1349,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     GB_CHECK(cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(clo_a, chi_a, cidx_a, n, node_next, bnlo, bnhi, bncnt, d_root,
-                                                      d_iters, nnodes_bin, &acc->pad, nseg); note_launches(1);
+                                                      d_iters, nnodes_bin, &acc->pad, nseg, radius); note_launches(1);
     GB_CHECK(cudaGetLastError());
   }
   uint32_t small_iters = 0, berr = 0;

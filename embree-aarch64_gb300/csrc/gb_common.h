@@ -117,6 +117,7 @@ struct BuildOptions {
   int robust = 0;       // RTC_SCENE_FLAG_ROBUST: triangle records hold v0, v1, v2
   int segmented = 0;    // one tree per geometry slot (batched scenes), roots at the first level
   int collapse = 1;     // binary -> 8-wide: 1 SAH-optimal (gpu.collapse=sah), 0 greedy (gpu.collapse=greedy)
+  int ploc_radius = 1;  // PLOC search radius: 1, 2, 4, 8 or 16 (gpu.ploc_radius)
 };
 
 // Build statistics reported through the extension API.
