@@ -989,23 +989,31 @@ __device__ __forceinline__ void write_tri(const GeomDesc* __restrict__ geoms, co
 // Writes wide node k of the level and the triangle records of its leaves;
 // adds the node's SAH terms and leaf count to sah_out / nleaf_out.
 __device__ __forceinline__ void collapse_emit_node(
-    const BinTree& t, const GeomDesc* __restrict__ geoms, const float4* __restrict__ plo,
-    const float4* __restrict__ phi, const uint32_t* __restrict__ kids_in, uint32_t k,
-    const uint32_t* __restrict__ off_int, const uint32_t* __restrict__ off_tri, uint32_t level_base,
-    uint32_t next_base, uint32_t tri_next, WideNode* __restrict__ nodes, TriRecord* __restrict__ tris,
-    uint32_t* __restrict__ next_items, uint32_t node_cap, uint32_t tri_cap, uint32_t* err, double& sah_out,
-    double& sahx_out, uint32_t& nleaf_out) {
+    const BinTree& t, const uint32_t* __restrict__ kids_in, uint32_t k, const uint32_t* __restrict__ off_int,
+    const uint32_t* __restrict__ off_tri, uint32_t level_base, uint32_t next_base, uint32_t tri_next,
+    WideNode* __restrict__ nodes, uint32_t* __restrict__ leaf_root, uint32_t* __restrict__ next_items,
+    uint32_t node_cap, uint32_t tri_cap, uint32_t* err, double& sah_out, double& sahx_out, uint32_t& nleaf_out) {
+  // all loops over the 8 children are unrolled, so the per-child values stay
+  // in registers (no local-memory arrays)
   uint32_t kids[8];
   int nk = 0;
+#pragma unroll
   for (int i = 0; i < 8; i++) {
     kids[i] = kids_in[8 * (size_t)k + i];
     if (kids[i] != 0xFFFFFFFFu) nk = i + 1;
   }
   // union box and quantisation frame
+  float3 klo[8], khi[8];
   float3 ulo = make_float3(INFINITY, INFINITY, INFINITY), uhi = make_float3(-INFINITY, -INFINITY, -INFINITY);
-  for (int i = 0; i < nk; i++) {
-    ulo = f3min(ulo, bt_lo(t, kids[i]));
-    uhi = f3max(uhi, bt_hi(t, kids[i]));
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    klo[i] = khi[i] = make_float3(0.f, 0.f, 0.f);
+    if (i < nk) {
+      klo[i] = bt_lo(t, kids[i]);
+      khi[i] = bt_hi(t, kids[i]);
+      ulo = f3min(ulo, klo[i]);
+      uhi = f3max(uhi, khi[i]);
+    }
   }
   const uint32_t Ex = exp_for(__fsub_ru(uhi.x, ulo.x));
   const uint32_t Ey = exp_for(__fsub_ru(uhi.y, ulo.y));
@@ -1017,32 +1025,34 @@ __device__ __forceinline__ void collapse_emit_node(
   // with sign bits s (bit set = negative axis), so that visiting slots in
   // ascending order of (slot ^ ray octant) is roughly near-to-far.
   const float3 pc = make_float3((ulo.x + uhi.x) * 0.5f, (ulo.y + uhi.y) * 0.5f, (ulo.z + uhi.z) * 0.5f);
-  float cost[8][8];
-  for (int i = 0; i < nk; i++) {
-    const float3 a = bt_lo(t, kids[i]), b = bt_hi(t, kids[i]);
-    const float3 d = make_float3((a.x + b.x) * 0.5f - pc.x, (a.y + b.y) * 0.5f - pc.y, (a.z + b.z) * 0.5f - pc.z);
-    for (int s = 0; s < 8; s++)
-      cost[i][s] = ((s & 1) ? -d.x : d.x) + ((s & 2) ? -d.y : d.y) + ((s & 4) ? -d.z : d.z);
+  float dx[8], dy[8], dz[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    dx[i] = (klo[i].x + khi[i].x) * 0.5f - pc.x;
+    dy[i] = (klo[i].y + khi[i].y) * 0.5f - pc.y;
+    dz[i] = (klo[i].z + khi[i].z) * 0.5f - pc.z;
   }
-  int slot_of[8];
+  // greedy: repeatedly the cheapest (child, free slot) pair, cost = the child's
+  // offset from the node centre along the slot's octant direction
   uint32_t used = 0, assigned = 0;
+  uint32_t kid_at = 0xFFFFFFFFu;  // 4 bits per slot: child index, 0xF = empty
   for (int it = 0; it < nk; it++) {
     float bc = INFINITY;
     int bi = -1, bs = -1;
-    for (int i = 0; i < nk; i++) {
-      if (assigned >> i & 1) continue;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      if (i >= nk || (assigned >> i & 1)) continue;
+#pragma unroll
       for (int s = 0; s < 8; s++) {
         if (used >> s & 1) continue;
-        if (bi < 0 || cost[i][s] < bc) { bc = cost[i][s]; bi = i; bs = s; }
+        const float c = ((s & 1) ? -dx[i] : dx[i]) + ((s & 2) ? -dy[i] : dy[i]) + ((s & 4) ? -dz[i] : dz[i]);
+        if (bi < 0 || c < bc) { bc = c; bi = i; bs = s; }
       }
     }
-    slot_of[bi] = bs;
     assigned |= 1u << bi;
     used |= 1u << bs;
+    kid_at = (kid_at & ~(0xFu << (4 * bs))) | ((uint32_t)bi << (4 * bs));
   }
-  int kid_at[8];
-  for (int s = 0; s < 8; s++) kid_at[s] = -1;
-  for (int i = 0; i < nk; i++) kid_at[slot_of[i]] = i;
 
   WideNode node;
   node.px = ulo.x;
@@ -1057,16 +1067,25 @@ __device__ __forceinline__ void collapse_emit_node(
   uint32_t int_rank = 0, tri_off = 0;
   double sah = 0.0, sahx = 0.0;  // on the decoded (quantised) and on the exact boxes
   uint32_t nleaf = 0;
+#pragma unroll
   for (int s = 0; s < 8; s++) {
-    const int i = kid_at[s];
-    if (i < 0) {
+    const uint32_t i = (kid_at >> (4 * s)) & 0xFu;
+    if (i == 0xFu) {
       node.meta[s] = 0;
       node.qlo_x[s] = node.qlo_y[s] = node.qlo_z[s] = 255;
       node.qhi_x[s] = node.qhi_y[s] = node.qhi_z[s] = 0;
       continue;
     }
-    const uint32_t c = kids[i];
-    const float3 a = bt_lo(t, c), b = bt_hi(t, c);
+    uint32_t c = 0;
+    float3 a = make_float3(0.f, 0.f, 0.f), b = a;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if ((uint32_t)j == i) {
+        c = kids[j];
+        a = klo[j];
+        b = khi[j];
+      }
+    }
     const float qlx = fminf(fmaxf(floorf(__fsub_rd(a.x, ulo.x) * ix), 0.f), 255.f);
     const float qly = fminf(fmaxf(floorf(__fsub_rd(a.y, ulo.y) * iy), 0.f), 255.f);
     const float qlz = fminf(fmaxf(floorf(__fsub_rd(a.z, ulo.z) * iz), 0.f), 255.f);
@@ -1094,29 +1113,14 @@ __device__ __forceinline__ void collapse_emit_node(
       sahx += Ax;
     } else {
       node.meta[s] = (uint8_t)(0x80u | ((cnt - 1u) << 5) | tri_off);
-      // collect the subtree's primitives (<= leaf_max) in depth-first order
-      uint32_t st[8];
-      int sp = 0;
-      st[sp++] = c;
-      uint32_t w = 0;
-      while (sp > 0) {
-        const uint32_t x = st[--sp];
-        if (bt_leaf(t, x)) {
-          if (node.tri_base + tri_off + w >= tri_cap || w >= cnt) {
-            atomicOr(err, kErrBuild);
-            return;
-          }
-          write_tri(geoms, plo, phi, bt_right(t, x), &tris[node.tri_base + tri_off + w], t.robust != 0);
-          w++;
-        } else {
-          if (sp + 2 > 8) {
-            atomicOr(err, kErrBuild);
-            return;
-          }
-          st[sp++] = bt_right(t, x);
-          st[sp++] = bt_left(t, x);
-        }
+      // the leaf's triangle records are written after the last level by
+      // k_write_leaves, one thread per leaf: here only its binary subtree is
+      // recorded at the slot of its first triangle
+      if (node.tri_base + tri_off + cnt > tri_cap) {
+        atomicOr(err, kErrBuild);
+        return;
       }
+      leaf_root[node.tri_base + tri_off] = c;
       tri_off += cnt;
       sah += A * (double)((cnt + 3) / 4);  // leaf term: area x Triangle4 blocks
       sahx += Ax * (double)((cnt + 3) / 4);
@@ -1138,20 +1142,54 @@ constexpr int COLLAPSE_THREADS = 128;
 // One wide node per thread; the SAH sums and the leaf count are reduced per
 // CTA first (one atomic per CTA instead of one per node).
 __global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
-    BinTree t, const GeomDesc* __restrict__ geoms, const float4* __restrict__ plo, const float4* __restrict__ phi,
-    const uint32_t* __restrict__ kids_in, uint32_t nitems, const uint32_t* __restrict__ off_int,
+    BinTree t, const uint32_t* __restrict__ kids_in, uint32_t nitems, const uint32_t* __restrict__ off_int,
     const uint32_t* __restrict__ off_tri, uint32_t level_base, uint32_t next_base, uint32_t tri_next,
-    WideNode* __restrict__ nodes, TriRecord* __restrict__ tris, uint32_t* __restrict__ next_items, double* sah_acc,
-    uint32_t* leaf_count, uint32_t node_cap, uint32_t tri_cap, uint32_t* err) {
+    WideNode* __restrict__ nodes, uint32_t* __restrict__ leaf_root, uint32_t* __restrict__ next_items,
+    double* sah_acc, uint32_t* leaf_count, uint32_t node_cap, uint32_t tri_cap, uint32_t* err) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   double sah = 0.0, sahx = 0.0;
   uint32_t nleaf = 0;
   if (k < nitems)
-    collapse_emit_node(t, geoms, plo, phi, kids_in, k, off_int, off_tri, level_base, next_base, tri_next, nodes, tris,
-                       next_items, node_cap, tri_cap, err, sah, sahx, nleaf);
+    collapse_emit_node(t, kids_in, k, off_int, off_tri, level_base, next_base, tri_next, nodes, leaf_root, next_items,
+                       node_cap, tri_cap, err, sah, sahx, nleaf);
   nleaf = __reduce_add_sync(0xFFFFFFFFu, nleaf);
   if ((threadIdx.x & 31) == 0 && nleaf) atomicAdd(leaf_count, nleaf);
   block_add2(sah, sahx, sah_acc);
+}
+
+// Writes the triangle records of every leaf: slot t holds the binary subtree of
+// the leaf whose first triangle goes to t (kInvalidID elsewhere); its
+// primitives (at most 4) are written in depth-first order, left first.
+__global__ void __launch_bounds__(256) k_write_leaves(BinTree t, const GeomDesc* __restrict__ geoms,
+                                                      const float4* __restrict__ plo, const float4* __restrict__ phi,
+                                                      const uint32_t* __restrict__ leaf_root, uint32_t ntris,
+                                                      TriRecord* __restrict__ tris, uint32_t* err) {
+  const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  if (first >= ntris) return;
+  const uint32_t c = leaf_root[first];
+  if (c == kInvalidID) return;
+  uint32_t st[8];
+  int sp = 0;
+  st[sp++] = c;
+  uint32_t w = 0;
+  while (sp > 0) {
+    const uint32_t x = st[--sp];
+    if (bt_leaf(t, x)) {
+      if (first + w >= ntris || w >= (uint32_t)kLeafMaxLimit) {
+        atomicOr(err, kErrBuild);
+        return;
+      }
+      write_tri(geoms, plo, phi, bt_right(t, x), &tris[first + w], t.robust != 0);
+      w++;
+    } else {
+      if (sp + 2 > 8) {
+        atomicOr(err, kErrBuild);
+        return;
+      }
+      st[sp++] = bt_right(t, x);
+      st[sp++] = bt_left(t, x);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1413,6 +1451,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(dalloc(&kids, (size_t)8 * maxw, st));
   GB_CHECK(dalloc(&nint, maxw, st));
   GB_CHECK(dalloc(&ntri, maxw, st));
+  uint32_t* leaf_root = nullptr;  // binary subtree of each leaf, at its first triangle's slot
+  GB_CHECK(dalloc(&leaf_root, N, st));
+  GB_CHECK(cudaMemsetAsync(leaf_root, 0xFF, sizeof(uint32_t) * N, st));
   double* d_sah = nullptr;
   uint32_t* d_leaves = nullptr;
   GB_CHECK(dalloc(&d_sah, 2, st));  // quantised, exact
@@ -1430,8 +1471,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     scan_excl(nint, nitems, d_tot + 0, scan_sums, st);
     scan_excl(ntri, nitems, d_tot + 1, scan_sums, st);
     const uint32_t next_base = level_base + nitems;
-    k_collapse_emit<<<nb, 128, 0, st>>>(bt, d_geoms, plo, phi, kids, nitems, nint, ntri, level_base, next_base,
-                                        tri_next, wnodes, wtris, items_b, d_sah, d_leaves, maxw, N, &acc->pad); note_launches(1);
+    k_collapse_emit<<<nb, COLLAPSE_THREADS, 0, st>>>(bt, kids, nitems, nint, ntri, level_base, next_base, tri_next,
+                                                     wnodes, leaf_root, items_b, d_sah, d_leaves, maxw, N, &acc->pad);
+    note_launches(1);
     GB_CHECK(cudaGetLastError());
     GB_CHECK(cudaMemcpyAsync(h_tot, d_tot, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GB_CHECK(cudaStreamSynchronize(st));
@@ -1443,6 +1485,10 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     std::swap(items_a, items_b);
   }
   const uint32_t num_nodes = level_base;
+  k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, d_geoms, plo, phi, leaf_root, N, wtris, &acc->pad);
+  note_launches(1);
+  GB_CHECK(cudaGetLastError());
+  cudaFreeAsync(leaf_root, st);
   GB_CHECK(cudaMemcpyAsync(&berr, &acc->pad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
   if (berr || tri_next != N) {
@@ -1577,10 +1623,12 @@ __device__ __forceinline__ bool refit_tri_vertices(const GeomDesc* __restrict__ 
   return vtx_ok(p0.x, p0.y, p0.z) && vtx_ok(p1.x, p1.y, p1.z) && vtx_ok(p2.x, p2.y, p2.z);
 }
 
+// Rewrites every triangle record from the current vertices and stores the
+// triangle's box (tri_box[2i] = lo, [2i + 1] = hi) for the node levels.
 __global__ void __launch_bounds__(256) k_refit_tris(const GeomDesc* __restrict__ geoms,
                                                     const uint32_t* __restrict__ slot_of, uint32_t nslots,
                                                     TriRecord* __restrict__ tris, uint32_t n, int robust,
-                                                    uint32_t* err) {
+                                                    float4* __restrict__ tri_box, uint32_t* err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   TriRecord rec = tris[i];
@@ -1595,13 +1643,16 @@ __global__ void __launch_bounds__(256) k_refit_tris(const GeomDesc* __restrict__
   rec.b = make_float4(e1.x, e1.y, e1.z, rec.b.w);
   rec.c = make_float4(e2.x, e2.y, e2.z, 0.f);
   tris[i] = rec;
+  const float3 lo = f3min(f3min(p0, p1), p2), hi = f3max(f3max(p0, p1), p2);
+  tri_box[2 * (size_t)i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+  tri_box[2 * (size_t)i + 1] = make_float4(hi.x, hi.y, hi.z, 0.f);
 }
 
 // Refits wide node k from its children's boxes (inner children: node_box of the
-// level below; leaf children: their triangles' current vertices); returns the
-// node's SAH terms on the decoded and on the exact boxes.
-__device__ __forceinline__ void refit_node(const GeomDesc* __restrict__ geoms, const uint32_t* __restrict__ slot_of,
-                                           uint32_t nslots, const TriRecord* __restrict__ tris, uint32_t num_tris,
+// level below; leaf children: the boxes k_refit_tris stored for their
+// triangles, independent loads); returns the node's SAH terms on the decoded
+// and on the exact boxes.
+__device__ __forceinline__ void refit_node(const float4* __restrict__ tri_box, uint32_t num_tris,
                                            WideNode* __restrict__ nodes, uint32_t num_nodes,
                                            float* __restrict__ node_box, uint32_t k, uint32_t* err, double& sah_out,
                                            double& sahx_out) {
@@ -1624,14 +1675,17 @@ __device__ __forceinline__ void refit_node(const GeomDesc* __restrict__ geoms, c
       chi[s] = make_float3(node_box[6 * (size_t)c + 3], node_box[6 * (size_t)c + 4], node_box[6 * (size_t)c + 5]);
     } else {
       const uint32_t cnt = ((m >> 5) & 3u) + 1u, first = node.tri_base + (m & 31u);
-      for (uint32_t t = first; t < first + cnt; t++) {
-        float3 p0, p1, p2;
-        if (t >= num_tris || !refit_tri_vertices(geoms, slot_of, nslots, tris[t], p0, p1, p2)) {
-          atomicOr(err, kErrBuild);
-          return;
+      if (first + cnt > num_tris) {
+        atomicOr(err, kErrBuild);
+        return;
+      }
+#pragma unroll
+      for (uint32_t q = 0; q < 4; q++) {
+        if (q < cnt) {
+          const float4 a = tri_box[2 * (size_t)(first + q)], b = tri_box[2 * (size_t)(first + q) + 1];
+          clo[s] = f3min(clo[s], make_float3(a.x, a.y, a.z));
+          chi[s] = f3max(chi[s], make_float3(b.x, b.y, b.z));
         }
-        clo[s] = f3min(clo[s], f3min(f3min(p0, p1), p2));
-        chi[s] = f3max(chi[s], f3max(f3max(p0, p1), p2));
       }
     }
     ulo = f3min(ulo, clo[s]);
@@ -1674,16 +1728,13 @@ __device__ __forceinline__ void refit_node(const GeomDesc* __restrict__ geoms, c
 }
 
 // One node of the level [begin, end) per thread; SAH sums reduced per CTA.
-__global__ void __launch_bounds__(128) k_refit_level(const GeomDesc* __restrict__ geoms,
-                                                     const uint32_t* __restrict__ slot_of, uint32_t nslots,
-                                                     const TriRecord* __restrict__ tris, uint32_t num_tris,
+__global__ void __launch_bounds__(128) k_refit_level(const float4* __restrict__ tri_box, uint32_t num_tris,
                                                      WideNode* __restrict__ nodes, uint32_t num_nodes,
                                                      float* __restrict__ node_box, uint32_t begin, uint32_t end,
                                                      double* sah_acc, uint32_t* err) {
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
   double sah = 0.0, sahx = 0.0;
-  if (k < end && k < num_nodes)
-    refit_node(geoms, slot_of, nslots, tris, num_tris, nodes, num_nodes, node_box, k, err, sah, sahx);
+  if (k < end && k < num_nodes) refit_node(tri_box, num_tris, nodes, num_nodes, node_box, k, err, sah, sahx);
   block_add2(sah, sahx, sah_acc);
 }
 
@@ -1705,8 +1756,10 @@ cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   GeomDesc* d_geoms = nullptr;
   uint32_t *d_slot = nullptr, *d_err = nullptr;
   float* node_box = nullptr;
+  float4* tri_box = nullptr;
   double* d_sah = nullptr;
   GB_CHECK(dalloc(&d_geoms, ngeoms, st));
+  GB_CHECK(dalloc(&tri_box, 2 * (size_t)bvh->num_tris, st));
   GB_CHECK(dalloc(&d_slot, slot_of.size(), st));
   GB_CHECK(dalloc(&d_err, 1, st));
   GB_CHECK(dalloc(&node_box, (size_t)6 * bvh->num_nodes, st));
@@ -1716,14 +1769,13 @@ cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   GB_CHECK(cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st));
   GB_CHECK(cudaMemsetAsync(d_sah, 0, 2 * sizeof(double), st));
   k_refit_tris<<<cdiv(bvh->num_tris, 256), 256, 0, st>>>(d_geoms, d_slot, (uint32_t)slot_of.size(), bvh->tris,
-                                                         bvh->num_tris, bvh->robust, d_err);
+                                                         bvh->num_tris, bvh->robust, tri_box, d_err);
   note_launches(1);
   for (size_t l = bvh->level_start.size() - 1; l-- > 0;) {
     const uint32_t b = bvh->level_start[l], e = bvh->level_start[l + 1];
     if (e <= b) continue;
-    k_refit_level<<<cdiv(e - b, 128), 128, 0, st>>>(d_geoms, d_slot, (uint32_t)slot_of.size(), bvh->tris,
-                                                   bvh->num_tris, bvh->nodes, bvh->num_nodes, node_box, b, e, d_sah,
-                                                   d_err);
+    k_refit_level<<<cdiv(e - b, 128), 128, 0, st>>>(tri_box, bvh->num_tris, bvh->nodes, bvh->num_nodes, node_box, b,
+                                                   e, d_sah, d_err);
     note_launches(1);
   }
   GB_CHECK(cudaGetLastError());
@@ -1738,6 +1790,7 @@ cudaError_t refit_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, Devi
   cudaFreeAsync(d_slot, st);
   cudaFreeAsync(d_err, st);
   cudaFreeAsync(node_box, st);
+  cudaFreeAsync(tri_box, st);
   cudaFreeAsync(d_sah, st);
   GB_CHECK(cudaStreamSynchronize(st));
   float ms = 0;
@@ -1777,6 +1830,7 @@ cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& 
   GB_CHECK(cudaMalloc(&out->d_slot, sizeof(uint32_t) * slot_of.size()));
   GB_CHECK(cudaMalloc(&out->d_err, sizeof(uint32_t)));
   GB_CHECK(cudaMalloc(&out->node_box, sizeof(float) * 6 * bvh.num_nodes));
+  GB_CHECK(cudaMalloc(&out->tri_box, sizeof(float4) * 2 * std::max<size_t>(bvh.num_tris, 1)));
   GB_CHECK(cudaMalloc(&out->d_sah, 2 * sizeof(double)));
   GB_CHECK(cudaMemcpyAsync(out->d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
   GB_CHECK(cudaMemcpyAsync(out->d_slot, slot_of.data(), sizeof(uint32_t) * slot_of.size(), cudaMemcpyHostToDevice, st));
@@ -1787,20 +1841,20 @@ cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& 
 cudaError_t refit_enqueue(const DeviceBVH& bvh, const RefitScratch& s, cudaStream_t st) {
   GB_CHECK(cudaMemsetAsync(s.d_sah, 0, 2 * sizeof(double), st));
   k_refit_tris<<<cdiv(bvh.num_tris, 256), 256, 0, st>>>(s.d_geoms, s.d_slot, s.nslots, bvh.tris, bvh.num_tris,
-                                                        bvh.robust, s.d_err);
+                                                        bvh.robust, s.tri_box, s.d_err);
   note_launches(1);
   for (size_t l = bvh.level_start.size() - 1; l-- > 0;) {
     const uint32_t b = bvh.level_start[l], e = bvh.level_start[l + 1];
     if (e <= b) continue;
-    k_refit_level<<<cdiv(e - b, 128), 128, 0, st>>>(s.d_geoms, s.d_slot, s.nslots, bvh.tris, bvh.num_tris, bvh.nodes,
-                                                   bvh.num_nodes, s.node_box, b, e, s.d_sah, s.d_err);
+    k_refit_level<<<cdiv(e - b, 128), 128, 0, st>>>(s.tri_box, bvh.num_tris, bvh.nodes, bvh.num_nodes, s.node_box, b,
+                                                   e, s.d_sah, s.d_err);
     note_launches(1);
   }
   return cudaGetLastError();
 }
 
 void refit_release(RefitScratch* s) {
-  void* ptrs[] = {s->d_geoms, s->d_slot, s->d_err, s->node_box, s->d_sah};
+  void* ptrs[] = {s->d_geoms, s->d_slot, s->d_err, s->node_box, s->tri_box, s->d_sah};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   *s = RefitScratch{};

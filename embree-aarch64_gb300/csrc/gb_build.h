@@ -28,6 +28,7 @@ struct RefitScratch {
   uint32_t nslots = 0;
   uint32_t* d_err = nullptr;
   float* node_box = nullptr;
+  float4* tri_box = nullptr;  // per-triangle boxes written by the triangle pass
   double* d_sah = nullptr;  // SAH sums on the decoded and on the exact boxes
 };
 cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& bvh, RefitScratch* out,
