@@ -520,7 +520,7 @@ def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds):
            "l2": "rays fit in L2: a 256 MB buffer is written before every timed launch",
            "build": {"device_ms": float(statistics.median(builds)), "first_commit_wall_ms": first_s * 1e3,
                      "Mtris_per_s": float(bst["num_prims"] / (statistics.median(builds) * 1e-3) / 1e6),
-                     "sah": bst["sah"], "sah_exact_boxes": bst["sah_exact"]},
+                     "sah": bst["sah"], "sah_exact_boxes": bst["sah_exact"], "leaf_max": bst["leaf_max"]},
            "closest": {"kernel_ms": kernel_ms, "Mrays_per_s": n / (kernel_ms * 1e-3) / 1e6,
                        "hit_rate": float(np.mean(out_rays["geomID"] != 0xFFFFFFFF))},
            "shadow": {"kernel_ms": sh_ms, "Mrays_per_s": active / (sh_ms * 1e-3) / 1e6, "active_rays": active},
@@ -857,7 +857,7 @@ def run_gpu(args, rank, world):
                        "occluded_rate": float(np.mean(sh_work.cpu().numpy().view(R.RAY_DTYPE)["tfar"] == -np.inf))},
             "build": {"device_ms": build_ms, "wall_ms": build_wall_ms, "first_commit_wall_ms": build_wall * 1e3,
                       "Mtris_per_s": bst["num_prims"] / (build_ms * 1e-3) / 1e6, "sah": bst["sah"],
-                      "sah_exact_boxes": bst["sah_exact"],
+                      "sah_exact_boxes": bst["sah_exact"], "leaf_max": bst["leaf_max"],
                       "nodes": bst["num_nodes"], "depth": bst["depth"], "ploc_iterations": bst["ploc_iterations"],
                       "bvh_MB": bst["bvh_bytes"] / 1e6},
             "learned": None, "animated": None, "batched": None, "heightfield": None,

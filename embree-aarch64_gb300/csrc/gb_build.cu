@@ -1415,7 +1415,23 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   cudaFreeAsync(nn, st); cudaFreeAsync(bsurv, st); cudaFreeAsync(bmerge, st); cudaFreeAsync(ploc_state, st);
 
   // ---- collapse, level by level (breadth-first node order)
-  BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(opt.leaf_max, 1), kLeafMaxLimit),
+  // leaf size: explicit, or by the shape of the centroid box -- flat scenes
+  // (smallest extent below half the largest: heightfields, terrain) take 2
+  // triangles per leaf, volumetric ones 1 (measured on a GB300: the 4M soup
+  // traces 5 % faster with 1, a 724^2 heightfield 8 % faster with 2, and its
+  // SAH is 1.12x the reference builder's with 2, 1.31x with 1)
+  int leaf_max = opt.leaf_max;
+  if (leaf_max <= 0) {
+    float emin = INFINITY, emax = 0.f;
+    for (int d = 0; d < 3; d++) {
+      const float e = ord2f(h_acc.chi[d]) - ord2f(h_acc.clo[d]);
+      emin = std::min(emin, e);
+      emax = std::max(emax, e);
+    }
+    leaf_max = emin < 0.5f * emax ? 2 : 1;
+  }
+  stats->leaf_max = (uint32_t)std::min(leaf_max, kLeafMaxLimit);
+  BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(leaf_max, 1), kLeafMaxLimit),
              (uint32_t)(opt.robust != 0), nullptr};
   uint2* d_choice = nullptr;
   if (opt.collapse == 1) {  // SAH-optimal collapse decisions

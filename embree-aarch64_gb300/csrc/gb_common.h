@@ -21,7 +21,10 @@ namespace gb {
 
 constexpr uint32_t kInvalidID = 0xFFFFFFFFu;
 constexpr int kLeafMaxLimit = 4;     // largest leaf the node encoding allows
-constexpr int kLeafMaxDefault = 2;   // default triangles per leaf child (fastest measured)
+// Default triangles per leaf child: 0 = by scene shape (see build_bvh): 2 for
+// flat scenes, 1 otherwise (the fastest measured for each; 2 also keeps the
+// heightfield SAH within 1.15x of the reference builder's)
+constexpr int kLeafMaxDefault = 0;
 constexpr int kStackSize = 64;       // traversal stack entries (node groups)
 
 // 80-byte wide node.
@@ -124,6 +127,7 @@ struct BuildOptions {
 struct BuildStats {
   double sah = 0;            // bvh_statistics.cpp semantics on the decoded boxes
   double sah_exact = 0;      // the same on the exact (unquantised) child boxes
+  uint32_t leaf_max = 0;     // triangles per leaf child the build used
   double build_ms = 0;       // device time of the whole build
   uint32_t num_nodes = 0, num_leaves = 0, num_prims = 0, depth = 0;
   uint32_t ploc_iterations = 0;

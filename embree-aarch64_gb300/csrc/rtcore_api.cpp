@@ -1776,6 +1776,7 @@ RTC_API void rtcgbGetSceneBuildStats(RTCScene hs, RTCGBBuildStats* out) {
   memset(out, 0, sizeof(*out));
   out->sah = s->stats.sah;
   out->sah_exact = s->stats.sah_exact;
+  out->leaf_max = s->stats.leaf_max;
   out->build_ms = s->stats.build_ms;
   out->num_nodes = s->stats.num_nodes;
   out->num_leaves = s->stats.num_leaves;

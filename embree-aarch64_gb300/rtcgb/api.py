@@ -64,7 +64,7 @@ class RTCGBBuildStats(ctypes.Structure):
     _fields_ = [("sah", ctypes.c_double), ("build_ms", ctypes.c_double), ("num_nodes", ctypes.c_uint),
                 ("num_leaves", ctypes.c_uint), ("num_prims", ctypes.c_uint), ("depth", ctypes.c_uint),
                 ("ploc_iterations", ctypes.c_uint), ("refit", ctypes.c_uint), ("bvh_bytes", ctypes.c_ulonglong),
-                ("sah_exact", ctypes.c_double)]
+                ("sah_exact", ctypes.c_double), ("leaf_max", ctypes.c_uint), ("reserved", ctypes.c_uint)]
 
 
 class RTCGBQueryStats(ctypes.Structure):

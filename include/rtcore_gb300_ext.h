@@ -24,6 +24,8 @@ typedef struct RTCGBBuildStats {
   unsigned int refit;       /* 1 when the last commit refitted the BVH instead of rebuilding */
   unsigned long long bvh_bytes; /* node + triangle record bytes in HBM */
   double sah_exact;         /* the same SAH on the exact (unquantised) child boxes */
+  unsigned int leaf_max;    /* triangles per leaf child the build used (gpu.leaf_max, or by scene shape) */
+  unsigned int reserved;
 } RTCGBBuildStats;
 
 typedef struct RTCGBQueryStats {

@@ -75,13 +75,13 @@ def test_structure_and_determinism(rtc, device):
         assert np.array_equal(nodes, nodes2) and np.array_equal(tris, tris2)
 
 
-@pytest.mark.parametrize("name,config,limit", [("heightfield", b"", 1.36), ("heightfield", b"gpu.leaf_max=4,gpu.morton=cube", 1.22),
-                                               ("soup", b"", 1.15)])
-def test_sah_against_reference_builder(rtc, oracle, name, config, limit):
-    """SAH of the GPU BVH vs the oracle's binned-SAH builder.  The soup carries
-    the <= 1.15x target at the default (throughput-oriented) settings; flat
-    heightfields reach 1.2x with 4-triangle leaves and cube-scaled Morton
-    codes, the setting that favours this SAH metric."""
+@pytest.mark.parametrize("name,config,limit,leaf", [("heightfield", b"", 1.15, 2), ("heightfield", b"gpu.leaf_max=4", 1.15, 4),
+                                                    ("soup", b"", 1.15, 1), ("soup", b"gpu.leaf_max=2", 1.15, 2)])
+def test_sah_against_reference_builder(rtc, oracle, name, config, limit, leaf):
+    """SAH of the GPU BVH vs the oracle's binned-SAH builder: within the 1.15x
+    target at the default settings (radius-1 PLOC, SAH-optimal collapse, leaf
+    size by scene shape: 2 for the flat heightfield, 1 for the soup) and with
+    other leaf sizes."""
     device = rtc.Device(config)
     if name == "heightfield":
         verts, idx = W.heightfield(256)
@@ -95,7 +95,37 @@ def test_sah_against_reference_builder(rtc, oracle, name, config, limit):
     ratio = gpu["sah"] / ref.sah
     print(name, "gpu SAH", gpu["sah"], "reference-builder SAH", ref.sah, "ratio", ratio)
     assert gpu["num_prims"] == ref.num_prims
+    assert gpu["leaf_max"] == leaf
     assert ratio <= limit
+    sc.release()
+    device.release()
+
+
+@pytest.mark.parametrize("config", [b"gpu.collapse=greedy", b"gpu.ploc_radius=2", b"gpu.ploc_radius=4",
+                                    b"gpu.ploc_radius=8", b"gpu.ploc_radius=16", b"gpu.morton=axis",
+                                    b"gpu.morton=cube", b"gpu.leaf_max=1", b"gpu.leaf_max=3", b"gpu.leaf_max=4"])
+def test_builder_options_valid_and_exact(rtc, oracle, config):
+    """Every build option (collapse rule, PLOC radius, Morton scaling, leaf
+    size) yields a well-formed BVH over every triangle, and closest hits equal
+    the oracle's on a heightfield + soup scene."""
+    from parity import assert_clean, compare_closest
+    device = rtc.Device(config)
+    hv, hi = W.heightfield(64, seed=5)
+    sv, si = W.gaussian_soup(30_000, seed=6)
+    verts = np.concatenate([hv, sv])
+    idx = np.concatenate([hi, si + hv.shape[0]]).astype(np.uint32)
+    sc = rtc.Scene(device)
+    sc.add_mesh(verts, idx)
+    sc.commit()
+    nodes, tris = sc.bvh()
+    check_structure(nodes, tris, verts, idx)
+    rays = W.sphere_rays(100_000, seed=7)
+    g = rays.copy()
+    sc.intersect(g)
+    r = rays.copy()
+    orc = oracle.OracleScene([(0, verts, idx)])
+    orc.intersect(r)
+    assert_clean(compare_closest(orc, rays, g, r))
     sc.release()
     device.release()
 
