@@ -548,28 +548,6 @@ def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds):
     return out
 
 
-def fp32_order_tie(mesh, ray, a, b, oracle_ffi):
-    """True when both reported triangles pass the reference's single-triangle
-    FP32 test for the ray and their distances are at most 2 ulps apart: the
-    ray crosses their shared edge, and the answer depends on which triangle is
-    tested first, because the test accepts T <= absDen * tfar before dividing
-    (triangle_intersector_moeller.h:62-104), so the first accepted hit's tfar
-    still admits a hit one ulp farther."""
-    v, idx = mesh
-    o = (float(ray["org_x"]), float(ray["org_y"]), float(ray["org_z"]))
-    d = (float(ray["dir_x"]), float(ray["dir_y"]), float(ray["dir_z"]))
-    ts = []
-    for h in (a, b):
-        if int(h["geomID"]) == 0xFFFFFFFF:
-            return False
-        t = idx[int(h["primID"])]
-        ok, _, tuv, _ = oracle_ffi.moeller1(v[t[0]], v[t[1]], v[t[2]], o, d, float(ray["tnear"]), float(ray["tfar"]))
-        if not ok:
-            return False
-        ts.append(np.float32(tuv[0]))
-    return abs(int(ts[0].view(np.int32)) - int(ts[1].view(np.int32))) <= 2
-
-
 def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
     """512 independent scenes (log-uniform 1k-200k triangles, ~20M in total;
     even scenes noise heightfields of matching grid size, odd scenes Gaussian
@@ -681,7 +659,7 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
             g = res[lo + j]
             code = orc.adjudicate(src[lo + j], (g["geomID"], g["primID"], g["tfar"]),
                                   (ref["geomID"][j], ref["primID"][j], ref["tfar"][j]))
-            if code != 1 and fp32_order_tie(meshes[k], src[lo + j], g, ref[j], oracle_ffi):
+            if code != 1 and orc.order_tie(src[lo + j], (g["geomID"], g["primID"]), (ref["geomID"][j], ref["primID"][j])):
                 code = 5
             verdicts[code] = verdicts.get(code, 0) + 1
         total += hi - lo

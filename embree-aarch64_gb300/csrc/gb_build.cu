@@ -1221,6 +1221,49 @@ static void scan_excl(uint32_t* a, uint32_t n, uint32_t* total, uint32_t* sums, 
   note_launches(3);
 }
 
+// Stream-ordered scratch of one build: device allocations, pinned host
+// buffers and events are released when the arena goes out of scope, on every
+// return path (free() releases a buffer early to lower the peak).
+struct BuildArena {
+  cudaStream_t st;
+  std::vector<void*> dev, pinned;
+  std::vector<cudaEvent_t> events;
+  explicit BuildArena(cudaStream_t s) : st(s) {}
+  BuildArena(const BuildArena&) = delete;
+  BuildArena& operator=(const BuildArena&) = delete;
+  template <typename T>
+  cudaError_t alloc(T** p, size_t count) {
+    const cudaError_t e = cudaMallocAsync((void**)p, std::max<size_t>(count, 1) * sizeof(T), st);
+    if (e == cudaSuccess) dev.push_back(*p);
+    return e;
+  }
+  template <typename T>
+  cudaError_t host(T** p, size_t count) {
+    const cudaError_t e = cudaMallocHost((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) pinned.push_back(*p);
+    return e;
+  }
+  cudaError_t event(cudaEvent_t* e) {
+    const cudaError_t r = cudaEventCreate(e);
+    if (r == cudaSuccess) events.push_back(*e);
+    return r;
+  }
+  void free(void* p) {
+    for (size_t i = 0; i < dev.size(); i++)
+      if (dev[i] == p) {
+        cudaFreeAsync(p, st);
+        dev.erase(dev.begin() + (long)i);
+        return;
+      }
+  }
+  ~BuildArena() {
+    for (void* p : dev) cudaFreeAsync(p, st);
+    if (!pinned.empty()) cudaStreamSynchronize(st);  // copies into them may still be in flight
+    for (void* p : pinned) cudaFreeHost(p);
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+  }
+};
+
 cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, const BuildOptions& opt, DeviceBVH* out,
                       BuildStats* stats) {
   *out = DeviceBVH();
@@ -1232,20 +1275,21 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   if (total64 >= 0x7FFFFFFFull) return cudaErrorInvalidValue;
   const uint32_t total = (uint32_t)total64;
 
-  cudaEvent_t ev0, ev1;
-  GB_CHECK(cudaEventCreate(&ev0));
-  GB_CHECK(cudaEventCreate(&ev1));
+  BuildArena arena(st);  // scratch and events of this build, released on every return
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  GB_CHECK(arena.event(&ev0));
+  GB_CHECK(arena.event(&ev1));
   GB_CHECK(cudaEventRecord(ev0, st));
 
   GeomDesc* d_geoms = nullptr;
-  GB_CHECK(dalloc(&d_geoms, ngeoms, st));
+  GB_CHECK(arena.alloc(&d_geoms, ngeoms));
   GB_CHECK(cudaMemcpyAsync(d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
 
   float4 *plo = nullptr, *phi = nullptr;
   BoundsAcc* acc = nullptr;
-  GB_CHECK(dalloc(&plo, total, st));
-  GB_CHECK(dalloc(&phi, total, st));
-  GB_CHECK(dalloc(&acc, 1, st));
+  GB_CHECK(arena.alloc(&plo, total));
+  GB_CHECK(arena.alloc(&phi, total));
+  GB_CHECK(arena.alloc(&acc, 1));
   BoundsAcc h_acc;
   for (int d = 0; d < 3; d++) { h_acc.glo[d] = h_acc.clo[d] = 0xFFFFFFFFu; h_acc.ghi[d] = h_acc.chi[d] = 0u; }
   h_acc.nvalid = 0;
@@ -1257,10 +1301,10 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
 
   uint64_t *keys_a = nullptr, *keys_b = nullptr;
   uint32_t *vals_a = nullptr, *vals_b = nullptr;
-  GB_CHECK(dalloc(&keys_a, total, st));
-  GB_CHECK(dalloc(&keys_b, total, st));
-  GB_CHECK(dalloc(&vals_a, total, st));
-  GB_CHECK(dalloc(&vals_b, total, st));
+  GB_CHECK(arena.alloc(&keys_a, total));
+  GB_CHECK(arena.alloc(&keys_b, total));
+  GB_CHECK(arena.alloc(&vals_a, total));
+  GB_CHECK(arena.alloc(&vals_b, total));
   const bool segmented = opt.segmented != 0;
   const uint32_t nseg = segmented ? (uint32_t)ngeoms : 1u;
   if (segmented && (uint32_t)ngeoms > kMaxSegments) return cudaErrorInvalidValue;
@@ -1273,9 +1317,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   for (int d = 0; d < 3; d++) { out->lo[d] = ord2f(h_acc.glo[d]); out->hi[d] = ord2f(h_acc.ghi[d]); }
   if (N == 0) {
     for (int d = 0; d < 3; d++) { out->lo[d] = INFINITY; out->hi[d] = -INFINITY; }
-    cudaFreeAsync(d_geoms, st); cudaFreeAsync(plo, st); cudaFreeAsync(phi, st); cudaFreeAsync(acc, st);
-    cudaFreeAsync(keys_a, st); cudaFreeAsync(keys_b, st); cudaFreeAsync(vals_a, st); cudaFreeAsync(vals_b, st);
-    cudaEventDestroy(ev0); cudaEventDestroy(ev1);
+    arena.free(d_geoms); arena.free(plo); arena.free(phi); arena.free(acc);
+    arena.free(keys_a); arena.free(keys_b); arena.free(vals_a); arena.free(vals_b);
     return cudaStreamSynchronize(st);
   }
 
@@ -1283,7 +1326,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   {
     const uint32_t nb = cdiv(total, RS_TILE);
     uint32_t* hist = nullptr;
-    GB_CHECK(dalloc(&hist, (size_t)sort_hist_entries(total), st));
+    GB_CHECK(arena.alloc(&hist, (size_t)sort_hist_entries(total)));
     for (int pass = 0; pass < 8; pass++) {
       const int shift = 8 * pass;
       const uint64_t a = (h_acc.kand >> shift) & 0xFF, o = (h_acc.kor >> shift) & 0xFF;
@@ -1295,47 +1338,47 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
       std::swap(vals_a, vals_b);
     }
     GB_CHECK(cudaGetLastError());
-    cudaFreeAsync(hist, st);
+    arena.free(hist);
   }
 
   // ---- PLOC over the N valid primitives (sorted positions 0..N-1)
   float4 *bnlo = nullptr, *bnhi = nullptr;
   uint32_t* bncnt = nullptr;
   const uint32_t nnodes_bin = 2 * N - 1;
-  GB_CHECK(dalloc(&bnlo, nnodes_bin, st));
-  GB_CHECK(dalloc(&bnhi, nnodes_bin, st));
-  GB_CHECK(dalloc(&bncnt, nnodes_bin, st));
+  GB_CHECK(arena.alloc(&bnlo, nnodes_bin));
+  GB_CHECK(arena.alloc(&bnhi, nnodes_bin));
+  GB_CHECK(arena.alloc(&bncnt, nnodes_bin));
   float4 *clo_a, *chi_a, *clo_b, *chi_b;
   uint32_t *cidx_a, *cidx_b, *nn;
-  GB_CHECK(dalloc(&clo_a, N, st));
-  GB_CHECK(dalloc(&chi_a, N, st));
-  GB_CHECK(dalloc(&clo_b, N, st));
-  GB_CHECK(dalloc(&chi_b, N, st));
-  GB_CHECK(dalloc(&cidx_a, N, st));
-  GB_CHECK(dalloc(&cidx_b, N, st));
-  GB_CHECK(dalloc(&nn, N, st));
+  GB_CHECK(arena.alloc(&clo_a, N));
+  GB_CHECK(arena.alloc(&chi_a, N));
+  GB_CHECK(arena.alloc(&clo_b, N));
+  GB_CHECK(arena.alloc(&chi_b, N));
+  GB_CHECK(arena.alloc(&cidx_a, N));
+  GB_CHECK(arena.alloc(&cidx_b, N));
+  GB_CHECK(arena.alloc(&nn, N));
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, bnlo, bnhi, bncnt, cidx_a, clo_a, chi_a,
                                             segmented ? 1 : 0);
   note_launches(1);
   uint32_t *bsurv, *bmerge, *d_tot, *d_root, *d_iters;
   const uint32_t maxb = cdiv(N, PLOC_BLOCK);
-  GB_CHECK(dalloc(&bsurv, maxb, st));
-  GB_CHECK(dalloc(&bmerge, maxb, st));
+  GB_CHECK(arena.alloc(&bsurv, maxb));
+  GB_CHECK(arena.alloc(&bmerge, maxb));
   uint32_t* scan_sums = nullptr;  // tile sums of the PLOC and collapse scans
-  GB_CHECK(dalloc(&scan_sums, scan_scratch(std::max(maxb, N)), st));
-  GB_CHECK(dalloc(&d_tot, 4, st));
-  GB_CHECK(dalloc(&d_root, nseg, st));
+  GB_CHECK(arena.alloc(&scan_sums, scan_scratch(std::max(maxb, N))));
+  GB_CHECK(arena.alloc(&d_tot, 4));
+  GB_CHECK(arena.alloc(&d_root, nseg));
   GB_CHECK(cudaMemsetAsync(d_root, 0xFF, sizeof(uint32_t) * nseg, st));
-  GB_CHECK(dalloc(&d_iters, 1, st));
+  GB_CHECK(arena.alloc(&d_iters, 1));
   GB_CHECK(cudaMemsetAsync(d_iters, 0, sizeof(uint32_t), st));
   // rounds in batches of kPlocBatch between host reads of the state; the
   // count only shrinks, so the count read last bounds the grids of a batch
   // (a batch may run a few rounds past PLOC_SMALL: they are ordinary rounds)
   constexpr int kPlocBatch = 4;
   uint32_t* ploc_state = nullptr;
-  GB_CHECK(dalloc(&ploc_state, 4, st));
+  GB_CHECK(arena.alloc(&ploc_state, 4));
   uint32_t* h_tot = nullptr;
-  GB_CHECK(cudaMallocHost((void**)&h_tot, 4 * sizeof(uint32_t)));
+  GB_CHECK(arena.host(&h_tot, 4));
   h_tot[0] = N;
   h_tot[1] = N;
   h_tot[2] = 0;
@@ -1375,7 +1418,6 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
       // globally closest pair is mutual); with segments it means every
       // segment is down to one cluster
       if (!segmented || n > PLOC_SMALL) {
-        cudaFreeHost(h_tot);
         return cudaErrorUnknown;
       }
       break;
@@ -1406,13 +1448,12 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     root_items.push_back(seg_root[s]);
   }
   if (berr || root_items.empty() || (!segmented && root_items.size() != 1)) {
-    cudaFreeHost(h_tot);
     return cudaErrorUnknown;
   }
   stats->ploc_iterations = iters + small_iters;
-  cudaFreeAsync(clo_b, st); cudaFreeAsync(chi_b, st); cudaFreeAsync(cidx_b, st);
-  cudaFreeAsync(clo_a, st); cudaFreeAsync(chi_a, st); cudaFreeAsync(cidx_a, st);
-  cudaFreeAsync(nn, st); cudaFreeAsync(bsurv, st); cudaFreeAsync(bmerge, st); cudaFreeAsync(ploc_state, st);
+  arena.free(clo_b); arena.free(chi_b); arena.free(cidx_b);
+  arena.free(clo_a); arena.free(chi_a); arena.free(cidx_a);
+  arena.free(nn); arena.free(bsurv); arena.free(bmerge); arena.free(ploc_state);
 
   // ---- collapse, level by level (breadth-first node order)
   // leaf size: explicit, or by the shape of the centroid box -- flat scenes
@@ -1438,10 +1479,10 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     const uint32_t nbin = 2 * N - (uint32_t)root_items.size();  // binary nodes of all trees
     uint32_t *parent = nullptr, *arrivals = nullptr;
     float4* cost = nullptr;
-    GB_CHECK(dalloc(&parent, nbin, st));
-    GB_CHECK(dalloc(&arrivals, nbin, st));
-    GB_CHECK(dalloc(&cost, 2 * (size_t)nbin, st));
-    GB_CHECK(dalloc(&d_choice, nbin, st));
+    GB_CHECK(arena.alloc(&parent, nbin));
+    GB_CHECK(arena.alloc(&arrivals, nbin));
+    GB_CHECK(arena.alloc(&cost, 2 * (size_t)nbin));
+    GB_CHECK(arena.alloc(&d_choice, nbin));
     GB_CHECK(cudaMemsetAsync(parent, 0xFF, sizeof(uint32_t) * nbin, st));
     GB_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * nbin, st));
     if (nbin > N) {
@@ -1451,29 +1492,29 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     k_collapse_dp<<<cdiv(N, 256), 256, 0, st>>>(bt, parent, nbin, arrivals, cost, d_choice);
     note_launches(1);
     GB_CHECK(cudaGetLastError());
-    cudaFreeAsync(parent, st);
-    cudaFreeAsync(arrivals, st);
-    cudaFreeAsync(cost, st);
+    arena.free(parent);
+    arena.free(arrivals);
+    arena.free(cost);
     bt.choice = d_choice;
   }
   WideNode* wnodes = nullptr;
   TriRecord* wtris = nullptr;
   const uint32_t maxw = N;  // wide internal nodes <= binary internal nodes + 1
-  GB_CHECK(dalloc(&wnodes, maxw, st));
-  GB_CHECK(dalloc(&wtris, N, st));
+  GB_CHECK(arena.alloc(&wnodes, maxw));
+  GB_CHECK(arena.alloc(&wtris, N));
   uint32_t *items_a, *items_b, *kids, *nint, *ntri;
-  GB_CHECK(dalloc(&items_a, maxw, st));
-  GB_CHECK(dalloc(&items_b, maxw, st));
-  GB_CHECK(dalloc(&kids, (size_t)8 * maxw, st));
-  GB_CHECK(dalloc(&nint, maxw, st));
-  GB_CHECK(dalloc(&ntri, maxw, st));
+  GB_CHECK(arena.alloc(&items_a, maxw));
+  GB_CHECK(arena.alloc(&items_b, maxw));
+  GB_CHECK(arena.alloc(&kids, (size_t)8 * maxw));
+  GB_CHECK(arena.alloc(&nint, maxw));
+  GB_CHECK(arena.alloc(&ntri, maxw));
   uint32_t* leaf_root = nullptr;  // binary subtree of each leaf, at its first triangle's slot
-  GB_CHECK(dalloc(&leaf_root, N, st));
+  GB_CHECK(arena.alloc(&leaf_root, N));
   GB_CHECK(cudaMemsetAsync(leaf_root, 0xFF, sizeof(uint32_t) * N, st));
   double* d_sah = nullptr;
   uint32_t* d_leaves = nullptr;
-  GB_CHECK(dalloc(&d_sah, 2, st));  // quantised, exact
-  GB_CHECK(dalloc(&d_leaves, 1, st));
+  GB_CHECK(arena.alloc(&d_sah, 2));  // quantised, exact
+  GB_CHECK(arena.alloc(&d_leaves, 1));
   GB_CHECK(cudaMemsetAsync(d_sah, 0, 2 * sizeof(double), st));
   GB_CHECK(cudaMemsetAsync(d_leaves, 0, sizeof(uint32_t), st));
   GB_CHECK(cudaMemcpyAsync(items_a, root_items.data(), sizeof(uint32_t) * root_items.size(), cudaMemcpyHostToDevice,
@@ -1497,18 +1538,17 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     level_base = next_base;
     tri_next += h_tot[1];
     nitems = h_tot[0];
-    if (level_base + nitems > maxw) { cudaFreeHost(h_tot); return cudaErrorUnknown; }
+    if (level_base + nitems > maxw) return cudaErrorUnknown;
     std::swap(items_a, items_b);
   }
   const uint32_t num_nodes = level_base;
   k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, d_geoms, plo, phi, leaf_root, N, wtris, &acc->pad);
   note_launches(1);
   GB_CHECK(cudaGetLastError());
-  cudaFreeAsync(leaf_root, st);
+  arena.free(leaf_root);
   GB_CHECK(cudaMemcpyAsync(&berr, &acc->pad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
   if (berr || tri_next != N) {
-    cudaFreeHost(h_tot);
     return cudaErrorUnknown;
   }
   double sah_sum[2] = {0.0, 0.0};
@@ -1528,21 +1568,18 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   level_start.push_back(num_nodes);
   out->level_start = level_start;
 
-  cudaFreeAsync(wnodes, st); cudaFreeAsync(wtris, st);
-  cudaFreeAsync(items_a, st); cudaFreeAsync(items_b, st); cudaFreeAsync(kids, st);
-  cudaFreeAsync(nint, st); cudaFreeAsync(ntri, st); cudaFreeAsync(d_sah, st); cudaFreeAsync(d_leaves, st);
-  if (d_choice) cudaFreeAsync(d_choice, st);
-  cudaFreeAsync(d_tot, st); cudaFreeAsync(d_root, st); cudaFreeAsync(d_iters, st); cudaFreeAsync(scan_sums, st);
-  cudaFreeAsync(bnlo, st); cudaFreeAsync(bnhi, st); cudaFreeAsync(bncnt, st);
-  cudaFreeAsync(plo, st); cudaFreeAsync(phi, st); cudaFreeAsync(acc, st); cudaFreeAsync(d_geoms, st);
-  cudaFreeAsync(keys_a, st); cudaFreeAsync(keys_b, st); cudaFreeAsync(vals_a, st); cudaFreeAsync(vals_b, st);
+  arena.free(wnodes); arena.free(wtris);
+  arena.free(items_a); arena.free(items_b); arena.free(kids);
+  arena.free(nint); arena.free(ntri); arena.free(d_sah); arena.free(d_leaves);
+  if (d_choice) arena.free(d_choice);
+  arena.free(d_tot); arena.free(d_root); arena.free(d_iters); arena.free(scan_sums);
+  arena.free(bnlo); arena.free(bnhi); arena.free(bncnt);
+  arena.free(plo); arena.free(phi); arena.free(acc); arena.free(d_geoms);
+  arena.free(keys_a); arena.free(keys_b); arena.free(vals_a); arena.free(vals_b);
   GB_CHECK(cudaEventRecord(ev1, st));
   GB_CHECK(cudaStreamSynchronize(st));
   float ms = 0;
   cudaEventElapsedTime(&ms, ev0, ev1);
-  cudaEventDestroy(ev0);
-  cudaEventDestroy(ev1);
-  cudaFreeHost(h_tot);
 
   // SAH relative to the root box (bvh_statistics.cpp: root node counts once)
   const float gx = out->hi[0] - out->lo[0], gy = out->hi[1] - out->lo[1], gz = out->hi[2] - out->lo[2];

@@ -1254,6 +1254,26 @@ int orc_fp64_hit(const OracleScene* s, const void* rayhit_in, unsigned geomID, u
   return hit64(s, &r, geomID, primID, t, u, v) == 1;
 }
 
+int orc_fp32_hit(const OracleScene* s, const void* rayhit_in, unsigned geomID, unsigned primID, float* t) {
+  ORay r;
+  load_ray((const char*)rayhit_in, &r);
+  const OMesh* m = find_mesh(s, geomID);
+  if (!m || primID >= m->nt) return 0;
+  const unsigned* tri = &m->idx[3 * (size_t)primID];
+  if (tri[0] >= m->nv || tri[1] >= m->nv || tri[2] >= m->nv) return 0;
+  const v3 p0 = mesh_vertex(m, tri[0]), p1 = mesh_vertex(m, tri[1]), p2 = mesh_vertex(m, tri[2]);
+  if (s->robust) {
+    PHit h;
+    if (!pluecker(p0, p1, p2, r.org, r.dir, r.tnear, r.tfar, &h)) return 0;
+    *t = h.t;
+    return 1;
+  }
+  MHit h;
+  if (!moeller(p0, v3sub(p0, p1), v3sub(p2, p0), r.org, r.dir, r.tnear, r.tfar, &h)) return 0;
+  *t = h.T * (1.0f / h.absDen);
+  return 1;
+}
+
 static inline int grazing(double u, double v) {
   const double e = 1e-6;
   return fabs(u) < e || fabs(v) < e || fabs(1.0 - u - v) < e;

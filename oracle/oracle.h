@@ -115,6 +115,14 @@ int orc_adjudicate(const OracleScene* s, const void* rayhit_in,
 int orc_fp64_hit(const OracleScene* s, const void* rayhit_in, unsigned geomID,
                  unsigned primID, double* t, double* u, double* v);
 
+/* The reference's single-triangle FP32 test (Moeller, or Pluecker in robust
+   scenes) of one primitive against the ray's own (tnear, tfar]: returns 1 and
+   writes t (the epilog's T * rcp(absDen)) when the test accepts the hit.
+   Two triangles that both pass with distances a few ulps apart form an
+   order tie: the test accepts T <= absDen * tfar before dividing, so which
+   one a traversal reports depends on the order it tests them in. */
+int orc_fp32_hit(const OracleScene* s, const void* rayhit_in, unsigned geomID, unsigned primID, float* t);
+
 /* Single-triangle Moeller test with the reference arithmetic; exposes the
    intermediate values for unit tests.  Returns 1 when valid. */
 int orc_moeller1(const float v0[3], const float v1[3], const float v2[3],

@@ -53,6 +53,8 @@ def lib():
         L.orc_fp64_hit.argtypes = [vp, vp, u, u, ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.orc_fp64_hit.restype = i
+        L.orc_fp32_hit.argtypes = [vp, vp, u, u, ctypes.POINTER(f)]
+        L.orc_fp32_hit.restype = i
         L.orc_moeller1.argtypes = [ctypes.POINTER(f)] * 5 + [f, f] + [ctypes.POINTER(f)] * 3
         L.orc_moeller1.restype = i
         L.orc_scene_set_robust.argtypes = [vp, i]
@@ -130,6 +132,27 @@ class OracleScene:
         rec = np.ascontiguousarray(np.asarray(ray_in).reshape(1))
         return lib().orc_adjudicate(self._h, _ptr(rec), int(hitA[0]), int(hitA[1]), float(hitA[2]),
                                     int(hitB[0]), int(hitB[1]), float(hitB[2]), int(tie_ulps))
+
+    def fp32_hit(self, ray_in, geomID, primID):
+        """(accepted, t) of the reference's single-triangle FP32 test."""
+        rec = np.ascontiguousarray(np.asarray(ray_in).reshape(1))
+        t = ctypes.c_float()
+        ok = lib().orc_fp32_hit(self._h, _ptr(rec), int(geomID), int(primID), ctypes.byref(t))
+        return bool(ok), t.value
+
+    def order_tie(self, ray_in, hitA, hitB, max_ulps=2):
+        """True when both reported triangles pass the reference's FP32 test for
+        the ray with distances at most max_ulps apart (the visiting order
+        decides which one a traversal reports)."""
+        if int(hitA[0]) == 0xFFFFFFFF or int(hitB[0]) == 0xFFFFFFFF:
+            return False
+        oa, ta = self.fp32_hit(ray_in, hitA[0], hitA[1])
+        ob, tb = self.fp32_hit(ray_in, hitB[0], hitB[1])
+        if not (oa and ob):
+            return False
+        ia = int(np.float32(ta).view(np.int32))
+        ib = int(np.float32(tb).view(np.int32))
+        return abs(ia - ib) <= max_ulps
 
     def fp64_hit(self, ray_in, geomID, primID):
         rec = np.ascontiguousarray(np.asarray(ray_in).reshape(1))

@@ -3,8 +3,11 @@
 Rules (the parity bar of this path):
   * geomID/primID identical, except rays the FP64 adjudicator classifies as a
     near tie (both triangles hit at the same distance within `tie_ulps` FP32
-    ulps), a grazing hit (within 1e-6 of an edge or an interval end), or a
-    case where the GPU's triangle is genuinely closer;
+    ulps), a grazing hit (within 1e-6 of an edge or an interval end), a case
+    where the GPU's triangle is genuinely closer, or an FP32 order tie (both
+    triangles pass the reference's FP32 test with distances <= 2 ulps apart:
+    the test accepts T <= absDen * tfar before dividing, so the visiting
+    order decides);
   * where both report the same triangle, t/u/v/Ng are bit-identical (the
     arithmetic is the same); the documented tolerance is 1e-6 relative;
   * rays that miss come back bit-identical to their input;
@@ -23,7 +26,7 @@ def compare_closest(orc_scene, rays_in, gpu, ref, tie_ulps=TIE_ULPS):
     """Returns a report dict; report['failures'] lists unexplained rays."""
     same_id = (gpu["geomID"] == ref["geomID"]) & (gpu["primID"] == ref["primID"])
     rep = dict(n=int(rays_in.shape[0]), hits=int((ref["geomID"] != INVALID).sum()),
-               id_mismatch=int((~same_id).sum()), near_tie=0, grazing=0, gpu_closer=0, failures=[])
+               id_mismatch=int((~same_id).sum()), near_tie=0, grazing=0, gpu_closer=0, order_tie=0, failures=[])
     for i in np.nonzero(~same_id)[0]:
         code = orc_scene.adjudicate(rays_in[i], (gpu["geomID"][i], gpu["primID"][i], gpu["tfar"][i]),
                                     (ref["geomID"][i], ref["primID"][i], ref["tfar"][i]), tie_ulps)
@@ -33,6 +36,8 @@ def compare_closest(orc_scene, rays_in, gpu, ref, tie_ulps=TIE_ULPS):
             rep["grazing"] += 1
         elif code == 3:
             rep["gpu_closer"] += 1
+        elif orc_scene.order_tie(rays_in[i], (gpu["geomID"][i], gpu["primID"][i]), (ref["geomID"][i], ref["primID"][i])):
+            rep["order_tie"] += 1
         else:
             rep["failures"].append((int(i), code))
     both = same_id & (ref["geomID"] != INVALID)

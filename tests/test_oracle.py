@@ -262,3 +262,28 @@ def test_robust_bvh_matches_brute_force(oracle):
     assert R.hits_equal_bits(a, b).mean() > 0.999
     ok, tuv, ng = oracle.pluecker1((0, 0, 0), (1, 0, 0), (0, 1, 0), (0.25, 0.25, -1), (0, 0, 1))
     assert ok and tuv == (1.0, 0.25, 0.25) and ng == (0.0, 0.0, 1.0)
+
+
+def test_fp32_hit_and_order_tie(oracle):
+    """orc_fp32_hit is the single-triangle test the traversal uses: for every
+    closest hit of the oracle's own traversal it accepts the reported triangle
+    with the reported t, bit for bit; order_tie holds for a triangle with
+    itself and fails against a triangle the ray misses."""
+    v, i = W.heightfield(24, seed=2)
+    orc = oracle.OracleScene([(0, v, i)])
+    rays = W.camera_rays(96, 96)
+    ref = rays.copy()
+    orc.intersect(ref)
+    hits = np.nonzero(ref["geomID"] == 0)[0]
+    assert hits.size > 1000
+    for k in hits[::7]:
+        ok, t = orc.fp32_hit(rays[k], 0, ref["primID"][k])
+        assert ok and np.float32(t).view(np.uint32) == ref["tfar"][k].view(np.uint32)
+    k = hits[0]
+    p = int(ref["primID"][k])
+    assert orc.order_tie(rays[k], (0, p), (0, p))
+    far = (p + i.shape[0] // 2) % i.shape[0]
+    assert not orc.fp32_hit(rays[k], 0, far)[0]
+    assert not orc.order_tie(rays[k], (0, p), (0, far))
+    assert not orc.order_tie(rays[k], (0, p), (0xFFFFFFFF, 0))
+    orc.close()
