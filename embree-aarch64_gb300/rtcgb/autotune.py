@@ -1,20 +1,22 @@
 """Autotuner for batched scenes: picks the build parameters (triangles per
-leaf, Morton scaling) that give the shortest build + trace time on a sample of
-the batch, by running each candidate through the library's C ABI on the GPU.
+leaf, Morton scaling of the sort key, PLOC search radius) that give the
+shortest build + trace time on a sample of the batch, by running each
+candidate through the library's C ABI on the GPU.
 
-Candidates are device configurations (rtcNewDevice keys gpu.leaf_max and
-gpu.morton); the traversal's launch shape is sized by the library from the
-kernel's occupancy and needs no tuning."""
+Candidates are device configurations (rtcNewDevice keys gpu.leaf_max,
+gpu.morton and gpu.ploc_radius); the traversal's launch shape is sized by the
+library from the kernel's occupancy and needs no tuning."""
 import numpy as np
 
 from . import api
 
 CANDIDATES = [
-    {"gpu.leaf_max": 1, "gpu.morton": "axis"},
-    {"gpu.leaf_max": 2, "gpu.morton": "axis"},
-    {"gpu.leaf_max": 3, "gpu.morton": "axis"},
-    {"gpu.leaf_max": 2, "gpu.morton": "cube"},
-    {"gpu.leaf_max": 4, "gpu.morton": "cube"},
+    {"gpu.leaf_max": 1, "gpu.morton": "axis", "gpu.ploc_radius": 1},
+    {"gpu.leaf_max": 2, "gpu.morton": "axis", "gpu.ploc_radius": 1},
+    {"gpu.leaf_max": 2, "gpu.morton": "cube", "gpu.ploc_radius": 1},
+    {"gpu.leaf_max": 4, "gpu.morton": "cube", "gpu.ploc_radius": 1},
+    {"gpu.leaf_max": 1, "gpu.morton": "axis", "gpu.ploc_radius": 4},
+    {"gpu.leaf_max": 2, "gpu.morton": "cube", "gpu.ploc_radius": 4},
 ]
 
 

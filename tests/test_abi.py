@@ -133,3 +133,11 @@ def test_packet_layouts(tmp_path):
     assert soa.view(np.float32)[0, 2 * 4 + 1] == rh["org_z"][1]
     back = R.from_soa(soa, 4, 5, R.RAYHIT_DTYPE)
     assert (back.view(np.uint8) == rh.view(np.uint8)).all()
+
+
+def test_autotune_config_strings():
+    """Autotuner candidates become rtcNewDevice configuration strings."""
+    from rtcgb import autotune
+    s = autotune.config_string({"gpu.leaf_max": 2, "gpu.morton": "cube", "gpu.ploc_radius": 4}, "gpu.device=0")
+    assert s == "gpu.device=0,gpu.leaf_max=2,gpu.morton=cube,gpu.ploc_radius=4"
+    assert all(set(c) == {"gpu.leaf_max", "gpu.morton", "gpu.ploc_radius"} for c in autotune.CANDIDATES)

@@ -114,3 +114,22 @@ def test_batched_refit(rtc, device, oracle):
         orc.intersect(ref)
         assert_clean(compare_closest(orc, rays[start[b]:start[b + 1]], gpu[start[b]:start[b + 1]], ref))
     sc.release()
+
+
+def test_autotuner_picks_the_fastest_candidate(rtc):
+    """The autotuner runs every candidate configuration through the C ABI on a
+    sample of batched scenes and returns the one with the least build + trace
+    time, with the timings of all."""
+    from rtcgb import autotune
+    meshes = [W.heightfield(40, seed=3), W.gaussian_soup(20_000, seed=4)]
+    parts, start = [], [0]
+    for k in range(2):
+        r = W.sphere_rays(20_000, seed=10 + k)
+        parts.append(r)
+        start.append(start[-1] + r.shape[0])
+    rays = np.concatenate(parts)
+    cands = autotune.CANDIDATES[:3]
+    best, results = autotune.tune(meshes, rays, np.array(start, np.uint32), candidates=cands)
+    assert [r["config"] for r in results] == cands
+    assert all(r["build_ms"] > 0 and r["trace_ms"] > 0 for r in results)
+    assert best == min(results, key=lambda r: r["total_ms"])["config"]

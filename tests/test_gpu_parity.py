@@ -371,3 +371,32 @@ def test_robust_mode_parity(rtc, device, oracle):
         assert_clean(compare_occluded(so, shadow, a, b, sg))
         sg.release()
     assert np.mean(g["geomID"] == 0xFFFFFFFF) <= 2e-5
+
+
+def test_update_buffers_then_commit_rebuilds(rtc, device, oracle):
+    """rtcUpdateGeometryBuffer on a default-quality geometry (vertices, then
+    indices) followed by rtcCommitScene rebuilds the BVH (no refit), and the
+    hits are the oracle's on the new buffers (the reference's UpdateTest)."""
+    verts, idx = W.gaussian_soup(40_000, seed=71)
+    rays = W.sphere_rays(100_000, seed=72)
+    sc = rtc.Scene(device)
+    gid = sc.add_mesh(verts, idx)
+    sc.commit()
+    rng = np.random.default_rng(73)
+    for step in range(2):
+        if step == 0:
+            sc.update_vertices(gid, verts + rng.normal(0, 0.01, verts.shape).astype(np.float32))
+        else:
+            sc.update_indices(gid, idx[rng.permutation(idx.shape[0])])
+        sc.commit()
+        assert sc.build_stats()["refit"] == 0
+        v_now, i_now = sc._by_id[gid]
+        g = rays.copy()
+        sc.intersect(g)
+        orc = oracle.OracleScene([(gid, v_now.copy(), i_now.copy())])
+        r = rays.copy()
+        orc.intersect(r)
+        assert (r["geomID"] != 0xFFFFFFFF).sum() > 1000
+        assert_clean(compare_closest(orc, rays, g, r))
+        orc.close()
+    sc.release()
