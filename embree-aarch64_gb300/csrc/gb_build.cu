@@ -1456,11 +1456,13 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   arena.free(nn); arena.free(bsurv); arena.free(bmerge); arena.free(ploc_state);
 
   // ---- collapse, level by level (breadth-first node order)
-  // leaf size: explicit, or by the shape of the centroid box -- flat scenes
-  // (smallest extent below half the largest: heightfields, terrain) take 2
-  // triangles per leaf, volumetric ones 1 (measured on a GB300: the 4M soup
-  // traces 5 % faster with 1, a 724^2 heightfield 8 % faster with 2, and its
-  // SAH is 1.12x the reference builder's with 2, 1.31x with 1)
+  // leaf size: explicit, or by the scene -- flat scenes (centroid box's
+  // smallest extent below half the largest: heightfields, terrain) and scenes
+  // that will be refitted every frame take 2 triangles per leaf, the rest 1
+  // (measured on a GB300: the 4M soup traces 5 % faster with 1; a 724^2
+  // heightfield 8 % faster with 2, and its SAH is 1.12x the reference
+  // builder's with 2, 1.31x with 1; the animated 4M soup, refitted per frame,
+  // renders 4 % faster with 2, whose tree has 40 % fewer nodes to refit)
   int leaf_max = opt.leaf_max;
   if (leaf_max <= 0) {
     float emin = INFINITY, emax = 0.f;
@@ -1469,7 +1471,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
       emin = std::min(emin, e);
       emax = std::max(emax, e);
     }
-    leaf_max = emin < 0.5f * emax ? 2 : 1;
+    leaf_max = (emin < 0.5f * emax || opt.refit_target) ? 2 : 1;
   }
   stats->leaf_max = (uint32_t)std::min(leaf_max, kLeafMaxLimit);
   BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(leaf_max, 1), kLeafMaxLimit),

@@ -21,9 +21,10 @@ namespace gb {
 
 constexpr uint32_t kInvalidID = 0xFFFFFFFFu;
 constexpr int kLeafMaxLimit = 4;     // largest leaf the node encoding allows
-// Default triangles per leaf child: 0 = by scene shape (see build_bvh): 2 for
-// flat scenes, 1 otherwise (the fastest measured for each; 2 also keeps the
-// heightfield SAH within 1.15x of the reference builder's)
+// Default triangles per leaf child: 0 = by scene (see build_bvh): 2 for flat
+// scenes and for scenes built to be refitted, 1 otherwise (the fastest measured
+// for each; 2 also keeps the heightfield SAH within 1.15x of the reference
+// builder's)
 constexpr int kLeafMaxDefault = 0;
 constexpr int kStackSize = 64;       // traversal stack entries (node groups)
 
@@ -121,6 +122,7 @@ struct BuildOptions {
   int segmented = 0;    // one tree per geometry slot (batched scenes), roots at the first level
   int collapse = 1;     // binary -> 8-wide: 1 SAH-optimal (gpu.collapse=sah), 0 greedy (gpu.collapse=greedy)
   int ploc_radius = 1;  // PLOC search radius: 1, 2, 4, 8 or 16 (gpu.ploc_radius)
+  int refit_target = 0; // every geometry is RTC_BUILD_QUALITY_REFIT: the tree will be refitted
 };
 
 // Build statistics reported through the extension API.

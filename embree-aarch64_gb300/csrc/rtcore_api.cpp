@@ -676,6 +676,7 @@ struct Scene : RefCounted {
     gb::BuildOptions opt = device->build_opt;
     opt.robust = robust;
     opt.segmented = batched ? 1 : 0;
+    opt.refit_target = all_refit ? 1 : 0;
     cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, opt, &bvh, &bs), "rtcCommitScene");
     if (d_roots) cudaFree(d_roots);
     d_roots = nullptr;

@@ -141,6 +141,7 @@ def test_refit_after_displacement(rtc, device, oracle):
     gid = sc.add_mesh(verts, idx, quality=rtc.RTC_BUILD_QUALITY_REFIT)
     sc.commit()
     assert sc.build_stats()["refit"] == 0
+    assert sc.build_stats()["leaf_max"] == 2  # a tree built to be refitted takes 2-triangle leaves
     nodes0, _ = sc.bvh()
     for frame in (1, 7):
         moved = W.displace_soup(verts, frame)
