@@ -313,34 +313,51 @@ __device__ __forceinline__ uint32_t scan_tile(uint32_t* __restrict__ a, uint32_t
   return tile_total;
 }
 
+// Element counts of the scans: n itself, or -- when the count is produced on
+// the device (builds that run without host reads) -- ceil(*d_n / div) capped
+// at n.  Grids are then sized for the cap and the tile loops are grid-stride.
+__device__ __forceinline__ uint32_t scan_count(uint32_t n, const uint32_t* d_n, uint32_t div) {
+  return d_n ? min(n, (*d_n + div - 1) / div) : n;
+}
+
 // One CTA of 1024 threads over the whole array; optionally writes the total.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_excl(uint32_t* __restrict__ a, uint32_t n, uint32_t* total) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_excl(uint32_t* __restrict__ a, uint32_t n,
+                                                            const uint32_t* __restrict__ d_n, uint32_t div,
+                                                            uint32_t* total) {
   __shared__ uint32_t s_w[32];
+  n = scan_count(n, d_n, div);
   uint32_t carry = 0;
   for (uint32_t base = 0; base < n; base += SCAN_TILE) carry += scan_tile(a, n, base, carry, s_w);
   if (total && threadIdx.x == 0) *total = carry;
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(const uint32_t* __restrict__ a, uint32_t n,
+                                                                 const uint32_t* __restrict__ d_n,
                                                                  uint32_t* __restrict__ sums) {
   __shared__ uint32_t s_w[32];
-  const uint32_t i0 = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
-  uint32_t sum = 0;
+  n = scan_count(n, d_n, 1);
+  for (uint32_t t = blockIdx.x; t * SCAN_TILE < n; t += gridDim.x) {
+    const uint32_t i0 = t * SCAN_TILE + threadIdx.x * SCAN_PER;
+    uint32_t sum = 0;
 #pragma unroll
-  for (int k = 0; k < SCAN_PER; k++) sum += (i0 + k < n) ? a[i0 + k] : 0u;
-  sum = __reduce_add_sync(0xFFFFFFFFu, sum);
-  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = sum;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, s_w[threadIdx.x]);
-    if (threadIdx.x == 0) sums[blockIdx.x] = w;
+    for (int k = 0; k < SCAN_PER; k++) sum += (i0 + k < n) ? a[i0 + k] : 0u;
+    sum = __reduce_add_sync(0xFFFFFFFFu, sum);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, s_w[threadIdx.x]);
+      if (threadIdx.x == 0) sums[t] = w;
+    }
+    __syncthreads();
   }
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(uint32_t* __restrict__ a, uint32_t n,
+                                                             const uint32_t* __restrict__ d_n,
                                                              const uint32_t* __restrict__ offs) {
   __shared__ uint32_t s_w[32];
-  scan_tile(a, n, blockIdx.x * SCAN_TILE, offs[blockIdx.x], s_w);
+  n = scan_count(n, d_n, 1);
+  for (uint32_t t = blockIdx.x; t * SCAN_TILE < n; t += gridDim.x) scan_tile(a, n, t * SCAN_TILE, offs[t], s_w);
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin,
@@ -414,11 +431,12 @@ constexpr int PLOC_SMALL_THREADS = 1024;
 // Cluster boxes carry their segment in clo.w (0 unless the build is segmented).
 __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                    const uint32_t* __restrict__ sorted, uint32_t n,
+                                                   const uint32_t* __restrict__ d_n,
                                                    float4* __restrict__ bnlo, float4* __restrict__ bnhi,
                                                    uint32_t* __restrict__ bncnt, uint32_t* __restrict__ cidx,
                                                    float4* __restrict__ clo, float4* __restrict__ chi, int segmented) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || i >= *d_n) return;  // n bounds the grid, *d_n is the count of valid primitives
   const uint32_t p = sorted[i];
   const float4 a = plo[p], b = phi[p];
   bnlo[i] = make_float4(a.x, a.y, a.z, __int_as_float(-1));
@@ -429,61 +447,91 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
   chi[i] = make_float4(b.x, b.y, b.z, 0.f);
 }
 
-// PLOC rounds run back to back without the host: the cluster count and the
-// next binary node index live in device memory (ploc_state[0], [1]); grids are
-// sized for an upper bound of the count, and CTAs past the count have no work.
+// PLOC rounds run back to back without the host.  ploc_state (device memory):
+// [0] cluster count n, [1] next binary node index, [2] rounds that merged,
+// [3] 256-cluster tiles of n, [4] done -- set once n <= PLOC_SMALL (the one-CTA
+// kernel finishes) or a round merged nothing; every kernel of a later round is
+// then a no-op, so a fixed number of rounds can be enqueued (or captured) and
+// the tree is the same whatever the number of extra rounds.  The kernels loop
+// over the tiles grid-stride, so the grid is any size.
+enum : int { kPlocN = 0, kPlocNext = 1, kPlocRounds = 2, kPlocTiles = 3, kPlocDone = 4, kPlocParity = 5,
+             kPlocStateWords = 8 };
+
+// The clusters alternate between two buffers, one round reading A and writing
+// B, the next the reverse; kPlocParity counts (mod 2) the rounds that ran, so
+// the current clusters are in B when it is 1 whatever no-op rounds followed.
+__global__ void k_ploc_state_init(const BoundsAcc* __restrict__ acc, uint32_t* __restrict__ ploc_state) {
+  if (threadIdx.x == 0) {
+    const uint32_t n = acc->nvalid;
+    ploc_state[kPlocN] = n;
+    ploc_state[kPlocNext] = n;  // binary leaves are the primitives 0..n-1
+    ploc_state[kPlocRounds] = 0;
+    ploc_state[kPlocTiles] = (n + PLOC_BLOCK - 1) / PLOC_BLOCK;
+    ploc_state[kPlocDone] = n <= PLOC_SMALL ? 1u : 0u;
+    ploc_state[kPlocParity] = 0;
+  }
+}
+
 template <int PLOC_R>
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict__ clo, const float4* __restrict__ chi,
                                                         const uint32_t* __restrict__ ploc_state,
                                                         uint32_t* __restrict__ nn) {
   __shared__ float3 s_lo[PLOC_BLOCK + 2 * PLOC_R], s_hi[PLOC_BLOCK + 2 * PLOC_R];
   __shared__ uint32_t s_seg[PLOC_BLOCK + 2 * PLOC_R];
-  const uint32_t n = ploc_state[0];
-  const int base = blockIdx.x * PLOC_BLOCK;
-  if ((uint32_t)base >= n) return;
-  for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
-    const int j = base - PLOC_R + k;
-    if (j >= 0 && j < (int)n) {
-      const float4 a = clo[j], b = chi[j];
-      s_lo[k] = make_float3(a.x, a.y, a.z);
-      s_hi[k] = make_float3(b.x, b.y, b.z);
-      s_seg[k] = __float_as_uint(a.w);
+  if (ploc_state[kPlocDone]) return;
+  const uint32_t n = ploc_state[kPlocN];
+  for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x) {
+    const int base = (int)(tile * PLOC_BLOCK);
+    for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
+      const int j = base - PLOC_R + k;
+      if (j >= 0 && j < (int)n) {
+        const float4 a = clo[j], b = chi[j];
+        s_lo[k] = make_float3(a.x, a.y, a.z);
+        s_hi[k] = make_float3(b.x, b.y, b.z);
+        s_seg[k] = __float_as_uint(a.w);
+      }
     }
-  }
-  __syncthreads();
-  const int i = base + threadIdx.x;
-  if (i >= (int)n) return;
-  const float3 lo = s_lo[threadIdx.x + PLOC_R], hi = s_hi[threadIdx.x + PLOC_R];
-  const uint32_t seg = s_seg[threadIdx.x + PLOC_R];
-  unsigned long long best = ~0ull;
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    if (i < (int)n) {
+      const float3 lo = s_lo[threadIdx.x + PLOC_R], hi = s_hi[threadIdx.x + PLOC_R];
+      const uint32_t seg = s_seg[threadIdx.x + PLOC_R];
+      unsigned long long best = ~0ull;
 #pragma unroll 4
-  for (int o = -PLOC_R; o <= PLOC_R; o++) {
-    const int j = i + o;
-    if (o == 0 || j < 0 || j >= (int)n || s_seg[threadIdx.x + PLOC_R + o] != seg) continue;
-    const float a = half_area(f3min(lo, s_lo[threadIdx.x + PLOC_R + o]), f3max(hi, s_hi[threadIdx.x + PLOC_R + o]));
-    const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
-    best = key < best ? key : best;
+      for (int o = -PLOC_R; o <= PLOC_R; o++) {
+        const int j = i + o;
+        if (o == 0 || j < 0 || j >= (int)n || s_seg[threadIdx.x + PLOC_R + o] != seg) continue;
+        const float a = half_area(f3min(lo, s_lo[threadIdx.x + PLOC_R + o]), f3max(hi, s_hi[threadIdx.x + PLOC_R + o]));
+        const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
+        best = key < best ? key : best;
+      }
+      nn[i] = best != ~0ull ? (uint32_t)best : (uint32_t)i;  // no neighbour in the segment: stays alone
+    }
+    __syncthreads();  // the window is reloaded for the next tile
   }
-  nn[i] = best != ~0ull ? (uint32_t)best : (uint32_t)i;  // no neighbour in the segment: stays alone
 }
 
+// Survivor and merge counts of every tile of the round.
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_count(const uint32_t* __restrict__ nn,
                                                            const uint32_t* __restrict__ ploc_state,
                                                            uint32_t* __restrict__ bsurv, uint32_t* __restrict__ bmerge) {
-  const uint32_t n = ploc_state[0];  // CTAs past it write zero counts
-  const uint32_t i = blockIdx.x * PLOC_BLOCK + threadIdx.x;
-  int surv = 0, merge = 0;
-  if (i < n) {
-    const uint32_t j = nn[i];
-    const bool mutual = (j != i) && nn[j] == i;
-    merge = mutual && i < j;
-    surv = !(mutual && j < i);
-  }
-  const int cs = __syncthreads_count(surv);
-  const int cm = __syncthreads_count(merge);
-  if (threadIdx.x == 0) {
-    bsurv[blockIdx.x] = cs;
-    bmerge[blockIdx.x] = cm;
+  if (ploc_state[kPlocDone]) return;
+  const uint32_t n = ploc_state[kPlocN];
+  for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x) {
+    const uint32_t i = tile * PLOC_BLOCK + threadIdx.x;
+    int surv = 0, merge = 0;
+    if (i < n) {
+      const uint32_t j = nn[i];
+      const bool mutual = (j != i) && nn[j] == i;
+      merge = mutual && i < j;
+      surv = !(mutual && j < i);
+    }
+    const int cs = __syncthreads_count(surv);
+    const int cm = __syncthreads_count(merge);
+    if (threadIdx.x == 0) {
+      bsurv[tile] = cs;
+      bmerge[tile] = cm;
+    }
   }
 }
 
@@ -510,64 +558,76 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const float4* __restri
                                                           float4* __restrict__ ohi, uint32_t* __restrict__ oidx,
                                                           uint32_t node_cap, uint32_t* err) {
   __shared__ uint32_t s_w[PLOC_BLOCK / 32];
-  const uint32_t n = ploc_state[0], node_next = ploc_state[1];
-  if (blockIdx.x * PLOC_BLOCK >= n) return;
-  const uint32_t i = blockIdx.x * PLOC_BLOCK + threadIdx.x;
-  int surv = 0, merge = 0;
-  uint32_t j = 0;
-  if (i < n) {
-    j = nn[i];
-    const bool mutual = (j != i) && nn[j] == i;
-    merge = mutual && i < j;
-    surv = !(mutual && j < i);
-  }
-  const uint32_t rs = block_excl_scan_flag(surv, s_w);
-  const uint32_t rm = block_excl_scan_flag(merge, s_w);
-  if (i >= n || !surv) return;
-  const uint32_t pos = bsurv_off[blockIdx.x] + rs;
-  const float4 a = clo[i], b = chi[i];
-  if (pos >= n) {
-    atomicOr(err, kErrBuild);
-    return;
-  }
-  if (merge) {
-    const float4 c = clo[j], d = chi[j];
-    const uint32_t id = node_next + bmerge_off[blockIdx.x] + rm;
-    if (id >= node_cap) {
-      atomicOr(err, kErrBuild);
-      return;
+  if (ploc_state[kPlocDone]) return;
+  const uint32_t n = ploc_state[kPlocN], node_next = ploc_state[kPlocNext];
+  for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x) {
+    const uint32_t i = tile * PLOC_BLOCK + threadIdx.x;
+    int surv = 0, merge = 0;
+    uint32_t j = 0;
+    if (i < n) {
+      j = nn[i];
+      const bool mutual = (j != i) && nn[j] == i;
+      merge = mutual && i < j;
+      surv = !(mutual && j < i);
     }
-    const uint32_t l = cidx[i], r = cidx[j];
-    const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), a.w);
-    const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
-    bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
-    bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-    bncnt[id] = bncnt[l] + bncnt[r];
-    olo[pos] = lo;
-    ohi[pos] = hi;
-    oidx[pos] = id;
-  } else {
-    olo[pos] = a;
-    ohi[pos] = b;
-    oidx[pos] = cidx[i];
+    const uint32_t rs = block_excl_scan_flag(surv, s_w);
+    const uint32_t rm = block_excl_scan_flag(merge, s_w);
+    if (i >= n || !surv) continue;
+    const uint32_t pos = bsurv_off[tile] + rs;
+    const float4 a = clo[i], b = chi[i];
+    if (pos >= n) {
+      atomicOr(err, kErrBuild);
+      continue;
+    }
+    if (merge) {
+      const float4 c = clo[j], d = chi[j];
+      const uint32_t id = node_next + bmerge_off[tile] + rm;
+      if (id >= node_cap) {
+        atomicOr(err, kErrBuild);
+        continue;
+      }
+      const uint32_t l = cidx[i], r = cidx[j];
+      const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), a.w);
+      const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
+      bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
+      bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
+      bncnt[id] = bncnt[l] + bncnt[r];
+      olo[pos] = lo;
+      ohi[pos] = hi;
+      oidx[pos] = id;
+    } else {
+      olo[pos] = a;
+      ohi[pos] = b;
+      oidx[pos] = cidx[i];
+    }
   }
 }
 
 // After a round: the survivors are the new clusters, the merges took the next
-// binary node indices; ploc_state[2] counts the rounds that merged anything.
+// binary node indices; rounds end once n <= PLOC_SMALL or nothing merged.
 __global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ ploc_state) {
-  if (threadIdx.x == 0) {
-    ploc_state[0] = tot[0];
-    ploc_state[1] += tot[1];
-    ploc_state[2] += tot[1] > 0 ? 1u : 0u;
+  if (threadIdx.x == 0 && !ploc_state[kPlocDone]) {
+    const uint32_t n = tot[0], merged = tot[1];
+    ploc_state[kPlocN] = n;
+    ploc_state[kPlocNext] += merged;
+    ploc_state[kPlocRounds] += merged > 0 ? 1u : 0u;
+    ploc_state[kPlocTiles] = (n + PLOC_BLOCK - 1) / PLOC_BLOCK;
+    ploc_state[kPlocParity] ^= 1u;
+    if (n <= PLOC_SMALL || merged == 0) ploc_state[kPlocDone] = 1u;
   }
 }
 
-// Finishes clustering of n <= PLOC_SMALL clusters inside one CTA.
-__global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4* __restrict__ clo,
-                                                                  const float4* __restrict__ chi,
-                                                                  const uint32_t* __restrict__ cidx, uint32_t n0,
-                                                                  uint32_t node_next0, float4* __restrict__ bnlo,
+// Finishes clustering of the n <= PLOC_SMALL clusters left by the rounds
+// inside one CTA (n and the next node index from ploc_state, where the final
+// node count is written back).
+__global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4* __restrict__ clo_a,
+                                                                  const float4* __restrict__ chi_a,
+                                                                  const uint32_t* __restrict__ cidx_a,
+                                                                  const float4* __restrict__ clo_b,
+                                                                  const float4* __restrict__ chi_b,
+                                                                  const uint32_t* __restrict__ cidx_b,
+                                                                  uint32_t* __restrict__ ploc_state,
+                                                                  float4* __restrict__ bnlo,
                                                                   float4* __restrict__ bnhi,
                                                                   uint32_t* __restrict__ bncnt, uint32_t* root_out,
                                                                   uint32_t* iters_out, uint32_t node_cap,
@@ -581,6 +641,15 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
   __shared__ uint32_t s_w[32];
   __shared__ uint32_t s_tot[2];
   constexpr int EPT = PLOC_SMALL / PLOC_SMALL_THREADS;  // elements per thread (contiguous)
+  const uint32_t n0 = ploc_state[kPlocN], node_next0 = ploc_state[kPlocNext];
+  const bool in_b = ploc_state[kPlocParity] != 0;
+  const float4* __restrict__ clo = in_b ? clo_b : clo_a;
+  const float4* __restrict__ chi = in_b ? chi_b : chi_a;
+  const uint32_t* __restrict__ cidx = in_b ? cidx_b : cidx_a;
+  if (n0 > PLOC_SMALL) {  // the rounds did not get below the threshold (too few enqueued)
+    if (threadIdx.x == 0) atomicOr(err, kErrBuild);
+    return;
+  }
   for (uint32_t k = threadIdx.x; k < n0; k += blockDim.x) {
     const float4 a = clo[k], b = chi[k];
     s_lo[k] = make_float3(a.x, a.y, a.z);
@@ -709,7 +778,10 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
     const uint32_t seg = nseg > 1 ? s_seg[k] : 0u;
     if (seg < nseg) root_out[seg] = s_idx[k];
   }
-  if (threadIdx.x == 0) *iters_out += iters;
+  if (threadIdx.x == 0) {
+    *iters_out += iters;
+    ploc_state[kPlocNext] = node_next;  // binary nodes in use: [0, node_next)
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1203,21 +1275,35 @@ static cudaError_t dalloc(T** p, size_t count, cudaStream_t st) {
 
 static inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
+static int num_sms_build() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n < 1) n = 1;
+  }
+  return n;
+}
+
 // Entries of tile-sum scratch that scan_excl needs for n elements.
 static inline uint32_t scan_scratch(uint32_t n) { return cdiv(n, SCAN_TILE) + 1; }
 
 // Exclusive scan of a[0, n) in place (total to *total when non-null); sums
-// holds scan_scratch(n) entries.
-static void scan_excl(uint32_t* a, uint32_t n, uint32_t* total, uint32_t* sums, cudaStream_t st) {
+// holds scan_scratch(n) entries.  With d_n the count is *d_n (at most n), read
+// on the device, so the scan can be enqueued before the count is known.
+static void scan_excl(uint32_t* a, uint32_t n, uint32_t* total, uint32_t* sums, cudaStream_t st,
+                      const uint32_t* d_n = nullptr) {
   if (n <= 2 * SCAN_TILE) {
-    k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(a, n, total);
+    k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(a, n, d_n, 1, total);
     note_launches(1);
     return;
   }
   const uint32_t nt = cdiv(n, SCAN_TILE);
-  k_scan_tile_sums<<<nt, SCAN_THREADS, 0, st>>>(a, n, sums);
-  k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(sums, nt, total);
-  k_scan_tiles<<<nt, SCAN_THREADS, 0, st>>>(a, n, sums);
+  const uint32_t grid = d_n ? std::min<uint32_t>(nt, 2 * (uint32_t)num_sms_build()) : nt;
+  k_scan_tile_sums<<<grid, SCAN_THREADS, 0, st>>>(a, n, d_n, sums);
+  k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(sums, nt, d_n, d_n ? SCAN_TILE : 1, total);
+  k_scan_tiles<<<grid, SCAN_THREADS, 0, st>>>(a, n, d_n, sums);
   note_launches(3);
 }
 
@@ -1357,8 +1443,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&cidx_a, N));
   GB_CHECK(arena.alloc(&cidx_b, N));
   GB_CHECK(arena.alloc(&nn, N));
-  k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, bnlo, bnhi, bncnt, cidx_a, clo_a, chi_a,
-                                            segmented ? 1 : 0);
+  k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, &acc->nvalid, bnlo, bnhi, bncnt, cidx_a, clo_a,
+                                            chi_a, segmented ? 1 : 0);
   note_launches(1);
   uint32_t *bsurv, *bmerge, *d_tot, *d_root, *d_iters;
   const uint32_t maxb = cdiv(N, PLOC_BLOCK);
@@ -1371,65 +1457,63 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(cudaMemsetAsync(d_root, 0xFF, sizeof(uint32_t) * nseg, st));
   GB_CHECK(arena.alloc(&d_iters, 1));
   GB_CHECK(cudaMemsetAsync(d_iters, 0, sizeof(uint32_t), st));
-  // rounds in batches of kPlocBatch between host reads of the state; the
-  // count only shrinks, so the count read last bounds the grids of a batch
-  // (a batch may run a few rounds past PLOC_SMALL: they are ordinary rounds)
+  // PLOC rounds in batches of kPlocBatch between host reads of the state; the
+  // count only shrinks, so the count read last bounds the grids of a batch,
+  // and rounds after the last real one are no-ops (the done flag)
   constexpr int kPlocBatch = 4;
   uint32_t* ploc_state = nullptr;
-  GB_CHECK(arena.alloc(&ploc_state, 4));
+  GB_CHECK(arena.alloc(&ploc_state, kPlocStateWords));
   uint32_t* h_tot = nullptr;
-  GB_CHECK(arena.host(&h_tot, 4));
-  h_tot[0] = N;
-  h_tot[1] = N;
-  h_tot[2] = 0;
-  h_tot[3] = 0;
-  GB_CHECK(cudaMemcpyAsync(ploc_state, h_tot, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  GB_CHECK(arena.host(&h_tot, kPlocStateWords));
+  k_ploc_state_init<<<1, 32, 0, st>>>(acc, ploc_state);
+  note_launches(1);
   const int radius = opt.ploc_radius == 1 || opt.ploc_radius == 2 || opt.ploc_radius == 4 || opt.ploc_radius == 8
                          ? opt.ploc_radius
                          : PLOC_R_MAX;
+  float4* cl[2] = {clo_a, clo_b};
+  float4* ch[2] = {chi_a, chi_b};
+  uint32_t* ci[2] = {cidx_a, cidx_b};
+  uint32_t round = 0;
+  auto enqueue_round = [&](uint32_t grid) {
+    const int a = round & 1, b = a ^ 1;
+    switch (radius) {
+      case 1: k_ploc_nn<1><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
+      case 2: k_ploc_nn<2><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
+      case 4: k_ploc_nn<4><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
+      case 8: k_ploc_nn<8><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
+      default: k_ploc_nn<PLOC_R_MAX><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
+    }
+    k_ploc_count<<<grid, PLOC_BLOCK, 0, st>>>(nn, ploc_state, bsurv, bmerge);
+    note_launches(2);
+    scan_excl(bsurv, maxb, d_tot + 0, scan_sums, st, ploc_state + kPlocTiles);
+    scan_excl(bmerge, maxb, d_tot + 1, scan_sums, st, ploc_state + kPlocTiles);
+    k_ploc_emit<<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ci[a], nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt,
+                                             cl[b], ch[b], ci[b], nnodes_bin, &acc->pad);
+    k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state);
+    note_launches(2);
+    round++;
+  };
   uint32_t n = N;
   while (n > PLOC_SMALL) {
     const uint32_t nb = cdiv(n, PLOC_BLOCK);
-    for (int b = 0; b < kPlocBatch; b++) {
-      switch (radius) {
-        case 1: k_ploc_nn<1><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
-        case 2: k_ploc_nn<2><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
-        case 4: k_ploc_nn<4><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
-        case 8: k_ploc_nn<8><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
-        default: k_ploc_nn<PLOC_R_MAX><<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, ploc_state, nn); break;
-      }
-      k_ploc_count<<<nb, PLOC_BLOCK, 0, st>>>(nn, ploc_state, bsurv, bmerge);
-      note_launches(2);
-      scan_excl(bsurv, nb, d_tot + 0, scan_sums, st);
-      scan_excl(bmerge, nb, d_tot + 1, scan_sums, st);
-      k_ploc_emit<<<nb, PLOC_BLOCK, 0, st>>>(clo_a, chi_a, cidx_a, nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt,
-                                             clo_b, chi_b, cidx_b, nnodes_bin, &acc->pad);
-      k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state);
-      note_launches(2);
-      std::swap(clo_a, clo_b);
-      std::swap(chi_a, chi_b);
-      std::swap(cidx_a, cidx_b);
-    }
+    for (int b = 0; b < kPlocBatch; b++) enqueue_round(nb);
     GB_CHECK(cudaGetLastError());
-    GB_CHECK(cudaMemcpyAsync(h_tot, ploc_state, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GB_CHECK(cudaMemcpyAsync(h_tot, ploc_state, kPlocStateWords * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GB_CHECK(cudaStreamSynchronize(st));
-    if (h_tot[0] == n) {
-      // no merge in a whole batch: without segments this cannot happen (the
-      // globally closest pair is mutual); with segments it means every
-      // segment is down to one cluster
-      if (!segmented || n > PLOC_SMALL) {
-        return cudaErrorUnknown;
-      }
-      break;
-    }
-    n = h_tot[0];
+    n = h_tot[kPlocN];
+    if (h_tot[kPlocDone]) break;
   }
-  const uint32_t node_next = h_tot[1], iters = h_tot[2];
+  // a round without merges while more than PLOC_SMALL clusters remain cannot
+  // happen without segments (the globally closest pair is mutual); with
+  // segments it means every segment is down to one cluster (<= kMaxSegments)
+  const uint32_t iters = round > 0 ? h_tot[kPlocRounds] : 0u;
   {
     const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     GB_CHECK(cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(clo_a, chi_a, cidx_a, n, node_next, bnlo, bnhi, bncnt, d_root,
-                                                      d_iters, nnodes_bin, &acc->pad, nseg, radius); note_launches(1);
+    k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(clo_a, chi_a, cidx_a, clo_b, chi_b, cidx_b, ploc_state, bnlo,
+                                                      bnhi, bncnt, d_root, d_iters, nnodes_bin, &acc->pad, nseg,
+                                                      radius);
+    note_launches(1);
     GB_CHECK(cudaGetLastError());
   }
   uint32_t small_iters = 0, berr = 0;
