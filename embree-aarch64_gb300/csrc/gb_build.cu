@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gb_build.h"
@@ -1002,26 +1003,122 @@ __device__ int gather_children(const BinTree& t, uint32_t b, uint32_t kids[8]) {
   return nk;
 }
 
-__global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const uint32_t* __restrict__ items, uint32_t nitems,
+// The collapse runs level by level from a state in device memory, so levels
+// can be enqueued (or captured) before their sizes are known: [kColN] items of
+// the current level, [kColBase] its first wide node, [kColTri] its first
+// triangle record, [kColDepth] levels done, [kColErr] overflow, and from
+// [kColLevels] the first node of every level (plus the end).  Kernels loop
+// grid-stride over the level's items; a level with no items is a no-op.
+enum : int { kColN = 0, kColBase = 1, kColTri = 2, kColDepth = 3, kColErr = 4, kColLevels = 8, kColMaxLevels = 64,
+             kColStateWords = kColLevels + kColMaxLevels + 1 };
+
+// Exclusive scan of one value per thread over a CTA of 1024 threads.
+__device__ __forceinline__ uint32_t cta_excl_scan_1024(uint32_t v, uint32_t* s_w, uint32_t& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = s_w[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
+    }
+    s_w[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t excl = (warp ? s_w[warp - 1] : 0u) + x - v;
+  total = s_w[31];
+  __syncthreads();
+  return excl;
+}
+
+// First level: the roots of the non-empty segments in segment order (one CTA
+// of 1024 threads, nseg <= 4 x 1024); seg_index[s] = position of segment s's
+// root (kInvalidID for an empty segment).
+__global__ void __launch_bounds__(1024) k_collapse_roots(const uint32_t* __restrict__ d_root, uint32_t nseg,
+                                                         uint32_t nbin, uint32_t* __restrict__ items,
+                                                         uint32_t* __restrict__ seg_index,
+                                                         uint32_t* __restrict__ cstate) {
+  __shared__ uint32_t s_w[32];
+  uint32_t r[4], cnt = 0;
+  const uint32_t s0 = threadIdx.x * 4;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    r[q] = s0 + q < nseg ? d_root[s0 + q] : kInvalidID;
+    if (r[q] != kInvalidID && r[q] >= nbin) r[q] = kInvalidID, cstate[kColErr] = 1u;
+    cnt += r[q] != kInvalidID;
+  }
+  uint32_t total = 0;
+  uint32_t pos = cta_excl_scan_1024(cnt, s_w, total);
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (s0 + q >= nseg) break;
+    if (r[q] != kInvalidID) items[pos] = r[q];
+    seg_index[s0 + q] = r[q] != kInvalidID ? pos++ : kInvalidID;
+  }
+  if (threadIdx.x == 0) {
+    cstate[kColN] = total;
+    cstate[kColBase] = 0;
+    cstate[kColTri] = 0;
+    cstate[kColDepth] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const uint32_t* __restrict__ items,
+                                                        const uint32_t* __restrict__ cstate,
                                                         uint32_t* __restrict__ kids_out, uint32_t* __restrict__ nint,
                                                         uint32_t* __restrict__ ntri) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nitems) return;
-  uint32_t kids[8];
-  const int nk = gather_children(t, items[k], kids);
-  uint32_t ni = 0, nt = 0;
-  for (int i = 0; i < 8; i++) {
-    if (i < nk) {
-      const uint32_t c = kids[i];
-      const uint32_t cnt = t.cnt[c];
-      if (cnt > t.leaf_max) ni++; else nt += cnt;
-      kids_out[8 * (size_t)k + i] = c;
-    } else {
-      kids_out[8 * (size_t)k + i] = 0xFFFFFFFFu;
+  const uint32_t nitems = cstate[kColN];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nitems; k += gridDim.x * blockDim.x) {
+    uint32_t kids[8];
+    const int nk = gather_children(t, items[k], kids);
+    uint32_t ni = 0, nt = 0;
+    for (int i = 0; i < 8; i++) {
+      if (i < nk) {
+        const uint32_t c = kids[i];
+        const uint32_t cnt = t.cnt[c];
+        if (cnt > t.leaf_max) ni++; else nt += cnt;
+        kids_out[8 * (size_t)k + i] = c;
+      } else {
+        kids_out[8 * (size_t)k + i] = 0xFFFFFFFFu;
+      }
     }
+    nint[k] = ni;
+    ntri[k] = nt;
   }
-  nint[k] = ni;
-  ntri[k] = nt;
+}
+
+// After a level: its wide nodes are written; the next level's items are its
+// internal children (tot[0]), their triangles follow (tot[1]).  Level starts
+// are kept for the first kColMaxLevels levels; max_levels bounds the depth of
+// builds that need them all on the device (the host-driven build records
+// them itself and has no bound: a chain-like binary tree, e.g. thousands of
+// identical triangles, collapses into thousands of levels).
+__global__ void k_collapse_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ cstate, uint32_t node_cap,
+                                   uint32_t max_levels) {
+  if (threadIdx.x != 0) return;
+  const uint32_t n = cstate[kColN];
+  if (n == 0) return;
+  const uint32_t d = cstate[kColDepth];
+  if (d < (uint32_t)kColMaxLevels) cstate[kColLevels + d] = cstate[kColBase];
+  const uint32_t base = cstate[kColBase] + n;
+  cstate[kColBase] = base;
+  cstate[kColTri] += tot[1];
+  cstate[kColDepth] = d + 1;
+  uint32_t next = tot[0];
+  if ((next > 0 && d + 1 >= max_levels) || base + next > node_cap) {
+    cstate[kColErr] = 1u;
+    next = 0;
+  }
+  cstate[kColN] = next;
+  if (next == 0 && d + 1 <= (uint32_t)kColMaxLevels) cstate[kColLevels + d + 1] = base;  // end of the last level
 }
 
 __device__ __forceinline__ uint32_t exp_for(float ext) {
@@ -1214,16 +1311,23 @@ constexpr int COLLAPSE_THREADS = 128;
 // One wide node per thread; the SAH sums and the leaf count are reduced per
 // CTA first (one atomic per CTA instead of one per node).
 __global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
-    BinTree t, const uint32_t* __restrict__ kids_in, uint32_t nitems, const uint32_t* __restrict__ off_int,
-    const uint32_t* __restrict__ off_tri, uint32_t level_base, uint32_t next_base, uint32_t tri_next,
-    WideNode* __restrict__ nodes, uint32_t* __restrict__ leaf_root, uint32_t* __restrict__ next_items,
-    double* sah_acc, uint32_t* leaf_count, uint32_t node_cap, uint32_t tri_cap, uint32_t* err) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    BinTree t, const uint32_t* __restrict__ kids_in, const uint32_t* __restrict__ cstate,
+    const uint32_t* __restrict__ off_int, const uint32_t* __restrict__ off_tri, WideNode* __restrict__ nodes,
+    uint32_t* __restrict__ leaf_root, uint32_t* __restrict__ next_items, double* sah_acc, uint32_t* leaf_count,
+    uint32_t node_cap, uint32_t tri_cap, uint32_t* err) {
+  const uint32_t nitems = cstate[kColN], level_base = cstate[kColBase], tri_next = cstate[kColTri];
+  const uint32_t next_base = level_base + nitems;
   double sah = 0.0, sahx = 0.0;
   uint32_t nleaf = 0;
-  if (k < nitems)
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nitems; k += gridDim.x * blockDim.x) {
+    double a = 0.0, b = 0.0;
+    uint32_t l = 0;
     collapse_emit_node(t, kids_in, k, off_int, off_tri, level_base, next_base, tri_next, nodes, leaf_root, next_items,
-                       node_cap, tri_cap, err, sah, sahx, nleaf);
+                       node_cap, tri_cap, err, a, b, l);
+    sah += a;
+    sahx += b;
+    nleaf += l;
+  }
   nleaf = __reduce_add_sync(0xFFFFFFFFu, nleaf);
   if ((threadIdx.x & 31) == 0 && nleaf) atomicAdd(leaf_count, nleaf);
   block_add2(sah, sahx, sah_acc);
@@ -1535,6 +1639,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     return cudaErrorUnknown;
   }
   stats->ploc_iterations = iters + small_iters;
+  stats->ploc_rounds = iters;
   arena.free(clo_b); arena.free(chi_b); arena.free(cidx_b);
   arena.free(clo_a); arena.free(chi_a); arena.free(cidx_a);
   arena.free(nn); arena.free(bsurv); arena.free(bmerge); arena.free(ploc_state);
@@ -1603,31 +1708,45 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&d_leaves, 1));
   GB_CHECK(cudaMemsetAsync(d_sah, 0, 2 * sizeof(double), st));
   GB_CHECK(cudaMemsetAsync(d_leaves, 0, sizeof(uint32_t), st));
-  GB_CHECK(cudaMemcpyAsync(items_a, root_items.data(), sizeof(uint32_t) * root_items.size(), cudaMemcpyHostToDevice,
-                           st));
-  uint32_t nitems = (uint32_t)root_items.size(), level_base = 0, tri_next = 0, depth = 0;
+  uint32_t *cstate = nullptr, *seg_index = nullptr, *h_col = nullptr;
+  GB_CHECK(arena.alloc(&cstate, kColStateWords));
+  GB_CHECK(arena.alloc(&seg_index, nseg));
+  GB_CHECK(arena.host(&h_col, kColStateWords));
+  GB_CHECK(cudaMemsetAsync(cstate, 0, sizeof(uint32_t) * kColStateWords, st));
+  k_collapse_roots<<<1, 1024, 0, st>>>(d_root, nseg, nnodes_bin, items_a, seg_index, cstate);
+  note_launches(1);
+  uint32_t* items[2] = {items_a, items_b};
+  uint32_t level = 0;
+  const uint32_t max_levels = 0xFFFFFFFFu;  // host-driven: level starts recorded here, no bound
+  auto enqueue_level = [&](uint32_t nitems_known) {  // the level's size, read by the host
+    const int a = level & 1, b = a ^ 1;
+    const uint32_t grid = cdiv(nitems_known, 128);
+    k_collapse_count<<<grid, 128, 0, st>>>(bt, items[a], cstate, kids, nint, ntri);
+    note_launches(1);
+    scan_excl(nint, nitems_known, d_tot + 0, scan_sums, st);
+    scan_excl(ntri, nitems_known, d_tot + 1, scan_sums, st);
+    k_collapse_emit<<<grid, COLLAPSE_THREADS, 0, st>>>(bt, kids, cstate, nint, ntri, wnodes, leaf_root, items[b],
+                                                       d_sah, d_leaves, maxw, N, &acc->pad);
+    k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels);
+    note_launches(2);
+    level++;
+  };
+  // one level per host read of the state: the grid fits the level
+  uint32_t nitems = (uint32_t)root_items.size();
   std::vector<uint32_t> level_start;
+  uint32_t level_base = 0;
   while (nitems > 0) {
     level_start.push_back(level_base);
-    const uint32_t nb = cdiv(nitems, 128);
-    k_collapse_count<<<nb, 128, 0, st>>>(bt, items_a, nitems, kids, nint, ntri); note_launches(1);
-    scan_excl(nint, nitems, d_tot + 0, scan_sums, st);
-    scan_excl(ntri, nitems, d_tot + 1, scan_sums, st);
-    const uint32_t next_base = level_base + nitems;
-    k_collapse_emit<<<nb, COLLAPSE_THREADS, 0, st>>>(bt, kids, nitems, nint, ntri, level_base, next_base, tri_next,
-                                                     wnodes, leaf_root, items_b, d_sah, d_leaves, maxw, N, &acc->pad);
-    note_launches(1);
+    enqueue_level(nitems);
     GB_CHECK(cudaGetLastError());
-    GB_CHECK(cudaMemcpyAsync(h_tot, d_tot, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GB_CHECK(cudaMemcpyAsync(h_col, cstate, sizeof(uint32_t) * kColLevels, cudaMemcpyDeviceToHost, st));
     GB_CHECK(cudaStreamSynchronize(st));
-    depth++;
-    level_base = next_base;
-    tri_next += h_tot[1];
-    nitems = h_tot[0];
-    if (level_base + nitems > maxw) return cudaErrorUnknown;
-    std::swap(items_a, items_b);
+    if (h_col[kColErr]) return cudaErrorUnknown;
+    nitems = h_col[kColN];
+    level_base = h_col[kColBase];
   }
-  const uint32_t num_nodes = level_base;
+  const uint32_t num_nodes = level_base, depth = (uint32_t)level_start.size();
+  const uint32_t tri_next = level < 1 ? 0u : h_col[kColTri];
   k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, d_geoms, plo, phi, leaf_root, N, wtris, &acc->pad);
   note_launches(1);
   GB_CHECK(cudaGetLastError());
@@ -1678,6 +1797,212 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   stats->num_prims = N;
   stats->depth = depth;
   return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// builds without host reads (captured into CUDA graphs)
+// ---------------------------------------------------------------------------
+
+__global__ void k_acc_init(BoundsAcc* __restrict__ acc) {
+  if (threadIdx.x == 0) {
+    for (int d = 0; d < 3; d++) {
+      acc->glo[d] = acc->clo[d] = 0xFFFFFFFFu;
+      acc->ghi[d] = acc->chi[d] = 0u;
+    }
+    acc->nvalid = 0;
+    acc->pad = 0;
+    acc->kand = ~0ull;
+    acc->kor = 0ull;
+  }
+}
+
+// Status of a replayed build: the plan's counts still hold, the rounds and
+// levels sufficed, and no kernel flagged an error.
+__global__ void k_graph_build_check(const BoundsAcc* __restrict__ acc, const uint32_t* __restrict__ ploc_state,
+                                    const uint32_t* __restrict__ cstate, uint32_t valid_tris,
+                                    uint32_t* __restrict__ status) {
+  if (threadIdx.x != 0) return;
+  uint32_t s = 0;
+  if (acc->nvalid != valid_tris) s |= kGraphBuildCount;
+  if (!ploc_state[kPlocDone] || ploc_state[kPlocN] > PLOC_SMALL) s |= kGraphBuildRounds;
+  if (cstate[kColN] != 0 || cstate[kColTri] != valid_tris) s |= kGraphBuildLevels;
+  if (acc->pad || cstate[kColErr]) s |= kGraphBuildError;
+  *status = s;
+}
+
+cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const BuildOptions& opt,
+                                const GraphBuildPlan& plan, GraphBuild* g) {
+  *g = GraphBuild{};
+  g->plan = plan;
+  g->opt = opt;
+  g->ngeoms = ngeoms;
+  uint64_t total64 = 0;
+  for (int k = 0; k < ngeoms; k++) total64 += h_geoms[k].ntris;
+  const uint32_t N = plan.valid_tris;
+  if (total64 == 0 || total64 >= 0x7FFFFFFFull || N == 0 || N > total64 || plan.roots == 0 || plan.roots > N ||
+      plan.levels == 0 || plan.levels > (uint32_t)kColMaxLevels)
+    return cudaErrorInvalidValue;
+  if (opt.segmented && (uint32_t)ngeoms > kMaxSegments) return cudaErrorInvalidValue;
+  g->total = (uint32_t)total64;
+  g->nseg = opt.segmented ? (uint32_t)ngeoms : 1u;
+  g->nbin = 2 * N - plan.roots;
+  g->maxw = N;
+  g->maxb = cdiv(N, PLOC_BLOCK);
+  g->rs_blocks = cdiv(g->total, RS_TILE);
+  g->radius = (opt.ploc_radius == 1 || opt.ploc_radius == 2 || opt.ploc_radius == 4 || opt.ploc_radius == 8)
+                  ? (uint32_t)opt.ploc_radius
+                  : (uint32_t)PLOC_R_MAX;
+  auto alloc = [&](auto** p, size_t count) -> cudaError_t {
+    using T = std::remove_pointer_t<std::remove_reference_t<decltype(*p)>>;
+    const cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) g->allocs.push_back((void*)*p);
+    return e;
+  };
+  const uint32_t T = g->total, maxw = g->maxw;
+  BoundsAcc* acc = nullptr;
+  cudaError_t e = cudaSuccess;
+  if ((e = alloc(&g->d_geoms, ngeoms)) || (e = alloc(&g->plo, T)) || (e = alloc(&g->phi, T)) ||
+      (e = alloc(&acc, 1)) || (e = alloc(&g->keys_a, T)) || (e = alloc(&g->keys_b, T)) ||
+      (e = alloc(&g->vals_a, T)) || (e = alloc(&g->vals_b, T)) || (e = alloc(&g->hist, sort_hist_entries(T))) ||
+      (e = alloc(&g->bnlo, 2 * (size_t)N)) || (e = alloc(&g->bnhi, 2 * (size_t)N)) ||
+      (e = alloc(&g->bncnt, 2 * (size_t)N)) || (e = alloc(&g->clo[0], N)) || (e = alloc(&g->clo[1], N)) ||
+      (e = alloc(&g->chi[0], N)) || (e = alloc(&g->chi[1], N)) || (e = alloc(&g->cidx[0], N)) ||
+      (e = alloc(&g->cidx[1], N)) || (e = alloc(&g->nn, N)) || (e = alloc(&g->bsurv, g->maxb)) ||
+      (e = alloc(&g->bmerge, g->maxb)) || (e = alloc(&g->scan_sums, scan_scratch(std::max(g->maxb, maxw)))) ||
+      (e = alloc(&g->d_tot, 4)) || (e = alloc(&g->d_root, g->nseg)) || (e = alloc(&g->d_iters, 1)) ||
+      (e = alloc(&g->ploc_state, kPlocStateWords)) || (e = alloc(&g->parent, g->nbin)) ||
+      (e = alloc(&g->arrivals, g->nbin)) || (e = alloc(&g->cost, 2 * (size_t)g->nbin)) ||
+      (e = alloc(&g->choice, g->nbin)) || (e = alloc(&g->nodes, maxw)) || (e = alloc(&g->tris, N)) ||
+      (e = alloc(&g->items[0], maxw)) || (e = alloc(&g->items[1], maxw)) || (e = alloc(&g->kids, 8 * (size_t)maxw)) ||
+      (e = alloc(&g->nint, maxw)) || (e = alloc(&g->ntri, maxw)) || (e = alloc(&g->leaf_root, N)) ||
+      (e = alloc(&g->d_sah, 2)) || (e = alloc(&g->d_leaves, 1)) || (e = alloc(&g->cstate, kColStateWords)) ||
+      (e = alloc(&g->seg_index, g->nseg)) || (e = alloc(&g->status, 1))) {
+    graph_build_release(g);
+    return e;
+  }
+  g->acc = acc;
+  e = cudaMemcpy(g->d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) graph_build_release(g);
+  const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return e;
+}
+
+cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
+  const uint32_t T = g.total, N = g.plan.valid_tris, maxw = g.maxw;
+  BoundsAcc* acc = reinterpret_cast<BoundsAcc*>(g.acc);
+  const int fixed_grid = 8 * num_sms_build();
+  k_acc_init<<<1, 32, 0, st>>>(acc);
+  k_primrefs<<<cdiv(T, 256), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc);
+  k_morton<<<cdiv(T, 256), 256, 0, st>>>(g.plo, g.phi, T, acc, g.keys_a, g.vals_a, g.opt.morton_cube,
+                                         g.opt.segmented ? 1 : 0);
+  note_launches(3);
+  // all 8 digits (the ordinary build skips constant ones: the same order)
+  uint64_t *ka = g.keys_a, *kb = g.keys_b;
+  uint32_t *va = g.vals_a, *vb = g.vals_b;
+  for (int pass = 0; pass < 8; pass++) {
+    const int shift = 8 * pass;
+    k_rs_hist<<<g.rs_blocks, RS_THREADS, 0, st>>>(ka, T, shift, g.hist, g.rs_blocks);
+    scan_excl(g.hist, 256 * g.rs_blocks, nullptr, g.hist + 256 * g.rs_blocks, st);
+    k_rs_scatter<<<g.rs_blocks, RS_THREADS, 0, st>>>(ka, va, kb, vb, T, shift, g.hist, g.rs_blocks);
+    note_launches(2);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  // PLOC: a fixed number of rounds, then the one-CTA finish
+  GB_CHECK(cudaMemsetAsync(g.d_root, 0xFF, sizeof(uint32_t) * g.nseg, st));
+  GB_CHECK(cudaMemsetAsync(g.d_iters, 0, sizeof(uint32_t), st));
+  k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(g.plo, g.phi, va, N, &acc->nvalid, g.bnlo, g.bnhi, g.bncnt, g.cidx[0],
+                                            g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0);
+  k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state);
+  note_launches(2);
+  const uint32_t pgrid = std::min<uint32_t>(g.maxb, (uint32_t)fixed_grid);
+  const uint32_t nbin_cap = 2 * N;
+  for (uint32_t r = 0; r < g.plan.ploc_rounds; r++) {
+    const int a = r & 1, b = a ^ 1;
+    switch (g.radius) {
+      case 1: k_ploc_nn<1><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
+      case 2: k_ploc_nn<2><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
+      case 4: k_ploc_nn<4><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
+      case 8: k_ploc_nn<8><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
+      default: k_ploc_nn<PLOC_R_MAX><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
+    }
+    k_ploc_count<<<pgrid, PLOC_BLOCK, 0, st>>>(g.nn, g.ploc_state, g.bsurv, g.bmerge);
+    scan_excl(g.bsurv, g.maxb, g.d_tot + 0, g.scan_sums, st, g.ploc_state + kPlocTiles);
+    scan_excl(g.bmerge, g.maxb, g.d_tot + 1, g.scan_sums, st, g.ploc_state + kPlocTiles);
+    k_ploc_emit<<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.cidx[a], g.nn, g.ploc_state, g.bsurv, g.bmerge,
+                                              g.bnlo, g.bnhi, g.bncnt, g.clo[b], g.chi[b], g.cidx[b], nbin_cap,
+                                              &acc->pad);
+    k_ploc_advance<<<1, 32, 0, st>>>(g.d_tot, g.ploc_state);
+    note_launches(4);
+  }
+  {
+    const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
+    k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(g.clo[0], g.chi[0], g.cidx[0], g.clo[1], g.chi[1], g.cidx[1],
+                                                      g.ploc_state, g.bnlo, g.bnhi, g.bncnt, g.d_root, g.d_iters,
+                                                      nbin_cap, &acc->pad, g.nseg, (int)g.radius);
+    note_launches(1);
+  }
+  // collapse decisions and levels
+  BinTree bt{g.bnlo, g.bnhi, g.bncnt, N, (uint32_t)std::min(std::max(g.plan.leaf_max, 1), kLeafMaxLimit),
+             (uint32_t)(g.opt.robust != 0), nullptr};
+  if (g.opt.collapse == 1) {
+    GB_CHECK(cudaMemsetAsync(g.parent, 0xFF, sizeof(uint32_t) * g.nbin, st));
+    GB_CHECK(cudaMemsetAsync(g.arrivals, 0, sizeof(uint32_t) * g.nbin, st));
+    if (g.nbin > N) {
+      k_bin_parents<<<cdiv(g.nbin - N, 256), 256, 0, st>>>(g.bnlo, g.bnhi, N, g.nbin, g.parent);
+      note_launches(1);
+    }
+    k_collapse_dp<<<cdiv(N, 256), 256, 0, st>>>(bt, g.parent, g.nbin, g.arrivals, g.cost, g.choice);
+    note_launches(1);
+    bt.choice = g.choice;
+  }
+  GB_CHECK(cudaMemsetAsync(g.leaf_root, 0xFF, sizeof(uint32_t) * N, st));
+  GB_CHECK(cudaMemsetAsync(g.d_sah, 0, 2 * sizeof(double), st));
+  GB_CHECK(cudaMemsetAsync(g.d_leaves, 0, sizeof(uint32_t), st));
+  GB_CHECK(cudaMemsetAsync(g.cstate, 0, sizeof(uint32_t) * kColStateWords, st));
+  k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate);
+  note_launches(1);
+  const uint32_t cgrid = std::min<uint32_t>(cdiv(maxw, 128), (uint32_t)fixed_grid);
+  for (uint32_t l = 0; l < g.plan.levels; l++) {
+    const int a = l & 1, b = a ^ 1;
+    k_collapse_count<<<cgrid, 128, 0, st>>>(bt, g.items[a], g.cstate, g.kids, g.nint, g.ntri);
+    scan_excl(g.nint, maxw, g.d_tot + 0, g.scan_sums, st, g.cstate + kColN);
+    scan_excl(g.ntri, maxw, g.d_tot + 1, g.scan_sums, st, g.cstate + kColN);
+    k_collapse_emit<<<cgrid, COLLAPSE_THREADS, 0, st>>>(bt, g.kids, g.cstate, g.nint, g.ntri, g.nodes, g.leaf_root,
+                                                        g.items[b], g.d_sah, g.d_leaves, maxw, N, &acc->pad);
+    k_collapse_advance<<<1, 32, 0, st>>>(g.d_tot, g.cstate, maxw, g.plan.levels);
+    note_launches(3);
+  }
+  k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, g.d_geoms, g.plo, g.phi, g.leaf_root, N, g.tris, &acc->pad);
+  k_graph_build_check<<<1, 32, 0, st>>>(acc, g.ploc_state, g.cstate, N, g.status);
+  note_launches(2);
+  return cudaGetLastError();
+}
+
+cudaError_t graph_build_result(const GraphBuild& g, const float scene_lo[3], const float scene_hi[3],
+                               GraphBuildResult* out, cudaStream_t st) {
+  *out = GraphBuildResult{};
+  std::vector<uint32_t> col(kColStateWords);
+  double sah[2] = {0.0, 0.0};
+  GB_CHECK(cudaMemcpyAsync(&out->status, g.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(col.data(), g.cstate, sizeof(uint32_t) * kColStateWords, cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(sah, g.d_sah, sizeof(sah), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(&out->num_leaves, g.d_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaStreamSynchronize(st));
+  out->num_nodes = col[kColBase];
+  out->depth = std::min<uint32_t>(col[kColDepth], (uint32_t)kColMaxLevels);
+  out->level_start.assign(col.begin() + kColLevels, col.begin() + kColLevels + out->depth + 1);
+  const float gx = scene_hi[0] - scene_lo[0], gy = scene_hi[1] - scene_lo[1], gz = scene_hi[2] - scene_lo[2];
+  const double Aroot = std::max(0.0, (double)(gx * (gy + gz) + gy * gz));
+  out->sah = Aroot > 0 ? (Aroot + sah[0]) / Aroot : 0.0;
+  out->sah_exact = Aroot > 0 ? (Aroot + sah[1]) / Aroot : 0.0;
+  return cudaSuccess;
+}
+
+void graph_build_release(GraphBuild* g) {
+  for (void* p : g->allocs) cudaFree(p);
+  *g = GraphBuild{};
 }
 
 // Sorts (key, value) pairs with the builder's radix sort (all 8 digits,

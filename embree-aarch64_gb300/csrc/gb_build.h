@@ -1,5 +1,7 @@
 // gb_build.h -- host entry points of the GPU BVH builder (gb_build.cu).
 #pragma once
+#include <vector>
+
 #include "gb_common.h"
 
 namespace gb {
@@ -35,6 +37,59 @@ cudaError_t refit_prepare(const GeomDesc* h_geoms, int ngeoms, const DeviceBVH& 
                           cudaStream_t st);
 cudaError_t refit_enqueue(const DeviceBVH& bvh, const RefitScratch& s, cudaStream_t st);
 void refit_release(RefitScratch* s);
+
+// A build that runs without host reads, so that it can be captured into a
+// CUDA graph and replayed: every buffer is allocated up front, and the loops
+// whose trip counts depend on the data (PLOC rounds, collapse levels) are
+// enqueued a fixed number of times -- rounds and levels past the last real one
+// are no-ops.  The plan comes from an ordinary build of the same geometries:
+// the number of valid triangles, of non-empty segments, of PLOC rounds and of
+// levels (the replay checks that they still suffice and flags it otherwise).
+// The BVH stays in the build's own node and triangle arrays (sized for the
+// maximum), with the roots of the segments in seg_index.
+struct GraphBuildPlan {
+  uint32_t valid_tris = 0;   // valid triangles of the ordinary build
+  uint32_t roots = 0;        // non-empty segments (1 without segments)
+  uint32_t ploc_rounds = 0;  // rounds enqueued
+  uint32_t levels = 0;       // collapse levels enqueued (at most 64)
+  int leaf_max = 2;          // resolved leaf size
+};
+struct GraphBuild {
+  GraphBuildPlan plan;
+  BuildOptions opt;
+  int ngeoms = 0;
+  uint32_t total = 0, nseg = 1, nbin = 0, maxw = 0, maxb = 0, rs_blocks = 0, radius = 1;
+  std::vector<void*> allocs;  // every device allocation (released by graph_build_release)
+  GeomDesc* d_geoms = nullptr;
+  float4 *plo = nullptr, *phi = nullptr;
+  void* acc = nullptr;
+  uint64_t *keys_a = nullptr, *keys_b = nullptr;
+  uint32_t *vals_a = nullptr, *vals_b = nullptr, *hist = nullptr;
+  float4 *bnlo = nullptr, *bnhi = nullptr, *clo[2] = {nullptr, nullptr}, *chi[2] = {nullptr, nullptr};
+  uint32_t *bncnt = nullptr, *cidx[2] = {nullptr, nullptr}, *nn = nullptr, *bsurv = nullptr, *bmerge = nullptr;
+  uint32_t *scan_sums = nullptr, *d_tot = nullptr, *d_root = nullptr, *d_iters = nullptr, *ploc_state = nullptr;
+  uint32_t *parent = nullptr, *arrivals = nullptr;
+  float4* cost = nullptr;
+  uint2* choice = nullptr;
+  WideNode* nodes = nullptr;
+  TriRecord* tris = nullptr;
+  uint32_t *items[2] = {nullptr, nullptr}, *kids = nullptr, *nint = nullptr, *ntri = nullptr, *leaf_root = nullptr;
+  double* d_sah = nullptr;
+  uint32_t *d_leaves = nullptr, *cstate = nullptr, *seg_index = nullptr, *status = nullptr;
+};
+struct GraphBuildResult {
+  uint32_t status = 0;  // 0: the build is complete and consistent; else kGraphBuild* bits
+  uint32_t num_nodes = 0, depth = 0, num_leaves = 0;
+  double sah = 0, sah_exact = 0;
+  std::vector<uint32_t> level_start;
+};
+enum : uint32_t { kGraphBuildCount = 1, kGraphBuildRounds = 2, kGraphBuildLevels = 4, kGraphBuildError = 8 };
+cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const BuildOptions& opt,
+                                const GraphBuildPlan& plan, GraphBuild* gbuild);
+cudaError_t graph_build_enqueue(const GraphBuild& gbuild, cudaStream_t st);  // capturable
+cudaError_t graph_build_result(const GraphBuild& gbuild, const float scene_lo[3], const float scene_hi[3],
+                               GraphBuildResult* out, cudaStream_t st);  // synchronises st
+void graph_build_release(GraphBuild* gbuild);
 
 // Stable LSD radix sort of 64-bit keys with 32-bit values (device buffers).
 cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st);

@@ -133,6 +133,7 @@ struct BuildStats {
   double build_ms = 0;       // device time of the whole build
   uint32_t num_nodes = 0, num_leaves = 0, num_prims = 0, depth = 0;
   uint32_t ploc_iterations = 0;
+  uint32_t ploc_rounds = 0;  // PLOC rounds over all clusters (before the one-CTA finish) that merged
   uint32_t refit = 0;        // 1 when the last commit refitted instead of rebuilding
 };
 

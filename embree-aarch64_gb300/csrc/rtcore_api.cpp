@@ -2294,6 +2294,178 @@ RTC_API void rtcgbIntersect1MBatched(RTCScene hs, struct RTCRayHit* rayhit, unsi
   API_END(s ? s->device : nullptr)
 }
 
+// ---------------------------------------------------------------------------
+// batched frames: restore + build + batched closest-hit query of a batched
+// scene, captured into one CUDA graph and replayed
+// ---------------------------------------------------------------------------
+
+struct BatchedFrame {
+  Scene* scene;
+  uint64_t commit_serial;
+  gb::GraphBuild gbuild;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint32_t* d_start = nullptr;
+  unsigned int* scratch = nullptr;  // [0] ray counter, [1] error flags, [2..] counters
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  RTCGBBatchedFrameStats stats{};
+  explicit BatchedFrame(Scene* s) : scene(s), commit_serial(s->commit_serial) { scene->inc(); }
+  ~BatchedFrame() {
+    scene->device->set_current();
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (d_start) cudaFree(d_start);
+    if (scratch) cudaFree(scratch);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    gb::graph_build_release(&gbuild);
+    scene->dec();
+  }
+};
+
+RTC_API RTCGBBatchedFrame rtcgbNewBatchedFrame(RTCScene hs, struct RTCRayHit* rayhit, const struct RTCRayHit* pristine,
+                                               unsigned int M, size_t byteStride, const unsigned int* batch_start,
+                                               unsigned int num_batches) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  std::lock_guard<std::mutex> lk(s->mtx);
+  if (!s->batched || !s->committed) fail(RTC_ERROR_INVALID_OPERATION, "a committed batched scene is required");
+  if (s->ninsts) fail(RTC_ERROR_INVALID_OPERATION, "batched frames do not take instances");
+  if (s->bvh.num_nodes == 0) fail(RTC_ERROR_INVALID_OPERATION, "empty scene");
+  for (size_t k = 0; k < s->descs.size(); k++)
+    if (s->descs[k].geomID != k)
+      fail(RTC_ERROR_INVALID_OPERATION, "batched frames need geometry IDs 0..n-1 without gaps");
+  if (!rayhit || M == 0 || num_batches == 0 || num_batches > s->descs.size() || byteStride < sizeof(RTCRayHit) ||
+      byteStride % 4)
+    fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  const cudaMemoryType mt = pointer_type(rayhit);
+  if (mt != cudaMemoryTypeDevice && mt != cudaMemoryTypeManaged) fail(RTC_ERROR_INVALID_ARGUMENT, "rays must be device memory");
+  if (pristine) {
+    const cudaMemoryType mp = pointer_type(pristine);
+    if (mp != cudaMemoryTypeDevice && mp != cudaMemoryTypeManaged)
+      fail(RTC_ERROR_INVALID_ARGUMENT, "pristine rays must be device memory");
+  }
+  std::vector<uint32_t> hs_start(num_batches + 1);
+  cuda_ok(cudaMemcpy(hs_start.data(), batch_start, hs_start.size() * sizeof(uint32_t), cudaMemcpyDefault), "batches");
+  if (hs_start[0] != 0 || hs_start.back() != M) fail(RTC_ERROR_INVALID_ARGUMENT, "batches must cover the rays exactly");
+  for (size_t b = 1; b < hs_start.size(); b++)
+    if (hs_start[b] < hs_start[b - 1]) fail(RTC_ERROR_INVALID_ARGUMENT, "batch boundaries must not decrease");
+  // the plan of the replayed build: this scene's last build, with margins
+  gb::GraphBuildPlan plan;
+  plan.valid_tris = s->stats.num_prims;
+  plan.roots = 0;
+  for (uint32_t r : s->bvh.roots) plan.roots += r != gb::kInvalidID ? 1u : 0u;
+  plan.ploc_rounds = s->stats.ploc_rounds + 8;
+  plan.levels = s->stats.depth + 4;
+  plan.leaf_max = (int)s->stats.leaf_max;
+  if (plan.levels > 64) fail(RTC_ERROR_INVALID_OPERATION, "the scene's tree is too deep for a captured build");
+  gb::BuildOptions opt = s->device->build_opt;
+  opt.robust = (s->flags & RTC_SCENE_FLAG_ROBUST) != 0;
+  opt.segmented = 1;
+  opt.leaf_max = plan.leaf_max;
+  Device* dev = s->device;
+  dev->set_current();
+  t_ctx.ensure(dev->cuda_device);
+  cudaStream_t st = t_ctx.stream();
+  BatchedFrame* f = new BatchedFrame(s);
+  try {
+    cuda_ok(gb::graph_build_prepare(s->descs.data(), (int)s->descs.size(), opt, plan, &f->gbuild), "frame build buffers");
+    cuda_ok(cudaMalloc((void**)&f->d_start, hs_start.size() * sizeof(uint32_t)), "cudaMalloc batches");
+    cuda_ok(cudaMemcpy(f->d_start, hs_start.data(), hs_start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+            "batches");
+    cuda_ok(cudaMalloc((void**)&f->scratch, 64), "cudaMalloc scratch");
+    cuda_ok(cudaEventCreate(&f->e0), "event");
+    cuda_ok(cudaEventCreate(&f->e1), "event");
+    gb::TraceParams P{};
+    P.nodes = f->gbuild.nodes;
+    P.tris = f->gbuild.tris;
+    P.rays = (char*)rayhit;
+    P.stride = byteStride;
+    P.nrays = M;
+    P.ray_counter = f->scratch;
+    P.err = f->scratch + 1;
+    P.counters = reinterpret_cast<gb::TraceCounters*>(f->scratch + 2);
+    P.max_iters = 4 * f->gbuild.maxw + 64;
+    P.num_nodes = f->gbuild.maxw;
+    P.num_tris = plan.valid_tris;
+    P.robust = opt.robust;
+    P.batch_start = f->d_start;
+    P.batch_root = f->gbuild.seg_index;  // geometry IDs are the segments
+    P.nbatches = num_batches;
+    const size_t span = (size_t)(M - 1) * byteStride + sizeof(RTCRayHit);
+    cuda_ok(cudaStreamSynchronize(st), "frame");
+    cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t e = cudaSuccess;
+    if (pristine) e = cudaMemcpyAsync(rayhit, pristine, span, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = gb::graph_build_enqueue(f->gbuild, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(f->scratch, 0, 64, st);
+    if (e == cudaSuccess) e = gb::launch_trace(P, false, false, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    f->graph = g;
+    cuda_ok(e, "frame capture");
+    cuda_ok(e2, "end capture");
+    cuda_ok(cudaGraphInstantiate(&f->exec, f->graph, 0), "instantiate frame");
+    size_t nnodes = 0;
+    cuda_ok(cudaGraphGetNodes(f->graph, nullptr, &nnodes), "graph nodes");
+    f->stats.graph_nodes = (unsigned int)nnodes;
+    f->stats.ploc_rounds = plan.ploc_rounds;
+    f->stats.levels = plan.levels;
+  } catch (...) {
+    delete f;
+    throw;
+  }
+  return (RTCGBBatchedFrame)f;
+  API_END(s ? s->device : nullptr)
+  return nullptr;
+}
+
+RTC_API void rtcgbBatchedFrameReplay(RTCGBBatchedFrame hf) {
+  BatchedFrame* f = (BatchedFrame*)hf;
+  API_BEGIN
+  if (!f) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid frame");
+  Scene* s = f->scene;
+  if (s->commit_serial != f->commit_serial)
+    fail(RTC_ERROR_INVALID_OPERATION, "the scene was committed again: create a new frame");
+  s->device->set_current();
+  t_ctx.ensure(s->device->cuda_device);
+  cudaStream_t st = t_ctx.stream();
+  cuda_ok(cudaEventRecord(f->e0, st), "event");
+  cuda_ok(cudaGraphLaunch(f->exec, st), "frame launch");
+  cuda_ok(cudaEventRecord(f->e1, st), "event");
+  gb::GraphBuildResult r;
+  cuda_ok(gb::graph_build_result(f->gbuild, s->bvh.lo, s->bvh.hi, &r, st), "frame result");
+  unsigned int err = 0;
+  cuda_ok(cudaMemcpy(&err, f->scratch + 1, sizeof(err), cudaMemcpyDeviceToHost), "frame status");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, f->e0, f->e1);
+  f->stats.frame_ms = ms;
+  f->stats.status = r.status;
+  f->stats.num_nodes = r.num_nodes;
+  f->stats.build_sah = r.sah;
+  f->stats.replays++;
+  if (r.status) fail(RTC_ERROR_UNKNOWN, "the replayed build no longer matches its plan: create a new frame");
+  if (err) fail(RTC_ERROR_UNKNOWN, "traversal error in a frame");
+  API_END(f ? f->scene->device : nullptr)
+}
+
+RTC_API void rtcgbGetBatchedFrameStats(RTCGBBatchedFrame hf, RTCGBBatchedFrameStats* out) {
+  BatchedFrame* f = (BatchedFrame*)hf;
+  API_BEGIN
+  if (!f || !out) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
+  *out = f->stats;
+  API_END(f ? f->scene->device : nullptr)
+}
+
+RTC_API void rtcgbReleaseBatchedFrame(RTCGBBatchedFrame hf) {
+  BatchedFrame* f = (BatchedFrame*)hf;
+  API_BEGIN
+  if (!f) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid frame");
+  delete f;
+  API_END(nullptr)
+}
+
 RTC_API void rtcgbOccluded1MBatched(RTCScene hs, struct RTCRay* ray, unsigned int M, size_t byteStride,
                                     const unsigned int* batch_start, unsigned int num_batches) {
   Scene* s = (Scene*)hs;

@@ -48,7 +48,8 @@ rtcgbProposerParamCount rtcgbProposerGetParams rtcgbProposerSetParams rtcgbPropo
 rtcgbIntersect1MLearned rtcgbOccluded1MLearned rtcgbNewPathTracer rtcgbRetainPathTracer rtcgbReleasePathTracer
 rtcgbPathTracerAnimateSoup rtcgbPathTracerSetProposer rtcgbPathTracerRenderFrame rtcgbPathTracerTrainProposer
 rtcgbPathTracerGetImage rtcgbSetSceneBatched rtcgbIntersect1MBatched rtcgbOccluded1MBatched
-rtcSetGeometryInstancedScene rtcSetGeometryTransform rtcGetGeometryTransform""".split()
+rtcSetGeometryInstancedScene rtcSetGeometryTransform rtcGetGeometryTransform rtcgbNewBatchedFrame
+rtcgbBatchedFrameReplay rtcgbGetBatchedFrameStats rtcgbReleaseBatchedFrame""".split()
 
 
 class RTCBounds(ctypes.Structure):
@@ -76,6 +77,12 @@ class RTCGBQueryStats(ctypes.Structure):
 class RTCGBFrameStats(ctypes.Structure):
     _fields_ = [("frame_ms", ctypes.c_double), ("rays", ctypes.c_ulonglong), ("proposal_hits", ctypes.c_ulonglong),
                 ("rays_per_bounce", ctypes.c_uint * 8), ("learned", ctypes.c_uint), ("errors", ctypes.c_uint)]
+
+
+class RTCGBBatchedFrameStats(ctypes.Structure):
+    _fields_ = [("frame_ms", ctypes.c_double), ("build_sah", ctypes.c_double), ("status", ctypes.c_uint),
+                ("num_nodes", ctypes.c_uint), ("ploc_rounds", ctypes.c_uint), ("levels", ctypes.c_uint),
+                ("graph_nodes", ctypes.c_uint), ("replays", ctypes.c_uint)]
 
 
 class RTCGBProposerStats(ctypes.Structure):
@@ -174,6 +181,10 @@ def load(build=True):
         "rtcGetGeometryTransform": (None, [vp, ctypes.c_float, i, vp]),
         "rtcgbIntersect1MBatched": (None, [vp, vp, u, sz, vp, u]),
         "rtcgbOccluded1MBatched": (None, [vp, vp, u, sz, vp, u]),
+        "rtcgbNewBatchedFrame": (vp, [vp, vp, vp, u, sz, vp, u]),
+        "rtcgbBatchedFrameReplay": (None, [vp]),
+        "rtcgbGetBatchedFrameStats": (None, [vp, ctypes.POINTER(RTCGBBatchedFrameStats)]),
+        "rtcgbReleaseBatchedFrame": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -492,6 +503,35 @@ class Proposer:
     def release(self):
         if self.h:
             self.L.rtcgbReleaseProposer(self.h)
+            self.h = None
+
+
+class BatchedFrame:
+    """Rebuild of a committed batched scene + batched closest-hit query on
+    device rays, captured into one CUDA graph (rtcgbNewBatchedFrame)."""
+
+    def __init__(self, scene, rays_ptr, count, batch_start, pristine_ptr=None, stride=80):
+        self.scene = scene
+        self.L = scene.L
+        bs = np.ascontiguousarray(batch_start, np.uint32)
+        self.h = ctypes.c_void_p(self.L.rtcgbNewBatchedFrame(scene.h, ctypes.c_void_p(rays_ptr),
+                                                             ctypes.c_void_p(pristine_ptr) if pristine_ptr else None,
+                                                             count, stride, _ptr(bs), bs.shape[0] - 1))
+        scene.dev.check("rtcgbNewBatchedFrame")
+
+    def replay(self):
+        self.L.rtcgbBatchedFrameReplay(self.h)
+        self.scene.dev.check("rtcgbBatchedFrameReplay")
+        return self.stats()
+
+    def stats(self):
+        s = RTCGBBatchedFrameStats()
+        self.L.rtcgbGetBatchedFrameStats(self.h, ctypes.byref(s))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def release(self):
+        if self.h:
+            self.L.rtcgbReleaseBatchedFrame(self.h)
             self.h = None
 
 

@@ -224,4 +224,32 @@ RTC_API void rtcgbIntersect1MBatched(RTCScene scene, struct RTCRayHit* rayhit, u
 RTC_API void rtcgbOccluded1MBatched(RTCScene scene, struct RTCRay* ray, unsigned int M, size_t byteStride,
                                     const unsigned int* batch_start, unsigned int num_batches);
 
+/* Batched frames: the rebuild of every BVH of a committed batched scene and a
+   batched closest-hit query over device-resident rays, captured once into one
+   CUDA graph and replayed with one launch (optionally preceded by a copy of
+   `pristine` over `rayhit`, both device memory).  The captured build runs with
+   no host reads: its PLOC rounds and collapse levels are enqueued a fixed
+   number of times, planned from the scene's last build (rounds and levels past
+   the last real one do nothing); a replay whose build no longer fits its plan
+   reports RTC_ERROR_UNKNOWN.  The scene's geometry IDs must be 0..n-1; a new
+   commit of the scene invalidates the frame.  Results are those of
+   rtcCommitScene + rtcgbIntersect1MBatched on the same data. */
+typedef struct RTCGBBatchedFrameTy* RTCGBBatchedFrame;
+typedef struct RTCGBBatchedFrameStats {
+  double frame_ms;           /* device time of the last replay (copy + build + query) */
+  double build_sah;          /* SAH of the replayed build */
+  unsigned int status;       /* 0: the replayed build fitted its plan */
+  unsigned int num_nodes;    /* wide nodes of the replayed build */
+  unsigned int ploc_rounds;  /* PLOC rounds enqueued */
+  unsigned int levels;       /* collapse levels enqueued */
+  unsigned int graph_nodes;  /* nodes of the captured graph */
+  unsigned int replays;
+} RTCGBBatchedFrameStats;
+RTC_API RTCGBBatchedFrame rtcgbNewBatchedFrame(RTCScene scene, struct RTCRayHit* rayhit,
+                                               const struct RTCRayHit* pristine, unsigned int M, size_t byteStride,
+                                               const unsigned int* batch_start, unsigned int num_batches);
+RTC_API void rtcgbBatchedFrameReplay(RTCGBBatchedFrame frame);
+RTC_API void rtcgbGetBatchedFrameStats(RTCGBBatchedFrame frame, RTCGBBatchedFrameStats* stats);
+RTC_API void rtcgbReleaseBatchedFrame(RTCGBBatchedFrame frame);
+
 #endif
