@@ -678,6 +678,36 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
                                      f"another by the single-threaded oracle builder and traced on {cores} threads",
                            "build_Mtris_per_s": done_tris / build_s / 1e6, "trace_Mrays_per_s": total / trace_s / 1e6}
     out["gpu_build_plus_trace_Mrays_per_s"] = nrays / ((float(statistics.median(builds)) + kernel_ms) * 1e-3) / 1e6
+    # the same step as one CUDA graph: ray restore copy + rebuild of every BVH +
+    # batched closest-hit query (rtcgbNewBatchedFrame), replayed
+    separate = work.clone()  # the separate calls' results, kept on the device for the comparison
+    # the restore copy alone (part of every frame)
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    copy_ms = []
+    for _ in range(3):
+        c0.record()
+        work.copy_(pristine)
+        c1.record()
+        torch.cuda.synchronize()
+        copy_ms.append(c0.elapsed_time(c1))
+    frame = api.BatchedFrame(sc, work.data_ptr(), nrays, start, pristine_ptr=pristine.data_ptr())
+    fms = []
+    for k in range(warmup + steps):
+        fst = frame.replay()
+        if k >= warmup:
+            fms.append(fst["frame_ms"])
+    # bitwise: the records' integer fields (e.g. instID = 0xFFFFFFFF) are NaN as floats
+    same = bool(torch.equal(work.view(torch.int32), separate.view(torch.int32)))
+    del separate
+    out["graph"] = {"frame": "ray restore copy + rebuild of all BVHs + batched closest-hit query, one CUDA graph launch",
+                    "ms_per_step": float(statistics.median(fms)),
+                    "Mrays_per_s": nrays / (statistics.median(fms) * 1e-3) / 1e6,
+                    "restore_copy_ms": float(statistics.median(copy_ms)),
+                    "build_ms_in_graph": float(statistics.median(fms)) - float(statistics.median(copy_ms)) - kernel_ms,
+                    "graph_nodes": fst["graph_nodes"], "ploc_rounds_enqueued": fst["ploc_rounds"],
+                    "levels_enqueued": fst["levels"], "build_status": fst["status"],
+                    "identical_to_separate_calls": same}
+    frame.release()
     sc.release()
     dev.release()
     del pristine, work

@@ -133,3 +133,42 @@ def test_autotuner_picks_the_fastest_candidate(rtc):
     assert [r["config"] for r in results] == cands
     assert all(r["build_ms"] > 0 and r["trace_ms"] > 0 for r in results)
     assert best == min(results, key=lambda r: r["total_ms"])["config"]
+
+
+def test_batched_frame_graph_matches_separate_calls(rtc, device):
+    """A batched frame -- the rebuild of every BVH of the scene and the batched
+    closest-hit query, captured into one CUDA graph with the copy that restores
+    the rays -- gives the bytes of rtcCommitScene + rtcgbIntersect1MBatched on
+    the same rays, replay after replay; a new commit invalidates it."""
+    torch = pytest.importorskip("torch")
+    meshes = [W.heightfield(32, seed=5), W.gaussian_soup(30_000, seed=6), W.heightfield(20, seed=7),
+              W.gaussian_soup(8_000, seed=8)]
+    parts, start = [], [0]
+    for k in range(len(meshes)):
+        cam = W.camera_rays(64, 64) if k % 2 == 0 else W.camera_rays(64, 64, eye=(0.5, -1.0, 0.5), look=(0.5, 0.5, 0.5))
+        r = np.concatenate([cam, W.sphere_rays(8000, seed=30 + k)])
+        parts.append(r)
+        start.append(start[-1] + r.shape[0])
+    rays = np.concatenate(parts)
+    sc = rtc.Scene(device)
+    sc.set_batched()
+    for v, i in meshes:
+        sc.add_mesh(v, i)
+    sc.commit()
+    ref = rays.copy()
+    sc.intersect_batched(ref, start)
+    assert (ref["geomID"] != 0xFFFFFFFF).sum() > 5000
+    pristine = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    work = torch.zeros_like(pristine)
+    frame = rtc.BatchedFrame(sc, work.data_ptr(), rays.shape[0], start, pristine_ptr=pristine.data_ptr())
+    for _ in range(2):
+        st = frame.replay()
+        got = work.cpu().numpy()
+        assert np.array_equal(got, ref.view(np.uint8))
+    assert st["status"] == 0 and st["replays"] == 2 and st["graph_nodes"] > 50 and st["frame_ms"] > 0
+    assert st["num_nodes"] == sc.build_stats()["num_nodes"]
+    sc.commit()
+    with pytest.raises(rtc.RTCError):
+        frame.replay()
+    frame.release()
+    sc.release()
