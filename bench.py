@@ -871,22 +871,27 @@ def run_gpu(args, rank, world):
             "learned": None, "animated": None, "batched": None, "heightfield": None,
         }
 
-    if rank == 0 and not args.no_learned:
+    # the other configurations (learned, animated, batched, heightfield) are
+    # single-GPU workloads: they run at N = 1 only, so that under torchrun no
+    # rank waits at the final barrier while rank 0 runs them; the CPU baseline
+    # is rank 0's at N = 1 only as well
+    single = world == 1
+    if single and not args.no_learned:
         del pristine, work, sh_pristine, sh_work
         torch.cuda.empty_cache()
         line["learned"] = run_learned(api, dev, torch, stream, args.learned_scale, args.steps, args.warmup,
                                       0.0 if args.no_cpu else min(6.0, args.cpu_seconds))
-    if rank == 0 and not args.no_animated:
+    if single and not args.no_animated:
         line["animated"] = run_animated(api, dev, torch, args.animated_scale, args.frames)
-    if rank == 0 and not args.no_batched:
+    if single and not args.no_batched:
         line["batched"] = run_batched(api, f"gpu.device={local}{',' + args.config if args.config else ''}", torch,
                                       args.batched_scale, args.steps, args.warmup,
                                       0.0 if args.no_cpu else min(8.0, args.cpu_seconds))
-    if rank == 0 and not args.no_heightfield:
+    if single and not args.no_heightfield:
         line["heightfield"] = run_heightfield(api, dev, torch, stream, args.steps, args.warmup,
                                               0.0 if args.no_cpu else min(3.0, args.cpu_seconds))
 
-    if rank == 0 and not args.no_cpu:
+    if single and not args.no_cpu:
         base, orc, sample = cpu_rate(verts, idx, rays, args.cpu_seconds, robust=args.robust)
         st = orc.stats()
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
