@@ -703,7 +703,7 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
                     "ms_per_step": float(statistics.median(fms)),
                     "Mrays_per_s": nrays / (statistics.median(fms) * 1e-3) / 1e6,
                     "restore_copy_ms": float(statistics.median(copy_ms)),
-                    "build_ms_in_graph": float(statistics.median(fms)) - float(statistics.median(copy_ms)) - kernel_ms,
+                    "separate_parts_ms": float(statistics.median(copy_ms)) + float(statistics.median(builds)) + kernel_ms,
                     "graph_nodes": fst["graph_nodes"], "ploc_rounds_enqueued": fst["ploc_rounds"],
                     "levels_enqueued": fst["levels"], "build_status": fst["status"],
                     "identical_to_separate_calls": same}
