@@ -290,11 +290,12 @@ __device__ __forceinline__ void to_instance(const float* __restrict__ m, TRay& r
 // Plain variants: 9 resident CTAs of 128 threads per SM (at most 56 registers a
 // thread), measured 4 % faster than the 8 that 64 registers allowed (10 and 12
 // were slower).  The counting, seeded and instance variants keep their
-// registers (under the same bound they would spill 32-150 bytes).
+// registers (under the same bound they would spill 32-150 bytes), and so does
+// the variant with per-ray exclusion lists (EXCL: filter callbacks).
 constexpr int TRACE_MIN_BLOCKS = 9;
 
-template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED, bool INST = false>
-__global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST) ? 1 : TRACE_MIN_BLOCKS)
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED, bool INST = false, bool EXCL = false>
+__global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXCL) ? 1 : TRACE_MIN_BLOCKS)
     k_trace(TraceParams P) {
   Ctx c{P.nodes, P.tris, P.err, P.max_iters, P.num_nodes, P.num_tris};
   uint32_t cur_inst = kInvalidID, hit_inst = kInvalidID;  // INST: instance being traversed / of the hit
@@ -308,6 +309,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST) ? 1 :
   TRay r;
   float t_best = 0.f, hu = 0.f, hv = 0.f;
   uint32_t hit_tri = kInvalidID, seed_tri = kInvalidID, g_base = 0, g_bits = 0, t_base = 0, t_bits = 0, iters = 0;
+  uint32_t ex_lo = 0, ex_hi = 0;  // EXCL: this ray's range of excluded triangles
   unsigned long long n_nodes = 0, n_tris = 0, n_rays = 0, n_prop = 0;
   for (;;) {
     // ---- refill idle lanes
@@ -322,6 +324,10 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST) ? 1 :
         uint32_t rid = base + __popc(idle & lt_mask);
         if (rid < nrays) {
           if (P.order) rid = __ldg(P.order + rid);  // the record this fetch slot traces
+          if (EXCL) {
+            ex_lo = __ldg(P.excl_off + rid);
+            ex_hi = __ldg(P.excl_off + rid + 1);
+          }
           rec = P.rays + (uint64_t)rid * P.stride;
           float tfar;
           load_ray<ALIGNED>(rec, r, tfar);
@@ -418,6 +424,14 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST) ? 1 :
       if (ti >= c.num_tris) { atomicOr(c.err, kErrBuild); active = false; break; }
       const float4* tp = reinterpret_cast<const float4*>(c.tris + ti);
       const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), d = __ldg(tp + 2);
+      if (EXCL) {  // a triangle whose hit a filter callback rejected
+        bool skip = false;
+        for (uint32_t e = ex_lo; e < ex_hi && !skip; e++) {
+          const uint2 x = __ldg(P.excl + e);
+          skip = x.x == __float_as_uint(a.w) && x.y == __float_as_uint(b.w);
+        }
+        if (skip) continue;
+      }
       if (INST && __float_as_uint(d.w) == kInstanceLeaf) {
         const uint32_t ii = __float_as_uint(a.w);
         if (cur_inst != kInvalidID) continue;  // nested instance: not traversed
@@ -545,14 +559,15 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST) ? 1 :
   }
 }
 
-template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED = false, bool INST = false>
+template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED = false, bool INST = false,
+          bool EXCL = false>
 static cudaError_t launch_one(const TraceParams& P, cudaStream_t st) {
   static int blocks_per_sm = -1, num_sms = 0;
   if (blocks_per_sm < 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED, INST>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED, INST, EXCL>,
                                                   TRACE_THREADS, 0);
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
@@ -560,7 +575,7 @@ static cudaError_t launch_one(const TraceParams& P, cudaStream_t st) {
   uint64_t grid = (uint64_t)num_sms * blocks_per_sm;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
-  k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED, INST><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
+  k_trace<ANYHIT, COUNT, ALIGNED, ROBUST, SEEDED, INST, EXCL><<<(unsigned)grid, TRACE_THREADS, 0, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -583,6 +598,13 @@ static cudaError_t launch_variant(const TraceParams& P, bool aligned, cudaStream
 
 cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStream_t st) {
   const bool aligned = ((uintptr_t)P.rays % 16 == 0) && (P.stride % 16 == 0);
+  // exclusion lists: closest hit on aligned records of plain scenes (checked here)
+  if (P.excl_off || P.excl) {
+    if (anyhit || count || !aligned || !P.excl_off || P.insts || P.seeds || P.batch_root || P.order)
+      return cudaErrorInvalidValue;
+    return P.robust ? launch_one<false, false, true, true, false, false, true>(P, st)
+                    : launch_one<false, false, true, false, false, false, true>(P, st);
+  }
   if (anyhit) return count ? launch_variant<true, true>(P, aligned, st) : launch_variant<true, false>(P, aligned, st);
   return count ? launch_variant<false, true>(P, aligned, st) : launch_variant<false, false>(P, aligned, st);
 }

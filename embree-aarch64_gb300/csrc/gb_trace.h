@@ -26,6 +26,11 @@ struct TraceParams {
   const uint32_t* batch_start;  // optional (segmented BVHs): rays [batch_start[b], batch_start[b+1])
   const uint32_t* batch_root;   //   start at node batch_root[b] (kInvalidID: the batch hits nothing)
   uint32_t nbatches;
+  // optional (closest hit, 16-byte aligned records, no instances/proposals/batches):
+  // ray i skips the triangles (primID, geomID) = excl[excl_off[i] .. excl_off[i+1]),
+  // the hits a filter callback rejected
+  const uint32_t* excl_off;
+  const uint2* excl;
 };
 
 // Launches the persistent closest-hit (anyhit = false) or any-hit kernel.

@@ -291,6 +291,8 @@ struct Geometry : RefCounted {
   unsigned mask = 0xFFFFFFFFu;
   RTCBuildQuality quality = RTC_BUILD_QUALITY_MEDIUM;
   void* user = nullptr;
+  RTCFilterFunctionN ifilter = nullptr;  // rtcSetGeometryIntersectFilterFunction
+  RTCFilterFunctionN ofilter = nullptr;  // rtcSetGeometryOccludedFilterFunction
   unsigned time_steps = 1;
   uint64_t topo_version = 0;  // bumped when the index buffer is set or updated
   // device copies of host buffers
@@ -503,6 +505,10 @@ struct Scene : RefCounted {
   uint32_t* d_roots = nullptr;      // batched BVH: root node per geometry ID (device)
   uint32_t nroots = 0;
   uint64_t commit_serial = 0;       // counts commits (builds and refits)
+  // filter callbacks are called: some geometry had one, or the scene had
+  // RTC_SCENE_FLAG_CONTEXT_FILTER_FUNCTION, at the last commit (the reference picks its
+  // filtering intersectors at commit, kernels/common/scene.cpp:679, 721)
+  bool filters = false;
   // instances of the committed BVH: device table, and the instanced scenes it
   // reads (retained) with their commit serials at this scene's commit
   gb::InstDesc* d_insts = nullptr;
@@ -568,9 +574,13 @@ struct Scene : RefCounted {
     std::vector<std::pair<Scene*, uint64_t>> irefs;
     uint64_t inodes = 0;
     const bool robust_now = (flags & RTC_SCENE_FLAG_ROBUST) != 0;
+    bool filters_now = (flags & RTC_SCENE_FLAG_CONTEXT_FILTER_FUNCTION) != 0;
+    for (const Geometry* g : geoms)
+      if (g && g->enabled && (g->ifilter || g->ofilter)) filters_now = true;
     for (unsigned id = 0; id < geoms.size(); id++) {
       Geometry* g = geoms[id];
       if (!g || !g->enabled || g->type != RTC_GEOMETRY_TYPE_INSTANCE || !g->inst_scene) continue;
+      if (g->inst_scene->filters) filters_now = true;  // queries then refuse (instances)
       if (batched) fail(RTC_ERROR_INVALID_OPERATION, "batched scenes hold triangle meshes only");
       if (robust_now) fail(RTC_ERROR_INVALID_OPERATION, "instances in robust scenes are not supported");
       Scene* is = g->inst_scene;
@@ -663,6 +673,7 @@ struct Scene : RefCounted {
       if (!fallback) {
         stats = bs;
         this->descs = descs;
+        filters = filters_now;
         commit_serial++;
         if (progress) progress(progress_ptr, 1.0);
         return;
@@ -693,6 +704,7 @@ struct Scene : RefCounted {
     }
     stats = bs;
     committed = true;
+    filters = filters_now;
     build_serial++;
     commit_serial++;
     this->descs = descs;
@@ -760,8 +772,170 @@ struct BatchArgs {
   uint32_t nbatches = 0;
 };
 
+// Filter callbacks (rtcSetGeometryIntersectFilterFunction, rtcSetGeometryOccludedFilterFunction,
+// RTCIntersectContext::filter).  The reference calls them for every candidate hit inside its
+// traversal (kernels/geometry/intersector_epilog.h:237-276, 397-435;
+// kernels/geometry/filter.h:14-37, 72-89): the geometry's callback, then the context's; a
+// hit is rejected when either clears valid[0]; a closest-hit query keeps the nearest
+// accepted hit, an occlusion query stops at the first accepted one.  Here the traversal
+// stays on the GPU and the callbacks run on the calling thread between launches.  Each round
+// traces the pending rays for their nearest hit among the triangles no callback has rejected
+// for them (the kernel skips each ray's rejected (primID, geomID) list), calls the callbacks
+// for those hits with N = 1, the ray's tfar set to the hit distance and the hit in an
+// RTCHit, and traces again only the rays whose hit was rejected.  For callbacks that decide
+// from their arguments, the result is the reference's: the nearest accepted hit, occlusion
+// iff some hit in range is accepted.  The callbacks see the hits in distance order (the
+// reference: traversal order), and what they write to the ray or hit is kept for accepted
+// hits only (the reference restores tfar only).
+void run_filtered(Scene* scene, const RTCIntersectContext* uctx, void* rays, unsigned M, size_t stride, bool anyhit,
+                  size_t recsize) {
+  ThreadCtx& c = t_ctx;
+  const gb::DeviceBVH& bvh = scene->bvh;
+  Device* dev = scene->device;
+  dev->set_current();
+  c.ensure(dev->cuda_device);
+  cudaStream_t st = c.stream();
+  const size_t span = (size_t)(M - 1) * stride + recsize;
+  // the caller's records, on the host
+  const bool on_device = is_device_pointer(rays);
+  std::vector<char> staged;
+  char* host = (char*)rays;
+  if (on_device) {
+    staged.resize(span);
+    cuda_ok(cudaMemcpyAsync(staged.data(), rays, span, cudaMemcpyDeviceToHost, st), "D2H rays");
+    cuda_ok(cudaStreamSynchronize(st), "D2H rays");
+    host = staged.data();
+  }
+  // stream validity (kernels/bvh/bvh_intersector_stream_filters.cpp:75, 145)
+  std::vector<uint32_t> pend;
+  for (unsigned i = 0; i < M; i++) {
+    RTCRay r;
+    std::memcpy(&r, host + (size_t)i * stride, sizeof(RTCRay));
+    if (!(r.tnear <= r.tfar) || (anyhit && r.tfar < 0.0f)) continue;
+    pend.push_back(i);
+  }
+  std::vector<std::vector<uint2>> rejected(pend.size());  // per pending ray
+  std::vector<RTCRayHit> work;
+  std::vector<uint32_t> off;
+  std::vector<uint2> items;
+  float k_ms_total = 0.0f;
+  unsigned launches = 0;
+  const unsigned inst0 = uctx ? uctx->instID[0] : RTC_INVALID_GEOMETRY_ID;
+  while (!pend.empty()) {
+    const size_t n = pend.size();
+    work.assign(n, RTCRayHit{});
+    off.resize(n + 1);
+    items.clear();
+    for (size_t j = 0; j < n; j++) {
+      std::memcpy(&work[j].ray, host + (size_t)pend[j] * stride, sizeof(RTCRay));
+      work[j].hit.geomID = work[j].hit.primID = work[j].hit.instID[0] = RTC_INVALID_GEOMETRY_ID;
+      off[j] = (uint32_t)items.size();
+      items.insert(items.end(), rejected[j].begin(), rejected[j].end());
+    }
+    off[n] = (uint32_t)items.size();
+    // device layout: records (80 B each), list offsets, lists
+    const size_t b_work = n * sizeof(RTCRayHit), b_off = ((n + 1) * 4 + 15) & ~size_t(15);
+    char* d = c.buffer(b_work + b_off + items.size() * sizeof(uint2) + 16);
+    cuda_ok(cudaMemcpyAsync(d, work.data(), b_work, cudaMemcpyHostToDevice, st), "H2D rays");
+    cuda_ok(cudaMemcpyAsync(d + b_work, off.data(), (n + 1) * 4, cudaMemcpyHostToDevice, st), "H2D rejected");
+    if (!items.empty())
+      cuda_ok(cudaMemcpyAsync(d + b_work + b_off, items.data(), items.size() * sizeof(uint2), cudaMemcpyHostToDevice,
+                              st), "H2D rejected");
+    gb::TraceParams P{};
+    P.nodes = bvh.nodes;
+    P.tris = bvh.tris;
+    P.rays = d;
+    P.stride = sizeof(RTCRayHit);
+    P.nrays = (uint32_t)n;
+    P.ray_counter = c.dscratch;
+    P.err = c.dscratch + 1;
+    P.counters = reinterpret_cast<gb::TraceCounters*>(c.dscratch + 2);
+    P.max_iters = 4 * bvh.num_nodes + 64;
+    P.num_nodes = bvh.num_nodes;
+    P.num_tris = bvh.num_tris;
+    P.robust = bvh.robust;
+    P.excl_off = reinterpret_cast<const uint32_t*>(d + b_work);
+    P.excl = reinterpret_cast<const uint2*>(d + b_work + b_off);
+    cuda_ok(cudaMemsetAsync(c.dscratch, 0, 64, st), "memset");
+    cuda_ok(cudaEventRecord(c.e1, st), "event");
+    cuda_ok(gb::launch_trace(P, false, false, st), "traversal launch");
+    cuda_ok(cudaEventRecord(c.e2, st), "event");
+    launches += 2;
+    cuda_ok(cudaMemcpyAsync(work.data(), d, b_work, cudaMemcpyDeviceToHost, st), "D2H rays");
+    cuda_ok(cudaMemcpyAsync(c.hscratch, c.dscratch, 64, cudaMemcpyDeviceToHost, st), "D2H status");
+    cuda_ok(cudaStreamSynchronize(st), "traversal");
+    float k_ms = 0.0f;
+    cudaEventElapsedTime(&k_ms, c.e1, c.e2);
+    k_ms_total += k_ms;
+    const unsigned err = c.hscratch[1];
+    if (err & gb::kErrStackOverflow) fail(RTC_ERROR_UNKNOWN, "traversal stack overflow");
+    if (err & gb::kErrIterationLimit) fail(RTC_ERROR_UNKNOWN, "traversal iteration limit reached");
+    if (err & gb::kErrBuild) fail(RTC_ERROR_UNKNOWN, "traversal found an invalid BVH reference");
+    // callbacks on this round's hits
+    size_t keep = 0;
+    for (size_t j = 0; j < n; j++) {
+      const RTCRayHit& w = work[j];
+      if (w.hit.geomID == RTC_INVALID_GEOMETRY_ID) continue;  // no further hit: done
+      char* rec = host + (size_t)pend[j] * stride;
+      const Geometry* g = w.hit.geomID < scene->geoms.size() ? scene->geoms[w.hit.geomID] : nullptr;
+      const RTCFilterFunctionN gf = g ? (anyhit ? g->ofilter : g->ifilter) : nullptr;
+      const RTCFilterFunctionN cf = uctx ? uctx->filter : nullptr;
+      RTCRayHit tmp;
+      std::memcpy(&tmp.ray, rec, sizeof(RTCRay));
+      tmp.ray.tfar = w.ray.tfar;  // the hit distance
+      tmp.hit = w.hit;
+      tmp.hit.instID[0] = inst0;
+      bool accepted = true;
+      if (gf || cf) {
+        int valid = -1;
+        RTCFilterFunctionNArguments args;
+        args.valid = &valid;
+        args.geometryUserPtr = g ? g->user : nullptr;
+        args.context = const_cast<RTCIntersectContext*>(uctx);
+        args.ray = reinterpret_cast<RTCRayN*>(&tmp.ray);
+        args.hit = reinterpret_cast<RTCHitN*>(&tmp.hit);
+        args.N = 1;
+        if (gf) {
+          gf(&args);
+          accepted = valid != 0;
+        }
+        if (accepted && cf) {
+          cf(&args);
+          accepted = valid != 0;
+        }
+      }
+      if (accepted) {
+        if (anyhit) {
+          const float ninf = -INFINITY;
+          std::memcpy(rec + 32, &ninf, 4);
+        } else {
+          std::memcpy(rec, &tmp, sizeof(RTCRayHit));  // copyHitToRay (kernels/common/ray.h)
+        }
+        continue;
+      }
+      rejected[j].push_back(make_uint2(w.hit.primID, w.hit.geomID));
+      if (keep != j) {
+        pend[keep] = pend[j];
+        rejected[keep].swap(rejected[j]);
+      }
+      keep++;
+    }
+    pend.resize(keep);
+    rejected.resize(keep);
+  }
+  if (on_device) {
+    cuda_ok(cudaMemcpyAsync(rays, host, span, cudaMemcpyHostToDevice, st), "H2D results");
+    cuda_ok(cudaStreamSynchronize(st), "H2D results");
+  }
+  gb::note_launches(launches);
+  c.last.kernel_ms = k_ms_total;
+  c.last.h2d_bytes = span;
+  c.last.d2h_bytes = span;
+}
+
 void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit, size_t recsize,
-               ProposerObj* prop = nullptr, const BatchArgs* batch = nullptr) {
+               ProposerObj* prop = nullptr, const BatchArgs* batch = nullptr,
+               const RTCIntersectContext* uctx = nullptr) {
   VERIFY_HANDLE(scene);
   if (!scene->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
   if (M == 0) return;
@@ -777,6 +951,13 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
                                                      : "not a batched scene (rtcgbSetSceneBatched)");
   if (prop && scene->batched) fail(RTC_ERROR_INVALID_OPERATION, "the proposer does not support batched scenes");
   if (prop && scene->ninsts) fail(RTC_ERROR_INVALID_OPERATION, "the proposer does not support scenes with instances");
+  if (scene->filters) {
+    if (prop || batch) fail(RTC_ERROR_INVALID_OPERATION, "learned and batched queries do not call filter callbacks");
+    if (scene->ninsts || !scene->inst_refs.empty())
+      fail(RTC_ERROR_INVALID_OPERATION, "filter callbacks in scenes with instances are not supported");
+    run_filtered(scene, uctx, rays, M, stride, anyhit, recsize);
+    return;
+  }
   // the BVHs the instance leaves point to must be those of this scene's commit
   for (const auto& r : scene->inst_refs)
     if (!r.first->committed || r.first->commit_serial != r.second)
@@ -949,13 +1130,13 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
 
 // array-of-pointers variants gather into a packed host array first
 template <typename Rec>
-void run_query_pointers(Scene* scene, Rec** recs, unsigned M, bool anyhit) {
+void run_query_pointers(Scene* scene, Rec** recs, unsigned M, bool anyhit, const RTCIntersectContext* uctx) {
   VERIFY_HANDLE(scene);
   if (M == 0) return;
   if (!recs) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
   std::vector<Rec> tmp(M);
   for (unsigned i = 0; i < M; i++) tmp[i] = *recs[i];
-  run_query(scene, tmp.data(), M, sizeof(Rec), anyhit, sizeof(Rec));
+  run_query(scene, tmp.data(), M, sizeof(Rec), anyhit, sizeof(Rec), nullptr, nullptr, uctx);
   for (unsigned i = 0; i < M; i++) *recs[i] = tmp[i];
 }
 
@@ -975,7 +1156,8 @@ enum SoaField {
 // written only when it hit something, an occlusion lane only when it is occluded
 // (ray.h:903-911, 988-1010), and null Ng/instID pointers are skipped.
 template <typename Addr>
-void run_query_soa(Scene* scene, size_t count, const int* valid, bool anyhit, Addr addr) {
+void run_query_soa(Scene* scene, size_t count, const int* valid, bool anyhit, const RTCIntersectContext* uctx,
+                   Addr addr) {
   VERIFY_HANDLE(scene);
   if (count == 0) return;
   if (count > 0xffffffffull) fail(RTC_ERROR_INVALID_ARGUMENT, "too many rays");
@@ -1007,7 +1189,7 @@ void run_query_soa(Scene* scene, size_t count, const int* valid, bool anyhit, Ad
   if (anyhit) {
     std::vector<RTCRay> tmp(M);
     for (unsigned j = 0; j < M; j++) load_ray(tmp[j], lane[j]);
-    run_query(scene, tmp.data(), M, sizeof(RTCRay), true, sizeof(RTCRay));
+    run_query(scene, tmp.data(), M, sizeof(RTCRay), true, sizeof(RTCRay), nullptr, nullptr, uctx);
     for (unsigned j = 0; j < M; j++)
       if (tmp[j].tfar < 0.0f) *(float*)addr(kTfar, lane[j]) = tmp[j].tfar;
     return;
@@ -1019,7 +1201,7 @@ void run_query_soa(Scene* scene, size_t count, const int* valid, bool anyhit, Ad
     tmp[j].hit.primID = RTC_INVALID_GEOMETRY_ID;
     tmp[j].hit.instID[0] = RTC_INVALID_GEOMETRY_ID;
   }
-  run_query(scene, tmp.data(), M, sizeof(RTCRayHit), false, sizeof(RTCRayHit));
+  run_query(scene, tmp.data(), M, sizeof(RTCRayHit), false, sizeof(RTCRayHit), nullptr, nullptr, uctx);
   for (unsigned j = 0; j < M; j++) {
     const RTCRayHit& h = tmp[j];
     if (h.hit.geomID == RTC_INVALID_GEOMETRY_ID) continue;
@@ -1038,20 +1220,21 @@ void run_query_soa(Scene* scene, size_t count, const int* valid, bool anyhit, Ad
 // packets of K lanes / NM streams: field f of lane i of packet p sits at
 // base + p * stride + (f * K + i) * 4 (rtcore_ray.h:222-248)
 void run_query_packets(Scene* scene, void* base, unsigned K, size_t packets, size_t stride, const int* valid,
-                       bool anyhit) {
+                       bool anyhit, const RTCIntersectContext* uctx) {
   if (!base) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
   if (is_device_pointer(base)) fail(RTC_ERROR_INVALID_ARGUMENT, "ray packets must be in host memory");
   if (packets > 1 && stride < (size_t)(anyhit ? 12 : 20) * K * 4)
     fail(RTC_ERROR_INVALID_ARGUMENT, "byteStride smaller than one ray packet");
   char* b = (char*)base;
-  run_query_soa(scene, (size_t)K * packets, valid, anyhit, [=](int f, size_t r) -> void* {
+  run_query_soa(scene, (size_t)K * packets, valid, anyhit, uctx, [=](int f, size_t r) -> void* {
     const size_t p = r / K, i = r % K;
     return b + p * stride + ((size_t)f * K + i) * 4;
   });
 }
 
 // pointer-SOA streams (rtcore_ray.h:170-213); optional fields may be null
-void run_query_pointer_soa(Scene* scene, const RTCRayHitNp* rh, const RTCRayNp* ray, unsigned N, bool anyhit) {
+void run_query_pointer_soa(Scene* scene, const RTCRayHitNp* rh, const RTCRayNp* ray, unsigned N, bool anyhit,
+                           const RTCIntersectContext* uctx) {
   if (!rh && !ray) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
   if (N == 0) return;
   const RTCRayNp& r = rh ? rh->ray : *ray;
@@ -1067,7 +1250,7 @@ void run_query_pointer_soa(Scene* scene, const RTCRayHitNp* rh, const RTCRayNp* 
     fail(RTC_ERROR_INVALID_ARGUMENT, "missing ray arrays");
   for (int k = 0; k < kNumSoaFields; k++)
     if (fld[k] && is_device_pointer(fld[k])) fail(RTC_ERROR_INVALID_ARGUMENT, "ray arrays must be in host memory");
-  run_query_soa(scene, N, nullptr, anyhit, [&](int f, size_t i) -> void* {
+  run_query_soa(scene, N, nullptr, anyhit, uctx, [&](int f, size_t i) -> void* {
     return fld[f] ? (char*)fld[f] + i * 4 : nullptr;
   });
 }
@@ -1126,10 +1309,10 @@ RTC_API ssize_t rtcGetDeviceProperty(RTCDevice hdevice, enum RTCDeviceProperty p
     case RTC_DEVICE_PROPERTY_BACKFACE_CULLING_CURVES_ENABLED:
     case RTC_DEVICE_PROPERTY_RAY_MASK_SUPPORTED:
     case RTC_DEVICE_PROPERTY_BACKFACE_CULLING_ENABLED:
-    case RTC_DEVICE_PROPERTY_FILTER_FUNCTION_SUPPORTED:
     case RTC_DEVICE_PROPERTY_IGNORE_INVALID_RAYS_ENABLED:
     case RTC_DEVICE_PROPERTY_COMPACT_POLYS_ENABLED: return 0;
     case RTC_DEVICE_PROPERTY_TRIANGLE_GEOMETRY_SUPPORTED: return 1;
+    case RTC_DEVICE_PROPERTY_FILTER_FUNCTION_SUPPORTED: return 1;
     case RTC_DEVICE_PROPERTY_QUAD_GEOMETRY_SUPPORTED:
     case RTC_DEVICE_PROPERTY_SUBDIVISION_GEOMETRY_SUPPORTED:
     case RTC_DEVICE_PROPERTY_CURVE_GEOMETRY_SUPPORTED:
@@ -1381,11 +1564,15 @@ RTC_API void rtcUpdateGeometryBuffer(RTCGeometry hg, enum RTCBufferType type, un
   API_END(g ? g->device : nullptr)
 }
 
+// Geometry::setIntersectionFilterFunctionN / setOcclusionFilterFunctionN
+// (kernels/common/geometry.cpp:136-150): triangle meshes take callbacks, instances do not
 RTC_API void rtcSetGeometryIntersectFilterFunction(RTCGeometry hg, RTCFilterFunctionN filter) {
   Geometry* g = (Geometry*)hg;
   API_BEGIN
   VERIFY_HANDLE(hg);
-  if (filter) fail(RTC_ERROR_INVALID_OPERATION, "filter functions are not supported by the GPU path");
+  if (g->type != RTC_GEOMETRY_TYPE_TRIANGLE)
+    fail(RTC_ERROR_INVALID_OPERATION, "filter functions not supported for this geometry");
+  g->ifilter = filter;
   API_END(g ? g->device : nullptr)
 }
 
@@ -1393,7 +1580,9 @@ RTC_API void rtcSetGeometryOccludedFilterFunction(RTCGeometry hg, RTCFilterFunct
   Geometry* g = (Geometry*)hg;
   API_BEGIN
   VERIFY_HANDLE(hg);
-  if (filter) fail(RTC_ERROR_INVALID_OPERATION, "filter functions are not supported by the GPU path");
+  if (g->type != RTC_GEOMETRY_TYPE_TRIANGLE)
+    fail(RTC_ERROR_INVALID_OPERATION, "filter functions not supported for this geometry");
+  g->ofilter = filter;
   API_END(g ? g->device : nullptr)
 }
 
@@ -1642,12 +1831,11 @@ RTC_API void rtcGetSceneLinearBounds(RTCScene hs, struct RTCLinearBounds* b) {
 RTC_API void rtcIntersect1(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRayHit* rayhit) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
   VERIFY_HANDLE(hs);
   if (!rayhit) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
   // rtcore.cpp:609-612: a single ray is traced only when tnear <= tfar
   if (!(rayhit->ray.tnear <= rayhit->ray.tfar)) return;
-  run_query(s, rayhit, 1, sizeof(RTCRayHit), false, sizeof(RTCRayHit));
+  run_query(s, rayhit, 1, sizeof(RTCRayHit), false, sizeof(RTCRayHit), nullptr, nullptr, ctx);
   API_END(s ? s->device : nullptr)
 }
 
@@ -1655,27 +1843,24 @@ RTC_API void rtcIntersect1M(RTCScene hs, struct RTCIntersectContext* ctx, struct
                             size_t byteStride) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
-  run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit));
+  run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit), nullptr, nullptr, ctx);
   API_END(s ? s->device : nullptr)
 }
 
 RTC_API void rtcIntersect1Mp(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRayHit** rayhit, unsigned int M) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
-  run_query_pointers<RTCRayHit>(s, rayhit, M, false);
+  run_query_pointers<RTCRayHit>(s, rayhit, M, false, ctx);
   API_END(s ? s->device : nullptr)
 }
 
 RTC_API void rtcOccluded1(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRay* ray) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
   VERIFY_HANDLE(hs);
   if (!ray) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
   if (!(ray->tnear <= ray->tfar)) return;
-  run_query(s, ray, 1, sizeof(RTCRay), true, sizeof(RTCRay));
+  run_query(s, ray, 1, sizeof(RTCRay), true, sizeof(RTCRay), nullptr, nullptr, ctx);
   API_END(s ? s->device : nullptr)
 }
 
@@ -1683,16 +1868,14 @@ RTC_API void rtcOccluded1M(RTCScene hs, struct RTCIntersectContext* ctx, struct 
                            size_t byteStride) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
-  run_query(s, ray, M, byteStride, true, sizeof(RTCRay));
+  run_query(s, ray, M, byteStride, true, sizeof(RTCRay), nullptr, nullptr, ctx);
   API_END(s ? s->device : nullptr)
 }
 
 RTC_API void rtcOccluded1Mp(RTCScene hs, struct RTCIntersectContext* ctx, struct RTCRay** ray, unsigned int M) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
-  run_query_pointers<RTCRay>(s, ray, M, true);
+  run_query_pointers<RTCRay>(s, ray, M, true, ctx);
   API_END(s ? s->device : nullptr)
 }
 
@@ -1700,10 +1883,9 @@ RTC_API void rtcOccluded1Mp(RTCScene hs, struct RTCIntersectContext* ctx, struct
   RTC_API void NAME(const int* valid, RTCScene hs, struct RTCIntersectContext* ctx, struct REC* r) { \
     Scene* s = (Scene*)hs;                                                                         \
     API_BEGIN                                                                                      \
-    (void)ctx;                                                                                     \
     VERIFY_HANDLE(hs);                                                                             \
     if (!valid) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid valid mask");                            \
-    run_query_packets(s, r, K, 1, sizeof(struct REC), valid, ANYHIT);                              \
+    run_query_packets(s, r, K, 1, sizeof(struct REC), valid, ANYHIT, ctx);                         \
     API_END(s ? s->device : nullptr)                                                               \
   }
 GB_PACKET_QUERY(rtcIntersect4, RTCRayHit4, 4, false)
@@ -1718,14 +1900,13 @@ RTC_API void rtcIntersectNM(RTCScene hs, struct RTCIntersectContext* ctx, struct
                             unsigned int M, size_t byteStride) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
   VERIFY_HANDLE(hs);
   // rtcore.cpp:672-686: N == 1 is an AOS stream of RTCRayHit records
   if (N == 1) {
     if (M == 1 && rayhit && !(((RTCRayHit*)rayhit)->ray.tnear <= ((RTCRayHit*)rayhit)->ray.tfar)) return;
-    run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit));
+    run_query(s, rayhit, M, byteStride, false, sizeof(RTCRayHit), nullptr, nullptr, ctx);
   } else if (N != 0 && M != 0) {
-    run_query_packets(s, rayhit, N, M, byteStride, nullptr, false);
+    run_query_packets(s, rayhit, N, M, byteStride, nullptr, false, ctx);
   }
   API_END(s ? s->device : nullptr)
 }
@@ -1734,10 +1915,9 @@ RTC_API void rtcIntersectNp(RTCScene hs, struct RTCIntersectContext* ctx, const 
                             unsigned int N) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
   VERIFY_HANDLE(hs);
   if (!rayhit) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
-  run_query_pointer_soa(s, rayhit, nullptr, N, false);
+  run_query_pointer_soa(s, rayhit, nullptr, N, false, ctx);
   API_END(s ? s->device : nullptr)
 }
 
@@ -1745,13 +1925,12 @@ RTC_API void rtcOccludedNM(RTCScene hs, struct RTCIntersectContext* ctx, struct 
                            unsigned int M, size_t byteStride) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
   VERIFY_HANDLE(hs);
   if (N == 1) {
     if (M == 1 && ray && !(((RTCRay*)ray)->tnear <= ((RTCRay*)ray)->tfar)) return;
-    run_query(s, ray, M, byteStride, true, sizeof(RTCRay));
+    run_query(s, ray, M, byteStride, true, sizeof(RTCRay), nullptr, nullptr, ctx);
   } else if (N != 0 && M != 0) {
-    run_query_packets(s, ray, N, M, byteStride, nullptr, true);
+    run_query_packets(s, ray, N, M, byteStride, nullptr, true, ctx);
   }
   API_END(s ? s->device : nullptr)
 }
@@ -1759,10 +1938,9 @@ RTC_API void rtcOccludedNM(RTCScene hs, struct RTCIntersectContext* ctx, struct 
 RTC_API void rtcOccludedNp(RTCScene hs, struct RTCIntersectContext* ctx, const struct RTCRayNp* ray, unsigned int N) {
   Scene* s = (Scene*)hs;
   API_BEGIN
-  (void)ctx;
   VERIFY_HANDLE(hs);
   if (!ray) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
-  run_query_pointer_soa(s, nullptr, ray, N, true);
+  run_query_pointer_soa(s, nullptr, ray, N, true, ctx);
   API_END(s ? s->device : nullptr)
 }
 

@@ -20,6 +20,7 @@ RTC_FORMAT_UINT3 = 0x5003
 RTC_FORMAT_FLOAT3 = 0x9003
 RTC_INVALID_GEOMETRY_ID = 0xFFFFFFFF
 RTC_SCENE_FLAG_ROBUST = 1 << 2
+RTC_SCENE_FLAG_CONTEXT_FILTER_FUNCTION = 1 << 3
 RTC_BUILD_QUALITY_REFIT = 3
 RTC_GEOMETRY_TYPE_INSTANCE = 121
 RTC_FORMAT_FLOAT3X4_ROW_MAJOR = 0x9134
@@ -59,6 +60,33 @@ class RTCBounds(ctypes.Structure):
 
 class RTCIntersectContext(ctypes.Structure):
     _fields_ = [("flags", ctypes.c_int), ("filter", ctypes.c_void_p), ("instID", ctypes.c_uint * 1)]
+
+
+class RTCFilterFunctionNArguments(ctypes.Structure):
+    _fields_ = [("valid", ctypes.POINTER(ctypes.c_int)), ("geometryUserPtr", ctypes.c_void_p),
+                ("context", ctypes.c_void_p), ("ray", ctypes.c_void_p), ("hit", ctypes.c_void_p),
+                ("N", ctypes.c_uint)]
+
+
+# void filter(const RTCFilterFunctionNArguments* args)
+FILTER_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(RTCFilterFunctionNArguments))
+
+
+def filter_callback(fn):
+    """Wraps a Python callable fn(geomID, primID, u, v, t) -> bool (True keeps
+    the hit) as an RTCFilterFunctionN for N = 1 calls."""
+    def cb(args):
+        a = args.contents
+        hf = ctypes.cast(a.hit, ctypes.POINTER(ctypes.c_float))
+        hu = ctypes.cast(a.hit, ctypes.POINTER(ctypes.c_uint))
+        rf = ctypes.cast(a.ray, ctypes.POINTER(ctypes.c_float))
+        for k in range(a.N):   # RTCHitN / RTCRayN: field f of lane k at f * N + k
+            if a.valid[k] == 0:
+                continue
+            n = a.N
+            if not fn(hu[6 * n + k], hu[5 * n + k], hf[3 * n + k], hf[4 * n + k], rf[8 * n + k]):
+                a.valid[k] = 0
+    return FILTER_FN(cb)
 
 
 class RTCGBBuildStats(ctypes.Structure):
@@ -297,6 +325,18 @@ class Scene:
         self.dev.check("add_instance")
         return gid
 
+    def set_filters(self, gid, intersect=None, occluded=None):
+        """rtcSetGeometryIntersectFilterFunction / rtcSetGeometryOccludedFilterFunction
+        on geometry gid with Python callables fn(geomID, primID, u, v, t) -> bool
+        (None removes a callback); takes effect at the next commit."""
+        g = ctypes.c_void_p(self.L.rtcGetGeometry(self.h, gid))
+        cbs = [filter_callback(f) if f is not None else None for f in (intersect, occluded)]
+        self._keep.append(cbs)
+        as_ptr = lambda c: ctypes.cast(c, ctypes.c_void_p) if c is not None else None  # noqa: E731
+        self.L.rtcSetGeometryIntersectFilterFunction(g, as_ptr(cbs[0]))
+        self.L.rtcSetGeometryOccludedFilterFunction(g, as_ptr(cbs[1]))
+        self.dev.check("rtcSetGeometry*FilterFunction")
+
     def update_vertices(self, gid, new_verts):
         """Writes new positions into geometry gid's shared vertex buffer and
         marks it updated (rtcUpdateGeometryBuffer); takes effect at commit."""
@@ -327,17 +367,26 @@ class Scene:
         self.dev.check("rtcgbGetSceneBuildStats")
         return {f: getattr(s, f) for f, _ in s._fields_}
 
-    def intersect(self, rays, stride=None, count=None):
-        """rtcIntersect1M on a host RTCRayHit array (in place)."""
-        ctx = RTCIntersectContext(0, None, (ctypes.c_uint * 1)(RTC_INVALID_GEOMETRY_ID))
+    @staticmethod
+    def _context(context_filter):
+        cb = filter_callback(context_filter) if context_filter is not None else None
+        ctx = RTCIntersectContext(0, ctypes.cast(cb, ctypes.c_void_p) if cb is not None else None,
+                                  (ctypes.c_uint * 1)(RTC_INVALID_GEOMETRY_ID))
+        return ctx, cb
+
+    def intersect(self, rays, stride=None, count=None, context_filter=None):
+        """rtcIntersect1M on a host RTCRayHit array (in place); context_filter:
+        optional callable fn(geomID, primID, u, v, t) -> bool set as the
+        intersect context's filter."""
+        ctx, _cb = self._context(context_filter)
         n = rays.shape[0] if count is None else count
         self.L.rtcIntersect1M(self.h, ctypes.byref(ctx), _ptr(rays), n, stride or rays.dtype.itemsize)
         self.dev.check("rtcIntersect1M")
         return rays
 
-    def occluded(self, rays, stride=None, count=None):
+    def occluded(self, rays, stride=None, count=None, context_filter=None):
         """rtcOccluded1M on a host RTCRay (or RTCRayHit) array (in place)."""
-        ctx = RTCIntersectContext(0, None, (ctypes.c_uint * 1)(RTC_INVALID_GEOMETRY_ID))
+        ctx, _cb = self._context(context_filter)
         n = rays.shape[0] if count is None else count
         self.L.rtcOccluded1M(self.h, ctypes.byref(ctx), _ptr(rays), n, stride or rays.dtype.itemsize)
         self.dev.check("rtcOccluded1M")

@@ -364,10 +364,15 @@ RTC_API void* rtcSetNewGeometryBuffer(RTCGeometry geometry, enum RTCBufferType t
 RTC_API void* rtcGetGeometryBufferData(RTCGeometry geometry, enum RTCBufferType type, unsigned int slot);
 /* replaces include/embree3/rtcore_geometry.h:186 / kernels/common/rtcore.cpp:1513 */
 RTC_API void rtcUpdateGeometryBuffer(RTCGeometry geometry, enum RTCBufferType type, unsigned int slot);
-/* replaces include/embree3/rtcore_geometry.h:190 / kernels/common/rtcore.cpp:1664 (filter callbacks are host code; setting one
-   raises RTC_ERROR_INVALID_OPERATION: the GPU path has no host callbacks) */
+/* replaces include/embree3/rtcore_geometry.h:190 / kernels/common/rtcore.cpp:1664.  Triangle meshes only
+   (RTC_ERROR_INVALID_OPERATION for instances, as geometry.cpp:136-142).  A scene that has a callback
+   on some geometry, or RTC_SCENE_FLAG_CONTEXT_FILTER_FUNCTION, at commit calls the callbacks (and
+   RTCIntersectContext::filter) during rtcIntersect* / rtcOccluded*: the traversal runs on the GPU,
+   the callbacks on the calling thread with N = 1, and each ray is traced again until its nearest
+   hit is accepted.  Not with instances, batched or learned queries (RTC_ERROR_INVALID_OPERATION). */
 RTC_API void rtcSetGeometryIntersectFilterFunction(RTCGeometry geometry, RTCFilterFunctionN filter);
-/* replaces include/embree3/rtcore_geometry.h:193 / kernels/common/rtcore.cpp:1674 (same restriction as above) */
+/* replaces include/embree3/rtcore_geometry.h:193 / kernels/common/rtcore.cpp:1674 (as above, for
+   rtcOccluded*: a ray is occluded iff some hit in range is accepted) */
 RTC_API void rtcSetGeometryOccludedFilterFunction(RTCGeometry geometry, RTCFilterFunctionN filter);
 /* replaces include/embree3/rtcore_geometry.h:224 / kernels/common/rtcore.cpp:996: the scene an
    RTC_GEOMETRY_TYPE_INSTANCE geometry instances (one instance level) */

@@ -101,8 +101,16 @@ struct OracleScene {
   float glo[3], ghi[3];
   int committed;
   int robust; /* RTC_SCENE_FLAG_ROBUST: Triangle4v leaves + Pluecker test */
+  orc_filter_fn ifilter, ofilter; /* filter callbacks (NULL: none) and their argument */
+  void* filter_user;
   pthread_mutex_t lock;
 };
+
+void orc_scene_set_filters(OracleScene* s, orc_filter_fn ifilter, orc_filter_fn ofilter, void* user) {
+  s->ifilter = ifilter;
+  s->ofilter = ofilter;
+  s->filter_user = user;
+}
 
 OracleScene* orc_scene_new(void) {
   OracleScene* s = (OracleScene*)calloc(1, sizeof(OracleScene));
@@ -808,9 +816,13 @@ static inline unsigned node_test(const ONode8* n, const TravRay* t, float dist[8
 }
 
 /* One Triangle4 block: all lanes against the same tfar, then the nearest
-   valid lane (lowest lane on ties, vfloat4_sse2.h:887-892) is committed. */
+   valid lane (lowest lane on ties, vfloat4_sse2.h:887-892) is committed.
+   With a filter callback (Intersect1EpilogM, intersector_epilog.h:237-276) the
+   nearest lane is offered to it: a rejected lane is dropped and the next
+   nearest offered; an accepted one is committed, tfar becomes its distance and
+   the lanes at that distance or nearer are still offered. */
 static inline int leaf_block_closest(const OTri4* tri, const ORay* r, float tfar_now, OHit* hit, OCount* cnt,
-                                     int robust) {
+                                     int robust, orc_filter_fn filter, void* fuser) {
   int valid[4];
   float tv[4];
   MHit h[4];
@@ -834,46 +846,70 @@ static inline int leaf_block_closest(const OTri4* tri, const ORay* r, float tfar
     any |= valid[i];
   }
   if (!any) return 0;
-  float best = INFINITY;
-  for (int i = 0; i < 4; i++)
-    if (valid[i] && tv[i] < best) best = tv[i];
-  int sel = -1;
-  for (int i = 0; i < 4 && sel < 0; i++)
-    if (valid[i] && tv[i] == best) sel = i;
-  if (sel < 0)
+  int found = 0;
+  for (;;) {
+    if (!(valid[0] | valid[1] | valid[2] | valid[3])) return found;
+    float best = INFINITY;
+    for (int i = 0; i < 4; i++)
+      if (valid[i] && tv[i] < best) best = tv[i];
+    int sel = -1;
     for (int i = 0; i < 4 && sel < 0; i++)
-      if (valid[i]) sel = i;
-  hit->valid = 1;
-  if (robust) {
-    hit->t = ph[sel].t;
-    pluecker_uv(&ph[sel], &hit->u, &hit->v);
-    hit->Ng = ph[sel].Ng;
-  } else {
-    const float rcp = 1.0f / h[sel].absDen;
-    hit->t = h[sel].T * rcp;
-    hit->u = h[sel].U * rcp;
-    hit->v = h[sel].V * rcp;
-    hit->Ng = h[sel].Ng;
+      if (valid[i] && tv[i] == best) sel = i;
+    if (sel < 0)
+      for (int i = 0; i < 4 && sel < 0; i++)
+        if (valid[i]) sel = i;
+    OHit c;
+    c.valid = 1;
+    if (robust) {
+      c.t = ph[sel].t;
+      pluecker_uv(&ph[sel], &c.u, &c.v);
+      c.Ng = ph[sel].Ng;
+    } else {
+      const float rcp = 1.0f / h[sel].absDen;
+      c.t = h[sel].T * rcp;
+      c.u = h[sel].U * rcp;
+      c.v = h[sel].V * rcp;
+      c.Ng = h[sel].Ng;
+    }
+    c.geomID = tri->geomID[sel];
+    c.primID = tri->primID[sel];
+    if (!filter) {
+      *hit = c;
+      return 1;
+    }
+    valid[sel] = 0;
+    if (!filter(fuser, c.geomID, c.primID, c.u, c.v, c.t)) continue;
+    *hit = c;
+    found = 1;
+    for (int i = 0; i < 4; i++) valid[i] &= tv[i] <= c.t;
   }
-  hit->geomID = tri->geomID[sel];
-  hit->primID = tri->primID[sel];
-  return 1;
 }
 
-static inline int leaf_block_any(const OTri4* tri, const ORay* r, OCount* cnt, int robust) {
+/* With a filter callback (Occluded1EpilogM, intersector_epilog.h:397-435) the
+   hit lanes are offered to it in lane order until one is accepted. */
+static inline int leaf_block_any(const OTri4* tri, const ORay* r, OCount* cnt, int robust, orc_filter_fn filter,
+                                 void* fuser) {
   for (int i = 0; i < 4; i++) {
     if (tri->geomID[i] == INVALID_ID) continue;
     cnt->tris++;
     v3 a = {tri->v0[0][i], tri->v0[1][i], tri->v0[2][i]};
     v3 b = {tri->e1[0][i], tri->e1[1][i], tri->e1[2][i]};
     v3 c = {tri->e2[0][i], tri->e2[1][i], tri->e2[2][i]};
+    float t, u, v;
     if (robust) {
       PHit h;
-      if (pluecker(a, b, c, r->org, r->dir, r->tnear, r->tfar, &h)) return 1;
+      if (!pluecker(a, b, c, r->org, r->dir, r->tnear, r->tfar, &h)) continue;
+      t = h.t;
+      pluecker_uv(&h, &u, &v);
     } else {
       MHit h;
-      if (moeller(a, b, c, r->org, r->dir, r->tnear, r->tfar, &h)) return 1;
+      if (!moeller(a, b, c, r->org, r->dir, r->tnear, r->tfar, &h)) continue;
+      const float rcp = 1.0f / h.absDen;
+      t = h.T * rcp;
+      u = h.U * rcp;
+      v = h.V * rcp;
     }
+    if (!filter || filter(fuser, tri->geomID[i], tri->primID[i], u, v, t)) return 1;
   }
   return 0;
 }
@@ -927,7 +963,8 @@ static void trace_closest(const OracleScene* s, char* rec, OCount* cnt) {
     cnt->leaves++;
     const OLeaf* lf = &s->leaves[cur & ~LEAF_BIT];
     for (uint32_t b = 0; b < lf->nblocks; b++) {
-      if (leaf_block_closest(&s->tris[lf->first + b], &r, r.tfar, &hit, cnt, s->robust)) r.tfar = hit.t;
+      if (leaf_block_closest(&s->tris[lf->first + b], &r, r.tfar, &hit, cnt, s->robust, s->ifilter, s->filter_user))
+        r.tfar = hit.t;
     }
     t.tfar = r.tfar;
   }
@@ -967,7 +1004,7 @@ static void trace_occluded(const OracleScene* s, char* rec, OCount* cnt) {
     cnt->leaves++;
     const OLeaf* lf = &s->leaves[cur & ~LEAF_BIT];
     for (uint32_t b = 0; b < lf->nblocks; b++) {
-      if (leaf_block_any(&s->tris[lf->first + b], &r, cnt, s->robust)) {
+      if (leaf_block_any(&s->tris[lf->first + b], &r, cnt, s->robust, s->ofilter, s->filter_user)) {
         float ninf = -INFINITY;
         memcpy(rec + 32, &ninf, 4);
         return;

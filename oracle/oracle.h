@@ -66,6 +66,15 @@ int orc_scene_add_mesh(OracleScene* s, unsigned geomID,
    Takes effect at the next commit. */
 void orc_scene_set_robust(OracleScene* s, int robust);
 
+/* Filter callbacks, the oracle's form of rtcSetGeometryIntersectFilterFunction /
+   rtcSetGeometryOccludedFilterFunction (kernels/geometry/filter.h:14-37, 72-89):
+   called for every candidate hit the traversal meets with its geometry ID,
+   primitive ID, u, v and distance; returns 0 to reject the hit.  ifilter is
+   used by orc_intersect1M, ofilter by orc_occluded1M (NULL: no callback).  The
+   callbacks apply to every geometry of the scene. */
+typedef int (*orc_filter_fn)(void* user, unsigned geomID, unsigned primID, float u, float v, float t);
+void orc_scene_set_filters(OracleScene* s, orc_filter_fn ifilter, orc_filter_fn ofilter, void* user);
+
 /* Builds the BVH8 (binned SAH).  Returns the number of valid primitives. */
 long orc_scene_commit(OracleScene* s);
 

@@ -58,12 +58,18 @@ def lib():
         L.orc_moeller1.argtypes = [ctypes.POINTER(f)] * 5 + [f, f] + [ctypes.POINTER(f)] * 3
         L.orc_moeller1.restype = i
         L.orc_scene_set_robust.argtypes = [vp, i]
+        L.orc_scene_set_filters.argtypes = [vp, FILTER_FN, FILTER_FN, vp]
         L.orc_pluecker1.argtypes = [ctypes.POINTER(f)] * 5 + [f, f] + [ctypes.POINTER(f)] * 2
         L.orc_pluecker1.restype = i
         L.orc_intersect_instanced.argtypes = [vp, u, vp, vp, vp, vp, u, sz]
         L.orc_occluded_instanced.argtypes = [vp, u, vp, vp, vp, u, sz]
         _lib = L
     return _lib
+
+
+# int filter(void* user, unsigned geomID, unsigned primID, float u, float v, float t)
+FILTER_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_float,
+                             ctypes.c_float, ctypes.c_float)
 
 
 def _ptr(a):
@@ -84,6 +90,17 @@ class OracleScene:
             self._keep.append((verts, idx))
             L.orc_scene_add_mesh(self._h, gid, _ptr(verts), 12, verts.shape[0], _ptr(idx), 12, idx.shape[0])
         self.num_prims = L.orc_scene_commit(self._h)
+
+    def set_filters(self, intersect=None, occluded=None):
+        """Python callables f(geomID, primID, u, v, t) -> bool (True accepts the
+        hit) offered every candidate hit, as the reference's filter callbacks
+        are; None removes one."""
+        def wrap(fn):
+            if fn is None:
+                return FILTER_FN()
+            return FILTER_FN(lambda _user, g, p, u, v, t: 1 if fn(g, p, u, v, t) else 0)
+        self._filters = (wrap(intersect), wrap(occluded))   # kept alive with the scene
+        lib().orc_scene_set_filters(self._h, self._filters[0], self._filters[1], None)
 
     def close(self):
         if self._h:

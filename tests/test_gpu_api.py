@@ -79,8 +79,16 @@ def test_buffer_alignment_rules(rtc, device):
     assert device.error() == E_OP
     L.rtcSetSharedGeometryBuffer(g, 0, 1, 0x5003, ib.ctypes.data, 0, 12, 16)  # index slot 1
     assert device.error() == E_ARG
+    # filter callbacks: triangle meshes take them, instances do not (geometry.cpp:136-150)
     L.rtcSetGeometryIntersectFilterFunction(g, ctypes.c_void_p(1))
+    assert device.error() == E_NONE
+    L.rtcSetGeometryIntersectFilterFunction(g, None)
+    assert device.error() == E_NONE
+    gi = L.rtcNewGeometry(device.h, rtc.RTC_GEOMETRY_TYPE_INSTANCE)
+    L.rtcSetGeometryOccludedFilterFunction(gi, ctypes.c_void_p(1))
     assert device.error() == E_OP
+    L.rtcReleaseGeometry(gi)
+    assert L.rtcGetDeviceProperty(device.h, 66) == 1   # RTC_DEVICE_PROPERTY_FILTER_FUNCTION_SUPPORTED
     L.rtcReleaseGeometry(g)
     assert device.error() == E_NONE
 
