@@ -121,22 +121,29 @@ __device__ __forceinline__ void init_ray(TRay& r) {
   r.tnear_c = fmaxf(r.tnear, 0.0f);
 }
 
-// Byte k of w as a float (exact): 0x4B0000bb reinterpreted is 2^23 + bb.
+// Byte k of w as the float 1 + bb * 2^-15 (exact): one byte permute puts bb
+// in mantissa bits 8..15 under the exponent of 1.0 (0x3F80bb00).
 __device__ __forceinline__ float ubyte_f(uint32_t w, uint32_t k) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k)) - 8388608.0f;
+  return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (k << 4)));
 }
 
-// Rounding slack of the slab test, relative to (|p - o| + 256 s) |1/d|: the
-// computed slab distances carry at most ~5 unit roundoffs of that magnitude
-// (one each from p - o, the product with 1/d, 1/d itself, the FMA and the
-// subtraction of the slack); 8u = 2^-21 covers them with margin.
+// Rounding slack of the slab test, relative to (|p - o| + 2^15 s) |1/d|: the
+// computed slab distances carry at most ~6 unit roundoffs of that magnitude
+// (one each from p - o, the product with 1/d, 1/d itself, the offset a - 2^15 b,
+// the FMA and the subtraction of the slack); 8u = 2^-21 covers them with
+// margin.  The 2^15 s term widens a box by 2^15 * 8u = 1.6 % of one
+// quantisation step.
 constexpr float kSlabEps = 4.76837158e-7f;
 
 // Intersects the 8 children of `np`.  Child box planes are p + q * 2^e; with
-// a = (p - o) / d and b = 2^e / d precomputed per node and axis, a plane
-// distance is one FMA q * b + a, widened by the rounding slack (near planes
-// down, far planes up) so a box that contains an accepted intersection is
-// never culled.  Returns the node group of hit internal children (hit bits
+// B = 2^15 * 2^e / d and A = (p - o) / d - B precomputed per node and axis, a
+// plane distance is one FMA (1 + q * 2^-15) * B + A = (p - o) / d + q * 2^e / d,
+// whose first factor is the plane byte placed in a float's mantissa (no
+// integer-to-float conversion or subtraction per plane), widened by the
+// rounding slack (near planes down, far planes up) so a box that contains an
+// accepted intersection is never culled.  Where B overflows (a 2^55 scale and
+// |1/d| near 1e18) the products are NaN and fminf/fmaxf drop that plane, so
+// the box only grows.  Returns the node group of hit internal children (hit bits
 // 24..31 keyed by slot ^ oct, imask in bits 0..7) and the triangle group of
 // hit leaves (up to 32 triangle bits).
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, const TRay& r, const float tfar,
@@ -158,15 +165,17 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
     const float yo = __fsub_rn(__uint_as_float(n0.y), r.org.y);
     const float zo = __fsub_rn(__uint_as_float(n0.z), r.org.z);
     const float ax = __fmul_rn(xo, r.rdir.x), ay = __fmul_rn(yo, r.rdir.y), az = __fmul_rn(zo, r.rdir.z);
-    bx = __fmul_rn(sx, r.rdir.x);
-    by = __fmul_rn(sy, r.rdir.y);
-    bz = __fmul_rn(sz, r.rdir.z);
-    const float ex = __fmul_ru(__fmul_ru(__fmaf_ru(256.0f, sx, fabsf(xo)), fabsf(r.rdir.x)), kSlabEps);
-    const float ey = __fmul_ru(__fmul_ru(__fmaf_ru(256.0f, sy, fabsf(yo)), fabsf(r.rdir.y)), kSlabEps);
-    const float ez = __fmul_ru(__fmul_ru(__fmaf_ru(256.0f, sz, fabsf(zo)), fabsf(r.rdir.z)), kSlabEps);
-    anx = __fsub_rd(ax, ex); afx = __fadd_ru(ax, ex);
-    any_ = __fsub_rd(ay, ey); afy = __fadd_ru(ay, ey);
-    anz = __fsub_rd(az, ez); afz = __fadd_ru(az, ez);
+    // B = 2^15 s / d (exact scaling of s / d by a power of two), A = a - B
+    bx = __fmul_rn(sx * 32768.0f, r.rdir.x);
+    by = __fmul_rn(sy * 32768.0f, r.rdir.y);
+    bz = __fmul_rn(sz * 32768.0f, r.rdir.z);
+    const float ax2 = __fsub_rn(ax, bx), ay2 = __fsub_rn(ay, by), az2 = __fsub_rn(az, bz);
+    const float ex = __fmul_ru(__fmul_ru(__fmaf_ru(32768.0f, sx, fabsf(xo)), fabsf(r.rdir.x)), kSlabEps);
+    const float ey = __fmul_ru(__fmul_ru(__fmaf_ru(32768.0f, sy, fabsf(yo)), fabsf(r.rdir.y)), kSlabEps);
+    const float ez = __fmul_ru(__fmul_ru(__fmaf_ru(32768.0f, sz, fabsf(zo)), fabsf(r.rdir.z)), kSlabEps);
+    anx = __fsub_rd(ax2, ex); afx = __fadd_ru(ax2, ex);
+    any_ = __fsub_rd(ay2, ey); afy = __fadd_ru(ay2, ey);
+    anz = __fsub_rd(az2, ez); afz = __fadd_ru(az2, ez);
   }
   // near / far quantised planes by the ray direction's sign per axis
   const bool px = r.rdir.x >= 0.0f, py = r.rdir.y >= 0.0f, pz = r.rdir.z >= 0.0f;
