@@ -182,13 +182,18 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
   const uint32_t nx0 = px ? n2.x : n3.z, nx1 = px ? n2.y : n3.w, fx0 = px ? n3.z : n2.x, fx1 = px ? n3.w : n2.y;
   const uint32_t ny0 = py ? n2.z : n4.x, ny1 = py ? n2.w : n4.y, fy0 = py ? n4.x : n2.z, fy1 = py ? n4.y : n2.w;
   const uint32_t nz0 = pz ? n3.x : n4.z, nz1 = pz ? n3.y : n4.w, fz0 = pz ? n4.z : n3.x, fz1 = pz ? n4.w : n3.y;
-  const float tfar_c = fmaxf(tfar, 0.0f);
+  // + 0.0f turns a -0 into +0: the sign test below reads tmax - tmin, which
+  // must not be -0 for the equal interval [+0, +0]
+  const float tfar_c = fmaxf(tfar, 0.0f) + 0.0f;
   // the per-child work is only the slab test; the masks are built once per
   // node (ALU is the kernel's busiest pipe: this form measured 6-8 % faster
-  // than testing validity and expanding leaves per child)
-  uint32_t hit8 = 0;
+  // than testing validity and expanding leaves per child).  A child is missed
+  // when tmax - tmin is negative: its sign bit is shifted into miss8 by one
+  // funnel shift (children 7..0, so child s lands in bit s); an overflowed
+  // plane pair (inf - inf = NaN, positive) counts as a hit, as tmin <= tmax did.
+  uint32_t miss8 = 0;
 #pragma unroll
-  for (int s = 0; s < 8; s++) {
+  for (int s = 7; s >= 0; s--) {
     const uint32_t k = s & 3;
     const float tnx = __fmaf_rn(ubyte_f(s < 4 ? nx0 : nx1, k), bx, anx);
     const float tfx = __fmaf_rn(ubyte_f(s < 4 ? fx0 : fx1, k), bx, afx);
@@ -198,8 +203,9 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
     const float tfz = __fmaf_rn(ubyte_f(s < 4 ? fz0 : fz1, k), bz, afz);
     const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear_c));
     const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_c));
-    hit8 |= (tmin <= tmax ? 1u : 0u) << s;
+    miss8 = __funnelshift_l(__float_as_uint(__fsub_rn(tmax, tmin)), miss8, 1);
   }
+  uint32_t hit8 = ~miss8 & 0xFFu;
   // valid children have bit 7 of their meta byte set: gather the 8 bits
   const uint32_t valid8 = (((n1.z & 0x80808080u) * 0x00204081u) >> 28) | ((((n1.w & 0x80808080u) * 0x00204081u) >> 28) << 4);
   hit8 &= valid8;
