@@ -308,6 +308,7 @@ __device__ __forceinline__ void to_instance(const float* __restrict__ m, TRay& r
 // registers (under the same bound they would spill 32-150 bytes), and so does
 // the variant with per-ray exclusion lists (EXCL: filter callbacks).
 constexpr int TRACE_MIN_BLOCKS = 9;
+constexpr int kSharedStack = 8;  // traversal stack entries kept in shared memory
 
 template <bool ANYHIT, bool COUNT, bool ALIGNED, bool ROBUST, bool SEEDED, bool INST = false, bool EXCL = false>
 __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXCL) ? 1 : TRACE_MIN_BLOCKS)
@@ -317,8 +318,22 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXC
   const int lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t nrays = P.nrays_ptr ? *P.nrays_ptr : P.nrays;
+  // stack of node / triangle groups: the first kSharedStack entries live in
+  // shared memory ([entry][thread]: a warp's accesses are conflict-free), the
+  // deeper ones in local memory.  8 entries measured 2.6 % faster than an
+  // all-local stack (4: 2 % slower, 16: as 8 minus 0.5 %).
   uint2 stack[kStackSize];
   int sp = 0;
+  __shared__ uint2 s_stack[kSharedStack][TRACE_THREADS];
+  const int stk_tid = threadIdx.x;
+  auto push = [&](uint2 e) {
+    if (sp < kSharedStack) s_stack[sp][stk_tid] = e; else stack[sp] = e;
+    sp++;
+  };
+  auto pop = [&]() -> uint2 {
+    --sp;
+    return sp < kSharedStack ? s_stack[sp][stk_tid] : stack[sp];
+  };
   bool active = false, exhausted = false, seeding = false;
   char* rec = nullptr;
   TRay r;
@@ -381,12 +396,12 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXC
               // a virtual group (n, root bits) visits node n alone
               const uint4 s4 = P.seeds[rid];
               const uint32_t sd[4] = {s4.x, s4.y, s4.z, s4.w};
-              stack[sp++] = make_uint2(g_base, g_bits);
+              push(make_uint2(g_base, g_bits));
               seed_tri = kInvalidID;
               seeding = false;
               for (int q = 3; q >= 0; q--) {
                 if (sd[q] == 0u || sd[q] >= c.num_nodes) continue;
-                if (seeding) stack[sp++] = make_uint2(g_base, g_bits);
+                if (seeding) push(make_uint2(g_base, g_bits));
                 g_base = sd[q];
                 seeding = true;
               }
@@ -413,7 +428,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXC
       const uint32_t slot = k ^ r.oct;
       const uint32_t child = g_base + __popc(g_bits & ((1u << slot) - 1u) & 0xFFu);
       if (g_bits & 0xFF000000u) {
-        if (sp < kStackSize) stack[sp++] = make_uint2(g_base, g_bits);
+        if (sp < kStackSize) push(make_uint2(g_base, g_bits));
         else { atomicOr(c.err, kErrStackOverflow); active = false; }
       }
       if (active && child >= c.num_nodes) { atomicOr(c.err, kErrBuild); active = false; }
@@ -428,7 +443,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXC
     const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
     if (visited && t_bits != 0 && __popc(want) * 100 < __popc(act) * kPostponePct) {
       if (sp < kStackSize) {
-        stack[sp++] = make_uint2(t_base | kTriGroup, t_bits);
+        push(make_uint2(t_base | kTriGroup, t_bits));
         t_bits = 0;
       }
     }
@@ -457,9 +472,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXC
         if (sp + 3 > kStackSize) { atomicOr(c.err, kErrStackOverflow); active = false; break; }
         // the node group of this visit (its hit internal children) and the rest of this
         // leaf group resume after the instance
-        if (g_bits & 0xFF000000u) stack[sp++] = make_uint2(g_base, g_bits);
-        if (t_bits) stack[sp++] = make_uint2(t_base | kTriGroup, t_bits);
-        stack[sp++] = make_uint2(kInstMarker, 0u);
+        if (g_bits & 0xFF000000u) push(make_uint2(g_base, g_bits));
+        if (t_bits) push(make_uint2(t_base | kTriGroup, t_bits));
+        push(make_uint2(kInstMarker, 0u));
         t_bits = 0;
         cur_inst = ii;
         c.nodes = in->nodes;
@@ -505,7 +520,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, (COUNT || SEEDED || INST || EXC
     // ---- (3) next group from the stack, or finish
     if (active && !done && t_bits == 0 && !(g_bits & 0xFF000000u)) {
       if (sp > 0) {
-        const uint2 e = stack[--sp];
+        const uint2 e = pop();
         if (INST && e.x == kInstMarker && e.y == 0u) {
           // leaving the instance: world ray and top-level BVH again
           float unused_tfar;
