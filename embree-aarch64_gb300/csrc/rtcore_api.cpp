@@ -814,25 +814,21 @@ void run_filtered(Scene* scene, const RTCIntersectContext* uctx, void* rays, uns
     if (!(r.tnear <= r.tfar) || (anyhit && r.tfar < 0.0f)) continue;
     pend.push_back(i);
   }
-  std::vector<std::vector<uint2>> rejected(pend.size());  // per pending ray
+  // rejected (primID, geomID) lists of the pending rays, CSR: ray j's list is
+  // items[off[j] .. off[j+1]); rebuilt for the rays kept after each round
+  std::vector<uint32_t> off(pend.size() + 1, 0u), next_off;
+  std::vector<uint2> items, next_items;
   std::vector<RTCRayHit> work;
-  std::vector<uint32_t> off;
-  std::vector<uint2> items;
   float k_ms_total = 0.0f;
   unsigned launches = 0;
   const unsigned inst0 = uctx ? uctx->instID[0] : RTC_INVALID_GEOMETRY_ID;
   while (!pend.empty()) {
     const size_t n = pend.size();
     work.assign(n, RTCRayHit{});
-    off.resize(n + 1);
-    items.clear();
     for (size_t j = 0; j < n; j++) {
       std::memcpy(&work[j].ray, host + (size_t)pend[j] * stride, sizeof(RTCRay));
       work[j].hit.geomID = work[j].hit.primID = work[j].hit.instID[0] = RTC_INVALID_GEOMETRY_ID;
-      off[j] = (uint32_t)items.size();
-      items.insert(items.end(), rejected[j].begin(), rejected[j].end());
     }
-    off[n] = (uint32_t)items.size();
     // device layout: records (80 B each), list offsets, lists
     const size_t b_work = n * sizeof(RTCRayHit), b_off = ((n + 1) * 4 + 15) & ~size_t(15);
     char* d = c.buffer(b_work + b_off + items.size() * sizeof(uint2) + 16);
@@ -873,6 +869,8 @@ void run_filtered(Scene* scene, const RTCIntersectContext* uctx, void* rays, uns
     if (err & gb::kErrBuild) fail(RTC_ERROR_UNKNOWN, "traversal found an invalid BVH reference");
     // callbacks on this round's hits
     size_t keep = 0;
+    next_off.assign(1, 0u);
+    next_items.clear();
     for (size_t j = 0; j < n; j++) {
       const RTCRayHit& w = work[j];
       if (w.hit.geomID == RTC_INVALID_GEOMETRY_ID) continue;  // no further hit: done
@@ -913,15 +911,14 @@ void run_filtered(Scene* scene, const RTCIntersectContext* uctx, void* rays, uns
         }
         continue;
       }
-      rejected[j].push_back(make_uint2(w.hit.primID, w.hit.geomID));
-      if (keep != j) {
-        pend[keep] = pend[j];
-        rejected[keep].swap(rejected[j]);
-      }
-      keep++;
+      next_items.insert(next_items.end(), items.begin() + off[j], items.begin() + off[j + 1]);
+      next_items.push_back(make_uint2(w.hit.primID, w.hit.geomID));
+      next_off.push_back((uint32_t)next_items.size());
+      pend[keep++] = pend[j];
     }
     pend.resize(keep);
-    rejected.resize(keep);
+    off.swap(next_off);
+    items.swap(next_items);
   }
   if (on_device) {
     cuda_ok(cudaMemcpyAsync(rays, host, span, cudaMemcpyHostToDevice, st), "H2D results");
