@@ -203,6 +203,100 @@ struct RTCRayHitNp {
 };
 struct RTCRayHitN;  /* packets of runtime size N (SOA, rtcore_ray.h:209-230) */
 
+#if defined(__cplusplus)
+/* C++ accessors of runtime-N SOA packets (include/embree3/rtcore_ray.h:219-375), the
+   form filter callbacks read their RTCRayN / RTCHitN arguments in: field f of lane i
+   is element f * N + i of the packet (ray fields 0..11, hit fields 0..6, then the
+   instance IDs, one row of N per level). */
+#define RTCGB_SOA_ACCESSOR(PACKET, FIELD, TYPE, INDEX)                                      \
+  RTC_FORCEINLINE TYPE& PACKET##_##FIELD(PACKET* p, unsigned int N, unsigned int i) {        \
+    return ((TYPE*)p)[(INDEX) * N + i];                                                      \
+  }
+RTCGB_SOA_ACCESSOR(RTCRayN, org_x, float, 0)
+RTCGB_SOA_ACCESSOR(RTCRayN, org_y, float, 1)
+RTCGB_SOA_ACCESSOR(RTCRayN, org_z, float, 2)
+RTCGB_SOA_ACCESSOR(RTCRayN, tnear, float, 3)
+RTCGB_SOA_ACCESSOR(RTCRayN, dir_x, float, 4)
+RTCGB_SOA_ACCESSOR(RTCRayN, dir_y, float, 5)
+RTCGB_SOA_ACCESSOR(RTCRayN, dir_z, float, 6)
+RTCGB_SOA_ACCESSOR(RTCRayN, time, float, 7)
+RTCGB_SOA_ACCESSOR(RTCRayN, tfar, float, 8)
+RTCGB_SOA_ACCESSOR(RTCRayN, mask, unsigned int, 9)
+RTCGB_SOA_ACCESSOR(RTCRayN, id, unsigned int, 10)
+RTCGB_SOA_ACCESSOR(RTCRayN, flags, unsigned int, 11)
+RTCGB_SOA_ACCESSOR(RTCHitN, Ng_x, float, 0)
+RTCGB_SOA_ACCESSOR(RTCHitN, Ng_y, float, 1)
+RTCGB_SOA_ACCESSOR(RTCHitN, Ng_z, float, 2)
+RTCGB_SOA_ACCESSOR(RTCHitN, u, float, 3)
+RTCGB_SOA_ACCESSOR(RTCHitN, v, float, 4)
+RTCGB_SOA_ACCESSOR(RTCHitN, primID, unsigned int, 5)
+RTCGB_SOA_ACCESSOR(RTCHitN, geomID, unsigned int, 6)
+#undef RTCGB_SOA_ACCESSOR
+RTC_FORCEINLINE unsigned int& RTCHitN_instID(RTCHitN* hit, unsigned int N, unsigned int i, unsigned int l) {
+  return ((unsigned int*)hit)[(7 + l) * N + i];
+}
+/* an RTCRayHitN packet: N rays (12 fields), then N hits */
+RTC_FORCEINLINE RTCRayN* RTCRayHitN_RayN(RTCRayHitN* rayhit, unsigned int N) {
+  (void)N;
+  return (RTCRayN*)rayhit;
+}
+RTC_FORCEINLINE RTCHitN* RTCRayHitN_HitN(RTCRayHitN* rayhit, unsigned int N) {
+  return (RTCHitN*)((float*)rayhit + 12 * N);
+}
+
+/* packets of compile-time size N */
+template <int N>
+struct RTCRayNt {
+  float org_x[N], org_y[N], org_z[N], tnear[N];
+  float dir_x[N], dir_y[N], dir_z[N], time[N];
+  float tfar[N];
+  unsigned int mask[N], id[N], flags[N];
+};
+template <int N>
+struct RTCHitNt {
+  float Ng_x[N], Ng_y[N], Ng_z[N], u[N], v[N];
+  unsigned int primID[N], geomID[N];
+  unsigned int instID[RTC_MAX_INSTANCE_LEVEL_COUNT][N];
+};
+template <int N>
+struct RTCRayHitNt {
+  RTCRayNt<N> ray;
+  RTCHitNt<N> hit;
+};
+
+/* lane i of a packet as a single record, and back */
+RTC_FORCEINLINE RTCRay rtcGetRayFromRayN(RTCRayN* rayN, unsigned int N, unsigned int i) {
+  RTCRay r;
+  r.org_x = RTCRayN_org_x(rayN, N, i); r.org_y = RTCRayN_org_y(rayN, N, i); r.org_z = RTCRayN_org_z(rayN, N, i);
+  r.tnear = RTCRayN_tnear(rayN, N, i);
+  r.dir_x = RTCRayN_dir_x(rayN, N, i); r.dir_y = RTCRayN_dir_y(rayN, N, i); r.dir_z = RTCRayN_dir_z(rayN, N, i);
+  r.time = RTCRayN_time(rayN, N, i);
+  r.tfar = RTCRayN_tfar(rayN, N, i);
+  r.mask = RTCRayN_mask(rayN, N, i); r.id = RTCRayN_id(rayN, N, i); r.flags = RTCRayN_flags(rayN, N, i);
+  return r;
+}
+RTC_FORCEINLINE RTCHit rtcGetHitFromHitN(RTCHitN* hitN, unsigned int N, unsigned int i) {
+  RTCHit h;
+  h.Ng_x = RTCHitN_Ng_x(hitN, N, i); h.Ng_y = RTCHitN_Ng_y(hitN, N, i); h.Ng_z = RTCHitN_Ng_z(hitN, N, i);
+  h.u = RTCHitN_u(hitN, N, i); h.v = RTCHitN_v(hitN, N, i);
+  h.primID = RTCHitN_primID(hitN, N, i); h.geomID = RTCHitN_geomID(hitN, N, i);
+  for (unsigned int l = 0; l < RTC_MAX_INSTANCE_LEVEL_COUNT; l++) h.instID[l] = RTCHitN_instID(hitN, N, i, l);
+  return h;
+}
+RTC_FORCEINLINE void rtcCopyHitToHitN(RTCHitN* hitN, const RTCHit* hit, unsigned int N, unsigned int i) {
+  RTCHitN_Ng_x(hitN, N, i) = hit->Ng_x; RTCHitN_Ng_y(hitN, N, i) = hit->Ng_y; RTCHitN_Ng_z(hitN, N, i) = hit->Ng_z;
+  RTCHitN_u(hitN, N, i) = hit->u; RTCHitN_v(hitN, N, i) = hit->v;
+  RTCHitN_primID(hitN, N, i) = hit->primID; RTCHitN_geomID(hitN, N, i) = hit->geomID;
+  for (unsigned int l = 0; l < RTC_MAX_INSTANCE_LEVEL_COUNT; l++) RTCHitN_instID(hitN, N, i, l) = hit->instID[l];
+}
+RTC_FORCEINLINE RTCRayHit rtcGetRayHitFromRayHitN(RTCRayHitN* rayhitN, unsigned int N, unsigned int i) {
+  RTCRayHit rh;
+  rh.ray = rtcGetRayFromRayN(RTCRayHitN_RayN(rayhitN, N), N, i);
+  rh.hit = rtcGetHitFromHitN(RTCRayHitN_HitN(rayhitN, N), N, i);
+  return rh;
+}
+#endif
+
 /* ---------------------------------------------------------------------- */
 /* Device (include/embree3/rtcore_device.h)                                */
 /* ---------------------------------------------------------------------- */

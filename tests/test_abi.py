@@ -135,6 +135,51 @@ def test_packet_layouts(tmp_path):
     assert (back.view(np.uint8) == rh.view(np.uint8)).all()
 
 
+SOA_HELPERS_CPP = textwrap.dedent("""
+    #include <embree3/rtcore.h>
+    #include <cstdio>
+    // the way filter callbacks read their arguments
+    static void cutout(const RTCFilterFunctionNArguments* args) {
+      for (unsigned i = 0; i < args->N; i++)
+        if (RTCHitN_u(args->hit, args->N, i) < 0.5f) args->valid[i] = 0;
+    }
+    int main() {
+      RTCRayHitNt<4> p{};
+      for (int i = 0; i < 4; i++) {
+        p.ray.tfar[i] = 1.0f + i; p.ray.id[i] = 30 + i;
+        p.hit.u[i] = 0.25f * i; p.hit.primID[i] = 10 + i; p.hit.instID[0][i] = 20 + i;
+      }
+      RTCRayHitN* rh = (RTCRayHitN*)&p;
+      RTCRayN* r = RTCRayHitN_RayN(rh, 4);
+      RTCHitN* h = RTCRayHitN_HitN(rh, 4);
+      RTCRayHit one = rtcGetRayHitFromRayHitN(rh, 4, 2);
+      RTCHit last = rtcGetHitFromHitN(h, 4, 3);
+      last.primID = 99;
+      rtcCopyHitToHitN(h, &last, 4, 0);
+      int valid[4] = {-1, -1, -1, -1};
+      RTCFilterFunctionNArguments args = {valid, nullptr, nullptr, r, h, 4};
+      cutout(&args);
+      std::printf("%g %u %u %u %g %u %u %d %d %d %d\\n", RTCRayN_tfar(r, 4, 1), RTCHitN_primID(h, 4, 2),
+                  one.hit.instID[0], one.ray.id, one.ray.tfar, p.hit.primID[0], RTCHitN_instID(h, 4, 0, 0),
+                  valid[0], valid[1], valid[2], valid[3]);
+      return 0;
+    }
+""")
+
+
+def test_soa_helpers_for_filter_callbacks(tmp_path):
+    """The C++ RTCRayN / RTCHitN accessors and packet templates of the reference's
+    include/embree3/rtcore_ray.h:219-375 compile against the drop-in header and
+    address the SOA layout (field f of lane i at f * N + i)."""
+    src = tmp_path / "soa.cpp"
+    src.write_text(SOA_HELPERS_CPP)
+    exe = tmp_path / "soa"
+    subprocess.run(["g++", "-Wall", "-Werror", "-I", INC, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    # lane 0 now holds lane 3's hit (u = 0.75, kept); lane 1 has u = 0.25 (rejected)
+    assert out == ["2", "12", "22", "32", "3", "99", "23", "-1", "0", "-1", "-1"]
+
+
 def test_autotune_config_strings():
     """Autotuner candidates become rtcNewDevice configuration strings."""
     from rtcgb import autotune

@@ -25,6 +25,27 @@ PROGRAM = textwrap.dedent(r"""
 
     static void on_error(void*, RTCError code, const char* msg) { std::printf("error %d %s\n", (int)code, msg); }
 
+    // filter callbacks as Embree programs write them (RTCRayN / RTCHitN accessors)
+    static int filter_calls = 0;
+    static void reject_odd_ids(const RTCFilterFunctionNArguments* args) {
+      filter_calls++;
+      for (unsigned i = 0; i < args->N; i++)
+        if (RTCRayN_id(args->ray, args->N, i) & 1u) args->valid[i] = 0;
+    }
+    static void reject_all(const RTCFilterFunctionNArguments* args) {
+      filter_calls++;
+      for (unsigned i = 0; i < args->N; i++) args->valid[i] = 0;
+    }
+    static RTCGeometry triangle_at(RTCDevice device, float z) {
+      RTCGeometry g = rtcNewGeometry(device, RTC_GEOMETRY_TYPE_TRIANGLE);
+      float* v = (float*)rtcSetNewGeometryBuffer(g, RTC_BUFFER_TYPE_VERTEX, 0, RTC_FORMAT_FLOAT3, 3 * sizeof(float), 3);
+      unsigned* ix = (unsigned*)rtcSetNewGeometryBuffer(g, RTC_BUFFER_TYPE_INDEX, 0, RTC_FORMAT_UINT3, 3 * sizeof(unsigned), 1);
+      v[0] = 0.f; v[1] = 0.f; v[2] = z;  v[3] = 1.f; v[4] = 0.f; v[5] = z;  v[6] = 0.f; v[7] = 1.f; v[8] = z;
+      ix[0] = 0; ix[1] = 1; ix[2] = 2;
+      rtcCommitGeometry(g);
+      return g;
+    }
+
     int main() {
       RTCDevice device = rtcNewDevice(nullptr);
       rtcSetDeviceErrorFunction(device, on_error, nullptr);
@@ -65,6 +86,33 @@ PROGRAM = textwrap.dedent(r"""
       std::printf("stream hits %d\n", hits);
       rtcIntersect1M(scene, &ctx, nullptr, 5, sizeof(RTCRayHit));  // invalid argument
       std::printf("last error %d\n", (int)rtcGetDeviceError(device));
+      // two stacked triangles; the near one (z = 0) has filter callbacks
+      RTCScene layered = rtcNewScene(device);
+      RTCGeometry near_g = triangle_at(device, 0.f), far_g = triangle_at(device, 1.f);
+      rtcSetGeometryIntersectFilterFunction(near_g, reject_odd_ids);
+      rtcSetGeometryOccludedFilterFunction(near_g, reject_all);
+      rtcAttachGeometry(layered, near_g);
+      rtcAttachGeometry(layered, far_g);
+      rtcReleaseGeometry(near_g);
+      rtcReleaseGeometry(far_g);
+      rtcCommitScene(layered);
+      std::vector<RTCRayHit> four(4, rh);
+      for (int i = 0; i < 4; i++) {
+        four[i].ray.id = i;
+        four[i].ray.tfar = std::numeric_limits<float>::infinity();
+        four[i].hit.geomID = RTC_INVALID_GEOMETRY_ID;
+      }
+      rtcIntersect1M(layered, &ctx, four.data(), 4, sizeof(RTCRayHit));
+      std::printf("filtered");
+      for (const RTCRayHit& r : four) std::printf(" %u:%.3f", r.hit.geomID, r.ray.tfar);
+      std::printf("\n");
+      RTCRay shadows[2] = {rh.ray, rh.ray};
+      shadows[0].tfar = 1.5f;  // reaches only the near triangle, whose occlusion callback rejects
+      shadows[1].tfar = 2.5f;  // reaches the far one too
+      rtcOccluded1M(layered, &ctx, shadows, 2, sizeof(RTCRay));
+      std::printf("filtered occluded %d %d calls %d error %d\n", shadows[0].tfar < 0.f ? 1 : 0,
+                  shadows[1].tfar < 0.f ? 1 : 0, filter_calls, (int)rtcGetDeviceError(device));
+      rtcReleaseScene(layered);
       rtcReleaseScene(scene);
       rtcReleaseDevice(device);
       return 0;
@@ -94,3 +142,7 @@ def test_cpp_host_program_links_and_runs(tmp_path):
     assert inside <= hits <= inside + edge, (hits, inside, edge)
     # the callback saw the invalid argument, which also stays set for rtcGetDeviceError
     assert "error 2" in out and "last error 2" in out
+    # filter callbacks: odd ray IDs pass through the near triangle to the far one
+    assert "filtered 0:1.000 1:2.000 0:1.000 1:2.000" in out, out
+    # 4 intersect calls (one per ray's near hit) + 2 occlusion calls (each shadow ray's near hit)
+    assert "filtered occluded 0 1 calls 6 error 0" in out, out
