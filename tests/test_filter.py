@@ -49,20 +49,21 @@ def degenerate(idx):
     return out
 
 
-def test_oracle_filter_equals_scene_without_rejected_triangles(oracle):
+@pytest.mark.parametrize("robust", [False, True], ids=["moeller", "pluecker"])
+def test_oracle_filter_equals_scene_without_rejected_triangles(oracle, robust):
     verts, idx, rays, shadow = soup()
-    filt = oracle.OracleScene([(0, verts, idx)])
+    filt = oracle.OracleScene([(0, verts, idx)], robust=robust)
     filt.set_filters(intersect=lambda g, p, u, v, t: not prim_rejected(p),
                      occluded=lambda g, p, u, v, t: not prim_rejected(p))
     got = filt.intersect(rays.copy(), nthreads=4)
     sh = filt.occluded(shadow.copy(), nthreads=4)
-    cut = oracle.OracleScene([(0, verts, degenerate(idx))])
+    cut = oracle.OracleScene([(0, verts, degenerate(idx))], robust=robust)
     want = cut.intersect(rays.copy(), nthreads=4)
     sh_want = cut.occluded(shadow.copy(), nthreads=4)
     assert (got.view(np.uint8) == want.view(np.uint8)).all()
     assert np.array_equal(sh["tfar"] == -np.inf, sh_want["tfar"] == -np.inf)
     # the callback did remove hits
-    plain = oracle.OracleScene([(0, verts, idx)]).intersect(rays.copy(), nthreads=4)
+    plain = oracle.OracleScene([(0, verts, idx)], robust=robust).intersect(rays.copy(), nthreads=4)
     assert (plain["primID"] != got["primID"]).sum() > 100
     for s in (filt, cut):
         s.close()
