@@ -1,6 +1,7 @@
 """Builds the C-ABI shared library librtcore_gb300.so for sm_103a.
 
-Three translation units are compiled in parallel with nvcc and linked into
+Five translation units (builder, traversal, proposer, path tracer, C ABI)
+are compiled in parallel with nvcc and linked into
 one shared object (soname libembree3.so.3, so a program linked against the
 reference's library name finds it).  The traversal and builder units use
 --fmad=false: the hit-deciding arithmetic spells out every FMA itself.
