@@ -11,8 +11,11 @@ larger than the 129 MB L2.
 Arms:
   --impl gb (default)   the GPU library through its C ABI
   --impl reference      the reference path's CPU implementation on the host
-                        cores (the oracle port: the reference itself cannot be
-                        built here without its cmake build system)
+                        cores: the reference library compiled from its own
+                        sources (oracle/ref.mk) where its source tree is present;
+                        elsewhere the oracle port, scaled by the reference/port
+                        rate ratio measured on identical rays
+                        (oracle/ref_rates.json), both rates reported
 
 Multi-GPU (torchrun): every rank builds the same scene and traces its own 16M
 rays (weak scaling, no collective on the data path); the time is the maximum
@@ -181,57 +184,112 @@ def job_rate(units_per_rank, world, seconds):
 
 
 # ---------------------------------------------------------------------------
-# CPU arm (the oracle port of the reference path)
+# CPU arm: the reference itself where it is built, else the oracle port scaled
+# by the reference/port rate ratio measured on identical rays
 # ---------------------------------------------------------------------------
 
-def cpu_rate(verts, idx, rays, budget_s, shadow=False, orc=None, robust=False):
-    """Mrays/s of the oracle on all host threads over a bounded sample."""
+REF_RATES = os.path.join(REPO, "oracle", "ref_rates.json")
+
+
+def _ref_ffi():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle_ffi
-    t0 = time.perf_counter()
-    if orc is None:
-        orc = oracle_ffi.OracleScene([(0, verts, idx)], robust=robust)
-    build_s = time.perf_counter() - t0
+    import ref_ffi
+    return ref_ffi if ref_ffi.available() else None
+
+
+def ref_over_port(workload_key, query):
+    """Rate ratio reference / port measured on identical rays and threads on the host
+    that has the reference built (oracle/measure_ref_rates.py -> oracle/ref_rates.json)."""
+    try:
+        with open(REF_RATES) as f:
+            d = json.load(f)
+        w = d["workloads"][workload_key][query]
+        return float(w["ref_over_port"]), (f"{REF_RATES.split(REPO + os.sep)[1]}: reference and port on identical "
+                                           f"rays, {d['threads']} threads of {d['host']} ({d['machine']})")
+    except (OSError, KeyError, ValueError):
+        return None, "no measured ratio"
+
+
+def cpu_rate(verts, idx, rays, budget_s, shadow=False, orc=None, robust=False, workload_key="soup4M"):
+    """Mrays/s of the reference path on all host threads over a bounded sample of
+    `rays`: the reference library itself (1024-ray chunks, INCOHERENT context) where
+    oracle/_ref is built; otherwise the oracle port, whose rate is reported as
+    measured and, in `value`, scaled by the measured reference/port ratio."""
     cores = os.cpu_count() or 1
+    ref = _ref_ffi() if not robust else None
+    if orc is None:
+        t0 = time.perf_counter()
+        if ref is not None:
+            orc = ref.RefScene([(verts, idx)], threads=cores)
+        else:
+            sys.path.insert(0, os.path.join(REPO, "oracle"))
+            import oracle_ffi
+            orc = oracle_ffi.OracleScene([(0, verts, idx)], robust=robust)
+        orc._build_wall_s = time.perf_counter() - t0
+    is_ref = not hasattr(orc, "stats")
+    query = orc.occluded if shadow else orc.intersect
     n0 = min(rays.shape[0], 65536)
     probe = rays[:n0].copy()
     t = time.perf_counter()
-    (orc.occluded if shadow else orc.intersect)(probe)
+    query(probe)
     rate = n0 / max(time.perf_counter() - t, 1e-6)
     n = int(min(rays.shape[0], max(n0, rate * budget_s)))
     sample = np.ascontiguousarray(rays[:n].copy())
     t = time.perf_counter()
-    (orc.occluded if shadow else orc.intersect)(sample)
+    query(sample)
     dt = time.perf_counter() - t
-    return dict(value=n / dt / 1e6, unit="Mrays/s", cores=cores, kind="port",
-                sample=f"first {n} of {rays.shape[0]} rays of the same workload, all {cores} host threads",
-                build_s=build_s), orc, sample
+    measured = n / dt / 1e6
+    out = dict(unit="Mrays/s", cores=cores, build_s=getattr(orc, "_build_wall_s", 0.0),
+               sample=f"first {n} of {rays.shape[0]} rays of the same workload, all {cores} host threads")
+    if is_ref:
+        out.update(value=measured, kind="reference",
+                   isa="x86 AVX2 build of the reference's own sources (oracle/ref.mk), internal tasking, "
+                       "1024-ray chunks, INCOHERENT context")
+        if orc.build_stats:
+            out["reference_builder"] = orc.build_stats
+    else:
+        factor, src = ref_over_port(workload_key, "shadow" if shadow else "closest")
+        out.update(kind="port", port_measured=measured, value=measured * factor if factor else measured,
+                   scaled_by_ref_over_port=factor, factor_source=src,
+                   note="the reference's sources are not on this host; value = the port's measured rate x the "
+                        "reference/port ratio measured on identical rays where the reference is built")
+    return out, orc, sample
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     verts, idx, rays, label = workload(args.workload, args.scale)
+    key = "soup4M" if args.workload == "soup" else "heightfield256"
     per = []
-    base, orc, _ = cpu_rate(verts, idx, rays, 1.0, robust=args.robust)
+    base, orc, _ = cpu_rate(verts, idx, rays, 1.0, robust=args.robust, workload_key=key)
     for s in range(args.warmup + args.steps):
-        r, orc, sample = cpu_rate(verts, idx, rays, max(1.0, args.cpu_seconds / max(1, args.steps)), orc=orc)
+        r, orc, sample = cpu_rate(verts, idx, rays, max(1.0, args.cpu_seconds / max(1, args.steps)), orc=orc,
+                                  workload_key=key)
         if s >= args.warmup:
             per.append(r)
     value = statistics.median(p["value"] for p in per)
-    st = orc.stats()
+    cb = {k: per[-1][k] for k in per[-1] if k not in ("build_s", "reference_builder")}
+    cb["value"] = value
+    if "port_measured" in cb:
+        cb["port_measured"] = statistics.median(p["port_measured"] for p in per)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": float(sample.shape[0]) / (value * 1e6) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": label, "rays_per_step": int(sample.shape[0])},
-        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": per[-1]["cores"], "kind": "port",
-                         "sample": per[-1]["sample"]},
+        "cpu_baseline": cb,
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "build": {"seconds": base["build_s"], "Mtris_per_s": st.num_prims / base["build_s"] / 1e6,
-                  "sah": st.sah, "threads": 1},
     }
+    if cb["kind"] == "reference":
+        rb = base.get("reference_builder") or {}
+        line["build"] = {"commit_s": base["build_s"], "builder_s": rb.get("builder_s"), "sah": rb.get("sah"),
+                         "threads": base["cores"], "source": "BENCHMARK_BUILD line of the reference builder"}
+    else:
+        st = orc.stats()
+        line["build"] = {"seconds": base["build_s"], "Mtris_per_s": st.num_prims / base["build_s"] / 1e6,
+                         "sah": st.sah, "threads": 1, "source": "oracle port builder (single thread)"}
     print(json.dumps(line), flush=True)
 
 
@@ -530,21 +588,27 @@ def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds):
     torch.cuda.empty_cache()
     sc.release()
     if cpu_seconds > 0:
-        base, orc, sample = cpu_rate(verts, idx, rays, cpu_seconds)
-        orc.intersect(rays)  # every ray (the sample may be shorter)
+        base, cpu_scene, sample = cpu_rate(verts, idx, rays, cpu_seconds, workload_key="heightfield256")
+        if cpu_scene is not None and not hasattr(cpu_scene, "stats"):
+            cpu_scene.close()
+        out["cpu_baseline"] = {k: v for k, v in base.items() if k not in ("build_s", "reference_builder")}
+        # every ray against the oracle (same arithmetic: same-triangle hits bit-identical)
+        orc = oracle_scene([(verts, idx)])
+        ref = rays.copy()
+        orc.intersect(ref)
         sh_ref = shadow.copy()
         orc.occluded(sh_ref)
-        st = orc.stats()
+        out["parity"] = classified_parity(orc, rays, out_rays, ref)
+        out["parity"]["shadow_rays"] = n
+        out["parity"]["identical_occlusion"] = int(((sh_out["tfar"] < 0) == (sh_ref["tfar"] < 0)).sum())
+        # every ray against the reference's own outputs (tests/golden/ref_heightfield256.npz)
+        out["parity_vs_reference"] = fixture_parity(orc, out_rays, "heightfield256")
+        ref_sah = reference_sah("heightfield256")
+        out["build"]["sah_oracle_restatement"] = orc.stats().sah
+        out["build"]["sah_reference_builder"] = ref_sah or orc.stats().sah
+        out["build"]["sah_ratio"] = bst["sah"] / out["build"]["sah_reference_builder"]
+        out["build"]["sah_ratio_exact_boxes"] = bst["sah_exact"] / out["build"]["sah_reference_builder"]
         orc.close()
-        same = R.hits_equal_bits(out_rays, rays)
-        out["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
-        out["build"]["sah_reference_builder"] = st.sah
-        out["build"]["sah_ratio"] = bst["sah"] / st.sah
-        out["build"]["sah_ratio_exact_boxes"] = bst["sah_exact"] / st.sah
-        out["parity"] = {"rays": n, "identical_hits": int(same.sum()),
-                         "identical_ids": int(((out_rays["geomID"] == rays["geomID"]) &
-                                               (out_rays["primID"] == rays["primID"])).sum()),
-                         "shadow_rays": n, "identical_occlusion": int(((sh_out["tfar"] < 0) == (sh_ref["tfar"] < 0)).sum())}
     return out
 
 
@@ -633,8 +697,8 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
     import oracle_ffi
     res = work.cpu().numpy().view(R.RAYHIT_DTYPE).reshape(-1)
     src = pristine.cpu().numpy().view(R.RAYHIT_DTYPE).reshape(-1)
-    same = ties = total = done_tris = 0
-    verdicts = {}
+    same = total = done_tris = 0
+    classes = {"near_tie": 0, "fp32_tie": 0, "grazing": 0, "unexplained": 0}
     build_s = trace_s = 0.0
     order = list(range(0, nscenes, 8)) + [k for k in range(nscenes) if k % 8]
     scenes_done = 0
@@ -651,27 +715,20 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
         trace_s += time.perf_counter() - t
         ids = (ref["geomID"] == res["geomID"][lo:hi]) & (ref["primID"] == res["primID"][lo:hi])
         same += int(ids.sum())
-        # different triangles at the same distance (shared edges): ties of the visiting order
-        tie = ~ids & (ref["tfar"].view(np.uint32) == res["tfar"][lo:hi].view(np.uint32))
-        ties += int(tie.sum())
-        # the other differences go to the FP64 adjudicator (near tie, grazing, or which side is right)
-        for j in np.nonzero(~ids & ~tie)[0][:2000]:
+        # every differing ray is classified (parity rule: near tie, FP32 order tie, grazing)
+        for j in np.nonzero(~ids)[0]:
             g = res[lo + j]
-            code = orc.adjudicate(src[lo + j], (g["geomID"], g["primID"], g["tfar"]),
-                                  (ref["geomID"][j], ref["primID"][j], ref["tfar"][j]))
-            if code != 1 and orc.order_tie(src[lo + j], (g["geomID"], g["primID"]), (ref["geomID"][j], ref["primID"][j])):
-                code = 5
-            verdicts[code] = verdicts.get(code, 0) + 1
+            c = orc.classify(src[lo + j], (g["geomID"], g["primID"], g["tfar"]),
+                             (ref["geomID"][j], ref["primID"][j], ref["tfar"][j]))
+            classes[c if isinstance(c, str) else "unexplained"] += 1
         total += hi - lo
         done_tris += int(tris[k])
         scenes_done += 1
         orc.close()
     cores = os.cpu_count() or 1
-    names = {0: "real_mismatch", 1: "near_tie_fp64", 2: "grazing", 3: "gpu_right_fp64", 4: "oracle_right_fp64",
-             5: "fp32_order_tie"}
-    out["parity_sample"] = {"scenes": scenes_done, "rays": total, "identical_ids": same, "equal_t_ties": ties,
-                            "differing_not_tie": total - same - ties,
-                            "fp64_adjudicated": {names[k]: v for k, v in sorted(verdicts.items())}}
+    out["parity_sample"] = {"scenes": scenes_done, "rays": total, "identical_ids": same,
+                            "differing": total - same, "classes": classes,
+                            "rule": "differing ids must be near ties (FP64, 4 ulps), FP32 order ties or grazing"}
     out["cpu_baseline"] = {"value": total / (build_s + trace_s) / 1e6, "unit": "Mrays/s (build + trace)",
                            "cores": cores, "kind": "port",
                            "sample": f"{scenes_done} whole scenes ({done_tris} tris, {total} rays), built one after "
@@ -713,6 +770,53 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
     del pristine, work
     torch.cuda.empty_cache()
     return out
+
+
+REF_BUILD_STATS_NAME = os.path.join("tests", "golden", "ref_build_stats.json")
+
+
+def reference_sah(scene_key):
+    """SAH of the reference builder's own tree on a benchmark scene, from the committed
+    BENCHMARK_BUILD record (tests/golden/make_golden.py ran the reference)."""
+    try:
+        with open(os.path.join(REPO, REF_BUILD_STATS_NAME)) as f:
+            return float(json.load(f)["scenes"][scene_key]["sah"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def oracle_scene(meshes, robust=False):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_ffi
+    return oracle_ffi.OracleScene([(g, v, i) for g, (v, i) in enumerate(meshes)], robust=robust)
+
+
+def classified_parity(orc, rays_in, got, ref):
+    """geomID/primID of `got` against `ref` on the same input rays: identical, or a
+    classified tie (FP64 near tie within 4 ulps, FP32 order tie, grazing); anything
+    else is counted as unexplained. t/u/v: largest relative difference of same-triangle hits."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from parity import compare_closest
+    rep = compare_closest(orc, rays_in, got, ref)
+    out = {k: rep[k] for k in ("n", "hits", "id_mismatch", "near_tie", "fp32_tie", "grazing", "max_rel_tuv",
+                               "same_hit_bit_identical")}
+    out["unexplained"] = len(rep["failures"])
+    out["identical_ids"] = rep["n"] - rep["id_mismatch"]
+    return out
+
+
+def fixture_parity(orc, got_all, which, rays_all=None):
+    """The GPU's results on the rays of a reference-made fixture (tests/golden) against
+    the reference's own outputs."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import refgold
+    case = (refgold.soup4M_sample(verts_idx=(None, None), rays_all=rays_all) if which == "soup4M"
+            else refgold.heightfield256())
+    got = got_all[case["sel"]] if which == "soup4M" else got_all
+    rep = classified_parity(orc, case["rays"], got, case["expected"])
+    rep["fixture"] = os.path.join("tests", "golden", "ref_soup4M_sample.npz" if which == "soup4M"
+                                  else "ref_heightfield256.npz")
+    return rep
 
 
 def ctypes_ptr(p):
@@ -892,17 +996,28 @@ def run_gpu(args, rank, world):
                                               0.0 if args.no_cpu else min(3.0, args.cpu_seconds))
 
     if single and not args.no_cpu:
-        base, orc, sample = cpu_rate(verts, idx, rays, args.cpu_seconds, robust=args.robust)
-        st = orc.stats()
-        line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
-        line["build"]["sah_reference_builder"] = st.sah
-        line["build"]["sah_ratio"] = bst["sah"] / st.sah
-        line["build"]["sah_ratio_exact_boxes"] = bst["sah_exact"] / st.sah
-        line["build"]["reference_builder_s_1thread"] = base["build_s"]
-        # exact-hit check of the sampled rays against the oracle
+        key = "soup4M" if args.workload == "soup" else "heightfield256"
+        base, cpu_scene, sample = cpu_rate(verts, idx, rays, args.cpu_seconds, robust=args.robust, workload_key=key)
+        line["cpu_baseline"] = {k: v for k, v in base.items() if k not in ("build_s", "reference_builder")}
+        orc = cpu_scene if hasattr(cpu_scene, "stats") else oracle_scene([(verts, idx)], args.robust)
+        # the GPU builder's SAH over the reference builder's own (BENCHMARK_BUILD, committed)
+        ref_sah = reference_sah(key) if args.scale == 1.0 and not args.robust else None
+        orc_sah = orc.stats().sah
+        line["build"]["sah_oracle_restatement"] = orc_sah
+        line["build"]["sah_reference_builder"] = ref_sah if ref_sah else orc_sah
+        line["build"]["sah_reference_source"] = (REF_BUILD_STATS_NAME + " (the reference builder's BENCHMARK_BUILD)"
+                                                 if ref_sah else "oracle restatement of the reference builder")
+        line["build"]["sah_ratio"] = bst["sah"] / line["build"]["sah_reference_builder"]
+        line["build"]["sah_ratio_exact_boxes"] = bst["sah_exact"] / line["build"]["sah_reference_builder"]
+        line["build"]["cpu_build_s"] = base["build_s"]
+        # every sampled ray against the CPU arm's result, differences classified
         n = sample.shape[0]
-        same = (out["geomID"][:n] == sample["geomID"]) & (out["primID"][:n] == sample["primID"])
-        line["parity"] = {"rays": int(n), "identical_ids": int(same.sum()), "differing_ids": int((~same).sum())}
+        line["parity"] = classified_parity(orc, rays[:n], out[:n], sample)
+        line["parity"]["against"] = base["kind"]
+        if args.workload == "soup" and args.scale == 1.0 and not args.robust and rank == 0:
+            line["parity_vs_reference"] = fixture_parity(orc, out, "soup4M", rays_all=rays)
+        if orc is not cpu_scene:
+            orc.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

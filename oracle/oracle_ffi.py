@@ -143,7 +143,7 @@ class OracleScene:
         lib().orc_counters(c)
         return dict(nodes=c[0], leaves=c[1], tris=c[2])
 
-    def adjudicate(self, ray_in, hitA, hitB, tie_ulps=16):
+    def adjudicate(self, ray_in, hitA, hitB, tie_ulps=4):
         """ray_in: one RTCRayHit record as originally submitted.
         hitA/hitB: (geomID, primID, t)."""
         rec = np.ascontiguousarray(np.asarray(ray_in).reshape(1))
@@ -170,6 +170,21 @@ class OracleScene:
         ia = int(np.float32(ta).view(np.int32))
         ib = int(np.float32(tb).view(np.int32))
         return abs(ia - ib) <= max_ulps
+
+    def classify(self, ray_in, hitA, hitB, tie_ulps=4):
+        """Class of a ray whose two implementations report different triangles
+        (hits are (geomID, primID, t)): 'near_tie' (both hit in FP64, distances within
+        tie_ulps FP32 ulps), 'grazing' (within 1e-6 of an edge or of tnear/tfar),
+        'fp32_tie' (both pass the reference's FP32 test, distances within 2 ulps: the
+        test order decides), else ('fail', adjudicator code)."""
+        code = self.adjudicate(ray_in, hitA, hitB, tie_ulps)
+        if code == 1:
+            return "near_tie"
+        if code == 2:
+            return "grazing"
+        if self.order_tie(ray_in, hitA[:2], hitB[:2]):
+            return "fp32_tie"
+        return ("fail", int(code))
 
     def fp64_hit(self, ray_in, geomID, primID):
         rec = np.ascontiguousarray(np.asarray(ray_in).reshape(1))

@@ -116,7 +116,10 @@ def test_heightfield_config_parity(rtc, device, oracle):
     print(rep)
     assert_clean(rep)
     assert rep["hits"] > 300000
-    assert rep["id_mismatch"] <= 1e-3 * rep["n"]
+    # same arithmetic as the oracle: every differing id is a classified tie, and
+    # same-triangle hits are bit-identical
+    assert rep["id_mismatch"] <= 8
+    assert rep["same_hit_bit_differs"] == 0
 
 
 def test_soup_parity(rtc, device, oracle):

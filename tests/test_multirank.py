@@ -62,7 +62,9 @@ def test_max_over_ranks_without_group():
 
 def test_reference_arm_prints_on_rank_zero_only():
     """`bench.py --impl reference` under torchrun at world size 2: rank 0 times
-    the oracle and prints one JSON line, rank 1 exits 0 without work."""
+    the reference path on the host (the reference library where it is built, else
+    the oracle port scaled by the measured reference/port ratio) and prints one
+    JSON line, rank 1 exits 0 without work."""
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(REPO, "bench.py"),
@@ -75,5 +77,8 @@ def test_reference_arm_prints_on_rank_zero_only():
     assert len(lines) == 1, r.stdout
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0
-    assert line["cpu_baseline"]["kind"] == "port"
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port")
+    if cb["kind"] == "port":
+        assert cb["port_measured"] > 0 and cb["value"] == pytest.approx(cb["port_measured"] * cb["scaled_by_ref_over_port"])
     assert line["e2e"]["h2d_bytes_per_step"] == 0
