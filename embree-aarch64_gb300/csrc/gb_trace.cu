@@ -725,6 +725,22 @@ static cudaError_t noalloc_scratch(unsigned char** out) {
   return cudaSuccess;
 }
 
+// Resolves the scratch array's address and loads the four traversal kernels the
+// no-allocation query can launch (plain / robust, 16-byte aligned or not) on the
+// current device.  With CUDA's lazy loading, the module that holds the array and
+// each kernel's code would otherwise be loaded -- taking device memory -- by the
+// first query; the library calls this once per device when the device is created.
+cudaError_t noalloc_prepare() {
+  unsigned char* p = nullptr;
+  cudaError_t e = noalloc_scratch(&p);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes a;
+  if ((e = cudaFuncGetAttributes(&a, k_trace<false, false, true, false, false, false, false>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, k_trace<false, false, false, false, false, false, false>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, k_trace<false, false, true, true, false, false, false>)) != cudaSuccess) return e;
+  return cudaFuncGetAttributes(&a, k_trace<false, false, false, true, false, false, false>);
+}
+
 cudaError_t noalloc_closest(const DeviceBVH& bvh, char* rays, bool rays_on_device, uint32_t M, uint64_t stride,
                             cudaStream_t st, uint32_t* err_flags) {
   *err_flags = 0;

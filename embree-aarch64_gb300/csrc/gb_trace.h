@@ -47,6 +47,10 @@ cudaError_t order_rays(const char* rays, uint64_t stride, uint32_t M, const floa
 // Size of the staging area for host-resident rays in the no-allocation query.
 constexpr uint64_t kNoAllocStagingBytes = 32ull << 20;
 
+// Loads the no-allocation query's static scratch and kernels on the current
+// device (called once per device when the device is created).
+cudaError_t noalloc_prepare();
+
 // Closest-hit query whose scratch (fetch counter, error flags, staging for
 // host rays) is a static device array: it allocates no memory.  `rays` is
 // device-accessible memory when rays_on_device, else host memory whose span

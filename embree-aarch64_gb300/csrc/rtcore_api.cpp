@@ -103,6 +103,14 @@ struct Device : RefCounted {
     cudaDeviceGetAttribute(&pageable_access, cudaDevAttrPageableMemoryAccess, cuda_device);
     cudaDeviceGetAttribute(&host_ptr_registered, cudaDevAttrCanUseHostPointerForRegisteredMem, cuda_device);
     cudaGetLastError();
+    // rtcgbIntersect1MNoAlloc's static scratch (32 MiB + 256 B) and kernels are loaded
+    // now, on this device, so that no call of it loads them (and takes memory) later
+    int prev = 0;
+    cuda_ok(cudaGetDevice(&prev), "cudaGetDevice");
+    cuda_ok(cudaSetDevice(cuda_device), "cudaSetDevice");
+    cudaError_t e = gb::noalloc_prepare();
+    cudaSetDevice(prev);
+    cuda_ok(e, "no-allocation query set-up");
   }
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
@@ -2004,6 +2012,13 @@ RTC_API void rtcgbIntersect1MNoAlloc(RTCScene hs, struct RTCRayHit* rayhit, unsi
   if (!rayhit) fail(RTC_ERROR_INVALID_ARGUMENT, "invalid argument");
   if (((size_t)rayhit & 0x3) || (byteStride & 0x3)) fail(RTC_ERROR_INVALID_ARGUMENT, "ray not aligned to 4 bytes");
   if (byteStride < sizeof(RTCRayHit)) fail(RTC_ERROR_INVALID_ARGUMENT, "byteStride smaller than the ray record");
+  // the no-allocation query runs the plain traversal only: scenes whose queries need
+  // more (filter callbacks on the host, instance leaves, per-geometry batch roots) are
+  // refused rather than traced as if they were plain triangle scenes
+  if (s->filters) fail(RTC_ERROR_INVALID_OPERATION, "rtcgbIntersect1MNoAlloc: scene has filter callbacks");
+  if (s->ninsts || !s->inst_refs.empty())
+    fail(RTC_ERROR_INVALID_OPERATION, "rtcgbIntersect1MNoAlloc: scene has instances");
+  if (s->batched) fail(RTC_ERROR_INVALID_OPERATION, "rtcgbIntersect1MNoAlloc: batched scene");
   if (s->bvh.num_nodes == 0) return;
   s->device->set_current();
   const bool on_device = is_device_pointer(rayhit);

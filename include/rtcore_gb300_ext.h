@@ -88,11 +88,15 @@ RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, 
    RTCGB_NOALLOC_STAGING_BYTES (32 MiB) for staging host-resident rays.  Rays
    in device memory are traced in place at any size; host rays whose span
    ((M-1)*byteStride + 80 bytes) exceeds the staging area are rejected with
-   RTC_ERROR_INVALID_ARGUMENT.  The array's device address is looked up on
-   the first call on each device, so make that first call before any stream
-   capture.  All calls share the array and it keeps the last call's contents:
-   each call clears the state it needs, and calls whose GPU work overlaps
-   (different streams or host threads at the same time) race on it. */
+   RTC_ERROR_INVALID_ARGUMENT.  The array's device address is looked up, and
+   the kernels the call launches are loaded, when the device is created
+   (rtcNewDevice), so the 32 MiB are taken then and no call loads anything.
+   Scenes whose queries need more than the plain traversal -- filter
+   callbacks, instances, batched scenes -- are refused with
+   RTC_ERROR_INVALID_OPERATION.  All calls share the array and it keeps the
+   last call's contents: each call clears the state it needs, and calls whose
+   GPU work overlaps (different streams or host threads at the same time) race
+   on it. */
 #define RTCGB_NOALLOC_STAGING_BYTES 33554432u
 RTC_API void rtcgbIntersect1MNoAlloc(RTCScene scene, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride,
                                      void* cuda_stream);
