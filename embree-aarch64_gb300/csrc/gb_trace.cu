@@ -121,6 +121,18 @@ __device__ __forceinline__ void init_ray(TRay& r) {
   r.tnear_c = fmaxf(r.tnear, 0.0f);
 }
 
+// Three-input minimum / maximum (PTX ISA 8.8, sm_100 and later).
+__device__ __forceinline__ float fmax3(const float a, const float b, const float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float fmin3(const float a, const float b, const float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Byte k of w as the float 1 + bb * 2^-15 (exact): one byte permute puts bb
 // in mantissa bits 8..15 under the exponent of 1.0 (0x3F80bb00).
 __device__ __forceinline__ float ubyte_f(uint32_t w, uint32_t k) {
@@ -201,8 +213,8 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
     const float tfy = __fmaf_rn(ubyte_f(s < 4 ? fy0 : fy1, k), by, afy);
     const float tnz = __fmaf_rn(ubyte_f(s < 4 ? nz0 : nz1, k), bz, anz);
     const float tfz = __fmaf_rn(ubyte_f(s < 4 ? fz0 : fz1, k), bz, afz);
-    const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear_c));
-    const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_c));
+    const float tmin = fmax3(tnx, tny, fmaxf(tnz, r.tnear_c));
+    const float tmax = fmin3(tfx, tfy, fminf(tfz, tfar_c));
     miss8 = __funnelshift_l(__float_as_uint(__fsub_rn(tmax, tmin)), miss8, 1);
   }
   uint32_t hit8 = ~miss8 & 0xFFu;
