@@ -191,15 +191,28 @@ __device__ __forceinline__ uint64_t spread21(uint32_t x) {
   return v;
 }
 
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+  uint32_t v = x & 0x3FFu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
 // Segmented builds put the geometry slot (< kMaxSegments) in the key's top 12
 // bits, so the sort groups every geometry's primitives.
+// bits30 (gpu.morton_bits=30): 10 bits per axis, the lattice of the reference's
+// Morton builder (kernels/builders/bvh_builder_morton.h:62-86, LATTICE_BITS_PER_DIM
+// 10), so valid keys fit in 30 bits (42 with the slot) and the sort needs 4 (6)
+// digit passes instead of 8; invalid primitives get the all-ones key of that width.
 constexpr uint32_t kMaxSegments = 4096;
 
 __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                 uint32_t n, BoundsAcc* acc, uint64_t* __restrict__ keys,
-                                                uint32_t* __restrict__ vals, int cube, int segmented) {
+                                                uint32_t* __restrict__ vals, int cube, int segmented, int bits30) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t key = ~0ull;
+  uint64_t key = bits30 ? (~0ull >> (segmented ? 22 : 34)) : ~0ull;
   if (i < n) {
     const float4 a = plo[i], b = phi[i];
     if (a.x <= b.x) {
@@ -215,14 +228,26 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
       const float emin = fminf(fminf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
       const bool one_scale = cube == 1 || (cube == 2 && emin < 0.5f * emax);
       uint64_t code = 0;
+      if (bits30) {
+        uint32_t c30 = 0;
 #pragma unroll
-      for (int d = 0; d < 3; d++) {
-        const float ext = one_scale ? emax : hi[d] - lo[d];
-        float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
-        x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
-        code |= spread21((uint32_t)x) << (2 - d);
+        for (int d = 0; d < 3; d++) {
+          const float ext = one_scale ? emax : hi[d] - lo[d];
+          float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
+          x = fminf(fmaxf(x * 1024.0f, 0.0f), 1023.0f);
+          c30 |= spread10((uint32_t)x) << (2 - d);
+        }
+        key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 30) | c30 : c30;
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float ext = one_scale ? emax : hi[d] - lo[d];
+          float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
+          x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
+          code |= spread21((uint32_t)x) << (2 - d);
+        }
+        key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 51) | (code >> 12) : code;
       }
-      key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 51) | (code >> 12) : code;
     }
     keys[i] = key;
     vals[i] = i;
@@ -241,26 +266,183 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
 }
 
 // ---------------------------------------------------------------------------
-// 3. stable LSD radix sort (64-bit keys, 32-bit values)
+// 3. stable LSD radix sort (64-bit keys, 32-bit values), onesweep style
 // ---------------------------------------------------------------------------
+//
+// One pass over the keys counts every digit (8 bits each) at once; its last CTA
+// turns the counts into each digit's bucket bases.  Then one scatter kernel per
+// digit pass: CTAs take 4096-key tiles in ticket order, publish their digit counts
+// and find the counts of all tiles before them by decoupled look-back (Merrill &
+// Garland, "Single-pass Parallel Prefix Scan with Decoupled Look-back", 2016), rank
+// their keys stably and scatter them.  No scan kernels and no host reads.  The
+// reference's CPU sort (common/algorithms/parallel_sort.h:256-449) is the same
+// stable 8-bit LSD sort, one histogram + scatter round per digit over task blocks.
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift,
-                                                        uint32_t* __restrict__ hist, uint32_t nblocks) {
-  __shared__ uint32_t s_h[256];
-  s_h[threadIdx.x] = 0;
+// look-back status words: flag bits over a 30-bit count
+constexpr uint32_t kLbAggregate = 1u << 30;   // the tile's own count is published
+constexpr uint32_t kLbPrefix = 2u << 30;      // the inclusive prefix through the tile is published
+constexpr uint32_t kLbValue = (1u << 30) - 1u;
+constexpr uint32_t kLbSpinLimit = 1u << 22;   // re-reads of an unpublished word before giving up
+// onesweep scratch (uint32 words, zeroed before each sort): bucket bases of the 8
+// digit passes, tile tickets per pass, the histogram kernel's done counter, an
+// error word, then per pass ntiles x 256 look-back status words
+constexpr uint32_t kOsBases = 0, kOsTickets = 8 * 256, kOsDone = kOsTickets + 8, kOsErr = kOsDone + 1;
+constexpr uint32_t kOsStatus = 2112;  // 16-byte aligned start of the status tables
+
+__device__ __forceinline__ void lb_store(uint32_t* p, uint32_t v) { *reinterpret_cast<volatile uint32_t*>(p) = v; }
+__device__ __forceinline__ uint32_t lb_load(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
+
+// Sum of the counts of the tiles before `tile` (status words status[j * stride],
+// j < tile), following the chain back to the nearest published inclusive prefix.
+// A word that stays unpublished for kLbSpinLimit re-reads sets kErrBuild in *err
+// and counts as zero (the sort's result is then invalid and the host reports it).
+__device__ __forceinline__ uint32_t lb_exclusive(const uint32_t* status, uint32_t tile, uint32_t stride,
+                                                 unsigned int* err) {
+  uint32_t excl = 0;
+  for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
+    uint32_t w = lb_load(status + (size_t)j * stride);
+    for (uint32_t it = 0; w == 0u && it < kLbSpinLimit; it++) {
+      __nanosleep(32);
+      w = lb_load(status + (size_t)j * stride);
+    }
+    if (w == 0u) {
+      atomicOr(err, kErrBuild);
+      break;
+    }
+    excl += w & kLbValue;
+    if (w & kLbPrefix) break;
+  }
+  return excl;
+}
+
+// Counts of every active digit (digit_mask bit d: digit d, bits 8d..8d+7) over all
+// keys; the last CTA writes each digit's exclusive bucket bases.
+__global__ void __launch_bounds__(256) k_os_hist(const uint64_t* __restrict__ keys, uint32_t n, uint32_t digit_mask,
+                                                 uint32_t* __restrict__ scratch) {
+  __shared__ uint32_t s_h[8][256];
+  __shared__ bool s_last;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int d = 0; d < 8; d++) s_h[d][tid] = 0;
   __syncthreads();
-  const uint32_t base = blockIdx.x * RS_TILE;
-#pragma unroll 4
-  for (int r = 0; r < RS_ITEMS; r++) {
-    const uint32_t i = base + r * RS_THREADS + threadIdx.x;
-    if (i < n) atomicAdd(&s_h[(uint32_t)(keys[i] >> shift) & 0xFFu], 1u);
+  for (uint32_t i = blockIdx.x * 256u + tid; i < n; i += gridDim.x * 256u) {
+    const uint64_t k = keys[i];
+#pragma unroll
+    for (int d = 0; d < 8; d++)
+      if (digit_mask >> d & 1u) atomicAdd(&s_h[d][(uint32_t)(k >> (8 * d)) & 0xFFu], 1u);
   }
   __syncthreads();
-  hist[threadIdx.x * nblocks + blockIdx.x] = s_h[threadIdx.x];
+#pragma unroll
+  for (int d = 0; d < 8; d++)
+    if ((digit_mask >> d & 1u) && s_h[d][tid]) atomicAdd(scratch + kOsBases + d * 256 + tid, s_h[d][tid]);
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = atomicAdd(scratch + kOsDone, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // exclusive scan of each digit's 256 counts (one bin per thread)
+  __shared__ uint32_t s_w[8];
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int d = 0; d < 8; d++) {
+    if (!(digit_mask >> d & 1u)) continue;
+    const uint32_t c = lb_load(scratch + kOsBases + d * 256 + tid);
+    uint32_t x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; w++) before += s_w[w];
+    scratch[kOsBases + d * 256 + tid] = before + x - c;
+    __syncthreads();
+  }
+}
+
+// One digit pass: tile `ticket` of kin/vin is ranked by digit (bits shift..shift+7)
+// and scattered stably to kout/vout.  status: this pass's ntiles x 256 table.
+__global__ void __launch_bounds__(RS_THREADS) k_os_scatter(const uint64_t* __restrict__ kin,
+                                                           const uint32_t* __restrict__ vin,
+                                                           uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           uint32_t n, int shift, uint32_t* __restrict__ scratch,
+                                                           uint32_t pass_slot, uint32_t* __restrict__ status,
+                                                           unsigned int* __restrict__ err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_hist[256];
+  __shared__ uint32_t s_run[256];
+  __shared__ uint32_t s_cnt[8][256];
+  __shared__ uint32_t s_off[8][256];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) s_tile = atomicAdd(scratch + kOsTickets + pass_slot, 1u);
+  s_hist[tid] = 0;
+#pragma unroll
+  for (int w = 0; w < 8; w++) s_cnt[w][tid] = 0;
+  __syncthreads();
+  const uint32_t tile = s_tile, base = tile * RS_TILE;
+  if (base >= n) return;  // (the grid has exactly one CTA per tile)
+  uint64_t k[RS_ITEMS];
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; r++) {
+    const uint32_t i = base + r * RS_THREADS + tid;
+    k[r] = i < n ? kin[i] : 0ull;
+    if (i < n) atomicAdd(&s_hist[(uint32_t)(k[r] >> shift) & 0xFFu], 1u);
+  }
+  __syncthreads();
+  // publish this tile's count of digit `tid`, then add up the tiles before it
+  {
+    const uint32_t c = s_hist[tid];
+    uint32_t excl = 0;
+    if (tile == 0) {
+      lb_store(status + tid, kLbPrefix | c);
+    } else {
+      lb_store(status + (size_t)tile * 256 + tid, kLbAggregate | c);
+      excl = lb_exclusive(status + tid, tile, 256, err);
+      lb_store(status + (size_t)tile * 256 + tid, kLbPrefix | ((excl + c) & kLbValue));
+    }
+    s_run[tid] = scratch[kOsBases + (shift >> 3) * 256 + tid] + excl;
+  }
+  __syncthreads();
+  // stable ranking: rounds in key order, warps in order within a round, lanes in
+  // order within a warp (match_any groups equal digits)
+  const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; r++) {
+    const uint32_t i = base + r * RS_THREADS + tid;
+    const bool in = i < n;
+    const uint32_t d = in ? (uint32_t)(k[r] >> shift) & 0xFFu : 256u;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    const uint32_t rank = __popc(peers & lt);
+    if (in && rank == 0) s_cnt[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t run = s_run[tid];
+#pragma unroll
+      for (int w = 0; w < 8; w++) {
+        const uint32_t c = s_cnt[w][tid];
+        s_off[w][tid] = run;
+        run += c;
+        s_cnt[w][tid] = 0;
+      }
+      s_run[tid] = run;
+    }
+    __syncthreads();
+    if (in) {
+      const uint32_t pos = s_off[warp][d] + rank;
+      if (pos < n) {
+        kout[pos] = k[r];
+        vout[pos] = vin[i];
+      } else {
+        atomicOr(err, kErrBuild);
+      }
+    }
+  }
 }
 
 // Exclusive scans of uint32 arrays.  One tile is 1024 threads x 8 consecutive
@@ -332,12 +514,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_excl(uint32_t* __restrict
   if (total && threadIdx.x == 0) *total = carry;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(const uint32_t* __restrict__ a, uint32_t n,
-                                                                 const uint32_t* __restrict__ d_n,
-                                                                 uint32_t* __restrict__ sums) {
+// Single-pass exclusive scan of larger arrays: CTAs take SCAN_TILE tiles in ticket
+// order, publish their tile sums and add up those of the tiles before them by
+// decoupled look-back, then scan their tile from that offset.  state: [0] ticket,
+// [1] CTAs finished, [2 + t] status word of tile t; zero on entry, and the last CTA
+// to finish zeroes it again for the next scan (graph replays included).
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_lb(uint32_t* __restrict__ a, uint32_t n,
+                                                          const uint32_t* __restrict__ d_n, uint32_t div,
+                                                          uint32_t* __restrict__ state, uint32_t* total,
+                                                          unsigned int* __restrict__ err) {
   __shared__ uint32_t s_w[32];
-  n = scan_count(n, d_n, 1);
-  for (uint32_t t = blockIdx.x; t * SCAN_TILE < n; t += gridDim.x) {
+  __shared__ uint32_t s_tile, s_excl;
+  __shared__ bool s_last;
+  n = scan_count(n, d_n, div);
+  const uint32_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (threadIdx.x == 0) s_tile = atomicAdd(state, 1u);
+  __syncthreads();
+  const uint32_t t = s_tile;
+  uint32_t* status = state + 2;
+  if (t < ntiles) {
     const uint32_t i0 = t * SCAN_TILE + threadIdx.x * SCAN_PER;
     uint32_t sum = 0;
 #pragma unroll
@@ -346,68 +541,36 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(const uint32_t*
     if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = sum;
     __syncthreads();
     if (threadIdx.x < 32) {
-      const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, s_w[threadIdx.x]);
-      if (threadIdx.x == 0) sums[t] = w;
+      const uint32_t tile_sum = __reduce_add_sync(0xFFFFFFFFu, s_w[threadIdx.x]);
+      if (threadIdx.x == 0) {
+        uint32_t excl = 0;
+        if (t == 0) {
+          lb_store(status, kLbPrefix | (tile_sum & kLbValue));
+        } else {
+          lb_store(status + t, kLbAggregate | (tile_sum & kLbValue));
+          excl = lb_exclusive(status, t, 1, err);
+          lb_store(status + t, kLbPrefix | ((excl + tile_sum) & kLbValue));
+        }
+        s_excl = excl;
+        if (t == ntiles - 1 && total) *total = excl + tile_sum;
+      }
     }
     __syncthreads();
+    scan_tile(a, n, t * SCAN_TILE, s_excl, s_w);
+  } else if (t == 0 && total && threadIdx.x == 0) {
+    *total = 0;  // empty input
   }
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(uint32_t* __restrict__ a, uint32_t n,
-                                                             const uint32_t* __restrict__ d_n,
-                                                             const uint32_t* __restrict__ offs) {
-  __shared__ uint32_t s_w[32];
-  n = scan_count(n, d_n, 1);
-  for (uint32_t t = blockIdx.x; t * SCAN_TILE < n; t += gridDim.x) scan_tile(a, n, t * SCAN_TILE, offs[t], s_w);
-}
-
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin,
-                                                           const uint32_t* __restrict__ vin,
-                                                           uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                           uint32_t n, int shift, const uint32_t* __restrict__ offs,
-                                                           uint32_t nblocks) {
-  __shared__ uint32_t s_run[256];
-  __shared__ uint32_t s_cnt[8][256];
-  __shared__ uint32_t s_off[8][256];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  s_run[tid] = offs[tid * nblocks + blockIdx.x];
-#pragma unroll
-  for (int w = 0; w < 8; w++) s_cnt[w][tid] = 0;
   __syncthreads();
-  const uint32_t base = blockIdx.x * RS_TILE;
-  const uint32_t lt = (1u << lane) - 1u;
-  for (int r = 0; r < RS_ITEMS; r++) {
-    const uint32_t i = base + r * RS_THREADS + tid;
-    const bool in = i < n;
-    uint64_t k = 0;
-    uint32_t v = 0, d = 256u;
-    if (in) {
-      k = kin[i];
-      v = vin[i];
-      d = (uint32_t)(k >> shift) & 0xFFu;
-    }
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-    const uint32_t rank = __popc(peers & lt);
-    if (in && rank == 0) s_cnt[warp][d] = __popc(peers);
-    __syncthreads();
-    {
-      uint32_t run = s_run[tid];
-#pragma unroll
-      for (int w = 0; w < 8; w++) {
-        const uint32_t c = s_cnt[w][tid];
-        s_off[w][tid] = run;
-        run += c;
-        s_cnt[w][tid] = 0;
-      }
-      s_run[tid] = run;
-    }
-    __syncthreads();
-    if (in) {
-      const uint32_t pos = s_off[warp][d] + rank;
-      if (pos < n) {
-        kout[pos] = k;
-        vout[pos] = v;
-      }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(state + 1, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    for (uint32_t j = threadIdx.x; j < gridDim.x; j += SCAN_THREADS) status[j] = 0;
+    if (threadIdx.x == 0) {
+      state[0] = 0;
+      state[1] = 0;
     }
   }
 }
@@ -1390,25 +1553,56 @@ static int num_sms_build() {
   return n;
 }
 
-// Entries of tile-sum scratch that scan_excl needs for n elements.
-static inline uint32_t scan_scratch(uint32_t n) { return cdiv(n, SCAN_TILE) + 1; }
+// Words of look-back state that scan_excl needs for n elements (ticket, done
+// counter, one status word per tile); zero when allocated, and every scan leaves
+// it zero again.
+static inline uint32_t scan_scratch(uint32_t n) { return cdiv(n, SCAN_TILE) + 2; }
 
-// Exclusive scan of a[0, n) in place (total to *total when non-null); sums
-// holds scan_scratch(n) entries.  With d_n the count is *d_n (at most n), read
-// on the device, so the scan can be enqueued before the count is known.
+// Exclusive scan of a[0, n) in place (total to *total when non-null); sums holds
+// scan_scratch(n) zeroed words.  With d_n the count is *d_n (at most n), read on
+// the device, so the scan can be enqueued before the count is known.  One launch:
+// one CTA for short arrays, else the look-back scan.
 static void scan_excl(uint32_t* a, uint32_t n, uint32_t* total, uint32_t* sums, cudaStream_t st,
-                      const uint32_t* d_n = nullptr) {
+                      unsigned int* err, const uint32_t* d_n = nullptr) {
   if (n <= 2 * SCAN_TILE) {
     k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(a, n, d_n, 1, total);
-    note_launches(1);
-    return;
+  } else {
+    k_scan_lb<<<cdiv(n, SCAN_TILE), SCAN_THREADS, 0, st>>>(a, n, d_n, 1, sums, total, err);
   }
-  const uint32_t nt = cdiv(n, SCAN_TILE);
-  const uint32_t grid = d_n ? std::min<uint32_t>(nt, 2 * (uint32_t)num_sms_build()) : nt;
-  k_scan_tile_sums<<<grid, SCAN_THREADS, 0, st>>>(a, n, d_n, sums);
-  k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(sums, nt, d_n, d_n ? SCAN_TILE : 1, total);
-  k_scan_tiles<<<grid, SCAN_THREADS, 0, st>>>(a, n, d_n, sums);
-  note_launches(3);
+  note_launches(1);
+}
+
+// Scratch words of onesweep_sort for n keys and `passes` digit passes.
+static inline size_t onesweep_scratch_words(uint32_t n, int passes) {
+  return kOsStatus + (size_t)passes * cdiv(n, RS_TILE) * 256u;
+}
+
+// Stable LSD sort of (ka, va) by the digits set in digit_mask (bit d: key bits
+// 8d..8d+7), least significant first, ping-ponging with (kb, vb): on return
+// (ka, va) name the buffers that hold the result.  scratch: at least
+// onesweep_scratch_words(n, passes) words, zeroed here.  A look-back that gives up
+// sets kErrBuild in *err (or in the scratch's error word when err is null).
+static cudaError_t onesweep_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& vb, uint32_t n,
+                                 uint32_t digit_mask, uint32_t* scratch, unsigned int* err, cudaStream_t st) {
+  const int passes = __builtin_popcount(digit_mask & 0xFFu);
+  if (n == 0 || passes == 0) return cudaSuccess;
+  if (n >= kLbValue) return cudaErrorInvalidValue;  // look-back counts are 30-bit
+  const uint32_t ntiles = cdiv(n, RS_TILE);
+  GB_CHECK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * onesweep_scratch_words(n, passes), st));
+  const uint32_t hgrid = std::min<uint32_t>(ntiles, 4u * (uint32_t)num_sms_build());
+  k_os_hist<<<hgrid, 256, 0, st>>>(ka, n, digit_mask & 0xFFu, scratch);
+  uint32_t slot = 0;
+  for (int d = 0; d < 8; d++) {
+    if (!(digit_mask >> d & 1u)) continue;
+    k_os_scatter<<<ntiles, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, 8 * d, scratch, slot,
+                                                 scratch + kOsStatus + (size_t)slot * ntiles * 256u,
+                                                 err ? err : scratch + kOsErr);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+    slot++;
+  }
+  note_launches(1 + passes);
+  return cudaGetLastError();
 }
 
 // Stream-ordered scratch of one build: device allocations, pinned host
@@ -1498,7 +1692,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   const bool segmented = opt.segmented != 0;
   const uint32_t nseg = segmented ? (uint32_t)ngeoms : 1u;
   if (segmented && (uint32_t)ngeoms > kMaxSegments) return cudaErrorInvalidValue;
-  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube, segmented ? 1 : 0);
+  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube, segmented ? 1 : 0,
+                                             opt.morton_bits == 30 ? 1 : 0);
   note_launches(1);
   GB_CHECK(cudaGetLastError());
   GB_CHECK(cudaMemcpyAsync(&h_acc, acc, sizeof(BoundsAcc), cudaMemcpyDeviceToHost, st));
@@ -1512,22 +1707,15 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     return cudaStreamSynchronize(st);
   }
 
-  // ---- radix sort (all `total` keys; invalid ones carry ~0 and sort last)
+  // ---- radix sort (all `total` keys; invalid ones carry ~0 and sort last), the
+  // digits that are constant over all keys skipped
   {
-    const uint32_t nb = cdiv(total, RS_TILE);
+    uint32_t digit_mask = 0;
+    for (int d = 0; d < 8; d++)
+      if (((h_acc.kand >> (8 * d)) & 0xFF) != ((h_acc.kor >> (8 * d)) & 0xFF)) digit_mask |= 1u << d;
     uint32_t* hist = nullptr;
-    GB_CHECK(arena.alloc(&hist, (size_t)sort_hist_entries(total)));
-    for (int pass = 0; pass < 8; pass++) {
-      const int shift = 8 * pass;
-      const uint64_t a = (h_acc.kand >> shift) & 0xFF, o = (h_acc.kor >> shift) & 0xFF;
-      if (a == o) continue;  // digit constant over all keys
-      k_rs_hist<<<nb, RS_THREADS, 0, st>>>(keys_a, total, shift, hist, nb); note_launches(1);
-      scan_excl(hist, 256 * nb, nullptr, hist + 256 * nb, st);
-      k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(keys_a, vals_a, keys_b, vals_b, total, shift, hist, nb); note_launches(1);
-      std::swap(keys_a, keys_b);
-      std::swap(vals_a, vals_b);
-    }
-    GB_CHECK(cudaGetLastError());
+    GB_CHECK(arena.alloc(&hist, onesweep_scratch_words(total, __builtin_popcount(digit_mask))));
+    GB_CHECK(onesweep_sort(keys_a, vals_a, keys_b, vals_b, total, digit_mask, hist, &acc->pad, st));
     arena.free(hist);
   }
 
@@ -1554,8 +1742,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   const uint32_t maxb = cdiv(N, PLOC_BLOCK);
   GB_CHECK(arena.alloc(&bsurv, maxb));
   GB_CHECK(arena.alloc(&bmerge, maxb));
-  uint32_t* scan_sums = nullptr;  // tile sums of the PLOC and collapse scans
+  uint32_t* scan_sums = nullptr;  // look-back state of the PLOC and collapse scans (zero between scans)
   GB_CHECK(arena.alloc(&scan_sums, scan_scratch(std::max(maxb, N))));
+  GB_CHECK(cudaMemsetAsync(scan_sums, 0, sizeof(uint32_t) * scan_scratch(std::max(maxb, N)), st));
   GB_CHECK(arena.alloc(&d_tot, 4));
   GB_CHECK(arena.alloc(&d_root, nseg));
   GB_CHECK(cudaMemsetAsync(d_root, 0xFF, sizeof(uint32_t) * nseg, st));
@@ -1589,8 +1778,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     }
     k_ploc_count<<<grid, PLOC_BLOCK, 0, st>>>(nn, ploc_state, bsurv, bmerge);
     note_launches(2);
-    scan_excl(bsurv, maxb, d_tot + 0, scan_sums, st, ploc_state + kPlocTiles);
-    scan_excl(bmerge, maxb, d_tot + 1, scan_sums, st, ploc_state + kPlocTiles);
+    scan_excl(bsurv, maxb, d_tot + 0, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
+    scan_excl(bmerge, maxb, d_tot + 1, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
     k_ploc_emit<<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ci[a], nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt,
                                              cl[b], ch[b], ci[b], nnodes_bin, &acc->pad);
     k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state);
@@ -1723,8 +1912,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     const uint32_t grid = cdiv(nitems_known, 128);
     k_collapse_count<<<grid, 128, 0, st>>>(bt, items[a], cstate, kids, nint, ntri);
     note_launches(1);
-    scan_excl(nint, nitems_known, d_tot + 0, scan_sums, st);
-    scan_excl(ntri, nitems_known, d_tot + 1, scan_sums, st);
+    scan_excl(nint, nitems_known, d_tot + 0, scan_sums, st, &acc->pad);
+    scan_excl(ntri, nitems_known, d_tot + 1, scan_sums, st, &acc->pad);
     k_collapse_emit<<<grid, COLLAPSE_THREADS, 0, st>>>(bt, kids, cstate, nint, ntri, wnodes, leaf_root, items[b],
                                                        d_sah, d_leaves, maxw, N, &acc->pad);
     k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels);
@@ -1882,6 +2071,8 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
   }
   g->acc = acc;
   e = cudaMemcpy(g->d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice);
+  // the scans' look-back state starts at zero and every scan leaves it so
+  if (e == cudaSuccess) e = cudaMemset(g->scan_sums, 0, sizeof(uint32_t) * scan_scratch(std::max(g->maxb, maxw)));
   if (e != cudaSuccess) graph_build_release(g);
   const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1895,20 +2086,14 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   k_acc_init<<<1, 32, 0, st>>>(acc);
   k_primrefs<<<cdiv(T, 256), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc);
   k_morton<<<cdiv(T, 256), 256, 0, st>>>(g.plo, g.phi, T, acc, g.keys_a, g.vals_a, g.opt.morton_cube,
-                                         g.opt.segmented ? 1 : 0);
+                                         g.opt.segmented ? 1 : 0, g.opt.morton_bits == 30 ? 1 : 0);
   note_launches(3);
-  // all 8 digits (the ordinary build skips constant ones: the same order)
+  // all digits of the key width (the ordinary build skips constant ones: the same order)
   uint64_t *ka = g.keys_a, *kb = g.keys_b;
   uint32_t *va = g.vals_a, *vb = g.vals_b;
-  for (int pass = 0; pass < 8; pass++) {
-    const int shift = 8 * pass;
-    k_rs_hist<<<g.rs_blocks, RS_THREADS, 0, st>>>(ka, T, shift, g.hist, g.rs_blocks);
-    scan_excl(g.hist, 256 * g.rs_blocks, nullptr, g.hist + 256 * g.rs_blocks, st);
-    k_rs_scatter<<<g.rs_blocks, RS_THREADS, 0, st>>>(ka, va, kb, vb, T, shift, g.hist, g.rs_blocks);
-    note_launches(2);
-    std::swap(ka, kb);
-    std::swap(va, vb);
-  }
+  // the digits the key width can use: 63-bit keys 8, 30-bit keys 4 (6 with the slot)
+  const uint32_t digits = g.opt.morton_bits == 30 ? (g.opt.segmented ? 0x3Fu : 0x0Fu) : 0xFFu;
+  GB_CHECK(onesweep_sort(ka, va, kb, vb, T, digits, g.hist, &acc->pad, st));
   // PLOC: a fixed number of rounds, then the one-CTA finish
   GB_CHECK(cudaMemsetAsync(g.d_root, 0xFF, sizeof(uint32_t) * g.nseg, st));
   GB_CHECK(cudaMemsetAsync(g.d_iters, 0, sizeof(uint32_t), st));
@@ -1928,8 +2113,8 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
       default: k_ploc_nn<PLOC_R_MAX><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
     }
     k_ploc_count<<<pgrid, PLOC_BLOCK, 0, st>>>(g.nn, g.ploc_state, g.bsurv, g.bmerge);
-    scan_excl(g.bsurv, g.maxb, g.d_tot + 0, g.scan_sums, st, g.ploc_state + kPlocTiles);
-    scan_excl(g.bmerge, g.maxb, g.d_tot + 1, g.scan_sums, st, g.ploc_state + kPlocTiles);
+    scan_excl(g.bsurv, g.maxb, g.d_tot + 0, g.scan_sums, st, &acc->pad, g.ploc_state + kPlocTiles);
+    scan_excl(g.bmerge, g.maxb, g.d_tot + 1, g.scan_sums, st, &acc->pad, g.ploc_state + kPlocTiles);
     k_ploc_emit<<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.cidx[a], g.nn, g.ploc_state, g.bsurv, g.bmerge,
                                               g.bnlo, g.bnhi, g.bncnt, g.clo[b], g.chi[b], g.cidx[b], nbin_cap,
                                               &acc->pad);
@@ -1967,8 +2152,8 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   for (uint32_t l = 0; l < g.plan.levels; l++) {
     const int a = l & 1, b = a ^ 1;
     k_collapse_count<<<cgrid, 128, 0, st>>>(bt, g.items[a], g.cstate, g.kids, g.nint, g.ntri);
-    scan_excl(g.nint, maxw, g.d_tot + 0, g.scan_sums, st, g.cstate + kColN);
-    scan_excl(g.ntri, maxw, g.d_tot + 1, g.scan_sums, st, g.cstate + kColN);
+    scan_excl(g.nint, maxw, g.d_tot + 0, g.scan_sums, st, &acc->pad, g.cstate + kColN);
+    scan_excl(g.ntri, maxw, g.d_tot + 1, g.scan_sums, st, &acc->pad, g.cstate + kColN);
     k_collapse_emit<<<cgrid, COLLAPSE_THREADS, 0, st>>>(bt, g.kids, g.cstate, g.nint, g.ntri, g.nodes, g.leaf_root,
                                                         g.items[b], g.d_sah, g.d_leaves, maxw, N, &acc->pad);
     k_collapse_advance<<<1, 32, 0, st>>>(g.d_tot, g.cstate, maxw, g.plan.levels);
@@ -2005,56 +2190,40 @@ void graph_build_release(GraphBuild* g) {
   *g = GraphBuild{};
 }
 
-// Sorts (key, value) pairs with the builder's radix sort (all 8 digits,
-// constant digits skipped).  Device pointers; results in keys/vals.
+// Sorts (key, value) pairs by their low `passes` digits with the builder's
+// radix sort.  Device pointers; results in keys/vals (even pass counts).
 cudaError_t sort_pairs_passes(uint64_t* keys, uint32_t* vals, uint64_t* kb, uint32_t* vb, uint32_t* hist, uint32_t n,
                               int passes, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (passes < 0 || passes > 8 || (passes & 1)) return cudaErrorInvalidValue;
-  const uint32_t nb = cdiv(n, RS_TILE);
   uint64_t* ka = keys;
   uint32_t* va = vals;
-  for (int pass = 0; pass < passes; pass++) {
-    const int shift = 8 * pass;
-    k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, shift, hist, nb);
-    scan_excl(hist, 256 * nb, nullptr, hist + 256 * nb, st);
-    k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
-    note_launches(2);
-    std::swap(ka, kb);
-    std::swap(va, vb);
-  }
-  return cudaGetLastError();
+  return onesweep_sort(ka, va, kb, vb, n, (1u << passes) - 1u, hist, nullptr, st);
 }
 
-// digit histograms of all tiles, then the scan's tile sums
-uint32_t sort_hist_entries(uint32_t n) { return 256u * cdiv(n, RS_TILE) + scan_scratch(256u * cdiv(n, RS_TILE)); }
+// onesweep scratch for all 8 digits of n keys
+uint32_t sort_hist_entries(uint32_t n) { return (uint32_t)onesweep_scratch_words(n, 8); }
 
 cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   uint64_t* kb = nullptr;
   uint32_t* vb = nullptr;
   uint32_t* hist = nullptr;
-  const uint32_t nb = cdiv(n, RS_TILE);
   GB_CHECK(dalloc(&kb, n, st));
   GB_CHECK(dalloc(&vb, n, st));
   GB_CHECK(dalloc(&hist, (size_t)sort_hist_entries(n), st));
   uint64_t* ka = keys;
   uint32_t* va = vals;
-  for (int pass = 0; pass < 8; pass++) {
-    const int shift = 8 * pass;
-    k_rs_hist<<<nb, RS_THREADS, 0, st>>>(ka, n, shift, hist, nb);
-    scan_excl(hist, 256 * nb, nullptr, hist + 256 * nb, st);
-    k_rs_scatter<<<nb, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, shift, hist, nb);
-    note_launches(2);
-    std::swap(ka, kb);
-    std::swap(va, vb);
-  }
-  GB_CHECK(cudaGetLastError());
-  // 8 passes: the result is back in the caller's buffers
+  cudaError_t e = onesweep_sort(ka, va, kb, vb, n, 0xFFu, hist, nullptr, st);  // 8 passes: back in keys/vals
+  uint32_t serr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&serr, hist + kOsErr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
   cudaFreeAsync(kb, st);
   cudaFreeAsync(vb, st);
   cudaFreeAsync(hist, st);
-  return cudaStreamSynchronize(st);
+  const cudaError_t s2 = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (s2 != cudaSuccess) return s2;
+  return serr ? cudaErrorUnknown : cudaSuccess;
 }
 
 

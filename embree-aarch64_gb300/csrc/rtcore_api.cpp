@@ -114,7 +114,7 @@ struct Device : RefCounted {
   }
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
-  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.collapse, gpu.ploc_radius,
+  // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.morton_bits, gpu.collapse, gpu.ploc_radius,
   // gpu.host_rays, gpu.proposer, gpu.reorder;
   // the CPU tasking and ISA keys
   // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
@@ -139,6 +139,7 @@ struct Device : RefCounted {
         else if (k == "gpu.morton") build_opt.morton_cube = v == "cube" ? 1 : v == "axis" ? 0 : 2;
         else if (k == "gpu.collapse") build_opt.collapse = v == "greedy" ? 0 : 1;
         else if (k == "gpu.ploc_radius") build_opt.ploc_radius = atoi(v.c_str());
+        else if (k == "gpu.morton_bits") build_opt.morton_bits = atoi(v.c_str()) == 30 ? 30 : 63;
         else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
         else if (k == "gpu.proposer") proposer_mma = (v == "mma");
         else if (k == "gpu.reorder") reorder = atoi(v.c_str());

@@ -229,7 +229,7 @@ def test_launch_counter_and_query_stats(rtc, device):
     st = rtc.last_query_stats()
     assert rtc.launch_count() >= mid + 1
     assert st["rays"] == rays.shape[0] and st["nodes"] > 0 and st["tris"] > 0
-    # host rays are read in place where the device can address host memory
-    # (48 B of ray record per ray), otherwise copied whole
+    # pageable host rays are read in place where the device can address pageable
+    # host memory (48 B of ray record per ray), otherwise copied whole
     direct = rtc.load().rtcgbGetDeviceHostAccess(device.h) & 1
     assert st["h2d_bytes"] == (rays.shape[0] * 48 if direct else rays.nbytes) and st["kernel_ms"] > 0

@@ -135,12 +135,15 @@ def test_autotuner_picks_the_fastest_candidate(rtc):
     assert best == min(results, key=lambda r: r["total_ms"])["config"]
 
 
-def test_batched_frame_graph_matches_separate_calls(rtc, device):
+@pytest.mark.parametrize("config", [b"", b"gpu.morton_bits=30"], ids=["key63", "key30"])
+def test_batched_frame_graph_matches_separate_calls(rtc, config):
     """A batched frame -- the rebuild of every BVH of the scene and the batched
     closest-hit query, captured into one CUDA graph with the copy that restores
     the rays -- gives the bytes of rtcCommitScene + rtcgbIntersect1MBatched on
-    the same rays, replay after replay; a new commit invalidates it."""
+    the same rays, replay after replay; a new commit invalidates it.  With 63-bit
+    and 30-bit sort keys."""
     torch = pytest.importorskip("torch")
+    device = rtc.Device(config)
     meshes = [W.heightfield(32, seed=5), W.gaussian_soup(30_000, seed=6), W.heightfield(20, seed=7),
               W.gaussian_soup(8_000, seed=8)]
     parts, start = [], [0]
@@ -172,3 +175,4 @@ def test_batched_frame_graph_matches_separate_calls(rtc, device):
         frame.replay()
     frame.release()
     sc.release()
+    device.release()

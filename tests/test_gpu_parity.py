@@ -298,7 +298,7 @@ def test_radix_sort_bit_exact_vs_host_stable_sort(rtc):
     rng = np.random.default_rng(5)
     # 300k and 2M keys: the digit histograms (256 per 4096-key tile) take the
     # multi-CTA scan (3 and 16 scan tiles)
-    for n in (1, 1000, 4097, 300_000, 2_000_000):
+    for n in (1, 1000, 4097, 300_000, 2_000_000, 9_000_000):
         keys = rng.integers(0, 1 << 20, n, dtype=np.uint64) << np.uint64(rng.integers(0, 40))
         keys[rng.random(n) < 0.1] = np.uint64(0xFFFFFFFFFFFFFFFF)
         vals = np.arange(n, dtype=np.uint32)
@@ -311,9 +311,9 @@ def test_radix_sort_bit_exact_vs_host_stable_sort(rtc):
 @pytest.mark.parametrize("mode", ["copy", "pipeline", "direct"])
 def test_host_ray_modes(rtc, mode):
     """Host-resident rays through each host path (copy all, chunked copy/trace
-    pipeline, direct access where the device can address host memory) give
-    the bytes of tracing the same rays in device memory, for pageable and
-    pinned host buffers."""
+    pipeline, direct access where the device can address host memory) give the bytes of tracing the
+    same rays in device memory, for pageable and pinned host buffers, 16-byte
+    aligned (stride 80) and not (stride 84), closest hit and occlusion."""
     torch = pytest.importorskip("torch")
     dev = rtc.Device(f"gpu.host_rays={mode}".encode())
     access = rtc.load().rtcgbGetDeviceHostAccess(dev.h)
@@ -336,13 +336,24 @@ def test_host_ray_modes(rtc, mode):
         assert st["h2d_bytes"] == rays.shape[0] * 48
     else:
         assert st["h2d_bytes"] == rays.nbytes
-    # occlusion through the same path
+    # unaligned records (stride 84) in pinned memory
+    n = 300_000
+    buf = np.zeros(n * 84, np.uint8)
+    buf.reshape(n, 84)[:, :80] = rays[:n].view(np.uint8).reshape(n, 80)
+    pin84 = torch.from_numpy(buf).pin_memory()
+    sc.intersect_ptr(pin84.data_ptr(), n, 84)
+    got84 = np.ascontiguousarray(pin84.numpy().reshape(n, 84)[:, :80])
+    assert (got84 == ref[:n].view(np.uint8).reshape(n, 80)).all()
+    # occlusion through the same paths, pageable and pinned
     shadow, _ = W.shadow_rays(ref, seed=43)
     a = shadow.copy()
     sc.occluded(a)
     ts = torch.from_numpy(shadow.view(np.uint8).copy()).cuda()
     sc.occluded_ptr(ts.data_ptr(), shadow.shape[0], 48)
     assert (a.view(np.uint8) == ts.cpu().numpy()).all()
+    ps = torch.from_numpy(shadow.view(np.uint8).copy()).pin_memory()
+    sc.occluded_ptr(ps.data_ptr(), shadow.shape[0], 48)
+    assert (ps.numpy() == ts.cpu().numpy()).all()
     sc.release()
     dev.release()
 
