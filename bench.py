@@ -756,13 +756,14 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
     # bitwise: the records' integer fields (e.g. instID = 0xFFFFFFFF) are NaN as floats
     same = bool(torch.equal(work.view(torch.int32), separate.view(torch.int32)))
     del separate
-    out["graph"] = {"frame": "ray restore copy + rebuild of all BVHs + batched closest-hit query, one CUDA graph launch",
+    out["graph"] = {"frame": "ray restore copy + rebuild of all BVHs (PLOC rounds and collapse levels in conditional "
+                             "WHILE nodes the device ends) + batched closest-hit query, one CUDA graph launch",
                     "ms_per_step": float(statistics.median(fms)),
                     "Mrays_per_s": nrays / (statistics.median(fms) * 1e-3) / 1e6,
                     "restore_copy_ms": float(statistics.median(copy_ms)),
                     "separate_parts_ms": float(statistics.median(copy_ms)) + float(statistics.median(builds)) + kernel_ms,
-                    "graph_nodes": fst["graph_nodes"], "ploc_rounds_enqueued": fst["ploc_rounds"],
-                    "levels_enqueued": fst["levels"], "build_status": fst["status"],
+                    "graph_nodes": fst["graph_nodes"], "ploc_rounds_device_loop": fst["ploc_rounds"],
+                    "levels_device_loop": fst["levels"], "build_status": fst["status"],
                     "identical_to_separate_calls": same}
     frame.release()
     sc.release()

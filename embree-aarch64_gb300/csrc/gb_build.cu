@@ -368,79 +368,108 @@ __global__ void __launch_bounds__(256) k_os_hist(const uint64_t* __restrict__ ke
 
 // One digit pass: tile `ticket` of kin/vin is ranked by digit (bits shift..shift+7)
 // and scattered stably to kout/vout.  status: this pass's ntiles x 256 table.
+// Warp w ranks keys base + w*512 .. +511 (16 rows of 32) by match_any into
+// per-warp digit counts; the tile's digit counts are published for the look-back;
+// the keys are placed in shared memory in (digit, original order) order and written
+// out in runs, consecutive threads to consecutive positions of a digit's bucket.
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr size_t kOsScatterSmem = (size_t)RS_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
+
 __global__ void __launch_bounds__(RS_THREADS) k_os_scatter(const uint64_t* __restrict__ kin,
                                                            const uint32_t* __restrict__ vin,
                                                            uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, uint32_t* __restrict__ scratch,
                                                            uint32_t pass_slot, uint32_t* __restrict__ status,
                                                            unsigned int* __restrict__ err) {
+  extern __shared__ uint64_t s_keys[];                                   // RS_TILE keys, then RS_TILE values
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + RS_TILE);
   __shared__ uint32_t s_tile;
-  __shared__ uint32_t s_hist[256];
-  __shared__ uint32_t s_run[256];
-  __shared__ uint32_t s_cnt[8][256];
-  __shared__ uint32_t s_off[8][256];
+  __shared__ uint32_t s_wcnt[RS_WARPS][256];  // per-warp digit counts, then per-warp offsets
+  __shared__ uint32_t s_lstart[256];          // tile-local start of each digit
+  __shared__ uint32_t s_glob[256];            // global position of local index 0 of each digit
+  __shared__ uint32_t s_w[RS_WARPS];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) s_tile = atomicAdd(scratch + kOsTickets + pass_slot, 1u);
-  s_hist[tid] = 0;
 #pragma unroll
-  for (int w = 0; w < 8; w++) s_cnt[w][tid] = 0;
+  for (int w = 0; w < RS_WARPS; w++) s_wcnt[w][tid] = 0;
   __syncthreads();
   const uint32_t tile = s_tile, base = tile * RS_TILE;
   if (base >= n) return;  // (the grid has exactly one CTA per tile)
-  uint64_t k[RS_ITEMS];
-#pragma unroll
-  for (int r = 0; r < RS_ITEMS; r++) {
-    const uint32_t i = base + r * RS_THREADS + tid;
-    k[r] = i < n ? kin[i] : 0ull;
-    if (i < n) atomicAdd(&s_hist[(uint32_t)(k[r] >> shift) & 0xFFu], 1u);
-  }
-  __syncthreads();
-  // publish this tile's count of digit `tid`, then add up the tiles before it
-  {
-    const uint32_t c = s_hist[tid];
-    uint32_t excl = 0;
-    if (tile == 0) {
-      lb_store(status + tid, kLbPrefix | c);
-    } else {
-      lb_store(status + (size_t)tile * 256 + tid, kLbAggregate | c);
-      excl = lb_exclusive(status + tid, tile, 256, err);
-      lb_store(status + (size_t)tile * 256 + tid, kLbPrefix | ((excl + c) & kLbValue));
-    }
-    s_run[tid] = scratch[kOsBases + (shift >> 3) * 256 + tid] + excl;
-  }
-  __syncthreads();
-  // stable ranking: rounds in key order, warps in order within a round, lanes in
-  // order within a warp (match_any groups equal digits)
+  const uint32_t tile_n = min((uint32_t)RS_TILE, n - base);
   const uint32_t lt = (1u << lane) - 1u;
+  // ---- per-warp ranking (warp-synchronous: each warp owns its row of s_wcnt)
+  uint64_t k[RS_ITEMS];
+  uint32_t pos[RS_ITEMS];
+  const uint32_t wbase = base + (uint32_t)warp * (RS_ITEMS * 32);
 #pragma unroll
   for (int r = 0; r < RS_ITEMS; r++) {
-    const uint32_t i = base + r * RS_THREADS + tid;
+    const uint32_t i = wbase + r * 32 + lane;
     const bool in = i < n;
+    k[r] = in ? kin[i] : 0ull;
     const uint32_t d = in ? (uint32_t)(k[r] >> shift) & 0xFFu : 256u;
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
     const uint32_t rank = __popc(peers & lt);
-    if (in && rank == 0) s_cnt[warp][d] = __popc(peers);
-    __syncthreads();
-    {
-      uint32_t run = s_run[tid];
+    pos[r] = (in ? s_wcnt[warp][d] : 0u) + rank;
+    __syncwarp();
+    if (in && rank == 0) s_wcnt[warp][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // ---- digit `tid`: tile count, per-warp offsets, tile-local start
+  uint32_t cnt = 0;
 #pragma unroll
-      for (int w = 0; w < 8; w++) {
-        const uint32_t c = s_cnt[w][tid];
-        s_off[w][tid] = run;
-        run += c;
-        s_cnt[w][tid] = 0;
-      }
-      s_run[tid] = run;
+  for (int w = 0; w < RS_WARPS; w++) {
+    const uint32_t c = s_wcnt[w][tid];
+    s_wcnt[w][tid] = cnt;
+    cnt += c;
+  }
+  {
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= o) x += y;
     }
+    if (lane == 31) s_w[warp] = x;
     __syncthreads();
-    if (in) {
-      const uint32_t pos = s_off[warp][d] + rank;
-      if (pos < n) {
-        kout[pos] = k[r];
-        vout[pos] = vin[i];
-      } else {
-        atomicOr(err, kErrBuild);
-      }
+    uint32_t before = 0;
+    for (int w = 0; w < warp; w++) before += s_w[w];
+    s_lstart[tid] = before + x - cnt;
+  }
+  // publish this tile's count of digit `tid`, then add up the tiles before it
+  {
+    uint32_t excl = 0;
+    if (tile == 0) {
+      lb_store(status + tid, kLbPrefix | cnt);
+    } else {
+      lb_store(status + (size_t)tile * 256 + tid, kLbAggregate | cnt);
+      excl = lb_exclusive(status + tid, tile, 256, err);
+      lb_store(status + (size_t)tile * 256 + tid, kLbPrefix | ((excl + cnt) & kLbValue));
+    }
+    s_glob[tid] = scratch[kOsBases + (shift >> 3) * 256 + tid] + excl - s_lstart[tid];
+  }
+  __syncthreads();
+  // ---- keys to shared memory in (digit, original order) order
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; r++) {
+    const uint32_t i = wbase + r * 32 + lane;
+    if (i < n) {
+      const uint32_t d = (uint32_t)(k[r] >> shift) & 0xFFu;
+      const uint32_t j = s_lstart[d] + s_wcnt[warp][d] + pos[r];
+      s_keys[j] = k[r];
+      s_vals[j] = vin[i];
+    }
+  }
+  __syncthreads();
+  // ---- runs out: local index j of digit d goes to s_glob[d] + j
+  for (uint32_t j = tid; j < tile_n; j += RS_THREADS) {
+    const uint64_t key = s_keys[j];
+    const uint32_t out = s_glob[(uint32_t)(key >> shift) & 0xFFu] + j;
+    if (out < n) {
+      kout[out] = key;
+      vout[out] = s_vals[j];
+    } else {
+      atomicOr(err, kErrBuild);
     }
   }
 }
@@ -619,12 +648,30 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
 // the tree is the same whatever the number of extra rounds.  The kernels loop
 // over the tiles grid-stride, so the grid is any size.
 enum : int { kPlocN = 0, kPlocNext = 1, kPlocRounds = 2, kPlocTiles = 3, kPlocDone = 4, kPlocParity = 5,
-             kPlocStateWords = 8 };
+             kPlocIters = 6, kPlocStateWords = 8 };
+// device-decided PLOC loops (conditional graph nodes) stop after this many rounds
+constexpr uint32_t kPlocMaxIters = 1024;
+
+// The two cluster buffers of the PLOC rounds; a round reads set ploc_state[kPlocParity]
+// and writes the other one, so every round runs the same kernels with the same
+// arguments (a loop body captured once serves every iteration).
+struct PlocBufs {
+  float4* clo[2];
+  float4* chi[2];
+  uint32_t* cidx[2];
+};
+
+// Sets the condition of the conditional graph node that repeats a build loop (when
+// the kernel runs inside such a graph; handle 0 otherwise).
+__device__ __forceinline__ void set_loop(cudaGraphConditionalHandle h, bool again) {
+  if (h) cudaGraphSetConditional(h, again ? 1u : 0u);
+}
 
 // The clusters alternate between two buffers, one round reading A and writing
 // B, the next the reverse; kPlocParity counts (mod 2) the rounds that ran, so
 // the current clusters are in B when it is 1 whatever no-op rounds followed.
-__global__ void k_ploc_state_init(const BoundsAcc* __restrict__ acc, uint32_t* __restrict__ ploc_state) {
+__global__ void k_ploc_state_init(const BoundsAcc* __restrict__ acc, uint32_t* __restrict__ ploc_state,
+                                  cudaGraphConditionalHandle loop) {
   if (threadIdx.x == 0) {
     const uint32_t n = acc->nvalid;
     ploc_state[kPlocN] = n;
@@ -633,17 +680,21 @@ __global__ void k_ploc_state_init(const BoundsAcc* __restrict__ acc, uint32_t* _
     ploc_state[kPlocTiles] = (n + PLOC_BLOCK - 1) / PLOC_BLOCK;
     ploc_state[kPlocDone] = n <= PLOC_SMALL ? 1u : 0u;
     ploc_state[kPlocParity] = 0;
+    ploc_state[kPlocIters] = 0;
+    set_loop(loop, n > PLOC_SMALL);
   }
 }
 
 template <int PLOC_R>
-__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const float4* __restrict__ clo, const float4* __restrict__ chi,
-                                                        const uint32_t* __restrict__ ploc_state,
+__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const PlocBufs bufs, const uint32_t* __restrict__ ploc_state,
                                                         uint32_t* __restrict__ nn) {
   __shared__ float3 s_lo[PLOC_BLOCK + 2 * PLOC_R], s_hi[PLOC_BLOCK + 2 * PLOC_R];
   __shared__ uint32_t s_seg[PLOC_BLOCK + 2 * PLOC_R];
   if (ploc_state[kPlocDone]) return;
   const uint32_t n = ploc_state[kPlocN];
+  const uint32_t par = ploc_state[kPlocParity] & 1u;
+  const float4* __restrict__ clo = bufs.clo[par];
+  const float4* __restrict__ chi = bufs.chi[par];
   for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x) {
     const int base = (int)(tile * PLOC_BLOCK);
     for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
@@ -711,19 +762,22 @@ __device__ __forceinline__ uint32_t block_excl_scan_flag(int flag, uint32_t* s_w
   return pre + __popc(bal & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const float4* __restrict__ clo, const float4* __restrict__ chi,
-                                                          const uint32_t* __restrict__ cidx,
-                                                          const uint32_t* __restrict__ nn,
+__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const PlocBufs bufs, const uint32_t* __restrict__ nn,
                                                           const uint32_t* __restrict__ ploc_state,
                                                           const uint32_t* __restrict__ bsurv_off,
                                                           const uint32_t* __restrict__ bmerge_off,
                                                           float4* __restrict__ bnlo, float4* __restrict__ bnhi,
-                                                          uint32_t* __restrict__ bncnt, float4* __restrict__ olo,
-                                                          float4* __restrict__ ohi, uint32_t* __restrict__ oidx,
-                                                          uint32_t node_cap, uint32_t* err) {
+                                                          uint32_t* __restrict__ bncnt, uint32_t node_cap, uint32_t* err) {
   __shared__ uint32_t s_w[PLOC_BLOCK / 32];
   if (ploc_state[kPlocDone]) return;
   const uint32_t n = ploc_state[kPlocN], node_next = ploc_state[kPlocNext];
+  const uint32_t par = ploc_state[kPlocParity] & 1u;
+  const float4* __restrict__ clo = bufs.clo[par];
+  const float4* __restrict__ chi = bufs.chi[par];
+  const uint32_t* __restrict__ cidx = bufs.cidx[par];
+  float4* __restrict__ olo = bufs.clo[par ^ 1u];
+  float4* __restrict__ ohi = bufs.chi[par ^ 1u];
+  uint32_t* __restrict__ oidx = bufs.cidx[par ^ 1u];
   for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x) {
     const uint32_t i = tile * PLOC_BLOCK + threadIdx.x;
     int surv = 0, merge = 0;
@@ -769,8 +823,10 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const float4* __restri
 
 // After a round: the survivors are the new clusters, the merges took the next
 // binary node indices; rounds end once n <= PLOC_SMALL or nothing merged.
-__global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ ploc_state) {
-  if (threadIdx.x == 0 && !ploc_state[kPlocDone]) {
+__global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ ploc_state,
+                               cudaGraphConditionalHandle loop) {
+  if (threadIdx.x != 0) return;
+  if (!ploc_state[kPlocDone]) {
     const uint32_t n = tot[0], merged = tot[1];
     ploc_state[kPlocN] = n;
     ploc_state[kPlocNext] += merged;
@@ -779,6 +835,10 @@ __global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __res
     ploc_state[kPlocParity] ^= 1u;
     if (n <= PLOC_SMALL || merged == 0) ploc_state[kPlocDone] = 1u;
   }
+  // a device-decided loop also stops at kPlocMaxIters rounds (the one-CTA finish then
+  // finds more than PLOC_SMALL clusters and reports the build as failed)
+  const uint32_t it = ++ploc_state[kPlocIters];
+  set_loop(loop, !ploc_state[kPlocDone] && it < kPlocMaxIters);
 }
 
 // Finishes clustering of the n <= PLOC_SMALL clusters left by the rounds
@@ -1208,7 +1268,8 @@ __device__ __forceinline__ uint32_t cta_excl_scan_1024(uint32_t v, uint32_t* s_w
 __global__ void __launch_bounds__(1024) k_collapse_roots(const uint32_t* __restrict__ d_root, uint32_t nseg,
                                                          uint32_t nbin, uint32_t* __restrict__ items,
                                                          uint32_t* __restrict__ seg_index,
-                                                         uint32_t* __restrict__ cstate) {
+                                                         uint32_t* __restrict__ cstate,
+                                                         cudaGraphConditionalHandle loop) {
   __shared__ uint32_t s_w[32];
   uint32_t r[4], cnt = 0;
   const uint32_t s0 = threadIdx.x * 4;
@@ -1231,14 +1292,23 @@ __global__ void __launch_bounds__(1024) k_collapse_roots(const uint32_t* __restr
     cstate[kColBase] = 0;
     cstate[kColTri] = 0;
     cstate[kColDepth] = 0;
+    set_loop(loop, total > 0);
   }
 }
 
-__global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const uint32_t* __restrict__ items,
+// The two item buffers of the collapse levels: level d reads items[d & 1] and writes
+// items[(d & 1) ^ 1] (d = cstate[kColDepth]), so every level runs the same kernels
+// with the same arguments.
+struct ColItems {
+  uint32_t* items[2];
+};
+
+__global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const ColItems ci,
                                                         const uint32_t* __restrict__ cstate,
                                                         uint32_t* __restrict__ kids_out, uint32_t* __restrict__ nint,
                                                         uint32_t* __restrict__ ntri) {
   const uint32_t nitems = cstate[kColN];
+  const uint32_t* __restrict__ items = ci.items[cstate[kColDepth] & 1u];
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nitems; k += gridDim.x * blockDim.x) {
     uint32_t kids[8];
     const int nk = gather_children(t, items[k], kids);
@@ -1265,10 +1335,13 @@ __global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const uint32_
 // them itself and has no bound: a chain-like binary tree, e.g. thousands of
 // identical triangles, collapses into thousands of levels).
 __global__ void k_collapse_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ cstate, uint32_t node_cap,
-                                   uint32_t max_levels) {
+                                   uint32_t max_levels, cudaGraphConditionalHandle loop) {
   if (threadIdx.x != 0) return;
   const uint32_t n = cstate[kColN];
-  if (n == 0) return;
+  if (n == 0) {
+    set_loop(loop, false);
+    return;
+  }
   const uint32_t d = cstate[kColDepth];
   if (d < (uint32_t)kColMaxLevels) cstate[kColLevels + d] = cstate[kColBase];
   const uint32_t base = cstate[kColBase] + n;
@@ -1282,6 +1355,7 @@ __global__ void k_collapse_advance(const uint32_t* __restrict__ tot, uint32_t* _
   }
   cstate[kColN] = next;
   if (next == 0 && d + 1 <= (uint32_t)kColMaxLevels) cstate[kColLevels + d + 1] = base;  // end of the last level
+  set_loop(loop, next > 0);  // max_levels bounds a device-decided loop: next is 0 beyond it
 }
 
 __device__ __forceinline__ uint32_t exp_for(float ext) {
@@ -1476,9 +1550,10 @@ constexpr int COLLAPSE_THREADS = 128;
 __global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
     BinTree t, const uint32_t* __restrict__ kids_in, const uint32_t* __restrict__ cstate,
     const uint32_t* __restrict__ off_int, const uint32_t* __restrict__ off_tri, WideNode* __restrict__ nodes,
-    uint32_t* __restrict__ leaf_root, uint32_t* __restrict__ next_items, double* sah_acc, uint32_t* leaf_count,
+    uint32_t* __restrict__ leaf_root, const ColItems ci, double* sah_acc, uint32_t* leaf_count,
     uint32_t node_cap, uint32_t tri_cap, uint32_t* err) {
   const uint32_t nitems = cstate[kColN], level_base = cstate[kColBase], tri_next = cstate[kColTri];
+  uint32_t* __restrict__ next_items = ci.items[(cstate[kColDepth] & 1u) ^ 1u];
   const uint32_t next_base = level_base + nitems;
   double sah = 0.0, sahx = 0.0;
   uint32_t nleaf = 0;
@@ -1590,11 +1665,17 @@ static cudaError_t onesweep_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, ui
   const uint32_t ntiles = cdiv(n, RS_TILE);
   GB_CHECK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * onesweep_scratch_words(n, passes), st));
   const uint32_t hgrid = std::min<uint32_t>(ntiles, 4u * (uint32_t)num_sms_build());
+  // 48 KB of staged keys and values beyond the static shared memory (per device; a
+  // captured build sets it in graph_build_prepare)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GB_CHECK(cudaStreamIsCapturing(st, &cap));
+  if (cap == cudaStreamCaptureStatusNone)
+    GB_CHECK(cudaFuncSetAttribute(k_os_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsScatterSmem));
   k_os_hist<<<hgrid, 256, 0, st>>>(ka, n, digit_mask & 0xFFu, scratch);
   uint32_t slot = 0;
   for (int d = 0; d < 8; d++) {
     if (!(digit_mask >> d & 1u)) continue;
-    k_os_scatter<<<ntiles, RS_THREADS, 0, st>>>(ka, va, kb, vb, n, 8 * d, scratch, slot,
+    k_os_scatter<<<ntiles, RS_THREADS, kOsScatterSmem, st>>>(ka, va, kb, vb, n, 8 * d, scratch, slot,
                                                  scratch + kOsStatus + (size_t)slot * ntiles * 256u,
                                                  err ? err : scratch + kOsErr);
     std::swap(ka, kb);
@@ -1758,31 +1839,28 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&ploc_state, kPlocStateWords));
   uint32_t* h_tot = nullptr;
   GB_CHECK(arena.host(&h_tot, kPlocStateWords));
-  k_ploc_state_init<<<1, 32, 0, st>>>(acc, ploc_state);
+  k_ploc_state_init<<<1, 32, 0, st>>>(acc, ploc_state, 0);
   note_launches(1);
   const int radius = opt.ploc_radius == 1 || opt.ploc_radius == 2 || opt.ploc_radius == 4 || opt.ploc_radius == 8
                          ? opt.ploc_radius
                          : PLOC_R_MAX;
-  float4* cl[2] = {clo_a, clo_b};
-  float4* ch[2] = {chi_a, chi_b};
-  uint32_t* ci[2] = {cidx_a, cidx_b};
+  const PlocBufs pb{{clo_a, clo_b}, {chi_a, chi_b}, {cidx_a, cidx_b}};
   uint32_t round = 0;
   auto enqueue_round = [&](uint32_t grid) {
-    const int a = round & 1, b = a ^ 1;
     switch (radius) {
-      case 1: k_ploc_nn<1><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
-      case 2: k_ploc_nn<2><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
-      case 4: k_ploc_nn<4><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
-      case 8: k_ploc_nn<8><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
-      default: k_ploc_nn<PLOC_R_MAX><<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ploc_state, nn); break;
+      case 1: k_ploc_nn<1><<<grid, PLOC_BLOCK, 0, st>>>(pb, ploc_state, nn); break;
+      case 2: k_ploc_nn<2><<<grid, PLOC_BLOCK, 0, st>>>(pb, ploc_state, nn); break;
+      case 4: k_ploc_nn<4><<<grid, PLOC_BLOCK, 0, st>>>(pb, ploc_state, nn); break;
+      case 8: k_ploc_nn<8><<<grid, PLOC_BLOCK, 0, st>>>(pb, ploc_state, nn); break;
+      default: k_ploc_nn<PLOC_R_MAX><<<grid, PLOC_BLOCK, 0, st>>>(pb, ploc_state, nn); break;
     }
     k_ploc_count<<<grid, PLOC_BLOCK, 0, st>>>(nn, ploc_state, bsurv, bmerge);
     note_launches(2);
     scan_excl(bsurv, maxb, d_tot + 0, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
     scan_excl(bmerge, maxb, d_tot + 1, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
-    k_ploc_emit<<<grid, PLOC_BLOCK, 0, st>>>(cl[a], ch[a], ci[a], nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt,
-                                             cl[b], ch[b], ci[b], nnodes_bin, &acc->pad);
-    k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state);
+    k_ploc_emit<<<grid, PLOC_BLOCK, 0, st>>>(pb, nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt, nnodes_bin,
+                                             &acc->pad);
+    k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state, 0);
     note_launches(2);
     round++;
   };
@@ -1902,21 +1980,20 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&seg_index, nseg));
   GB_CHECK(arena.host(&h_col, kColStateWords));
   GB_CHECK(cudaMemsetAsync(cstate, 0, sizeof(uint32_t) * kColStateWords, st));
-  k_collapse_roots<<<1, 1024, 0, st>>>(d_root, nseg, nnodes_bin, items_a, seg_index, cstate);
+  k_collapse_roots<<<1, 1024, 0, st>>>(d_root, nseg, nnodes_bin, items_a, seg_index, cstate, 0);
   note_launches(1);
-  uint32_t* items[2] = {items_a, items_b};
+  const ColItems citems{{items_a, items_b}};
   uint32_t level = 0;
   const uint32_t max_levels = 0xFFFFFFFFu;  // host-driven: level starts recorded here, no bound
   auto enqueue_level = [&](uint32_t nitems_known) {  // the level's size, read by the host
-    const int a = level & 1, b = a ^ 1;
     const uint32_t grid = cdiv(nitems_known, 128);
-    k_collapse_count<<<grid, 128, 0, st>>>(bt, items[a], cstate, kids, nint, ntri);
+    k_collapse_count<<<grid, 128, 0, st>>>(bt, citems, cstate, kids, nint, ntri);
     note_launches(1);
     scan_excl(nint, nitems_known, d_tot + 0, scan_sums, st, &acc->pad);
     scan_excl(ntri, nitems_known, d_tot + 1, scan_sums, st, &acc->pad);
-    k_collapse_emit<<<grid, COLLAPSE_THREADS, 0, st>>>(bt, kids, cstate, nint, ntri, wnodes, leaf_root, items[b],
+    k_collapse_emit<<<grid, COLLAPSE_THREADS, 0, st>>>(bt, kids, cstate, nint, ntri, wnodes, leaf_root, citems,
                                                        d_sah, d_leaves, maxw, N, &acc->pad);
-    k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels);
+    k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels, 0);
     note_launches(2);
     level++;
   };
@@ -2073,10 +2150,53 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
   e = cudaMemcpy(g->d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice);
   // the scans' look-back state starts at zero and every scan leaves it so
   if (e == cudaSuccess) e = cudaMemset(g->scan_sums, 0, sizeof(uint32_t) * scan_scratch(std::max(g->maxb, maxw)));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_os_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsScatterSmem);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->body_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) graph_build_release(g);
   const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return e;
+}
+
+// A new condition handle of the graph being captured on st; its value is 0 at every
+// launch of the graph until a kernel of the graph sets it.
+static cudaError_t loop_handle(cudaStream_t st, cudaGraphConditionalHandle* h) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  GB_CHECK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, nullptr, nullptr, nullptr));
+  if (cs != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureUnsupported;
+  return cudaGraphConditionalHandleCreate(h, graph, 0u, cudaGraphCondAssignDefault);
+}
+
+// Appends to the capture on st a conditional WHILE node on handle h, whose body --
+// enqueued by body(stream) on body_st, captured into the node's own graph -- runs
+// again as long as the condition is non-zero.  The kernels set the condition: one
+// enqueued before the node (whether to run at all), the body's last (whether to
+// run again).
+template <typename F>
+static cudaError_t capture_while(cudaStream_t st, cudaStream_t body_st, cudaGraphConditionalHandle h, F&& body) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  GB_CHECK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &ndeps));
+  if (cs != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureUnsupported;
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  GB_CHECK(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &p));
+  GB_CHECK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  GB_CHECK(cudaStreamBeginCaptureToGraph(body_st, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  body(body_st);
+  cudaGraph_t out = nullptr;
+  const cudaError_t e1 = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamEndCapture(body_st, &out);
+  return e1 != cudaSuccess ? e1 : e2;
 }
 
 cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
@@ -2094,33 +2214,35 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   // the digits the key width can use: 63-bit keys 8, 30-bit keys 4 (6 with the slot)
   const uint32_t digits = g.opt.morton_bits == 30 ? (g.opt.segmented ? 0x3Fu : 0x0Fu) : 0xFFu;
   GB_CHECK(onesweep_sort(ka, va, kb, vb, T, digits, g.hist, &acc->pad, st));
-  // PLOC: a fixed number of rounds, then the one-CTA finish
+  // PLOC: rounds in a loop the device ends (a conditional WHILE node), then the
+  // one-CTA finish
   GB_CHECK(cudaMemsetAsync(g.d_root, 0xFF, sizeof(uint32_t) * g.nseg, st));
   GB_CHECK(cudaMemsetAsync(g.d_iters, 0, sizeof(uint32_t), st));
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(g.plo, g.phi, va, N, &acc->nvalid, g.bnlo, g.bnhi, g.bncnt, g.cidx[0],
                                             g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0);
-  k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state);
+  cudaGraphConditionalHandle ploc_loop = 0;
+  GB_CHECK(loop_handle(st, &ploc_loop));
+  k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state, ploc_loop);
   note_launches(2);
   const uint32_t pgrid = std::min<uint32_t>(g.maxb, (uint32_t)fixed_grid);
   const uint32_t nbin_cap = 2 * N;
-  for (uint32_t r = 0; r < g.plan.ploc_rounds; r++) {
-    const int a = r & 1, b = a ^ 1;
+  const PlocBufs pb{{g.clo[0], g.clo[1]}, {g.chi[0], g.chi[1]}, {g.cidx[0], g.cidx[1]}};
+  GB_CHECK(capture_while(st, g.body_stream, ploc_loop, [&](cudaStream_t bs) {
     switch (g.radius) {
-      case 1: k_ploc_nn<1><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
-      case 2: k_ploc_nn<2><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
-      case 4: k_ploc_nn<4><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
-      case 8: k_ploc_nn<8><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
-      default: k_ploc_nn<PLOC_R_MAX><<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.ploc_state, g.nn); break;
+      case 1: k_ploc_nn<1><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
+      case 2: k_ploc_nn<2><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
+      case 4: k_ploc_nn<4><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
+      case 8: k_ploc_nn<8><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
+      default: k_ploc_nn<PLOC_R_MAX><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
     }
-    k_ploc_count<<<pgrid, PLOC_BLOCK, 0, st>>>(g.nn, g.ploc_state, g.bsurv, g.bmerge);
-    scan_excl(g.bsurv, g.maxb, g.d_tot + 0, g.scan_sums, st, &acc->pad, g.ploc_state + kPlocTiles);
-    scan_excl(g.bmerge, g.maxb, g.d_tot + 1, g.scan_sums, st, &acc->pad, g.ploc_state + kPlocTiles);
-    k_ploc_emit<<<pgrid, PLOC_BLOCK, 0, st>>>(g.clo[a], g.chi[a], g.cidx[a], g.nn, g.ploc_state, g.bsurv, g.bmerge,
-                                              g.bnlo, g.bnhi, g.bncnt, g.clo[b], g.chi[b], g.cidx[b], nbin_cap,
-                                              &acc->pad);
-    k_ploc_advance<<<1, 32, 0, st>>>(g.d_tot, g.ploc_state);
+    k_ploc_count<<<pgrid, PLOC_BLOCK, 0, bs>>>(g.nn, g.ploc_state, g.bsurv, g.bmerge);
+    scan_excl(g.bsurv, g.maxb, g.d_tot + 0, g.scan_sums, bs, &acc->pad, g.ploc_state + kPlocTiles);
+    scan_excl(g.bmerge, g.maxb, g.d_tot + 1, g.scan_sums, bs, &acc->pad, g.ploc_state + kPlocTiles);
+    k_ploc_emit<<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.nn, g.ploc_state, g.bsurv, g.bmerge, g.bnlo, g.bnhi, g.bncnt,
+                                              nbin_cap, &acc->pad);
+    k_ploc_advance<<<1, 32, 0, bs>>>(g.d_tot, g.ploc_state, ploc_loop);
     note_launches(4);
-  }
+  }));
   {
     const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(g.clo[0], g.chi[0], g.cidx[0], g.clo[1], g.chi[1], g.cidx[1],
@@ -2146,19 +2268,22 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   GB_CHECK(cudaMemsetAsync(g.d_sah, 0, 2 * sizeof(double), st));
   GB_CHECK(cudaMemsetAsync(g.d_leaves, 0, sizeof(uint32_t), st));
   GB_CHECK(cudaMemsetAsync(g.cstate, 0, sizeof(uint32_t) * kColStateWords, st));
-  k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate);
+  // collapse levels in a loop the device ends
+  cudaGraphConditionalHandle col_loop = 0;
+  GB_CHECK(loop_handle(st, &col_loop));
+  k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate, col_loop);
   note_launches(1);
   const uint32_t cgrid = std::min<uint32_t>(cdiv(maxw, 128), (uint32_t)fixed_grid);
-  for (uint32_t l = 0; l < g.plan.levels; l++) {
-    const int a = l & 1, b = a ^ 1;
-    k_collapse_count<<<cgrid, 128, 0, st>>>(bt, g.items[a], g.cstate, g.kids, g.nint, g.ntri);
-    scan_excl(g.nint, maxw, g.d_tot + 0, g.scan_sums, st, &acc->pad, g.cstate + kColN);
-    scan_excl(g.ntri, maxw, g.d_tot + 1, g.scan_sums, st, &acc->pad, g.cstate + kColN);
-    k_collapse_emit<<<cgrid, COLLAPSE_THREADS, 0, st>>>(bt, g.kids, g.cstate, g.nint, g.ntri, g.nodes, g.leaf_root,
-                                                        g.items[b], g.d_sah, g.d_leaves, maxw, N, &acc->pad);
-    k_collapse_advance<<<1, 32, 0, st>>>(g.d_tot, g.cstate, maxw, g.plan.levels);
+  const ColItems ci{{g.items[0], g.items[1]}};
+  GB_CHECK(capture_while(st, g.body_stream, col_loop, [&](cudaStream_t bs) {
+    k_collapse_count<<<cgrid, 128, 0, bs>>>(bt, ci, g.cstate, g.kids, g.nint, g.ntri);
+    scan_excl(g.nint, maxw, g.d_tot + 0, g.scan_sums, bs, &acc->pad, g.cstate + kColN);
+    scan_excl(g.ntri, maxw, g.d_tot + 1, g.scan_sums, bs, &acc->pad, g.cstate + kColN);
+    k_collapse_emit<<<cgrid, COLLAPSE_THREADS, 0, bs>>>(bt, g.kids, g.cstate, g.nint, g.ntri, g.nodes, g.leaf_root,
+                                                        ci, g.d_sah, g.d_leaves, maxw, N, &acc->pad);
+    k_collapse_advance<<<1, 32, 0, bs>>>(g.d_tot, g.cstate, maxw, (uint32_t)kColMaxLevels, col_loop);
     note_launches(3);
-  }
+  }));
   k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, g.d_geoms, g.plo, g.phi, g.leaf_root, N, g.tris, &acc->pad);
   k_graph_build_check<<<1, 32, 0, st>>>(acc, g.ploc_state, g.cstate, N, g.status);
   note_launches(2);
@@ -2174,6 +2299,7 @@ cudaError_t graph_build_result(const GraphBuild& g, const float scene_lo[3], con
   GB_CHECK(cudaMemcpyAsync(col.data(), g.cstate, sizeof(uint32_t) * kColStateWords, cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(sah, g.d_sah, sizeof(sah), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(&out->num_leaves, g.d_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GB_CHECK(cudaMemcpyAsync(&out->ploc_rounds, g.ploc_state + kPlocIters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
   out->num_nodes = col[kColBase];
   out->depth = std::min<uint32_t>(col[kColDepth], (uint32_t)kColMaxLevels);
@@ -2187,6 +2313,7 @@ cudaError_t graph_build_result(const GraphBuild& g, const float scene_lo[3], con
 
 void graph_build_release(GraphBuild* g) {
   for (void* p : g->allocs) cudaFree(p);
+  if (g->body_stream) cudaStreamDestroy(g->body_stream);
   *g = GraphBuild{};
 }
 

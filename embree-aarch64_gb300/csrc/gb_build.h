@@ -50,8 +50,8 @@ void refit_release(RefitScratch* s);
 struct GraphBuildPlan {
   uint32_t valid_tris = 0;   // valid triangles of the ordinary build
   uint32_t roots = 0;        // non-empty segments (1 without segments)
-  uint32_t ploc_rounds = 0;  // rounds enqueued
-  uint32_t levels = 0;       // collapse levels enqueued (at most 64)
+  uint32_t ploc_rounds = 0;  // PLOC rounds of the ordinary build (the captured build loops on the device)
+  uint32_t levels = 0;       // collapse levels of the ordinary build
   int leaf_max = 2;          // resolved leaf size
 };
 struct GraphBuild {
@@ -76,10 +76,12 @@ struct GraphBuild {
   uint32_t *items[2] = {nullptr, nullptr}, *kids = nullptr, *nint = nullptr, *ntri = nullptr, *leaf_root = nullptr;
   double* d_sah = nullptr;
   uint32_t *d_leaves = nullptr, *cstate = nullptr, *seg_index = nullptr, *status = nullptr;
+  cudaStream_t body_stream = nullptr;  // captures the bodies of the device-decided build loops
 };
 struct GraphBuildResult {
   uint32_t status = 0;  // 0: the build is complete and consistent; else kGraphBuild* bits
   uint32_t num_nodes = 0, depth = 0, num_leaves = 0;
+  uint32_t ploc_rounds = 0;  // PLOC rounds the device ran
   double sah = 0, sah_exact = 0;
   std::vector<uint32_t> level_start;
 };

@@ -2547,10 +2547,9 @@ RTC_API RTCGBBatchedFrame rtcgbNewBatchedFrame(RTCScene hs, struct RTCRayHit* ra
   plan.valid_tris = s->stats.num_prims;
   plan.roots = 0;
   for (uint32_t r : s->bvh.roots) plan.roots += r != gb::kInvalidID ? 1u : 0u;
-  plan.ploc_rounds = s->stats.ploc_rounds + 8;
-  plan.levels = s->stats.depth + 4;
+  plan.ploc_rounds = s->stats.ploc_rounds;
+  plan.levels = s->stats.depth;
   plan.leaf_max = (int)s->stats.leaf_max;
-  if (plan.levels > 64) fail(RTC_ERROR_INVALID_OPERATION, "the scene's tree is too deep for a captured build");
   gb::BuildOptions opt = s->device->build_opt;
   opt.robust = (s->flags & RTC_SCENE_FLAG_ROBUST) != 0;
   opt.segmented = 1;
@@ -2601,8 +2600,8 @@ RTC_API RTCGBBatchedFrame rtcgbNewBatchedFrame(RTCScene hs, struct RTCRayHit* ra
     size_t nnodes = 0;
     cuda_ok(cudaGraphGetNodes(f->graph, nullptr, &nnodes), "graph nodes");
     f->stats.graph_nodes = (unsigned int)nnodes;
-    f->stats.ploc_rounds = plan.ploc_rounds;
-    f->stats.levels = plan.levels;
+    f->stats.ploc_rounds = 0;  // set by each replay: the device decides
+    f->stats.levels = 0;
   } catch (...) {
     delete f;
     throw;
@@ -2635,8 +2634,10 @@ RTC_API void rtcgbBatchedFrameReplay(RTCGBBatchedFrame hf) {
   f->stats.status = r.status;
   f->stats.num_nodes = r.num_nodes;
   f->stats.build_sah = r.sah;
+  f->stats.ploc_rounds = r.ploc_rounds;
+  f->stats.levels = r.depth;
   f->stats.replays++;
-  if (r.status) fail(RTC_ERROR_UNKNOWN, "the replayed build no longer matches its plan: create a new frame");
+  if (r.status) fail(RTC_ERROR_UNKNOWN, "the replayed build failed (its status in rtcgbGetBatchedFrameStats)");
   if (err) fail(RTC_ERROR_UNKNOWN, "traversal error in a frame");
   API_END(f ? f->scene->device : nullptr)
 }

@@ -232,20 +232,22 @@ RTC_API void rtcgbOccluded1MBatched(RTCScene scene, struct RTCRay* ray, unsigned
    batched closest-hit query over device-resident rays, captured once into one
    CUDA graph and replayed with one launch (optionally preceded by a copy of
    `pristine` over `rayhit`, both device memory).  The captured build runs with
-   no host reads: its PLOC rounds and collapse levels are enqueued a fixed
-   number of times, planned from the scene's last build (rounds and levels past
-   the last real one do nothing); a replay whose build no longer fits its plan
-   reports RTC_ERROR_UNKNOWN.  The scene's geometry IDs must be 0..n-1; a new
+   no host reads: its PLOC rounds and its collapse levels are the bodies of two
+   conditional WHILE graph nodes whose conditions the build's own kernels set,
+   so the device runs exactly as many rounds and levels as the data needs; a
+   replay whose build fails (more than 1024 PLOC rounds, more than 64 levels, a
+   different number of valid triangles) reports RTC_ERROR_UNKNOWN.  The scene's
+   geometry IDs must be 0..n-1; a new
    commit of the scene invalidates the frame.  Results are those of
    rtcCommitScene + rtcgbIntersect1MBatched on the same data. */
 typedef struct RTCGBBatchedFrameTy* RTCGBBatchedFrame;
 typedef struct RTCGBBatchedFrameStats {
   double frame_ms;           /* device time of the last replay (copy + build + query) */
   double build_sah;          /* SAH of the replayed build */
-  unsigned int status;       /* 0: the replayed build fitted its plan */
+  unsigned int status;       /* 0: the replayed build completed and is consistent */
   unsigned int num_nodes;    /* wide nodes of the replayed build */
-  unsigned int ploc_rounds;  /* PLOC rounds enqueued */
-  unsigned int levels;       /* collapse levels enqueued */
+  unsigned int ploc_rounds;  /* PLOC rounds the replayed build ran (device loop) */
+  unsigned int levels;       /* collapse levels the replayed build ran (device loop) */
   unsigned int graph_nodes;  /* nodes of the captured graph */
   unsigned int replays;
 } RTCGBBatchedFrameStats;

@@ -168,7 +168,9 @@ def test_batched_frame_graph_matches_separate_calls(rtc, config):
         st = frame.replay()
         got = work.cpu().numpy()
         assert np.array_equal(got, ref.view(np.uint8))
-    assert st["status"] == 0 and st["replays"] == 2 and st["graph_nodes"] > 50 and st["frame_ms"] > 0
+    assert st["status"] == 0 and st["replays"] == 2 and st["graph_nodes"] > 10 and st["frame_ms"] > 0
+    # the build's loops ran on the device as often as the data needed
+    assert st["levels"] == sc.build_stats()["depth"] and st["ploc_rounds"] > 0
     assert st["num_nodes"] == sc.build_stats()["num_nodes"]
     sc.commit()
     with pytest.raises(rtc.RTCError):
