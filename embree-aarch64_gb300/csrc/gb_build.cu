@@ -266,6 +266,29 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
 }
 
 // ---------------------------------------------------------------------------
+// Device-to-device copies on the SMs.  A cudaMemcpyAsync between device buffers
+// runs on a copy engine: measured on a GB300, restoring 47.5 GB of ray records
+// inside a CUDA graph took 29.8 ms that way against 13.7 ms for this kernel.
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_copy16(uint4* __restrict__ dst, const uint4* __restrict__ src, size_t n16) {
+  for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n16; i += (size_t)gridDim.x * 256) dst[i] = src[i];
+}
+
+static int num_sms_build();
+
+cudaError_t copy_device(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return cudaSuccess;
+  if (((uintptr_t)dst | (uintptr_t)src | bytes) % 16 != 0)
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+  const size_t n16 = bytes / 16;
+  const size_t grid = std::min<size_t>((n16 + 255) / 256, (size_t)num_sms_build() * 8);
+  k_copy16<<<(unsigned)grid, 256, 0, st>>>(static_cast<uint4*>(dst), static_cast<const uint4*>(src), n16);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // 3. stable LSD radix sort (64-bit keys, 32-bit values), onesweep style
 // ---------------------------------------------------------------------------
 //
@@ -2030,8 +2053,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   // exact-size outputs
   GB_CHECK(cudaMalloc((void**)&out->nodes, (size_t)num_nodes * sizeof(WideNode)));
   GB_CHECK(cudaMalloc((void**)&out->tris, (size_t)N * sizeof(TriRecord)));
-  GB_CHECK(cudaMemcpyAsync(out->nodes, wnodes, (size_t)num_nodes * sizeof(WideNode), cudaMemcpyDeviceToDevice, st));
-  GB_CHECK(cudaMemcpyAsync(out->tris, wtris, (size_t)N * sizeof(TriRecord), cudaMemcpyDeviceToDevice, st));
+  GB_CHECK(copy_device(out->nodes, wnodes, (size_t)num_nodes * sizeof(WideNode), st));
+  GB_CHECK(copy_device(out->tris, wtris, (size_t)N * sizeof(TriRecord), st));
   out->num_nodes = num_nodes;
   out->num_tris = N;
   out->depth = depth;

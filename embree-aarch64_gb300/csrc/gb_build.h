@@ -93,6 +93,10 @@ cudaError_t graph_build_result(const GraphBuild& gbuild, const float scene_lo[3]
                                GraphBuildResult* out, cudaStream_t st);  // synchronises st
 void graph_build_release(GraphBuild* gbuild);
 
+// Device-to-device copy by a kernel when dst, src and bytes are 16-byte multiples
+// (faster than the copy engine), else cudaMemcpyAsync.  Capturable.
+cudaError_t copy_device(void* dst, const void* src, size_t bytes, cudaStream_t st);
+
 // Stable LSD radix sort of 64-bit keys with 32-bit values (device buffers).
 cudaError_t sort_pairs(uint64_t* keys, uint32_t* vals, uint32_t n, cudaStream_t st);
 // The low 8 * passes bits only (passes even), with caller scratch (kb, vb: n

@@ -262,7 +262,7 @@ struct FrameBody {
       }
       GB_TRY(launch_trace(P, false, false, st));
       nk++;
-      if (b == (bounces > 1 ? 1u : 0u)) GB_TRY(cudaMemcpyAsync(log, rays[cur], (size_t)n * 80, cudaMemcpyDeviceToDevice, st));
+      if (b == (bounces > 1 ? 1u : 0u)) GB_TRY(copy_device(log, rays[cur], (size_t)n * 80, st));
       k_shade<<<cdiv(n, 256), 256, 0, st>>>(rays[cur], counts + b, rays[cur ^ 1], counts + b + 1, thr, image, frame, b,
                                             b + 1 == bounces ? 1u : 0u, n);
       nk++;

@@ -2587,7 +2587,7 @@ RTC_API RTCGBBatchedFrame rtcgbNewBatchedFrame(RTCScene hs, struct RTCRayHit* ra
     cuda_ok(cudaStreamSynchronize(st), "frame");
     cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaError_t e = cudaSuccess;
-    if (pristine) e = cudaMemcpyAsync(rayhit, pristine, span, cudaMemcpyDeviceToDevice, st);
+    if (pristine) e = gb::copy_device(rayhit, pristine, span, st);
     if (e == cudaSuccess) e = gb::graph_build_enqueue(f->gbuild, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(f->scratch, 0, 64, st);
     if (e == cudaSuccess) e = gb::launch_trace(P, false, false, st);
