@@ -2323,11 +2323,22 @@ cudaError_t graph_build_result(const GraphBuild& g, const float scene_lo[3], con
   GB_CHECK(cudaMemcpyAsync(sah, g.d_sah, sizeof(sah), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(&out->num_leaves, g.d_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaMemcpyAsync(&out->ploc_rounds, g.ploc_state + kPlocIters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  BoundsAcc h_acc{};
+  GB_CHECK(cudaMemcpyAsync(&h_acc, g.acc, sizeof(BoundsAcc), cudaMemcpyDeviceToHost, st));
+  out->roots.assign(g.nseg, kInvalidID);
+  if (g.opt.segmented)
+    GB_CHECK(cudaMemcpyAsync(out->roots.data(), g.seg_index, sizeof(uint32_t) * g.nseg, cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
   out->num_nodes = col[kColBase];
   out->depth = std::min<uint32_t>(col[kColDepth], (uint32_t)kColMaxLevels);
   out->level_start.assign(col.begin() + kColLevels, col.begin() + kColLevels + out->depth + 1);
-  const float gx = scene_hi[0] - scene_lo[0], gy = scene_hi[1] - scene_lo[1], gz = scene_hi[2] - scene_lo[2];
+  // the replayed build's own geometry bounds, unless the caller passes the scene's
+  for (int d = 0; d < 3; d++) {
+    out->lo[d] = scene_lo ? scene_lo[d] : ord2f(h_acc.glo[d]);
+    out->hi[d] = scene_hi ? scene_hi[d] : ord2f(h_acc.ghi[d]);
+  }
+  if (!g.opt.segmented) out->roots.assign(1, 0u);
+  const float gx = out->hi[0] - out->lo[0], gy = out->hi[1] - out->lo[1], gz = out->hi[2] - out->lo[2];
   const double Aroot = std::max(0.0, (double)(gx * (gy + gz) + gy * gz));
   out->sah = Aroot > 0 ? (Aroot + sah[0]) / Aroot : 0.0;
   out->sah_exact = Aroot > 0 ? (Aroot + sah[1]) / Aroot : 0.0;
@@ -2338,6 +2349,79 @@ void graph_build_release(GraphBuild* g) {
   for (void* p : g->allocs) cudaFree(p);
   if (g->body_stream) cudaStreamDestroy(g->body_stream);
   *g = GraphBuild{};
+}
+
+void cached_build_release(CachedBuild* c) {
+  if (!c) return;
+  if (c->exec) cudaGraphExecDestroy(c->exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  graph_build_release(&c->g);
+  delete c;
+}
+
+cudaError_t cached_build_create(const GeomDesc* h_geoms, int ngeoms, const BuildOptions& opt,
+                                const GraphBuildPlan& plan, cudaStream_t st, CachedBuild** out) {
+  *out = nullptr;
+  CachedBuild* c = new CachedBuild;
+  cudaError_t e = graph_build_prepare(h_geoms, ngeoms, opt, plan, &c->g);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->e1);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    const cudaError_t e1 = graph_build_enqueue(c->g, st);
+    const cudaError_t e2 = cudaStreamEndCapture(st, &c->graph);
+    e = e1 != cudaSuccess ? e1 : e2;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&c->exec, c->graph, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cached_build_release(c);
+    return e;
+  }
+  *out = c;
+  return cudaSuccess;
+}
+
+cudaError_t cached_build_run(CachedBuild* c, const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* out,
+                             BuildStats* stats) {
+  if (!c || ngeoms != c->g.ngeoms) return cudaErrorNotReady;
+  // the geometry table is read by the graph's kernels: buffers may have moved
+  GB_CHECK(cudaMemcpyAsync(c->g.d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice, st));
+  GB_CHECK(cudaEventRecord(c->e0, st));
+  GB_CHECK(cudaGraphLaunch(c->exec, st));
+  GB_CHECK(cudaEventRecord(c->e1, st));
+  GraphBuildResult r;
+  GB_CHECK(graph_build_result(c->g, nullptr, nullptr, &r, st));
+  if (r.status != 0) return cudaErrorNotReady;
+  const uint32_t N = c->g.plan.valid_tris;
+  GB_CHECK(cudaMalloc((void**)&out->nodes, (size_t)r.num_nodes * sizeof(WideNode)));
+  GB_CHECK(cudaMalloc((void**)&out->tris, (size_t)N * sizeof(TriRecord)));
+  GB_CHECK(copy_device(out->nodes, c->g.nodes, (size_t)r.num_nodes * sizeof(WideNode), st));
+  GB_CHECK(copy_device(out->tris, c->g.tris, (size_t)N * sizeof(TriRecord), st));
+  GB_CHECK(cudaStreamSynchronize(st));
+  out->num_nodes = r.num_nodes;
+  out->num_tris = N;
+  out->depth = r.depth;
+  out->robust = c->g.opt.robust != 0;
+  for (int d = 0; d < 3; d++) { out->lo[d] = r.lo[d]; out->hi[d] = r.hi[d]; }
+  out->level_start = r.level_start;
+  out->roots = r.roots;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->e0, c->e1);
+  *stats = BuildStats{};
+  stats->sah = r.sah;
+  stats->sah_exact = r.sah_exact;
+  stats->leaf_max = (uint32_t)c->g.plan.leaf_max;
+  stats->build_ms = ms;
+  stats->num_nodes = r.num_nodes;
+  stats->num_leaves = r.num_leaves;
+  stats->num_prims = N;
+  stats->depth = r.depth;
+  stats->ploc_iterations = r.ploc_rounds;
+  return cudaSuccess;
 }
 
 // Sorts (key, value) pairs by their low `passes` digits with the builder's

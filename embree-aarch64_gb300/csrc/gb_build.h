@@ -84,6 +84,8 @@ struct GraphBuildResult {
   uint32_t ploc_rounds = 0;  // PLOC rounds the device ran
   double sah = 0, sah_exact = 0;
   std::vector<uint32_t> level_start;
+  float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // geometry bounds of the replayed build
+  std::vector<uint32_t> roots;  // segmented builds: root node of each geometry slot (kInvalidID: empty)
 };
 enum : uint32_t { kGraphBuildCount = 1, kGraphBuildRounds = 2, kGraphBuildLevels = 4, kGraphBuildError = 8 };
 cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const BuildOptions& opt,
@@ -92,6 +94,27 @@ cudaError_t graph_build_enqueue(const GraphBuild& gbuild, cudaStream_t st);  // 
 cudaError_t graph_build_result(const GraphBuild& gbuild, const float scene_lo[3], const float scene_hi[3],
                                GraphBuildResult* out, cudaStream_t st);  // synchronises st
 void graph_build_release(GraphBuild* gbuild);
+
+// A scene's rebuild replayed from a captured build graph: rtcCommitScene of a scene
+// whose layout (geometries, triangle counts, valid triangles, options) is that of
+// its last host-driven build launches the graph and reads the results once, at the
+// end (no host reads between the build's phases).
+struct CachedBuild {
+  GraphBuild g;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+// Captures the build of `ngeoms` geometries with the plan of the last build (its
+// valid triangles, non-empty roots, depth, PLOC rounds and resolved leaf size).
+cudaError_t cached_build_create(const GeomDesc* h_geoms, int ngeoms, const BuildOptions& opt,
+                                const GraphBuildPlan& plan, cudaStream_t st, CachedBuild** out);
+// Replays it for the geometries `h_geoms` (same layout; buffers may have moved).
+// cudaErrorNotReady: the replayed build does not match the plan (e.g. a different
+// number of valid triangles); the caller builds the ordinary way.
+cudaError_t cached_build_run(CachedBuild* c, const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, DeviceBVH* out,
+                             BuildStats* stats);
+void cached_build_release(CachedBuild* c);
 
 // Device-to-device copy by a kernel when dst, src and bytes are 16-byte multiples
 // (faster than the copy engine), else cudaMemcpyAsync.  Capturable.

@@ -89,6 +89,10 @@ struct Device : RefCounted {
   // consumes rays, so no copy phase is exposed.
   int host_mode = 2;
   bool proposer_mma = false;  // gpu.proposer=mma: proposer inference on mma.sync instead of tcgen05
+  // gpu.graph_rebuild=0 turns off rebuilds replayed from a captured build graph
+  // (scenes committed again with an unchanged layout; the graph keeps the build's
+  // buffers allocated while the scene lives)
+  int graph_rebuild = 1;
   int reorder = 0;            // gpu.reorder=1: streams of >= 65536 rays are traced in octant + origin-Morton order
   int pageable_access = 0;     // cudaDevAttrPageableMemoryAccess
   int host_ptr_registered = 0; // cudaDevAttrCanUseHostPointerForRegisteredMem
@@ -140,6 +144,7 @@ struct Device : RefCounted {
         else if (k == "gpu.collapse") build_opt.collapse = v == "greedy" ? 0 : 1;
         else if (k == "gpu.ploc_radius") build_opt.ploc_radius = atoi(v.c_str());
         else if (k == "gpu.morton_bits") build_opt.morton_bits = atoi(v.c_str()) == 30 ? 30 : 63;
+        else if (k == "gpu.graph_rebuild") graph_rebuild = atoi(v.c_str()) != 0;
         else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
         else if (k == "gpu.proposer") proposer_mma = (v == "mma");
         else if (k == "gpu.reorder") reorder = atoi(v.c_str());
@@ -508,6 +513,10 @@ struct Scene : RefCounted {
   };
   std::vector<SigEntry> built_sig;
   bool built_robust = false;
+  // rebuilds replayed from a captured build graph: the layout key of the last
+  // host-driven build and, once the scene was built twice with that layout, the graph
+  std::vector<uint64_t> layout_key;
+  gb::CachedBuild* gcache = nullptr;
   uint64_t build_serial = 0;  // counts full builds (a refit keeps the BVH's structure)
   std::vector<gb::GeomDesc> descs;  // geometry table of the committed BVH (device buffers)
   bool batched = false;             // rtcgbSetSceneBatched: one tree per geometry
@@ -533,6 +542,7 @@ struct Scene : RefCounted {
     drop_instances();
     if (d_roots) cudaFree(d_roots);
     gb::free_bvh(&bvh);
+    gb::cached_build_release(gcache);
     device->dec();
   }
 
@@ -697,7 +707,51 @@ struct Scene : RefCounted {
     opt.robust = robust;
     opt.segmented = batched ? 1 : 0;
     opt.refit_target = all_refit ? 1 : 0;
-    cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, opt, &bvh, &bs), "rtcCommitScene");
+    // the layout of this build: geometry slots and counts, options (buffer addresses
+    // and strides are read from the geometry table at run time)
+    std::vector<uint64_t> key = {(uint64_t)opt.robust, (uint64_t)opt.segmented, (uint64_t)opt.refit_target,
+                                 (uint64_t)opt.leaf_max, (uint64_t)opt.morton_cube, (uint64_t)opt.morton_bits,
+                                 (uint64_t)opt.collapse, (uint64_t)opt.ploc_radius};
+    for (const gb::GeomDesc& d : descs)
+      key.insert(key.end(), {(uint64_t)d.geomID, (uint64_t)d.ntris, (uint64_t)d.nverts, (uint64_t)d.kind});
+    const bool cacheable = device->graph_rebuild && iboxes.empty() && !descs.empty();
+    bool replayed = false;
+    if (cacheable && gcache && key == layout_key) {
+      const cudaError_t e = gb::cached_build_run(gcache, descs.data(), (int)descs.size(), st, &bvh, &bs);
+      if (e == cudaSuccess) {
+        replayed = true;
+      } else {
+        cudaGetLastError();
+        gb::free_bvh(&bvh);
+        gb::cached_build_release(gcache);
+        gcache = nullptr;
+        if (e != cudaErrorNotReady) cuda_ok(e, "rtcCommitScene (replayed build)");
+      }
+    } else if (gcache && key != layout_key) {
+      gb::cached_build_release(gcache);
+      gcache = nullptr;
+    }
+    if (!replayed) {
+      cuda_ok(gb::build_bvh(descs.data(), (int)descs.size(), st, opt, &bvh, &bs), "rtcCommitScene");
+      // built twice with this layout: capture the build for the next commits
+      if (cacheable && !gcache && key == layout_key && bs.num_prims > 0 && bs.depth >= 1 && bs.depth <= 64) {
+        gb::GraphBuildPlan plan;
+        plan.valid_tris = bs.num_prims;
+        plan.roots = 0;
+        for (uint32_t r : bvh.roots) plan.roots += r != gb::kInvalidID ? 1u : 0u;
+        if (!opt.segmented || plan.roots == 0) plan.roots = 1;
+        plan.ploc_rounds = bs.ploc_iterations;
+        plan.levels = bs.depth;
+        plan.leaf_max = (int)bs.leaf_max;
+        gb::BuildOptions gopt = opt;
+        gopt.leaf_max = plan.leaf_max;
+        if (gb::cached_build_create(descs.data(), (int)descs.size(), gopt, plan, st, &gcache) != cudaSuccess) {
+          cudaGetLastError();
+          gcache = nullptr;  // keep building the ordinary way
+        }
+      }
+      layout_key = key;
+    }
     if (d_roots) cudaFree(d_roots);
     d_roots = nullptr;
     nroots = 0;

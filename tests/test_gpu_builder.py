@@ -171,3 +171,75 @@ def test_refit_after_displacement(rtc, device, oracle):
     st = sc.build_stats()
     assert st["refit"] == 0 and st["num_prims"] == idx.shape[0] - 1
     sc.release()
+
+
+def _committed(rtc, config, meshes, batched=False):
+    device = rtc.Device(config)
+    sc = rtc.Scene(device)
+    if batched:
+        sc.set_batched()
+    for v, i in meshes:
+        sc.add_mesh(v, i)
+    return device, sc
+
+
+@pytest.mark.parametrize("batched", [False, True], ids=["plain", "batched"])
+def test_replayed_rebuild_equals_host_driven_build(rtc, batched):
+    """From its second commit with an unchanged layout a scene's rebuilds are replayed
+    from a captured build graph (no host reads between the build's phases): the BVH is
+    byte-identical to the host-driven build of a device with gpu.graph_rebuild=0, and so
+    are the hits; a vertex update between commits is picked up."""
+    meshes = ([W.heightfield(40, seed=2), W.gaussian_soup(20_000, seed=4), W.heightfield(24, seed=6)] if batched
+              else [W.gaussian_soup(60_000, seed=8)])
+    dref, ref = _committed(rtc, b"gpu.graph_rebuild=0", meshes, batched)
+    dgr, gr = _committed(rtc, b"", meshes, batched)
+    rays = W.sphere_rays(50_000, seed=9)
+    start = np.array([0, 20_000, 35_000, 50_000], np.uint32)
+    for step in range(4):
+        if step == 3:  # move the vertices of geometry 0 (same layout)
+            v0 = meshes[0][0] * np.float32(0.97) + np.float32(0.01)
+            ref.update_vertices(0, v0)
+            gr.update_vertices(0, v0)
+        ref.commit()
+        gr.commit()
+        n1, t1 = ref.bvh()
+        n2, t2 = gr.bvh()
+        assert np.array_equal(n1, n2) and np.array_equal(t1.view(np.uint32), t2.view(np.uint32)), step
+        a, b = rays.copy(), rays.copy()
+        if batched:
+            ref.intersect_batched(a, start)
+            gr.intersect_batched(b, start)
+        else:
+            ref.intersect(a)
+            gr.intersect(b)
+        assert (a.view(np.uint8) == b.view(np.uint8)).all()
+        sa, sb = ref.build_stats(), gr.build_stats()
+        assert sa["num_nodes"] == sb["num_nodes"] and abs(sa["sah"] - sb["sah"]) <= 1e-9 * sa["sah"]
+    for s, d in ((ref, dref), (gr, dgr)):
+        s.release()
+        d.release()
+
+
+def test_replayed_rebuild_falls_back_when_valid_count_changes(rtc, oracle):
+    """A replay whose number of valid triangles differs from the captured plan (here:
+    triangles made degenerate by NaN vertices) is detected on the device; the commit
+    then builds the host-driven way and the hits still match the oracle."""
+    from parity import assert_clean, compare_closest
+    v, i = W.gaussian_soup(30_000, seed=12)
+    device, sc = _committed(rtc, b"", [(v, i)])
+    for _ in range(3):
+        sc.commit()
+    bad = v.copy()
+    bad[: 3 * 500] = np.nan   # the first 500 triangles become invalid
+    sc.update_vertices(0, bad)
+    sc.commit()
+    assert sc.build_stats()["num_prims"] == 30_000 - 500
+    rays = W.sphere_rays(40_000, seed=13)
+    g = rays.copy()
+    sc.intersect(g)
+    orc = oracle.OracleScene([(0, bad, i)])
+    r = rays.copy()
+    orc.intersect(r)
+    assert_clean(compare_closest(orc, rays, g, r))
+    sc.release()
+    device.release()
