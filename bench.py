@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes run")
     ap.add_argument("--no-heightfield", action="store_true", help="skip the heightfield-view run")
     ap.add_argument("--batched-scale", type=float, default=1.0, help="fraction of the batched workload (tests only)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default traversal launch shape (skip rtcgbTuneSceneTraversal)")
     return ap.parse_args()
 
 
@@ -516,12 +518,13 @@ def flush_l2(torch, buf):
     buf.fill_(0)
 
 
-def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds):
+def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds, tune=True):
     """The heightfield view: a 256x256-cell value-noise heightfield (131,072
     triangles), 1024x1024 pinhole primary rays through rtcIntersect1M, then
     shadow rays from the hits through rtcOccluded1M.  The rays (80 MB) fit in
-    L2, so a 256 MB buffer is written between timed launches.  Every ray is
-    compared with the oracle, which is also timed as the CPU baseline."""
+    L2, so a 256 MB buffer is written between timed launches.  The traversal's
+    launch shape is tuned on the view's rays first.  Every ray is compared with
+    the oracle, which is also timed as the CPU baseline."""
     from rtcgb import rays as R
     from rtcgb import workloads as W
     verts, idx = W.heightfield(256)
@@ -540,6 +543,10 @@ def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     pristine = torch.from_numpy(rays.view(np.uint8)).cuda()
     work = torch.empty_like(pristine)
+    tuning = None
+    if tune:
+        from rtcgb import autotune
+        tuning = autotune.tune_scene(sc, ptr=pristine.data_ptr(), count=n, occluded=True, repeats=5)
     kms = []
     for k in range(warmup + steps):
         work.copy_(pristine)
@@ -583,7 +590,8 @@ def run_heightfield(api, dev, torch, stream, steps, warmup, cpu_seconds):
                        "hit_rate": float(np.mean(out_rays["geomID"] != 0xFFFFFFFF))},
            "shadow": {"kernel_ms": sh_ms, "Mrays_per_s": active / (sh_ms * 1e-3) / 1e6, "active_rays": active},
            "e2e": {"Mrays_per_s": n / statistics.median(e2e) / 1e6, "h2d_bytes_per_step": n * 80,
-                   "d2h_bytes_per_step": n * 36, "host_buffer": "pinned"}}
+                   "d2h_bytes_per_step": n * 36, "host_buffer": "pinned"},
+           "autotune": tuning}
     del pristine, work, sh_pristine, sh_work, flush, host
     torch.cuda.empty_cache()
     sc.release()
@@ -861,6 +869,11 @@ def run_gpu(args, rank, world):
 
     pristine = torch.from_numpy(rays.view(np.uint8)).cuda()
     work = torch.empty_like(pristine)
+    # the traversal's launch shape for this workload (closest + any hit on its rays)
+    tuning = None
+    if not args.no_tune:
+        from rtcgb import autotune
+        tuning = autotune.tune_scene(sc, ptr=pristine.data_ptr(), count=nrays, occluded=True, repeats=3)
 
     def step():
         work.copy_(pristine)
@@ -973,6 +986,7 @@ def run_gpu(args, rank, world):
                       "sah_exact_boxes": bst["sah_exact"], "leaf_max": bst["leaf_max"],
                       "nodes": bst["num_nodes"], "depth": bst["depth"], "ploc_iterations": bst["ploc_iterations"],
                       "bvh_MB": bst["bvh_bytes"] / 1e6},
+            "autotune": tuning,
             "learned": None, "animated": None, "batched": None, "heightfield": None,
         }
 
@@ -994,7 +1008,8 @@ def run_gpu(args, rank, world):
                                       0.0 if args.no_cpu else min(8.0, args.cpu_seconds))
     if single and not args.no_heightfield:
         line["heightfield"] = run_heightfield(api, dev, torch, stream, args.steps, args.warmup,
-                                              0.0 if args.no_cpu else min(3.0, args.cpu_seconds))
+                                              0.0 if args.no_cpu else min(3.0, args.cpu_seconds),
+                                              tune=not args.no_tune)
 
     if single and not args.no_cpu:
         key = "soup4M" if args.workload == "soup" else "heightfield256"

@@ -1302,8 +1302,9 @@ cudaError_t Proposer::set_params(const float* host, cudaStream_t st) {
 
 cudaError_t choose_treelets(const DeviceBVH& bvh, cudaStream_t st, std::vector<uint32_t>* roots,
                             std::vector<uint32_t>* record_treelet, std::vector<uint32_t>* record_prim,
-                            std::vector<uint32_t>* record_geom) {
+                            std::vector<uint32_t>* record_geom, uint32_t max_treelets) {
   roots->clear();
+  max_treelets = std::min<uint32_t>(std::max<uint32_t>(max_treelets, 1u), (uint32_t)kTreelets);
   const uint32_t nn = bvh.num_nodes, nt = bvh.num_tris;
   record_treelet->assign(nt, kInvalidID);
   record_prim->assign(nt, kInvalidID);
@@ -1358,7 +1359,7 @@ cudaError_t choose_treelets(const DeviceBVH& bvh, cudaStream_t st, std::vector<u
       else direct += ((n.meta[s] >> 5) & 3u) + 1u;
     }
     const bool splittable = nint > 0 && (top.second == 0u || direct * 8 <= top.first);
-    if (splittable && cut.size() + heap.size() + (size_t)nint <= (size_t)kTreelets) {
+    if (splittable && cut.size() + heap.size() + (size_t)nint <= (size_t)max_treelets) {
       for (int s = 0; s < 8; s++)
         if (n.meta[s] && (n.imask & (1u << s))) {
           const uint32_t ch = child_of(n, s);

@@ -125,13 +125,14 @@ class Proposer {
   float *Z_ = nullptr, *Z4_ = nullptr, *dH_ = nullptr, *dX0_ = nullptr;
 };
 
-// Chooses up to kTreelets subtree roots over the BVH's triangles: starting from
-// the root, the subtree with the most triangles is replaced by its internal
-// children while the count allows and while the triangles it holds directly
-// (which then belong to no treelet) are at most 1/8 of it.  Outputs the roots
-// and, per triangle record, the treelet that holds it (or kInvalidID).
+// Chooses up to max_treelets (<= kTreelets) subtree roots over the BVH's
+// triangles: starting from the root, the subtree with the most triangles is
+// replaced by its internal children while the count allows and while the
+// triangles it holds directly (which then belong to no treelet) are at most 1/8
+// of it.  Outputs the roots and, per triangle record, the treelet that holds it
+// (or kInvalidID).
 cudaError_t choose_treelets(const DeviceBVH& bvh, cudaStream_t st, std::vector<uint32_t>* roots,
                             std::vector<uint32_t>* record_treelet, std::vector<uint32_t>* record_prim,
-                            std::vector<uint32_t>* record_geom);
+                            std::vector<uint32_t>* record_geom, uint32_t max_treelets = kTreelets);
 
 }  // namespace gb

@@ -4,6 +4,26 @@
 
 namespace gb {
 
+// Launch shapes of the traversal kernel: threads per CTA, resident CTAs per SM
+// (the register budget of the plain variants: 65536 / (threads x ctas)),
+// traversal stack entries kept in shared memory, and the idle lanes at which a
+// warp fetches new rays.  Shape 0 is the default; the others are compiled for
+// the plain closest-hit and any-hit kernels on 16-byte aligned records and
+// chosen per scene by the traversal tuner.
+struct TraceShapeDesc {
+  int threads, ctas, shared_stack, refill;
+};
+inline constexpr TraceShapeDesc kTraceShapes[] = {
+    {128, 9, 8, 4},   // default
+    {128, 8, 8, 4},   // 64 registers a thread
+    {128, 9, 16, 4},  // deeper shared stack
+    {128, 9, 4, 4},   // shallower shared stack
+    {64, 18, 8, 4},   // two-warp CTAs
+    {256, 4, 8, 4},   // eight-warp CTAs, 64 registers
+    {128, 9, 8, 8},   // refill at 8 idle lanes
+};
+inline constexpr int kNumTraceShapes = (int)(sizeof(kTraceShapes) / sizeof(kTraceShapes[0]));
+
 struct TraceParams {
   const WideNode* nodes;
   const TriRecord* tris;
@@ -31,10 +51,18 @@ struct TraceParams {
   // the hits a filter callback rejected
   const uint32_t* excl_off;
   const uint2* excl;
+  int shape;                  // index into kTraceShapes (0: default)
 };
 
 // Launches the persistent closest-hit (anyhit = false) or any-hit kernel.
+// P.shape selects the launch shape of the plain kernels on 16-byte aligned
+// records; the other variants (counting, proposals, instances, exclusion lists,
+// unaligned records) always run in the default shape.
 cudaError_t launch_trace(const TraceParams& P, bool anyhit, bool count, cudaStream_t st);
+
+// The plain kernels in a tuned shape (1 <= P.shape < kNumTraceShapes; records
+// 16-byte aligned).  Compiled in gb_trace_shapes.cu.
+cudaError_t launch_tuned_shape(const TraceParams& P, bool anyhit, cudaStream_t st);
 
 // Ray reordering: writes, for M records, keys = direction octant (3 bits) over a
 // 45-bit Morton code of the origin in the box lo..hi (15 bits per axis) and

@@ -16,6 +16,7 @@
 // persistent traversal kernel and return after the stream is synchronised.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -94,6 +95,7 @@ struct Device : RefCounted {
   // buffers allocated while the scene lives)
   int graph_rebuild = 1;
   int reorder = 0;            // gpu.reorder=1: streams of >= 65536 rays are traced in octant + origin-Morton order
+  int trace_shape = 0;        // gpu.trace_shape=N: launch shape of the plain traversal (gb::kTraceShapes)
   int pageable_access = 0;     // cudaDevAttrPageableMemoryAccess
   int host_ptr_registered = 0; // cudaDevAttrCanUseHostPointerForRegisteredMem
   std::mutex mtx;
@@ -119,7 +121,7 @@ struct Device : RefCounted {
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
   // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.morton_bits, gpu.collapse, gpu.ploc_radius,
-  // gpu.host_rays, gpu.proposer, gpu.reorder;
+  // gpu.host_rays, gpu.proposer, gpu.reorder, gpu.graph_rebuild, gpu.trace_shape;
   // the CPU tasking and ISA keys
   // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
   void parse(const char* cfg) {
@@ -148,6 +150,11 @@ struct Device : RefCounted {
         else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
         else if (k == "gpu.proposer") proposer_mma = (v == "mma");
         else if (k == "gpu.reorder") reorder = atoi(v.c_str());
+        else if (k == "gpu.trace_shape") {
+          trace_shape = atoi(v.c_str());
+          if (trace_shape < 0 || trace_shape >= gb::kNumTraceShapes)
+            fail(RTC_ERROR_INVALID_ARGUMENT, "gpu.trace_shape: no such traversal launch shape");
+        }
       }
       i = j + 1;
     }
@@ -533,8 +540,12 @@ struct Scene : RefCounted {
   uint32_t ninsts = 0;
   uint64_t inst_nodes = 0;          // nodes of all instanced BVHs (iteration bound)
   std::vector<std::pair<Scene*, uint64_t>> inst_refs;
+  // launch shape of the plain traversal kernels for this scene's queries
+  // (rtcgbSetSceneTraversalShape / rtcgbTuneSceneTraversal; from the device's
+  // gpu.trace_shape until set)
+  std::atomic<int> trace_shape{0};
 
-  explicit Scene(Device* d) : device(d) { device->inc(); }
+  explicit Scene(Device* d) : device(d), trace_shape(d->trace_shape) { device->inc(); }
   void drop_instances();
   ~Scene() override {
     for (Geometry* g : geoms)
@@ -1054,6 +1065,7 @@ void run_query(Scene* scene, void* rays, unsigned M, size_t stride, bool anyhit,
   P.num_nodes = bvh.num_nodes;
   P.num_tris = bvh.num_tris;
   P.robust = bvh.robust;
+  P.shape = scene->trace_shape.load(std::memory_order_relaxed);
   // batched: the batch boundaries on the device, validated on the host
   std::unique_ptr<uint32_t, void (*)(uint32_t*)> d_start(nullptr, [](uint32_t* p) { if (p) cudaFree(p); });
   if (batch) {
@@ -2092,6 +2104,109 @@ RTC_API void rtcgbIntersect1MNoAlloc(RTCScene hs, struct RTCRayHit* rayhit, unsi
   API_END(s ? s->device : nullptr)
 }
 
+// ---- traversal launch shapes and their tuner
+
+RTC_API unsigned int rtcgbGetTraversalShapes(RTCGBTraversalShape* shapes, unsigned int max_shapes) {
+  for (unsigned i = 0; shapes && i < max_shapes && i < (unsigned)gb::kNumTraceShapes; i++) {
+    shapes[i].threads = (unsigned)gb::kTraceShapes[i].threads;
+    shapes[i].ctas_per_sm = (unsigned)gb::kTraceShapes[i].ctas;
+    shapes[i].shared_stack = (unsigned)gb::kTraceShapes[i].shared_stack;
+    shapes[i].refill = (unsigned)gb::kTraceShapes[i].refill;
+  }
+  return (unsigned)gb::kNumTraceShapes;
+}
+
+RTC_API void rtcgbSetSceneTraversalShape(RTCScene hs, unsigned int shape) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (shape >= (unsigned)gb::kNumTraceShapes) fail(RTC_ERROR_INVALID_ARGUMENT, "no such traversal launch shape");
+  s->trace_shape = (int)shape;
+  API_END(s ? s->device : nullptr)
+}
+
+RTC_API unsigned int rtcgbGetSceneTraversalShape(RTCScene hs) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  return (unsigned)s->trace_shape.load();
+  API_END(s ? s->device : nullptr)
+  return 0;
+}
+
+RTC_API unsigned int rtcgbTuneSceneTraversal(RTCScene hs, const struct RTCRayHit* rayhit, unsigned int M,
+                                             size_t byteStride, const unsigned int* batch_start,
+                                             unsigned int num_batches, unsigned int flags, unsigned int repeats,
+                                             double* ms_per_shape) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  if (!rayhit || M == 0) fail(RTC_ERROR_INVALID_ARGUMENT, "rtcgbTuneSceneTraversal: no rays");
+  if (byteStride < sizeof(RTCRayHit) || (byteStride % 16) != 0)
+    fail(RTC_ERROR_INVALID_ARGUMENT, "rtcgbTuneSceneTraversal: byteStride must be a multiple of 16, >= 80");
+  if (s->filters || s->ninsts || !s->inst_refs.empty())
+    fail(RTC_ERROR_INVALID_OPERATION,
+         "rtcgbTuneSceneTraversal: queries of scenes with filter callbacks or instances use the default shape");
+  if (s->batched != (batch_start != nullptr))
+    fail(RTC_ERROR_INVALID_ARGUMENT, s->batched ? "batched scene: pass its batch boundaries" : "not a batched scene");
+  if (repeats == 0) repeats = 5;
+  repeats = std::min(repeats, 64u);
+  Device* dev = s->device;
+  dev->set_current();
+  ThreadCtx& c = t_ctx;
+  c.ensure(dev->cuda_device);
+  cudaStream_t st = c.stream();
+  // the rays in device memory twice: a pristine copy and the records each timed query overwrites
+  const size_t span = (size_t)(M - 1) * byteStride + sizeof(RTCRayHit);
+  char* mem = nullptr;
+  cuda_ok(cudaMalloc((void**)&mem, 2 * ((span + 255) & ~size_t(255))), "cudaMalloc tuning rays");
+  std::unique_ptr<char, void (*)(char*)> hold(mem, [](char* p) { cudaFree(p); });
+  char* pristine = mem;
+  char* work = mem + ((span + 255) & ~size_t(255));
+  cuda_ok(cudaMemcpyAsync(pristine, rayhit, span, cudaMemcpyDefault, st), "copy tuning rays");
+  BatchArgs b;
+  b.start = batch_start;
+  b.nbatches = num_batches;
+  const int queries = (flags & RTCGB_TUNE_OCCLUDED) ? 2 : 1;
+  const int before = s->trace_shape.load();
+  std::vector<std::vector<double>> ms(gb::kNumTraceShapes);
+  try {
+    // round 0 loads each shape's kernels and warms the caches; shapes take turns
+    // within every round so that clock changes spread over all of them
+    for (unsigned r = 0; r <= repeats; r++)
+      for (int sh = 0; sh < gb::kNumTraceShapes; sh++) {
+        double t = 0;
+        for (int q = 0; q < queries; q++) {
+          cuda_ok(gb::copy_device(work, pristine, span, st), "restore tuning rays");
+          s->trace_shape = sh;
+          run_query(s, work, M, byteStride, q == 1, q == 1 ? sizeof(RTCRay) : sizeof(RTCRayHit), nullptr,
+                    s->batched ? &b : nullptr);
+          t += c.last.kernel_ms;
+        }
+        if (r > 0) ms[sh].push_back(t);
+      }
+  } catch (...) {
+    s->trace_shape = before;
+    throw;
+  }
+  // median per shape; a shape other than the default must beat it by 1 %
+  std::vector<double> med(gb::kNumTraceShapes);
+  for (int sh = 0; sh < gb::kNumTraceShapes; sh++) {
+    std::vector<double>& v = ms[sh];
+    std::sort(v.begin(), v.end());
+    med[sh] = v.size() % 2 ? v[v.size() / 2] : 0.5 * (v[v.size() / 2 - 1] + v[v.size() / 2]);
+    if (ms_per_shape) ms_per_shape[sh] = med[sh];
+  }
+  int pick = 0;
+  for (int sh = 1; sh < gb::kNumTraceShapes; sh++)
+    if (med[sh] < med[pick] && med[sh] <= 0.99 * med[0]) pick = sh;
+  s->trace_shape = pick;
+  return (unsigned)pick;
+  API_END(s ? s->device : nullptr)
+  return 0;
+}
+
 RTC_API int rtcgbGetDeviceHostAccess(RTCDevice hdevice) {
   Device* d = (Device*)hdevice;
   if (!d) return -1;
@@ -2159,8 +2274,14 @@ cudaStream_t proposer_stream(ProposerObj* p) {
 }  // namespace
 
 RTC_API RTCGBProposer rtcgbNewProposer(RTCScene hs, unsigned int seed) {
+  return rtcgbNewProposerEx(hs, seed, gb::kTreelets);
+}
+
+RTC_API RTCGBProposer rtcgbNewProposerEx(RTCScene hs, unsigned int seed, unsigned int max_treelets) {
   Scene* s = (Scene*)hs;
   API_BEGIN
+  if (max_treelets < 8 || max_treelets > (unsigned)gb::kTreelets)
+    fail(RTC_ERROR_INVALID_ARGUMENT, "max_treelets must be within 8..4096");
   VERIFY_HANDLE(hs);
   std::lock_guard<std::mutex> lk(s->mtx);
   if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
@@ -2171,7 +2292,8 @@ RTC_API RTCGBProposer rtcgbNewProposer(RTCScene hs, unsigned int seed) {
   ProposerObj* p = new ProposerObj(s);
   try {
     std::vector<uint32_t> prim, geom;
-    cuda_ok(gb::choose_treelets(s->bvh, st, &p->roots, &p->record_treelet, &prim, &geom), "treelet cut");
+    cuda_ok(gb::choose_treelets(s->bvh, st, &p->roots, &p->record_treelet, &prim, &geom, max_treelets),
+            "treelet cut");
     // primitive numbering of the labels: geometry slots in ID order
     std::vector<uint32_t> prefix(s->geoms.size(), gb::kInvalidID);
     uint64_t total = 0;
@@ -2637,6 +2759,7 @@ RTC_API RTCGBBatchedFrame rtcgbNewBatchedFrame(RTCScene hs, struct RTCRayHit* ra
     P.batch_start = f->d_start;
     P.batch_root = f->gbuild.seg_index;  // geometry IDs are the segments
     P.nbatches = num_batches;
+    P.shape = s->trace_shape.load(std::memory_order_relaxed);
     const size_t span = (size_t)(M - 1) * byteStride + sizeof(RTCRayHit);
     cuda_ok(cudaStreamSynchronize(st), "frame");
     cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");

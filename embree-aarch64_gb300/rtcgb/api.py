@@ -44,7 +44,8 @@ rtcGetSceneFlags rtcGetSceneBounds rtcGetSceneLinearBounds rtcIntersect1 rtcInte
 rtcOccluded1 rtcOccluded1M rtcOccluded1Mp rtcIntersect4 rtcIntersect8 rtcIntersect16 rtcIntersectNM
 rtcIntersectNp rtcOccluded4 rtcOccluded8 rtcOccluded16 rtcOccludedNM rtcOccludedNp rtcgbGetSceneBuildStats rtcgbGetLastQueryStats rtcgbSetQueryCounting
 rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs rtcgbIntersect1MNoAlloc rtcgbGetDeviceHostAccess
-rtcgbNewProposer rtcgbRetainProposer rtcgbReleaseProposer rtcgbProposerTrain rtcgbProposerPredict rtcgbProposerGetStats
+rtcgbGetTraversalShapes rtcgbSetSceneTraversalShape rtcgbGetSceneTraversalShape rtcgbTuneSceneTraversal
+rtcgbNewProposer rtcgbNewProposerEx rtcgbRetainProposer rtcgbReleaseProposer rtcgbProposerTrain rtcgbProposerPredict rtcgbProposerGetStats
 rtcgbProposerParamCount rtcgbProposerGetParams rtcgbProposerSetParams rtcgbProposerGradients rtcgbProposerGetTreelets
 rtcgbIntersect1MLearned rtcgbOccluded1MLearned rtcgbNewPathTracer rtcgbRetainPathTracer rtcgbReleasePathTracer
 rtcgbPathTracerAnimateSoup rtcgbPathTracerSetProposer rtcgbPathTracerRenderFrame rtcgbPathTracerTrainProposer
@@ -119,6 +120,13 @@ class RTCGBProposerStats(ctypes.Structure):
                 ("top4", ctypes.c_double)]
 
 
+class RTCGBTraversalShape(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_uint), ("ctas_per_sm", ctypes.c_uint), ("shared_stack", ctypes.c_uint),
+                ("refill", ctypes.c_uint)]
+
+
+RTCGB_TUNE_OCCLUDED = 1
+
 ERROR_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p)
 MEMORY_FN = ctypes.CFUNCTYPE(ctypes.c_bool, ctypes.c_void_p, ctypes.c_ssize_t, ctypes.c_bool)
 PROGRESS_FN = ctypes.CFUNCTYPE(ctypes.c_bool, ctypes.c_void_p, ctypes.c_double)
@@ -185,7 +193,12 @@ def load(build=True):
         "rtcgbRadixSortPairs": (i, [vp, vp, u]),
         "rtcgbIntersect1MNoAlloc": (None, [vp, vp, u, sz, vp]),
         "rtcgbGetDeviceHostAccess": (i, [vp]),
-        "rtcgbNewProposer": (vp, [vp, u]), "rtcgbRetainProposer": (None, [vp]),
+        "rtcgbGetTraversalShapes": (u, [ctypes.POINTER(RTCGBTraversalShape), u]),
+        "rtcgbSetSceneTraversalShape": (None, [vp, u]),
+        "rtcgbGetSceneTraversalShape": (u, [vp]),
+        "rtcgbTuneSceneTraversal": (u, [vp, vp, u, sz, vp, u, u, u, ctypes.POINTER(ctypes.c_double)]),
+        "rtcgbNewProposer": (vp, [vp, u]), "rtcgbNewProposerEx": (vp, [vp, u, u]),
+        "rtcgbRetainProposer": (None, [vp]),
         "rtcgbReleaseProposer": (None, [vp]),
         "rtcgbProposerTrain": (None, [vp, vp, u, sz, u, u, ctypes.c_float]),
         "rtcgbProposerPredict": (None, [vp, vp, u, sz, vp]),
@@ -430,6 +443,36 @@ class Scene:
         self.dev.check("rtcgbOccluded1MBatched")
         return rays
 
+    @property
+    def traversal_shape(self):
+        """Launch shape of this scene's plain queries (index into traversal_shapes())."""
+        v = self.L.rtcgbGetSceneTraversalShape(self.h)
+        self.dev.check("rtcgbGetSceneTraversalShape")
+        return v
+
+    @traversal_shape.setter
+    def traversal_shape(self, shape):
+        self.L.rtcgbSetSceneTraversalShape(self.h, shape)
+        self.dev.check("rtcgbSetSceneTraversalShape")
+
+    def tune_traversal(self, rays=None, batch_start=None, occluded=False, repeats=5, ptr=None, count=None,
+                       stride=80):
+        """rtcgbTuneSceneTraversal on host RTCRayHit records `rays` (or device records at
+        `ptr`): sets and returns the fastest launch shape, with the median milliseconds
+        of every shape."""
+        n = len(traversal_shapes())
+        ms = (ctypes.c_double * n)()
+        bs = None if batch_start is None else np.ascontiguousarray(batch_start, np.uint32)
+        if ptr is None:
+            ptr, count, stride = _ptr(rays), rays.shape[0], rays.dtype.itemsize
+        else:
+            ptr = ctypes.c_void_p(ptr)
+        pick = self.L.rtcgbTuneSceneTraversal(self.h, ptr, count, stride, None if bs is None else _ptr(bs),
+                                              0 if bs is None else bs.shape[0] - 1,
+                                              RTCGB_TUNE_OCCLUDED if occluded else 0, repeats, ms)
+        self.dev.check("rtcgbTuneSceneTraversal")
+        return pick, list(ms)
+
     def bvh(self):
         """Copies the committed BVH: (nodes uint8 [n,80], tris float32 [m,12])."""
         nt = ctypes.c_uint()
@@ -471,6 +514,15 @@ def radix_sort_pairs(keys, values):
     return k, v
 
 
+def traversal_shapes():
+    """The compiled launch shapes of the traversal kernels, shape 0 first (dicts)."""
+    L = load()
+    n = L.rtcgbGetTraversalShapes(None, 0)
+    arr = (RTCGBTraversalShape * n)()
+    L.rtcgbGetTraversalShapes(arr, n)
+    return [{f: getattr(a, f) for f, _ in a._fields_} for a in arr]
+
+
 def set_thread_stream(stream_ptr):
     load().rtcgbSetThreadStream(ctypes.c_void_p(stream_ptr) if stream_ptr else None)
 
@@ -478,10 +530,13 @@ def set_thread_stream(stream_ptr):
 class Proposer:
     """Learned hit proposer of a committed scene (rtcgbNewProposer)."""
 
-    def __init__(self, scene, seed=1):
+    def __init__(self, scene, seed=1, max_treelets=None):
         self.scene = scene
         self.L = scene.L
-        self.h = ctypes.c_void_p(self.L.rtcgbNewProposer(scene.h, seed))
+        if max_treelets is None:
+            self.h = ctypes.c_void_p(self.L.rtcgbNewProposer(scene.h, seed))
+        else:
+            self.h = ctypes.c_void_p(self.L.rtcgbNewProposerEx(scene.h, seed, max_treelets))
         scene.dev.check("rtcgbNewProposer")
 
     def train(self, records, epochs=1, batch=16384, lr=5e-3, count=None, stride=80):

@@ -1,8 +1,8 @@
 """Builds the C-ABI shared library librtcore_gb300.so for sm_103a.
 
-Five translation units (builder, traversal, proposer, path tracer, C ABI)
-are compiled in parallel with nvcc and linked into
-one shared object (soname libembree3.so.3, so a program linked against the
+Six translation units (builder, traversal, tuned traversal shapes, proposer,
+path tracer, C ABI) are compiled in parallel with nvcc and linked into one
+shared object (soname libembree3.so.3, so a program linked against the
 reference's library name finds it).  The traversal and builder units use
 --fmad=false: the hit-deciding arithmetic spells out every FMA itself.
 """
@@ -19,7 +19,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librtcore_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gb_build.cu", "gb_trace.cu", "gb_learned.cu", "gb_paths.cu", "rtcore_api.cpp"]
+SOURCES = ["gb_build.cu", "gb_trace.cu", "gb_trace_shapes.cu", "gb_learned.cu", "gb_paths.cu", "rtcore_api.cpp"]
 
 
 def _nvcc():

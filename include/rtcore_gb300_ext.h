@@ -101,6 +101,46 @@ RTC_API int rtcgbRadixSortPairs(unsigned long long* keys, unsigned int* values, 
 RTC_API void rtcgbIntersect1MNoAlloc(RTCScene scene, struct RTCRayHit* rayhit, unsigned int M, size_t byteStride,
                                      void* cuda_stream);
 
+/* ---- Traversal launch shapes and their tuner (no counterpart in the reference)
+
+   The plain closest-hit and any-hit traversal kernels (records 16-byte
+   aligned, scenes without filter callbacks or instances; plain, robust and
+   batched scenes) are compiled in several launch shapes: threads per CTA,
+   resident CTAs per SM (their register budget is 65536 / (threads x CTAs)),
+   traversal stack entries kept in shared memory, and the number of idle lanes
+   at which a warp fetches new rays.  Shape 0 is the default.  Every shape
+   returns the same hits; only the speed differs.  A scene's queries use its
+   shape, which starts as the device's gpu.trace_shape (default 0); the other
+   kernel variants (counting, learned, instances, filter callbacks, unaligned
+   records, the no-allocation query, the path tracer) always run shape 0, and
+   a batched frame keeps the shape its scene had when the frame was made. */
+typedef struct RTCGBTraversalShape {
+  unsigned int threads;       /* threads per CTA */
+  unsigned int ctas_per_sm;   /* resident CTAs per SM the kernels are compiled for */
+  unsigned int shared_stack;  /* traversal stack entries in shared memory (the rest in local memory) */
+  unsigned int refill;        /* a warp fetches new rays when this many of its lanes are idle */
+} RTCGBTraversalShape;
+
+/* Writes up to max_shapes shapes; returns the number of compiled shapes. */
+RTC_API unsigned int rtcgbGetTraversalShapes(RTCGBTraversalShape* shapes, unsigned int max_shapes);
+RTC_API void rtcgbSetSceneTraversalShape(RTCScene scene, unsigned int shape);
+RTC_API unsigned int rtcgbGetSceneTraversalShape(RTCScene scene);
+
+/* Picks the scene's shape for a workload: times rtcIntersect1M (batched
+   scenes: rtcgbIntersect1MBatched with the given batches) on a device copy of
+   the M records -- and with RTCGB_TUNE_OCCLUDED also rtcOccluded1M on the
+   same records -- in every shape, `repeats` rounds (0: 5) after one warm-up
+   round, the shapes taking turns within each round.  The shape with the
+   least median kernel time is set on the scene and returned; a shape other
+   than 0 must be at least 1 % faster than shape 0.  ms_per_shape (optional,
+   one entry per shape) receives the medians in milliseconds.  The records are
+   not modified.  Do not query the scene from other threads meanwhile. */
+#define RTCGB_TUNE_OCCLUDED 1u
+RTC_API unsigned int rtcgbTuneSceneTraversal(RTCScene scene, const struct RTCRayHit* rayhit, unsigned int M,
+                                             size_t byteStride, const unsigned int* batch_start,
+                                             unsigned int num_batches, unsigned int flags, unsigned int repeats,
+                                             double* ms_per_shape);
+
 /* ---- Learned hit proposer (no counterpart in the reference) ----------------
 
    A proposer belongs to one committed scene.  It cuts the scene's BVH into up
@@ -127,6 +167,10 @@ typedef struct RTCGBProposerStats {
 } RTCGBProposerStats;
 
 RTC_API RTCGBProposer rtcgbNewProposer(RTCScene scene, unsigned int seed);
+/* The same with a treelet budget: the cut has at most max_treelets (8..4096)
+   treelets; the network keeps its 4096 outputs, the unused ones never win.
+   rtcgbNewProposer(scene, seed) is rtcgbNewProposerEx(scene, seed, 4096). */
+RTC_API RTCGBProposer rtcgbNewProposerEx(RTCScene scene, unsigned int seed, unsigned int max_treelets);
 RTC_API void rtcgbRetainProposer(RTCGBProposer proposer);
 RTC_API void rtcgbReleaseProposer(RTCGBProposer proposer);
 

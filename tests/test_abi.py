@@ -185,4 +185,5 @@ def test_autotune_config_strings():
     from rtcgb import autotune
     s = autotune.config_string({"gpu.leaf_max": 2, "gpu.morton": "cube", "gpu.ploc_radius": 4}, "gpu.device=0")
     assert s == "gpu.device=0,gpu.leaf_max=2,gpu.morton=cube,gpu.ploc_radius=4"
-    assert all(set(c) == {"gpu.leaf_max", "gpu.morton", "gpu.ploc_radius"} for c in autotune.CANDIDATES)
+    assert all(set(c) == {"gpu.leaf_max", "gpu.morton", "gpu.ploc_radius", "gpu.morton_bits"} for c in autotune.CANDIDATES)
+    assert {c["gpu.morton_bits"] for c in autotune.CANDIDATES} == {63, 30}

@@ -128,11 +128,15 @@ def test_autotuner_picks_the_fastest_candidate(rtc):
         parts.append(r)
         start.append(start[-1] + r.shape[0])
     rays = np.concatenate(parts)
-    cands = autotune.CANDIDATES[:3]
-    best, results = autotune.tune(meshes, rays, np.array(start, np.uint32), candidates=cands)
-    assert [r["config"] for r in results] == cands
+    cands = autotune.CANDIDATES[:3] + [c for c in autotune.CANDIDATES if c["gpu.morton_bits"] == 30][:1]
+    best, results = autotune.tune(meshes, rays, np.array(start, np.uint32), candidates=cands, shape_repeats=2)
+    shapes = results.pop()["shapes"]
+    assert [r["config"] for r in results] == [autotune.DEFAULT] + cands
     assert all(r["build_ms"] > 0 and r["trace_ms"] > 0 for r in results)
-    assert best == min(results, key=lambda r: r["total_ms"])["config"]
+    chosen = dict(best)
+    assert chosen.pop("gpu.trace_shape") == shapes["pick"]
+    assert chosen == min(results, key=lambda r: r["total_ms"])["config"]
+    assert len(shapes["ms"]) == len(rtc.traversal_shapes()) and min(shapes["ms"]) > 0
 
 
 @pytest.mark.parametrize("config", [b"", b"gpu.morton_bits=30"], ids=["key63", "key30"])
