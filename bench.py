@@ -307,7 +307,8 @@ def run_learned(api, dev, torch, stream, scale, steps, warmup, cpu_seconds):
     724x724 heightfield + 300k soup triangles, 1024x1024 primary view, 8
     cosine-weighted AO rays (tfar 0.05) and 8 diffuse bounce rays per primary
     hit.  The proposer is trained on ~10M closest-hit records the plain
-    traversal logs for rays drawn with other seeds.  Times include the
+    traversal logs for rays drawn with other seeds, with the treelet budget the
+    autotuner picks for this workload.  Times include the
     proposer's inference (the learned calls' kernel time covers inference +
     seeded traversal)."""
     from rtcgb import rays as R
@@ -330,7 +331,27 @@ def run_learned(api, dev, torch, stream, scale, steps, warmup, cpu_seconds):
     nlog = log.numel() // 80
     del ao_t, b_t
     sc.intersect_ptr(log.data_ptr(), nlog, 80)
-    prop = api.Proposer(sc, seed=7)
+    # treelet budget for this workload, timed on 2 AO + 2 bounce rays per hit drawn
+    # with other seeds (speed only: every budget returns the plain traversal's hits)
+    from rtcgb import autotune
+    tq = []
+    for rec, stride, fn in ((W.hemisphere_rays(prim, 2, seed=51, tfar=0.05, record=R.RAY_DTYPE)[0], 48, "occluded_ptr"),
+                            (W.hemisphere_rays(prim, 2, seed=52)[0], 80, "intersect_ptr")):
+        tq.append((torch.from_numpy(rec.view(np.uint8)).cuda(), rec.shape[0], stride, fn))
+
+    def tuning_query(q):
+        src, n, stride, fn = q
+
+        def run(p):
+            w = src.clone()
+            getattr(p, fn)(w.data_ptr(), n, stride)
+            return api.last_query_stats()["kernel_ms"]
+        return run
+
+    max_treelets, treelet_tuning = autotune.tune_treelets(sc, log.data_ptr(), [tuning_query(q) for q in tq],
+                                                          count=nlog)
+    del tq
+    prop = api.Proposer(sc, seed=7, max_treelets=max_treelets)
     torch.cuda.synchronize()
     t = time.perf_counter()
     st = prop.train(log.data_ptr(), epochs=2, batch=16384, lr=5e-3, count=nlog)
@@ -354,7 +375,9 @@ def run_learned(api, dev, torch, stream, scale, steps, warmup, cpu_seconds):
                        f"8 AO rays (tfar 0.05) + 8 bounce rays per hit",
            "train": {"records": int(nlog), "labelled": int(st["samples"]), "epochs": 2, "batch": 16384,
                      "seconds": train_s, "loss": st["loss"], "top1": st["top1"], "top4": st["top4"],
-                     "treelets": int(st["num_treelets"])}}
+                     "treelets": int(st["num_treelets"])},
+           "autotune": {"max_treelets": max_treelets, "candidates": treelet_tuning,
+                        "objective": "learned AO + bounce kernel time on 2 + 2 rays per hit (other seeds)"}}
     total_plain = total_learned = 0.0
     for name, rays, stride, plain_fn, learned_fn in (
             ("ao", ao, 48, sc.occluded_ptr, prop.occluded_ptr),
