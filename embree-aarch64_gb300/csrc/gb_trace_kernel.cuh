@@ -143,8 +143,13 @@ __device__ __forceinline__ float ubyte_f(uint32_t w, uint32_t k) {
 // (one each from p - o, the product with 1/d, 1/d itself, the offset a - 2^15 b,
 // the FMA and the subtraction of the slack); 8u = 2^-21 covers them with
 // margin.  The 2^15 s term widens a box by 2^15 * 8u = 1.6 % of one
-// quantisation step.
-constexpr float kSlabEps = 4.76837158e-7f;
+// quantisation step.  It is formed from the products the test needs anyway:
+// |a| + |B| with a = fl((p - o) / d) >= |p - o| |1/d| (1 - u) and B = 2^15 s / d
+// exact, so (|a| + |B|) * 2^-21 (1 + 2^-21), all rounded up, is at least
+// (|p - o| + 2^15 s) |1/d| 8u; the floor 2^-144 (32 ulps of the smallest
+// subnormal) covers the absolute rounding errors where the products underflow.
+constexpr float kSlabEps = 0x1.000008p-21f;  // 2^-21 (1 + 2^-21)
+constexpr float kSlabFloor = 0x1p-144f;      // 2^-144
 
 // Intersects the 8 children of `np`.  Child box planes are p + q * 2^e; with
 // B = 2^15 * 2^e / d and A = (p - o) / d - B precomputed per node and axis, a
@@ -181,9 +186,9 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
     by = __fmul_rn(sy * 32768.0f, r.rdir.y);
     bz = __fmul_rn(sz * 32768.0f, r.rdir.z);
     const float ax2 = __fsub_rn(ax, bx), ay2 = __fsub_rn(ay, by), az2 = __fsub_rn(az, bz);
-    const float ex = __fmul_ru(__fmul_ru(__fmaf_ru(32768.0f, sx, fabsf(xo)), fabsf(r.rdir.x)), kSlabEps);
-    const float ey = __fmul_ru(__fmul_ru(__fmaf_ru(32768.0f, sy, fabsf(yo)), fabsf(r.rdir.y)), kSlabEps);
-    const float ez = __fmul_ru(__fmul_ru(__fmaf_ru(32768.0f, sz, fabsf(zo)), fabsf(r.rdir.z)), kSlabEps);
+    const float ex = __fmaf_ru(__fadd_ru(fabsf(ax), fabsf(bx)), kSlabEps, kSlabFloor);
+    const float ey = __fmaf_ru(__fadd_ru(fabsf(ay), fabsf(by)), kSlabEps, kSlabFloor);
+    const float ez = __fmaf_ru(__fadd_ru(fabsf(az), fabsf(bz)), kSlabEps, kSlabFloor);
     anx = __fsub_rd(ax2, ex); afx = __fadd_ru(ax2, ex);
     any_ = __fsub_rd(ay2, ey); afy = __fadd_ru(ay2, ey);
     anz = __fsub_rd(az2, ez); afz = __fadd_ru(az2, ez);
@@ -460,12 +465,14 @@ __global__ void __launch_bounds__(SH::kThreads, (COUNT || SEEDED || INST || EXCL
       }
     }
     // ---- (2) triangles, postponed while few lanes have any
-    const uint32_t want = __ballot_sync(0xFFFFFFFFu, active && t_bits != 0);
-    const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
-    if (visited && t_bits != 0 && __popc(want) * 100 < __popc(act) * kPostponePct) {
-      if (sp < kStackSize) {
-        push(make_uint2(t_base | kTriGroup, t_bits));
-        t_bits = 0;
+    if constexpr (kPostponePct > 0) {
+      const uint32_t want = __ballot_sync(0xFFFFFFFFu, active && t_bits != 0);
+      const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
+      if (visited && t_bits != 0 && __popc(want) * 100 < __popc(act) * kPostponePct) {
+        if (sp < kStackSize) {
+          push(make_uint2(t_base | kTriGroup, t_bits));
+          t_bits = 0;
+        }
       }
     }
     while (active && t_bits) {
