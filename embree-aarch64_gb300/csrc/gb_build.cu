@@ -104,7 +104,9 @@ __device__ __forceinline__ int find_geom(const GeomDesc* geoms, int ngeoms, uint
 }
 
 // plo[i] = (lo.xyz, geometry slot), phi[i] = (hi.xyz, primID); invalid
-// triangles get an empty box (+inf,-inf).
+// triangles get an empty box (+inf,-inf).  Grid-stride: the bounds and the
+// valid count are reduced per thread, per warp and per CTA, so the global
+// atomics are 13 per CTA (a grid of a few CTAs per SM).
 __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ geoms, int ngeoms, uint32_t total,
                                                   float4* __restrict__ plo, float4* __restrict__ phi,
                                                   BoundsAcc* acc) {
@@ -113,41 +115,49 @@ __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ g
   if (threadIdx.x < 12) s_b[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0xFFFFFFFFu : 0u;
   if (threadIdx.x == 0) s_cnt = 0;
   __syncthreads();
-  const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-  bool ok = false;
-  float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
-  if (gi < total) {
-    const int gs = find_geom(geoms, ngeoms, gi);
-    const GeomDesc g = geoms[gs];
-    const uint32_t j = gi - g.prim_offset;
-    if (g.kind == 1) {
-      const InstBox bx = reinterpret_cast<const InstBox*>(g.verts)[j];
-      if (vtx_ok(bx.lo[0], bx.lo[1], bx.lo[2]) && vtx_ok(bx.hi[0], bx.hi[1], bx.hi[2]) && bx.lo[0] <= bx.hi[0] &&
-          bx.lo[1] <= bx.hi[1] && bx.lo[2] <= bx.hi[2]) {
-        ok = true;
-        lo = make_float3(bx.lo[0], bx.lo[1], bx.lo[2]);
-        hi = make_float3(bx.hi[0], bx.hi[1], bx.hi[2]);
+  float v[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) v[k] = (k % 6) < 3 ? INFINITY : -INFINITY;
+  unsigned nok = 0;
+  for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < total; gi += gridDim.x * blockDim.x) {
+    bool ok = false;
+    float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+    {
+      const int gs = find_geom(geoms, ngeoms, gi);
+      const GeomDesc g = geoms[gs];
+      const uint32_t j = gi - g.prim_offset;
+      if (g.kind == 1) {
+        const InstBox bx = reinterpret_cast<const InstBox*>(g.verts)[j];
+        if (vtx_ok(bx.lo[0], bx.lo[1], bx.lo[2]) && vtx_ok(bx.hi[0], bx.hi[1], bx.hi[2]) && bx.lo[0] <= bx.hi[0] &&
+            bx.lo[1] <= bx.hi[1] && bx.lo[2] <= bx.hi[2]) {
+          ok = true;
+          lo = make_float3(bx.lo[0], bx.lo[1], bx.lo[2]);
+          hi = make_float3(bx.hi[0], bx.hi[1], bx.hi[2]);
+        }
+      } else {
+      const uint3 t = load_tri(g, j);
+      if (t.x < g.nverts && t.y < g.nverts && t.z < g.nverts) {
+        const float3 a = load_vtx(g, t.x), b = load_vtx(g, t.y), c = load_vtx(g, t.z);
+        if (vtx_ok(a.x, a.y, a.z) && vtx_ok(b.x, b.y, b.z) && vtx_ok(c.x, c.y, c.z)) {
+          ok = true;
+          lo = f3min(f3min(a, b), c);
+          hi = f3max(f3max(a, b), c);
+        }
       }
-    } else {
-    const uint3 t = load_tri(g, j);
-    if (t.x < g.nverts && t.y < g.nverts && t.z < g.nverts) {
-      const float3 a = load_vtx(g, t.x), b = load_vtx(g, t.y), c = load_vtx(g, t.z);
-      if (vtx_ok(a.x, a.y, a.z) && vtx_ok(b.x, b.y, b.z) && vtx_ok(c.x, c.y, c.z)) {
-        ok = true;
-        lo = f3min(f3min(a, b), c);
-        hi = f3max(f3max(a, b), c);
       }
+      plo[gi] = make_float4(lo.x, lo.y, lo.z, __uint_as_float((uint32_t)gs));
+      phi[gi] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(j));
     }
+    v[0] = fminf(v[0], lo.x); v[1] = fminf(v[1], lo.y); v[2] = fminf(v[2], lo.z);
+    v[3] = fmaxf(v[3], hi.x); v[4] = fmaxf(v[4], hi.y); v[5] = fmaxf(v[5], hi.z);
+    if (ok) {
+      const float3 c = make_float3((lo.x + hi.x) * 0.5f, (lo.y + hi.y) * 0.5f, (lo.z + hi.z) * 0.5f);
+      v[6] = fminf(v[6], c.x); v[7] = fminf(v[7], c.y); v[8] = fminf(v[8], c.z);
+      v[9] = fmaxf(v[9], c.x); v[10] = fmaxf(v[10], c.y); v[11] = fmaxf(v[11], c.z);
+      nok++;
     }
-    plo[gi] = make_float4(lo.x, lo.y, lo.z, __uint_as_float((uint32_t)gs));
-    phi[gi] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(j));
   }
   // warp-reduce bounds then shared atomics
-  float v[12];
-  const float3 c = make_float3((lo.x + hi.x) * 0.5f, (lo.y + hi.y) * 0.5f, (lo.z + hi.z) * 0.5f);
-  v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = hi.x; v[4] = hi.y; v[5] = hi.z;
-  if (ok) { v[6] = c.x; v[7] = c.y; v[8] = c.z; v[9] = c.x; v[10] = c.y; v[11] = c.z; }
-  else { v[6] = v[7] = v[8] = INFINITY; v[9] = v[10] = v[11] = -INFINITY; }
 #pragma unroll
   for (int k = 0; k < 12; k++) {
     float x = v[k];
@@ -159,7 +169,7 @@ __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ g
     }
     v[k] = x;
   }
-  const unsigned nok = __popc(__ballot_sync(0xFFFFFFFFu, ok));
+  nok = __reduce_add_sync(0xFFFFFFFFu, nok);
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
     for (int k = 0; k < 12; k++) {
@@ -208,60 +218,76 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
 // digit passes instead of 8; invalid primitives get the all-ones key of that width.
 constexpr uint32_t kMaxSegments = 4096;
 
+// Grid-stride; the AND / OR of all keys (constant digits are not sorted) is
+// reduced per thread, per warp and per CTA: two global atomics per CTA.
 __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                 uint32_t n, BoundsAcc* acc, uint64_t* __restrict__ keys,
                                                 uint32_t* __restrict__ vals, int cube, int segmented, int bits30) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t key = bits30 ? (~0ull >> (segmented ? 22 : 34)) : ~0ull;
-  if (i < n) {
-    const float4 a = plo[i], b = phi[i];
-    if (a.x <= b.x) {
-      const float lo[3] = {ord2f(acc->clo[0]), ord2f(acc->clo[1]), ord2f(acc->clo[2])};
-      const float hi[3] = {ord2f(acc->chi[0]), ord2f(acc->chi[1]), ord2f(acc->chi[2])};
-      const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
-      // one scale for all axes (the centroid box's largest extent) keeps the
-      // scene's aspect ratio, so flat scenes (heightfields) are ordered mostly
-      // in-plane, which lowers their SAH; per-axis scales trace faster on
-      // volumetric scenes.  cube: 0 per-axis, 1 one scale, 2 one scale when
-      // the centroid box is flat
-      const float emax = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-      const float emin = fminf(fminf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-      const bool one_scale = cube == 1 || (cube == 2 && emin < 0.5f * emax);
-      uint64_t code = 0;
-      if (bits30) {
-        uint32_t c30 = 0;
+  __shared__ unsigned long long s_and, s_or;
+  if (threadIdx.x == 0) {
+    s_and = ~0ull;
+    s_or = 0ull;
+  }
+  __syncthreads();
+  unsigned long long ka = ~0ull, ko = 0ull;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint64_t key = bits30 ? (~0ull >> (segmented ? 22 : 34)) : ~0ull;
+    {
+      const float4 a = plo[i], b = phi[i];
+      if (a.x <= b.x) {
+        const float lo[3] = {ord2f(acc->clo[0]), ord2f(acc->clo[1]), ord2f(acc->clo[2])};
+        const float hi[3] = {ord2f(acc->chi[0]), ord2f(acc->chi[1]), ord2f(acc->chi[2])};
+        const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+        // one scale for all axes (the centroid box's largest extent) keeps the
+        // scene's aspect ratio, so flat scenes (heightfields) are ordered mostly
+        // in-plane, which lowers their SAH; per-axis scales trace faster on
+        // volumetric scenes.  cube: 0 per-axis, 1 one scale, 2 one scale when
+        // the centroid box is flat
+        const float emax = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+        const float emin = fminf(fminf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+        const bool one_scale = cube == 1 || (cube == 2 && emin < 0.5f * emax);
+        uint64_t code = 0;
+        if (bits30) {
+          uint32_t c30 = 0;
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-          const float ext = one_scale ? emax : hi[d] - lo[d];
-          float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
-          x = fminf(fmaxf(x * 1024.0f, 0.0f), 1023.0f);
-          c30 |= spread10((uint32_t)x) << (2 - d);
-        }
-        key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 30) | c30 : c30;
-      } else {
+          for (int d = 0; d < 3; d++) {
+            const float ext = one_scale ? emax : hi[d] - lo[d];
+            float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
+            x = fminf(fmaxf(x * 1024.0f, 0.0f), 1023.0f);
+            c30 |= spread10((uint32_t)x) << (2 - d);
+          }
+          key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 30) | c30 : c30;
+        } else {
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-          const float ext = one_scale ? emax : hi[d] - lo[d];
-          float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
-          x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
-          code |= spread21((uint32_t)x) << (2 - d);
+          for (int d = 0; d < 3; d++) {
+            const float ext = one_scale ? emax : hi[d] - lo[d];
+            float x = ext > 0.0f ? (c[d] - lo[d]) / ext : 0.0f;
+            x = fminf(fmaxf(x * 2097152.0f, 0.0f), 2097151.0f);
+            code |= spread21((uint32_t)x) << (2 - d);
+          }
+          key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 51) | (code >> 12) : code;
         }
-        key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 51) | (code >> 12) : code;
       }
+      keys[i] = key;
+      vals[i] = i;
     }
-    keys[i] = key;
-    vals[i] = i;
+    ka &= key;
+    ko |= key;
   }
   // AND / OR over all keys to find constant digits
-  unsigned long long ka = (i < n) ? key : ~0ull, ko = (i < n) ? key : 0ull;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     ka &= __shfl_xor_sync(0xFFFFFFFFu, ka, o);
     ko |= __shfl_xor_sync(0xFFFFFFFFu, ko, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicAnd(&acc->kand, ka);
-    atomicOr(&acc->kor, ko);
+    atomicAnd(&s_and, ka);
+    atomicOr(&s_or, ko);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAnd(&acc->kand, s_and);
+    atomicOr(&acc->kor, s_or);
   }
 }
 
@@ -1651,6 +1677,11 @@ static int num_sms_build() {
   return n;
 }
 
+// Blocks of 256 threads for a grid-stride kernel over n items: up to 8 per SM.
+static unsigned grid_stride_blocks(uint64_t n) {
+  return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)num_sms_build() * 8));
+}
+
 // Words of look-back state that scan_excl needs for n elements (ticket, done
 // counter, one status word per tile); zero when allocated, and every scan leaves
 // it zero again.
@@ -1785,7 +1816,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   h_acc.kand = ~0ull;
   h_acc.kor = 0ull;
   GB_CHECK(cudaMemcpyAsync(acc, &h_acc, sizeof(BoundsAcc), cudaMemcpyHostToDevice, st));
-  k_primrefs<<<cdiv(total, 256), 256, 0, st>>>(d_geoms, ngeoms, total, plo, phi, acc); note_launches(1);
+  k_primrefs<<<grid_stride_blocks(total), 256, 0, st>>>(d_geoms, ngeoms, total, plo, phi, acc); note_launches(1);
 
   uint64_t *keys_a = nullptr, *keys_b = nullptr;
   uint32_t *vals_a = nullptr, *vals_b = nullptr;
@@ -1796,7 +1827,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   const bool segmented = opt.segmented != 0;
   const uint32_t nseg = segmented ? (uint32_t)ngeoms : 1u;
   if (segmented && (uint32_t)ngeoms > kMaxSegments) return cudaErrorInvalidValue;
-  k_morton<<<cdiv(total, 256), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube, segmented ? 1 : 0,
+  k_morton<<<grid_stride_blocks(total), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube, segmented ? 1 : 0,
                                              opt.morton_bits == 30 ? 1 : 0);
   note_launches(1);
   GB_CHECK(cudaGetLastError());
@@ -2227,8 +2258,8 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   BoundsAcc* acc = reinterpret_cast<BoundsAcc*>(g.acc);
   const int fixed_grid = 8 * num_sms_build();
   k_acc_init<<<1, 32, 0, st>>>(acc);
-  k_primrefs<<<cdiv(T, 256), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc);
-  k_morton<<<cdiv(T, 256), 256, 0, st>>>(g.plo, g.phi, T, acc, g.keys_a, g.vals_a, g.opt.morton_cube,
+  k_primrefs<<<grid_stride_blocks(T), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc);
+  k_morton<<<grid_stride_blocks(T), 256, 0, st>>>(g.plo, g.phi, T, acc, g.keys_a, g.vals_a, g.opt.morton_cube,
                                          g.opt.segmented ? 1 : 0, g.opt.morton_bits == 30 ? 1 : 0);
   note_launches(3);
   // all digits of the key width (the ordinary build skips constant ones: the same order)
