@@ -653,6 +653,77 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_lb(uint32_t* __restrict__
   }
 }
 
+// ---- SAH-optimal collapse (dynamic programming over the binary tree, after
+// Ylitie, Karras and Laine, "Efficient incoherent ray traversal on GPUs
+// through compressed wide BVHs", HPG 2017).  cost(n, i) is the least SAH cost
+// of the subtree of binary node n when it may take up to i child slots of a
+// wide node: i = 1 is n itself as one child (a leaf when it holds at most
+// leaf_max triangles -- then its cost is area x Triangle4 blocks -- else a wide
+// node of its own: area + D(n, 8)); i > 1 is min(cost(n, i - 1), D(n, i)) with
+// D(n, i) = min over k of cost(left, k) + cost(right, i - k).  The costs are
+// the SAH statistic's terms (bvh_statistics.cpp:10-160), so the tree minimises
+// the reported SAH for the given binary tree and leaf size.
+//
+// choice[n] packs the decisions: byte 0 = argmin k of D(n, 8) (the split of a
+// wide node made from n); byte i - 1 (i = 2..8) = the k of D(n, i) when it beat
+// cost(n, i - 1), else 0.
+
+__device__ __forceinline__ void dp_store(float4* cost, uint2* choice, uint32_t n, const float c[8], uint2 ch) {
+  __stcg(cost + 2 * (size_t)n, make_float4(c[0], c[1], c[2], c[3]));
+  __stcg(cost + 2 * (size_t)n + 1, make_float4(c[4], c[5], c[6], c[7]));
+  __stcg(choice + n, ch);
+}
+
+// cost(n, 1..8) and the choices of binary node n with children l and r, whose
+// costs are stored already; A is n's box area, cnt its triangles.  The PLOC
+// kernels call it as they create each node, so the table is complete when the
+// clustering ends (children are always created before their parent).
+__device__ __forceinline__ void dp_node(float4* cost, uint2* choice, uint32_t n, uint32_t l, uint32_t r, float A,
+                                        uint32_t cnt, uint32_t leaf_max) {
+  float cl[8], cr[8];
+  {
+    const float4 a = __ldcg(cost + 2 * (size_t)l), b = __ldcg(cost + 2 * (size_t)l + 1);
+    const float4 e = __ldcg(cost + 2 * (size_t)r), f = __ldcg(cost + 2 * (size_t)r + 1);
+    cl[0] = a.x; cl[1] = a.y; cl[2] = a.z; cl[3] = a.w; cl[4] = b.x; cl[5] = b.y; cl[6] = b.z; cl[7] = b.w;
+    cr[0] = e.x; cr[1] = e.y; cr[2] = e.z; cr[3] = e.w; cr[4] = f.x; cr[5] = f.y; cr[6] = f.z; cr[7] = f.w;
+  }
+  float D[9];
+  uint32_t K[9];
+#pragma unroll
+  for (int i = 2; i <= 8; i++) {
+    D[i] = INFINITY;
+    K[i] = 1;
+#pragma unroll
+    for (int k = 1; k < i; k++) {
+      const float v = cl[k - 1] + cr[i - k - 1];
+      if (v < D[i]) {
+        D[i] = v;
+        K[i] = (uint32_t)k;
+      }
+    }
+  }
+  const float c_int = A + D[8];
+  const float c_leaf = cnt <= leaf_max ? A * (float)((cnt + 3) / 4) : INFINITY;
+  float c[8];
+  c[0] = fminf(c_leaf, c_int);
+  uint32_t b[8];
+  b[0] = K[8];
+#pragma unroll
+  for (int i = 2; i <= 8; i++) {
+    const bool split = D[i] < c[i - 2];
+    c[i - 1] = split ? D[i] : c[i - 2];
+    b[i - 1] = split ? K[i] : 0u;
+  }
+  dp_store(cost, choice, n, c,
+           make_uint2(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24), b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24)));
+}
+
+// A primitive: one triangle, one block, whatever the number of slots.
+__device__ __forceinline__ void dp_leaf(float4* cost, uint2* choice, uint32_t n, float A) {
+  const float c[8] = {A, A, A, A, A, A, A, A};
+  dp_store(cost, choice, n, c, make_uint2(0u, 0u));
+}
+
 // ---------------------------------------------------------------------------
 // 4. PLOC
 // ---------------------------------------------------------------------------
@@ -676,7 +747,8 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
                                                    const uint32_t* __restrict__ d_n,
                                                    float4* __restrict__ bnlo, float4* __restrict__ bnhi,
                                                    uint32_t* __restrict__ bncnt, uint32_t* __restrict__ cidx,
-                                                   float4* __restrict__ clo, float4* __restrict__ chi, int segmented) {
+                                                   float4* __restrict__ clo, float4* __restrict__ chi, int segmented,
+                                                   float4* __restrict__ dp_cost, uint2* __restrict__ dp_choice) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || i >= *d_n) return;  // n bounds the grid, *d_n is the count of valid primitives
   const uint32_t p = sorted[i];
@@ -684,6 +756,7 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
   bnlo[i] = make_float4(a.x, a.y, a.z, __int_as_float(-1));
   bnhi[i] = make_float4(b.x, b.y, b.z, __uint_as_float(p));
   bncnt[i] = 1;
+  if (dp_cost) dp_leaf(dp_cost, dp_choice, i, half_area(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)));
   cidx[i] = i;
   clo[i] = make_float4(a.x, a.y, a.z, segmented ? a.w : __uint_as_float(0u));
   chi[i] = make_float4(b.x, b.y, b.z, 0.f);
@@ -816,7 +889,9 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const PlocBufs bufs, c
                                                           const uint32_t* __restrict__ bsurv_off,
                                                           const uint32_t* __restrict__ bmerge_off,
                                                           float4* __restrict__ bnlo, float4* __restrict__ bnhi,
-                                                          uint32_t* __restrict__ bncnt, uint32_t node_cap, uint32_t* err) {
+                                                          uint32_t* __restrict__ bncnt, uint32_t node_cap, uint32_t* err,
+                                                          float4* __restrict__ dp_cost, uint2* __restrict__ dp_choice,
+                                                          uint32_t leaf_max) {
   __shared__ uint32_t s_w[PLOC_BLOCK / 32];
   if (ploc_state[kPlocDone]) return;
   const uint32_t n = ploc_state[kPlocN], node_next = ploc_state[kPlocNext];
@@ -858,7 +933,11 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const PlocBufs bufs, c
       const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
       bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
       bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-      bncnt[id] = bncnt[l] + bncnt[r];
+      const uint32_t cnt = bncnt[l] + bncnt[r];
+      bncnt[id] = cnt;
+      if (dp_cost)
+        dp_node(dp_cost, dp_choice, id, l, r, half_area(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z)),
+                cnt, leaf_max);
       olo[pos] = lo;
       ohi[pos] = hi;
       oidx[pos] = id;
@@ -904,7 +983,9 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
                                                                   float4* __restrict__ bnhi,
                                                                   uint32_t* __restrict__ bncnt, uint32_t* root_out,
                                                                   uint32_t* iters_out, uint32_t node_cap,
-                                                                  uint32_t* err, uint32_t nseg, int radius) {
+                                                                  uint32_t* err, uint32_t nseg, int radius,
+                                                                  float4* __restrict__ dp_cost,
+                                                                  uint2* __restrict__ dp_choice, uint32_t leaf_max) {
   extern __shared__ unsigned char smem[];
   float3* s_lo = reinterpret_cast<float3*>(smem);
   float3* s_hi = s_lo + PLOC_SMALL;
@@ -1019,7 +1100,11 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
           hi = f3max(hi, s_hi[j]);
           bnlo[nid] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
           bnhi[nid] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-          bncnt[nid] = bncnt[l] + bncnt[r];
+          const uint32_t cnt = bncnt[l] + bncnt[r];
+          bncnt[nid] = cnt;
+          // children come from earlier rounds: their costs were stored before
+          // this round's barriers
+          if (dp_cost) dp_node(dp_cost, dp_choice, nid, l, r, half_area(lo, hi), cnt, leaf_max);
           id = nid;
           pm++;
         }
@@ -1109,96 +1194,6 @@ __device__ __forceinline__ float3 bt_hi(const BinTree& t, uint32_t k) {
   return make_float3(a.x, a.y, a.z);
 }
 
-// ---- SAH-optimal collapse (dynamic programming over the binary tree, after
-// Ylitie, Karras and Laine, "Efficient incoherent ray traversal on GPUs
-// through compressed wide BVHs", HPG 2017).  cost(n, i) is the least SAH cost
-// of the subtree of binary node n when it may take up to i child slots of a
-// wide node: i = 1 is n itself as one child (a leaf when it holds at most
-// leaf_max triangles -- then its cost is area x Triangle4 blocks -- else a wide
-// node of its own: area + D(n, 8)); i > 1 is min(cost(n, i - 1), D(n, i)) with
-// D(n, i) = min over k of cost(left, k) + cost(right, i - k).  The costs are
-// the SAH statistic's terms (bvh_statistics.cpp:10-160), so the tree minimises
-// the reported SAH for the given binary tree and leaf size.
-//
-// choice[n] packs the decisions: byte 0 = argmin k of D(n, 8) (the split of a
-// wide node made from n); byte i - 1 (i = 2..8) = the k of D(n, i) when it beat
-// cost(n, i - 1), else 0.  The pass runs bottom-up from the primitives: each
-// thread climbs through parent links, and at every node only the second child
-// to arrive (atomic counter) goes on, so every node is computed once, after
-// both children.
-
-__global__ void __launch_bounds__(256) k_bin_parents(const float4* __restrict__ bnlo, const float4* __restrict__ bnhi,
-                                                     uint32_t first, uint32_t end, uint32_t* __restrict__ parent) {
-  const uint32_t k = first + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= end) return;
-  parent[__float_as_uint(bnlo[k].w)] = k;
-  parent[__float_as_uint(bnhi[k].w)] = k;
-}
-
-__device__ __forceinline__ void dp_store(float4* cost, uint2* choice, uint32_t n, const float c[8], uint2 ch) {
-  __stcg(cost + 2 * (size_t)n, make_float4(c[0], c[1], c[2], c[3]));
-  __stcg(cost + 2 * (size_t)n + 1, make_float4(c[4], c[5], c[6], c[7]));
-  __stcg(choice + n, ch);
-}
-
-__global__ void __launch_bounds__(256) k_collapse_dp(BinTree t, const uint32_t* __restrict__ parent, uint32_t nnodes,
-                                                     uint32_t* __restrict__ arrivals, float4* __restrict__ cost,
-                                                     uint2* __restrict__ choice) {
-  uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= t.nleaves) return;
-  {  // a primitive: one triangle, one block, whatever the number of slots
-    const float A = half_area(bt_lo(t, n), bt_hi(t, n));
-    const float c[8] = {A, A, A, A, A, A, A, A};
-    dp_store(cost, choice, n, c, make_uint2(0u, 0u));
-  }
-  for (uint32_t guard = 0; guard < nnodes; guard++) {
-    __threadfence();  // this node's costs before the arrival count
-    const uint32_t p = parent[n];
-    if (p == kInvalidID || p >= nnodes) return;
-    if (atomicAdd(arrivals + p, 1u) == 0u) return;  // the sibling is not done: it continues
-    __threadfence();
-    n = p;
-    const uint32_t l = bt_left(t, n), r = bt_right(t, n);
-    float cl[8], cr[8];
-    {
-      const float4 a = __ldcg(cost + 2 * (size_t)l), b = __ldcg(cost + 2 * (size_t)l + 1);
-      const float4 e = __ldcg(cost + 2 * (size_t)r), f = __ldcg(cost + 2 * (size_t)r + 1);
-      cl[0] = a.x; cl[1] = a.y; cl[2] = a.z; cl[3] = a.w; cl[4] = b.x; cl[5] = b.y; cl[6] = b.z; cl[7] = b.w;
-      cr[0] = e.x; cr[1] = e.y; cr[2] = e.z; cr[3] = e.w; cr[4] = f.x; cr[5] = f.y; cr[6] = f.z; cr[7] = f.w;
-    }
-    float D[9];
-    uint32_t K[9];
-#pragma unroll
-    for (int i = 2; i <= 8; i++) {
-      D[i] = INFINITY;
-      K[i] = 1;
-#pragma unroll
-      for (int k = 1; k < i; k++) {
-        const float v = cl[k - 1] + cr[i - k - 1];
-        if (v < D[i]) {
-          D[i] = v;
-          K[i] = (uint32_t)k;
-        }
-      }
-    }
-    const float A = half_area(bt_lo(t, n), bt_hi(t, n));
-    const uint32_t cnt = t.cnt[n];
-    const float c_int = A + D[8];
-    const float c_leaf = cnt <= t.leaf_max ? A * (float)((cnt + 3) / 4) : INFINITY;
-    float c[8];
-    c[0] = fminf(c_leaf, c_int);
-    uint32_t b[8];
-    b[0] = K[8];
-#pragma unroll
-    for (int i = 2; i <= 8; i++) {
-      const bool split = D[i] < c[i - 2];
-      c[i - 1] = split ? D[i] : c[i - 2];
-      b[i - 1] = split ? K[i] : 0u;
-    }
-    dp_store(cost, choice, n, c,
-             make_uint2(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24), b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24)));
-  }
-}
 
 __device__ __forceinline__ uint32_t dp_choice(const BinTree& t, uint32_t n, int i) {
   const uint2 c = t.choice[n];
@@ -1857,7 +1852,32 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   // ---- PLOC over the N valid primitives (sorted positions 0..N-1)
   float4 *bnlo = nullptr, *bnhi = nullptr;
   uint32_t* bncnt = nullptr;
+  // leaf size: explicit, or by the scene -- flat scenes (centroid box's
+  // smallest extent below half the largest: heightfields, terrain) and scenes
+  // that will be refitted every frame take 2 triangles per leaf, the rest 1
+  // (measured on a GB300: the 4M soup traces 5 % faster with 1; a 724^2
+  // heightfield 8 % faster with 2, and its SAH is 1.12x the reference
+  // builder's with 2, 1.31x with 1; the animated 4M soup, refitted per frame,
+  // renders 4 % faster with 2, whose tree has 40 % fewer nodes to refit)
+  int leaf_max = opt.leaf_max;
+  if (leaf_max <= 0) {
+    float emin = INFINITY, emax = 0.f;
+    for (int d = 0; d < 3; d++) {
+      const float e = ord2f(h_acc.chi[d]) - ord2f(h_acc.clo[d]);
+      emin = std::min(emin, e);
+      emax = std::max(emax, e);
+    }
+    leaf_max = (emin < 0.5f * emax || opt.refit_target) ? 2 : 1;
+  }
+  stats->leaf_max = (uint32_t)std::min(leaf_max, kLeafMaxLimit);
   const uint32_t nnodes_bin = 2 * N - 1;
+  // SAH-optimal collapse: the cost table is filled as PLOC creates the nodes
+  float4* dp_cost = nullptr;
+  uint2* d_choice = nullptr;
+  if (opt.collapse == 1) {
+    GB_CHECK(arena.alloc(&dp_cost, 2 * (size_t)nnodes_bin));
+    GB_CHECK(arena.alloc(&d_choice, nnodes_bin));
+  }
   GB_CHECK(arena.alloc(&bnlo, nnodes_bin));
   GB_CHECK(arena.alloc(&bnhi, nnodes_bin));
   GB_CHECK(arena.alloc(&bncnt, nnodes_bin));
@@ -1870,8 +1890,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&cidx_a, N));
   GB_CHECK(arena.alloc(&cidx_b, N));
   GB_CHECK(arena.alloc(&nn, N));
+  const uint32_t leaf_max_used = (uint32_t)std::min(std::max(leaf_max, 1), kLeafMaxLimit);
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, &acc->nvalid, bnlo, bnhi, bncnt, cidx_a, clo_a,
-                                            chi_a, segmented ? 1 : 0);
+                                            chi_a, segmented ? 1 : 0, dp_cost, d_choice);
   note_launches(1);
   uint32_t *bsurv, *bmerge, *d_tot, *d_root, *d_iters;
   const uint32_t maxb = cdiv(N, PLOC_BLOCK);
@@ -1913,7 +1934,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     scan_excl(bsurv, maxb, d_tot + 0, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
     scan_excl(bmerge, maxb, d_tot + 1, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
     k_ploc_emit<<<grid, PLOC_BLOCK, 0, st>>>(pb, nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt, nnodes_bin,
-                                             &acc->pad);
+                                             &acc->pad, dp_cost, d_choice, leaf_max_used);
     k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state, 0);
     note_launches(2);
     round++;
@@ -1937,7 +1958,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     GB_CHECK(cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(clo_a, chi_a, cidx_a, clo_b, chi_b, cidx_b, ploc_state, bnlo,
                                                       bnhi, bncnt, d_root, d_iters, nnodes_bin, &acc->pad, nseg,
-                                                      radius);
+                                                      radius, dp_cost, d_choice, leaf_max_used);
     note_launches(1);
     GB_CHECK(cudaGetLastError());
   }
@@ -1966,49 +1987,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   arena.free(nn); arena.free(bsurv); arena.free(bmerge); arena.free(ploc_state);
 
   // ---- collapse, level by level (breadth-first node order)
-  // leaf size: explicit, or by the scene -- flat scenes (centroid box's
-  // smallest extent below half the largest: heightfields, terrain) and scenes
-  // that will be refitted every frame take 2 triangles per leaf, the rest 1
-  // (measured on a GB300: the 4M soup traces 5 % faster with 1; a 724^2
-  // heightfield 8 % faster with 2, and its SAH is 1.12x the reference
-  // builder's with 2, 1.31x with 1; the animated 4M soup, refitted per frame,
-  // renders 4 % faster with 2, whose tree has 40 % fewer nodes to refit)
-  int leaf_max = opt.leaf_max;
-  if (leaf_max <= 0) {
-    float emin = INFINITY, emax = 0.f;
-    for (int d = 0; d < 3; d++) {
-      const float e = ord2f(h_acc.chi[d]) - ord2f(h_acc.clo[d]);
-      emin = std::min(emin, e);
-      emax = std::max(emax, e);
-    }
-    leaf_max = (emin < 0.5f * emax || opt.refit_target) ? 2 : 1;
-  }
-  stats->leaf_max = (uint32_t)std::min(leaf_max, kLeafMaxLimit);
-  BinTree bt{bnlo, bnhi, bncnt, N, (uint32_t)std::min(std::max(leaf_max, 1), kLeafMaxLimit),
-             (uint32_t)(opt.robust != 0), nullptr};
-  uint2* d_choice = nullptr;
-  if (opt.collapse == 1) {  // SAH-optimal collapse decisions
-    const uint32_t nbin = 2 * N - (uint32_t)root_items.size();  // binary nodes of all trees
-    uint32_t *parent = nullptr, *arrivals = nullptr;
-    float4* cost = nullptr;
-    GB_CHECK(arena.alloc(&parent, nbin));
-    GB_CHECK(arena.alloc(&arrivals, nbin));
-    GB_CHECK(arena.alloc(&cost, 2 * (size_t)nbin));
-    GB_CHECK(arena.alloc(&d_choice, nbin));
-    GB_CHECK(cudaMemsetAsync(parent, 0xFF, sizeof(uint32_t) * nbin, st));
-    GB_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(uint32_t) * nbin, st));
-    if (nbin > N) {
-      k_bin_parents<<<cdiv(nbin - N, 256), 256, 0, st>>>(bnlo, bnhi, N, nbin, parent);
-      note_launches(1);
-    }
-    k_collapse_dp<<<cdiv(N, 256), 256, 0, st>>>(bt, parent, nbin, arrivals, cost, d_choice);
-    note_launches(1);
-    GB_CHECK(cudaGetLastError());
-    arena.free(parent);
-    arena.free(arrivals);
-    arena.free(cost);
-    bt.choice = d_choice;
-  }
+  BinTree bt{bnlo, bnhi, bncnt, N, leaf_max_used, (uint32_t)(opt.robust != 0), d_choice};
+  if (dp_cost) arena.free(dp_cost);
   WideNode* wnodes = nullptr;
   TriRecord* wtris = nullptr;
   const uint32_t maxw = N;  // wide internal nodes <= binary internal nodes + 1
@@ -2190,9 +2170,8 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
       (e = alloc(&g->cidx[1], N)) || (e = alloc(&g->nn, N)) || (e = alloc(&g->bsurv, g->maxb)) ||
       (e = alloc(&g->bmerge, g->maxb)) || (e = alloc(&g->scan_sums, scan_scratch(std::max(g->maxb, maxw)))) ||
       (e = alloc(&g->d_tot, 4)) || (e = alloc(&g->d_root, g->nseg)) || (e = alloc(&g->d_iters, 1)) ||
-      (e = alloc(&g->ploc_state, kPlocStateWords)) || (e = alloc(&g->parent, g->nbin)) ||
-      (e = alloc(&g->arrivals, g->nbin)) || (e = alloc(&g->cost, 2 * (size_t)g->nbin)) ||
-      (e = alloc(&g->choice, g->nbin)) || (e = alloc(&g->nodes, maxw)) || (e = alloc(&g->tris, N)) ||
+      (e = alloc(&g->ploc_state, kPlocStateWords)) || (e = alloc(&g->cost, 2 * (size_t)(2 * N))) ||
+      (e = alloc(&g->choice, 2 * N)) || (e = alloc(&g->nodes, maxw)) || (e = alloc(&g->tris, N)) ||
       (e = alloc(&g->items[0], maxw)) || (e = alloc(&g->items[1], maxw)) || (e = alloc(&g->kids, 8 * (size_t)maxw)) ||
       (e = alloc(&g->nint, maxw)) || (e = alloc(&g->ntri, maxw)) || (e = alloc(&g->leaf_root, N)) ||
       (e = alloc(&g->d_sah, 2)) || (e = alloc(&g->d_leaves, 1)) || (e = alloc(&g->cstate, kColStateWords)) ||
@@ -2272,8 +2251,11 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   // one-CTA finish
   GB_CHECK(cudaMemsetAsync(g.d_root, 0xFF, sizeof(uint32_t) * g.nseg, st));
   GB_CHECK(cudaMemsetAsync(g.d_iters, 0, sizeof(uint32_t), st));
+  const uint32_t leaf_max = (uint32_t)std::min(std::max(g.plan.leaf_max, 1), kLeafMaxLimit);
+  float4* dp_cost = g.opt.collapse == 1 ? g.cost : nullptr;
+  uint2* dp_choice = g.opt.collapse == 1 ? g.choice : nullptr;
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(g.plo, g.phi, va, N, &acc->nvalid, g.bnlo, g.bnhi, g.bncnt, g.cidx[0],
-                                            g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0);
+                                            g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0, dp_cost, dp_choice);
   cudaGraphConditionalHandle ploc_loop = 0;
   GB_CHECK(loop_handle(st, &ploc_loop));
   k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state, ploc_loop);
@@ -2293,7 +2275,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
     scan_excl(g.bsurv, g.maxb, g.d_tot + 0, g.scan_sums, bs, &acc->pad, g.ploc_state + kPlocTiles);
     scan_excl(g.bmerge, g.maxb, g.d_tot + 1, g.scan_sums, bs, &acc->pad, g.ploc_state + kPlocTiles);
     k_ploc_emit<<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.nn, g.ploc_state, g.bsurv, g.bmerge, g.bnlo, g.bnhi, g.bncnt,
-                                              nbin_cap, &acc->pad);
+                                              nbin_cap, &acc->pad, dp_cost, dp_choice, leaf_max);
     k_ploc_advance<<<1, 32, 0, bs>>>(g.d_tot, g.ploc_state, ploc_loop);
     note_launches(4);
   }));
@@ -2301,23 +2283,12 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
     const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(g.clo[0], g.chi[0], g.cidx[0], g.clo[1], g.chi[1], g.cidx[1],
                                                       g.ploc_state, g.bnlo, g.bnhi, g.bncnt, g.d_root, g.d_iters,
-                                                      nbin_cap, &acc->pad, g.nseg, (int)g.radius);
+                                                      nbin_cap, &acc->pad, g.nseg, (int)g.radius, dp_cost, dp_choice,
+                                                      leaf_max);
     note_launches(1);
   }
   // collapse decisions and levels
-  BinTree bt{g.bnlo, g.bnhi, g.bncnt, N, (uint32_t)std::min(std::max(g.plan.leaf_max, 1), kLeafMaxLimit),
-             (uint32_t)(g.opt.robust != 0), nullptr};
-  if (g.opt.collapse == 1) {
-    GB_CHECK(cudaMemsetAsync(g.parent, 0xFF, sizeof(uint32_t) * g.nbin, st));
-    GB_CHECK(cudaMemsetAsync(g.arrivals, 0, sizeof(uint32_t) * g.nbin, st));
-    if (g.nbin > N) {
-      k_bin_parents<<<cdiv(g.nbin - N, 256), 256, 0, st>>>(g.bnlo, g.bnhi, N, g.nbin, g.parent);
-      note_launches(1);
-    }
-    k_collapse_dp<<<cdiv(N, 256), 256, 0, st>>>(bt, g.parent, g.nbin, g.arrivals, g.cost, g.choice);
-    note_launches(1);
-    bt.choice = g.choice;
-  }
+  BinTree bt{g.bnlo, g.bnhi, g.bncnt, N, leaf_max, (uint32_t)(g.opt.robust != 0), dp_choice};
   GB_CHECK(cudaMemsetAsync(g.leaf_root, 0xFF, sizeof(uint32_t) * N, st));
   GB_CHECK(cudaMemsetAsync(g.d_sah, 0, 2 * sizeof(double), st));
   GB_CHECK(cudaMemsetAsync(g.d_leaves, 0, sizeof(uint32_t), st));

@@ -68,7 +68,6 @@ struct GraphBuild {
   float4 *bnlo = nullptr, *bnhi = nullptr, *clo[2] = {nullptr, nullptr}, *chi[2] = {nullptr, nullptr};
   uint32_t *bncnt = nullptr, *cidx[2] = {nullptr, nullptr}, *nn = nullptr, *bsurv = nullptr, *bmerge = nullptr;
   uint32_t *scan_sums = nullptr, *d_tot = nullptr, *d_root = nullptr, *d_iters = nullptr, *ploc_state = nullptr;
-  uint32_t *parent = nullptr, *arrivals = nullptr;
   float4* cost = nullptr;
   uint2* choice = nullptr;
   WideNode* nodes = nullptr;
