@@ -581,11 +581,20 @@ __device__ __forceinline__ uint32_t scan_count(uint32_t n, const uint32_t* d_n, 
   return d_n ? min(n, (*d_n + div - 1) / div) : n;
 }
 
+// Two arrays scanned by one launch (the survivors and merges of a PLOC round,
+// the internal children and triangles of a collapse level): blockIdx.y picks
+// the array, its total and (look-back scan) its state.
+struct ScanPair {
+  uint32_t* a[2];
+  uint32_t* total[2];
+};
+
 // One CTA of 1024 threads over the whole array; optionally writes the total.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_excl(uint32_t* __restrict__ a, uint32_t n,
-                                                            const uint32_t* __restrict__ d_n, uint32_t div,
-                                                            uint32_t* total) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_excl(ScanPair sp, uint32_t n,
+                                                            const uint32_t* __restrict__ d_n, uint32_t div) {
   __shared__ uint32_t s_w[32];
+  uint32_t* __restrict__ a = sp.a[blockIdx.y];
+  uint32_t* total = sp.total[blockIdx.y];
   n = scan_count(n, d_n, div);
   uint32_t carry = 0;
   for (uint32_t base = 0; base < n; base += SCAN_TILE) carry += scan_tile(a, n, base, carry, s_w);
@@ -594,16 +603,20 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_excl(uint32_t* __restrict
 
 // Single-pass exclusive scan of larger arrays: CTAs take SCAN_TILE tiles in ticket
 // order, publish their tile sums and add up those of the tiles before them by
-// decoupled look-back, then scan their tile from that offset.  state: [0] ticket,
-// [1] CTAs finished, [2 + t] status word of tile t; zero on entry, and the last CTA
-// to finish zeroes it again for the next scan (graph replays included).
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_lb(uint32_t* __restrict__ a, uint32_t n,
+// decoupled look-back, then scan their tile from that offset.  state (per array,
+// state_words apart): [0] ticket, [1] CTAs finished, [2 + t] status word of tile
+// t; zero on entry, and the last CTA to finish zeroes it again for the next scan
+// (graph replays included).
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_lb(ScanPair sp, uint32_t n,
                                                           const uint32_t* __restrict__ d_n, uint32_t div,
-                                                          uint32_t* __restrict__ state, uint32_t* total,
+                                                          uint32_t* __restrict__ state_base, uint32_t state_words,
                                                           unsigned int* __restrict__ err) {
   __shared__ uint32_t s_w[32];
   __shared__ uint32_t s_tile, s_excl;
   __shared__ bool s_last;
+  uint32_t* __restrict__ a = sp.a[blockIdx.y];
+  uint32_t* total = sp.total[blockIdx.y];
+  uint32_t* __restrict__ state = state_base + (size_t)blockIdx.y * state_words;
   n = scan_count(n, d_n, div);
   const uint32_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (threadIdx.x == 0) s_tile = atomicAdd(state, 1u);
@@ -1682,16 +1695,18 @@ static unsigned grid_stride_blocks(uint64_t n) {
 // it zero again.
 static inline uint32_t scan_scratch(uint32_t n) { return cdiv(n, SCAN_TILE) + 2; }
 
-// Exclusive scan of a[0, n) in place (total to *total when non-null); sums holds
-// scan_scratch(n) zeroed words.  With d_n the count is *d_n (at most n), read on
-// the device, so the scan can be enqueued before the count is known.  One launch:
-// one CTA for short arrays, else the look-back scan.
-static void scan_excl(uint32_t* a, uint32_t n, uint32_t* total, uint32_t* sums, cudaStream_t st,
-                      unsigned int* err, const uint32_t* d_n = nullptr) {
+// Exclusive scans of a[0, n) and b[0, n) in place, by one launch (totals to
+// *ta / *tb); sums holds 2 * scan_scratch(n) zeroed words.  With d_n the count
+// is *d_n (at most n), read on the device, so the scans can be enqueued before
+// the count is known.  One CTA per array for short arrays, else the look-back
+// scan.
+static void scan_excl2(uint32_t* a, uint32_t* b, uint32_t n, uint32_t* ta, uint32_t* tb, uint32_t* sums,
+                       cudaStream_t st, unsigned int* err, const uint32_t* d_n = nullptr) {
+  const ScanPair sp{{a, b}, {ta, tb}};
   if (n <= 2 * SCAN_TILE) {
-    k_scan_excl<<<1, SCAN_THREADS, 0, st>>>(a, n, d_n, 1, total);
+    k_scan_excl<<<dim3(1, 2), SCAN_THREADS, 0, st>>>(sp, n, d_n, 1);
   } else {
-    k_scan_lb<<<cdiv(n, SCAN_TILE), SCAN_THREADS, 0, st>>>(a, n, d_n, 1, sums, total, err);
+    k_scan_lb<<<dim3(cdiv(n, SCAN_TILE), 2), SCAN_THREADS, 0, st>>>(sp, n, d_n, 1, sums, scan_scratch(n), err);
   }
   note_launches(1);
 }
@@ -1899,8 +1914,8 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&bsurv, maxb));
   GB_CHECK(arena.alloc(&bmerge, maxb));
   uint32_t* scan_sums = nullptr;  // look-back state of the PLOC and collapse scans (zero between scans)
-  GB_CHECK(arena.alloc(&scan_sums, scan_scratch(std::max(maxb, N))));
-  GB_CHECK(cudaMemsetAsync(scan_sums, 0, sizeof(uint32_t) * scan_scratch(std::max(maxb, N)), st));
+  GB_CHECK(arena.alloc(&scan_sums, 2 * (size_t)scan_scratch(std::max(maxb, N))));
+  GB_CHECK(cudaMemsetAsync(scan_sums, 0, sizeof(uint32_t) * 2 * scan_scratch(std::max(maxb, N)), st));
   GB_CHECK(arena.alloc(&d_tot, 4));
   GB_CHECK(arena.alloc(&d_root, nseg));
   GB_CHECK(cudaMemsetAsync(d_root, 0xFF, sizeof(uint32_t) * nseg, st));
@@ -1931,8 +1946,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     }
     k_ploc_count<<<grid, PLOC_BLOCK, 0, st>>>(nn, ploc_state, bsurv, bmerge);
     note_launches(2);
-    scan_excl(bsurv, maxb, d_tot + 0, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
-    scan_excl(bmerge, maxb, d_tot + 1, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
+    scan_excl2(bsurv, bmerge, maxb, d_tot + 0, d_tot + 1, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
     k_ploc_emit<<<grid, PLOC_BLOCK, 0, st>>>(pb, nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt, nnodes_bin,
                                              &acc->pad, dp_cost, d_choice, leaf_max_used);
     k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state, 0);
@@ -2023,8 +2037,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     const uint32_t grid = cdiv(nitems_known, 128);
     k_collapse_count<<<grid, 128, 0, st>>>(bt, citems, cstate, kids, nint, ntri);
     note_launches(1);
-    scan_excl(nint, nitems_known, d_tot + 0, scan_sums, st, &acc->pad);
-    scan_excl(ntri, nitems_known, d_tot + 1, scan_sums, st, &acc->pad);
+    scan_excl2(nint, ntri, nitems_known, d_tot + 0, d_tot + 1, scan_sums, st, &acc->pad);
     k_collapse_emit<<<grid, COLLAPSE_THREADS, 0, st>>>(bt, kids, cstate, nint, ntri, wnodes, leaf_root, citems,
                                                        d_sah, d_leaves, maxw, N, &acc->pad);
     k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels, 0);
@@ -2168,7 +2181,8 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
       (e = alloc(&g->bncnt, 2 * (size_t)N)) || (e = alloc(&g->clo[0], N)) || (e = alloc(&g->clo[1], N)) ||
       (e = alloc(&g->chi[0], N)) || (e = alloc(&g->chi[1], N)) || (e = alloc(&g->cidx[0], N)) ||
       (e = alloc(&g->cidx[1], N)) || (e = alloc(&g->nn, N)) || (e = alloc(&g->bsurv, g->maxb)) ||
-      (e = alloc(&g->bmerge, g->maxb)) || (e = alloc(&g->scan_sums, scan_scratch(std::max(g->maxb, maxw)))) ||
+      (e = alloc(&g->bmerge, g->maxb)) ||
+      (e = alloc(&g->scan_sums, 2 * (size_t)scan_scratch(std::max(g->maxb, maxw)))) ||
       (e = alloc(&g->d_tot, 4)) || (e = alloc(&g->d_root, g->nseg)) || (e = alloc(&g->d_iters, 1)) ||
       (e = alloc(&g->ploc_state, kPlocStateWords)) || (e = alloc(&g->cost, 2 * (size_t)(2 * N))) ||
       (e = alloc(&g->choice, 2 * N)) || (e = alloc(&g->nodes, maxw)) || (e = alloc(&g->tris, N)) ||
@@ -2182,7 +2196,8 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
   g->acc = acc;
   e = cudaMemcpy(g->d_geoms, h_geoms, sizeof(GeomDesc) * ngeoms, cudaMemcpyHostToDevice);
   // the scans' look-back state starts at zero and every scan leaves it so
-  if (e == cudaSuccess) e = cudaMemset(g->scan_sums, 0, sizeof(uint32_t) * scan_scratch(std::max(g->maxb, maxw)));
+  if (e == cudaSuccess)
+    e = cudaMemset(g->scan_sums, 0, sizeof(uint32_t) * 2 * scan_scratch(std::max(g->maxb, maxw)));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_os_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsScatterSmem);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->body_stream, cudaStreamNonBlocking);
@@ -2272,8 +2287,8 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
       default: k_ploc_nn<PLOC_R_MAX><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
     }
     k_ploc_count<<<pgrid, PLOC_BLOCK, 0, bs>>>(g.nn, g.ploc_state, g.bsurv, g.bmerge);
-    scan_excl(g.bsurv, g.maxb, g.d_tot + 0, g.scan_sums, bs, &acc->pad, g.ploc_state + kPlocTiles);
-    scan_excl(g.bmerge, g.maxb, g.d_tot + 1, g.scan_sums, bs, &acc->pad, g.ploc_state + kPlocTiles);
+    scan_excl2(g.bsurv, g.bmerge, g.maxb, g.d_tot + 0, g.d_tot + 1, g.scan_sums, bs, &acc->pad,
+               g.ploc_state + kPlocTiles);
     k_ploc_emit<<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.nn, g.ploc_state, g.bsurv, g.bmerge, g.bnlo, g.bnhi, g.bncnt,
                                               nbin_cap, &acc->pad, dp_cost, dp_choice, leaf_max);
     k_ploc_advance<<<1, 32, 0, bs>>>(g.d_tot, g.ploc_state, ploc_loop);
@@ -2302,8 +2317,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   const ColItems ci{{g.items[0], g.items[1]}};
   GB_CHECK(capture_while(st, g.body_stream, col_loop, [&](cudaStream_t bs) {
     k_collapse_count<<<cgrid, 128, 0, bs>>>(bt, ci, g.cstate, g.kids, g.nint, g.ntri);
-    scan_excl(g.nint, maxw, g.d_tot + 0, g.scan_sums, bs, &acc->pad, g.cstate + kColN);
-    scan_excl(g.ntri, maxw, g.d_tot + 1, g.scan_sums, bs, &acc->pad, g.cstate + kColN);
+    scan_excl2(g.nint, g.ntri, maxw, g.d_tot + 0, g.d_tot + 1, g.scan_sums, bs, &acc->pad, g.cstate + kColN);
     k_collapse_emit<<<cgrid, COLLAPSE_THREADS, 0, bs>>>(bt, g.kids, g.cstate, g.nint, g.ntri, g.nodes, g.leaf_root,
                                                         ci, g.d_sah, g.d_leaves, maxw, N, &acc->pad);
     k_collapse_advance<<<1, 32, 0, bs>>>(g.d_tot, g.cstate, maxw, (uint32_t)kColMaxLevels, col_loop);
