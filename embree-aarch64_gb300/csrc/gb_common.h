@@ -123,7 +123,11 @@ struct BuildOptions {
   int collapse = 1;     // binary -> 8-wide: 1 SAH-optimal (gpu.collapse=sah), 0 greedy (gpu.collapse=greedy)
   int ploc_radius = 1;  // PLOC search radius: 1, 2, 4, 8 or 16 (gpu.ploc_radius)
   int refit_target = 0; // every geometry is RTC_BUILD_QUALITY_REFIT: the tree will be refitted
-  int morton_bits = 63; // sort key: 63-bit Morton codes (21 bits per axis) or 30-bit (10 per axis, gpu.morton_bits=30)
+  // sort key: 30-bit Morton codes (10 bits per axis, the default) or 63-bit (21 per
+  // axis, gpu.morton_bits=63).  On a GB300 the 30-bit key builds the 4M soup in
+  // 3.13 ms against 3.51 (4 radix passes instead of 8) with the same SAH within
+  // 0.02 % and the same trace time on the soup and the heightfields.
+  int morton_bits = 30;
 };
 
 // Build statistics reported through the extension API.

@@ -145,7 +145,7 @@ struct Device : RefCounted {
         else if (k == "gpu.morton") build_opt.morton_cube = v == "cube" ? 1 : v == "axis" ? 0 : 2;
         else if (k == "gpu.collapse") build_opt.collapse = v == "greedy" ? 0 : 1;
         else if (k == "gpu.ploc_radius") build_opt.ploc_radius = atoi(v.c_str());
-        else if (k == "gpu.morton_bits") build_opt.morton_bits = atoi(v.c_str()) == 30 ? 30 : 63;
+        else if (k == "gpu.morton_bits") build_opt.morton_bits = atoi(v.c_str()) == 63 ? 63 : 30;
         else if (k == "gpu.graph_rebuild") graph_rebuild = atoi(v.c_str()) != 0;
         else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
         else if (k == "gpu.proposer") proposer_mma = (v == "mma");

@@ -139,7 +139,7 @@ def test_autotuner_picks_the_fastest_candidate(rtc):
     assert len(shapes["ms"]) == len(rtc.traversal_shapes()) and min(shapes["ms"]) > 0
 
 
-@pytest.mark.parametrize("config", [b"", b"gpu.morton_bits=30"], ids=["key63", "key30"])
+@pytest.mark.parametrize("config", [b"", b"gpu.morton_bits=63"], ids=["key30", "key63"])
 def test_batched_frame_graph_matches_separate_calls(rtc, config):
     """A batched frame -- the rebuild of every BVH of the scene and the batched
     closest-hit query, captured into one CUDA graph with the copy that restores

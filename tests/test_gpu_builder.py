@@ -104,7 +104,7 @@ def test_sah_against_reference_builder(rtc, oracle, name, config, limit, leaf):
 @pytest.mark.parametrize("config", [b"gpu.collapse=greedy", b"gpu.ploc_radius=2", b"gpu.ploc_radius=4",
                                     b"gpu.ploc_radius=8", b"gpu.ploc_radius=16", b"gpu.morton=axis",
                                     b"gpu.morton=cube", b"gpu.leaf_max=1", b"gpu.leaf_max=3", b"gpu.leaf_max=4",
-                                    b"gpu.morton_bits=30", b"gpu.morton_bits=30,gpu.morton=axis"])
+                                    b"gpu.morton_bits=63", b"gpu.morton_bits=63,gpu.morton=axis"])
 def test_builder_options_valid_and_exact(rtc, oracle, config):
     """Every build option (collapse rule, PLOC radius, Morton scaling and key width,
     leaf size) yields a well-formed BVH over every triangle, and closest hits equal
