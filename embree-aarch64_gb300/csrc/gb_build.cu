@@ -1628,6 +1628,211 @@ __global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
   block_add2(sah, sahx, sah_acc);
 }
 
+// ---- all collapse levels in one cooperative launch (captured builds)
+//
+// A grid barrier between the phases of a level replaces the kernel boundaries
+// of the level-by-level form (count, scan, emit, advance: four launches and a
+// conditional graph node per level).  Every CTA keeps the level state in
+// registers and advances it alike; CTA 0 writes it back to cstate at the end.
+
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+};
+
+// Barrier over all CTAs of a cooperative launch; every thread calls it.  A CTA
+// that waits for more than kLbSpinLimit re-reads (a CTA missing) sets kErrBuild
+// in *err; a CTA that finds *err set does not wait.  Returns false once *err
+// is set, so the grid leaves its loop.
+__device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned int* err) {
+  __shared__ bool s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool ok = lb_load(err) == 0u;
+    if (ok) {
+      const unsigned int g = lb_load(&b->gen);
+      __threadfence();
+      if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+        lb_store(&b->count, 0u);
+        __threadfence();
+        atomicAdd(&b->gen, 1u);
+      } else {
+        uint32_t it = 0;
+        while (lb_load(&b->gen) == g && it < kLbSpinLimit) {
+          __nanosleep(64);
+          it++;
+        }
+        if (it == kLbSpinLimit) {
+          atomicOr(err, kErrBuild);
+          ok = false;
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok;
+}
+
+constexpr int COLLAPSE_ALL_THREADS = 256;
+
+// Exclusive block scan of two values (a, b); returns (prefix a, prefix b) and
+// the block totals in *ta, *tb.  All threads call it.
+__device__ __forceinline__ uint2 block_excl_scan2(uint32_t a, uint32_t b, uint32_t* ta, uint32_t* tb) {
+  __shared__ uint32_t s_a[COLLAPSE_ALL_THREADS / 32], s_b[COLLAPSE_ALL_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t xa = a, xb = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t ya = __shfl_up_sync(0xFFFFFFFFu, xa, o), yb = __shfl_up_sync(0xFFFFFFFFu, xb, o);
+    if (lane >= o) {
+      xa += ya;
+      xb += yb;
+    }
+  }
+  if (lane == 31) {
+    s_a[warp] = xa;
+    s_b[warp] = xb;
+  }
+  __syncthreads();
+  uint32_t oa = 0, ob = 0, sa = 0, sb = 0;
+#pragma unroll
+  for (int w = 0; w < COLLAPSE_ALL_THREADS / 32; w++) {
+    if (w < warp) {
+      oa += s_a[w];
+      ob += s_b[w];
+    }
+    sa += s_a[w];
+    sb += s_b[w];
+  }
+  __syncthreads();  // s_a, s_b are reused by the next call
+  *ta = sa;
+  *tb = sb;
+  return make_uint2(oa + xa - a, ob + xb - b);
+}
+
+// Every level of the collapse, from the roots in cstate: each CTA takes a
+// contiguous chunk of the level's items, (1) gathers their children and counts
+// internal children and leaf triangles, publishes its sums, [barrier], (2)
+// turns its counts into the level's exclusive offsets from the CTA sums, (3)
+// writes its wide nodes and the next level's items, [barrier].  cta_sums holds
+// 2 * gridDim.x words; *bar is zero on entry.
+__global__ void __launch_bounds__(COLLAPSE_ALL_THREADS, 2) k_collapse_all(
+    BinTree t, const ColItems ci, uint32_t* __restrict__ cstate, uint32_t* __restrict__ kids,
+    uint32_t* __restrict__ nint, uint32_t* __restrict__ ntri, uint32_t* __restrict__ cta_sums,
+    WideNode* __restrict__ nodes, uint32_t* __restrict__ leaf_root, double* sah_acc, uint32_t* leaf_count,
+    uint32_t node_cap, uint32_t tri_cap, uint32_t max_levels, GridBarrier* bar, unsigned int* err) {
+  uint32_t nitems = __ldcg(cstate + kColN), base = __ldcg(cstate + kColBase), tri_next = __ldcg(cstate + kColTri),
+           depth = __ldcg(cstate + kColDepth);
+  bool failed = __ldcg(cstate + kColErr) != 0u;
+  double sah = 0.0, sahx = 0.0;
+  uint32_t nleaf = 0;
+  while (nitems > 0 && !failed) {
+    const uint32_t* __restrict__ items = ci.items[depth & 1u];
+    uint32_t* __restrict__ next_items = ci.items[(depth & 1u) ^ 1u];
+    const uint32_t per = (nitems + gridDim.x - 1) / gridDim.x;
+    const uint32_t first = min(blockIdx.x * per, nitems), last = min(first + per, nitems);
+    // (1) children and counts
+    uint32_t ci_sum = 0, ct_sum = 0;
+    for (uint32_t k = first + threadIdx.x; k < last; k += blockDim.x) {
+      uint32_t kk[8];
+      const int nk = gather_children(t, items[k], kk);
+      uint32_t ni = 0, nt = 0;
+      for (int i = 0; i < 8; i++) {
+        if (i < nk) {
+          const uint32_t c = kk[i];
+          const uint32_t cnt = t.cnt[c];
+          if (cnt > t.leaf_max) ni++; else nt += cnt;
+          kids[8 * (size_t)k + i] = c;
+        } else {
+          kids[8 * (size_t)k + i] = 0xFFFFFFFFu;
+        }
+      }
+      nint[k] = ni;
+      ntri[k] = nt;
+      ci_sum += ni;
+      ct_sum += nt;
+    }
+    {
+      uint32_t ta, tb;
+      block_excl_scan2(ci_sum, ct_sum, &ta, &tb);
+      if (threadIdx.x == 0) {
+        __stcg(cta_sums + blockIdx.x, ta);
+        __stcg(cta_sums + gridDim.x + blockIdx.x, tb);
+      }
+    }
+    if (!grid_sync(bar, err)) break;
+    // (2) offsets: this CTA's prefix and the level's totals from the CTA sums
+    uint32_t pi = 0, pt = 0, ti = 0, tt = 0;
+    for (uint32_t c = threadIdx.x; c < gridDim.x; c += blockDim.x) {
+      const uint32_t a = __ldcg(cta_sums + c), b = __ldcg(cta_sums + gridDim.x + c);
+      ti += a;
+      tt += b;
+      if (c < blockIdx.x) {
+        pi += a;
+        pt += b;
+      }
+    }
+    {
+      uint32_t s0, s1, s2, s3;
+      block_excl_scan2(pi, pt, &s0, &s1);
+      block_excl_scan2(ti, tt, &s2, &s3);
+      pi = s0;
+      pt = s1;
+      ti = s2;
+      tt = s3;
+    }
+    for (uint32_t k0 = first; k0 < last; k0 += blockDim.x) {
+      const uint32_t k = k0 + threadIdx.x;
+      const uint32_t a = k < last ? nint[k] : 0u, b = k < last ? ntri[k] : 0u;
+      uint32_t ta, tb;
+      const uint2 e = block_excl_scan2(a, b, &ta, &tb);
+      if (k < last) {
+        nint[k] = pi + e.x;
+        ntri[k] = pt + e.y;
+      }
+      pi += ta;
+      pt += tb;
+    }
+    __syncthreads();
+    // (3) the wide nodes of this CTA's items (each thread reads back the offsets it wrote)
+    for (uint32_t k = first + threadIdx.x; k < last; k += blockDim.x) {
+      double a = 0.0, b = 0.0;
+      uint32_t l = 0;
+      collapse_emit_node(t, kids, k, nint, ntri, base, base + nitems, tri_next, nodes, leaf_root, next_items,
+                         node_cap, tri_cap, err, a, b, l);
+      sah += a;
+      sahx += b;
+      nleaf += l;
+    }
+    // (4) the next level, alike in every CTA
+    if (blockIdx.x == 0 && threadIdx.x == 0 && depth < (uint32_t)kColMaxLevels) cstate[kColLevels + depth] = base;
+    base += nitems;
+    tri_next += tt;
+    depth++;
+    uint32_t next = ti;
+    if ((next > 0 && depth >= max_levels) || base + next > node_cap) {
+      failed = true;
+      next = 0;
+      if (blockIdx.x == 0 && threadIdx.x == 0) cstate[kColErr] = 1u;
+    }
+    nitems = next;
+    if (!grid_sync(bar, err)) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cstate[kColN] = 0;
+    cstate[kColBase] = base;
+    cstate[kColTri] = tri_next;
+    cstate[kColDepth] = depth;
+    if (depth <= (uint32_t)kColMaxLevels) cstate[kColLevels + depth] = base;  // end of the last level
+    if (lb_load(err) != 0u) cstate[kColErr] = 1u;
+  }
+  nleaf = __reduce_add_sync(0xFFFFFFFFu, nleaf);
+  if ((threadIdx.x & 31) == 0 && nleaf) atomicAdd(leaf_count, nleaf);
+  block_add2(sah, sahx, sah_acc);
+}
+
 // Writes the triangle records of every leaf: slot t holds the binary subtree of
 // the leaf whose first triangle goes to t (kInvalidID elsewhere); its
 // primitives (at most 4) are written in depth-first order, left first.
@@ -2174,6 +2379,14 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
   const uint32_t T = g->total, maxw = g->maxw;
   BoundsAcc* acc = nullptr;
   cudaError_t e = cudaSuccess;
+  // the cooperative collapse: as many CTAs as can be resident at once
+  {
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_all, COLLAPSE_ALL_THREADS, 0)) !=
+        cudaSuccess)
+      return e;
+    g->col_grid = (uint32_t)std::max(1, std::min(per_sm, 4)) * (uint32_t)num_sms_build();
+  }
   if ((e = alloc(&g->d_geoms, ngeoms)) || (e = alloc(&g->plo, T)) || (e = alloc(&g->phi, T)) ||
       (e = alloc(&acc, 1)) || (e = alloc(&g->keys_a, T)) || (e = alloc(&g->keys_b, T)) ||
       (e = alloc(&g->vals_a, T)) || (e = alloc(&g->vals_b, T)) || (e = alloc(&g->hist, sort_hist_entries(T))) ||
@@ -2189,7 +2402,8 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
       (e = alloc(&g->items[0], maxw)) || (e = alloc(&g->items[1], maxw)) || (e = alloc(&g->kids, 8 * (size_t)maxw)) ||
       (e = alloc(&g->nint, maxw)) || (e = alloc(&g->ntri, maxw)) || (e = alloc(&g->leaf_root, N)) ||
       (e = alloc(&g->d_sah, 2)) || (e = alloc(&g->d_leaves, 1)) || (e = alloc(&g->cstate, kColStateWords)) ||
-      (e = alloc(&g->seg_index, g->nseg)) || (e = alloc(&g->status, 1))) {
+      (e = alloc(&g->seg_index, g->nseg)) || (e = alloc(&g->status, 1)) ||
+      (e = alloc(&g->col_sums, 2 * (size_t)g->col_grid)) || (e = alloc(&g->col_bar, 2))) {
     graph_build_release(g);
     return e;
   }
@@ -2309,20 +2523,26 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   GB_CHECK(cudaMemsetAsync(g.d_leaves, 0, sizeof(uint32_t), st));
   GB_CHECK(cudaMemsetAsync(g.cstate, 0, sizeof(uint32_t) * kColStateWords, st));
   // collapse levels in a loop the device ends
-  cudaGraphConditionalHandle col_loop = 0;
-  GB_CHECK(loop_handle(st, &col_loop));
-  k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate, col_loop);
-  note_launches(1);
-  const uint32_t cgrid = std::min<uint32_t>(cdiv(maxw, 128), (uint32_t)fixed_grid);
-  const ColItems ci{{g.items[0], g.items[1]}};
-  GB_CHECK(capture_while(st, g.body_stream, col_loop, [&](cudaStream_t bs) {
-    k_collapse_count<<<cgrid, 128, 0, bs>>>(bt, ci, g.cstate, g.kids, g.nint, g.ntri);
-    scan_excl2(g.nint, g.ntri, maxw, g.d_tot + 0, g.d_tot + 1, g.scan_sums, bs, &acc->pad, g.cstate + kColN);
-    k_collapse_emit<<<cgrid, COLLAPSE_THREADS, 0, bs>>>(bt, g.kids, g.cstate, g.nint, g.ntri, g.nodes, g.leaf_root,
-                                                        ci, g.d_sah, g.d_leaves, maxw, N, &acc->pad);
-    k_collapse_advance<<<1, 32, 0, bs>>>(g.d_tot, g.cstate, maxw, (uint32_t)kColMaxLevels, col_loop);
-    note_launches(3);
-  }));
+  // all collapse levels in one cooperative launch
+  k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate, 0);
+  GB_CHECK(cudaMemsetAsync(g.col_bar, 0, sizeof(GridBarrier), st));
+  {
+    const ColItems ci{{g.items[0], g.items[1]}};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.col_grid);
+    cfg.blockDim = dim3(COLLAPSE_ALL_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GB_CHECK(cudaLaunchKernelEx(&cfg, k_collapse_all, bt, ci, g.cstate, g.kids, g.nint, g.ntri, g.col_sums, g.nodes,
+                                g.leaf_root, g.d_sah, g.d_leaves, maxw, N, (uint32_t)kColMaxLevels,
+                                reinterpret_cast<GridBarrier*>(g.col_bar), &acc->pad));
+  }
+  note_launches(2);
   k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, g.d_geoms, g.plo, g.phi, g.leaf_root, N, g.tris, &acc->pad);
   k_graph_build_check<<<1, 32, 0, st>>>(acc, g.ploc_state, g.cstate, N, g.status);
   note_launches(2);
