@@ -1451,6 +1451,10 @@ __device__ __forceinline__ void write_tri(const GeomDesc* __restrict__ geoms, co
 
 // Writes wide node k of the level and the triangle records of its leaves;
 // adds the node's SAH terms and leaf count to sah_out / nleaf_out.
+
+// The wide node of item k by one thread: wide levels (more items than there
+// are lane groups to share them) are throughput-bound, and this form does the
+// least work per node; collapse_emit_group gives the same node.
 __device__ __forceinline__ void collapse_emit_node(
     const BinTree& t, const uint32_t* __restrict__ kids_in, uint32_t k, const uint32_t* __restrict__ off_int,
     const uint32_t* __restrict__ off_tri, uint32_t level_base, uint32_t next_base, uint32_t tri_next,
@@ -1600,10 +1604,179 @@ __device__ __forceinline__ void collapse_emit_node(
   nleaf_out = nleaf;
 }
 
-constexpr int COLLAPSE_THREADS = 128;
+// The wide node of item k, built by the 8 lanes of a lane group (lane & 7 is
+// the child index; all 8 lanes call it with the same k; gmask names them).
+// Children are placed in slots greedily, the cheapest (child, free slot) pair
+// first with ties to the lower child and then the lower slot, the cost being
+// the child's offset from the node centre along the slot's octant direction
+// (slot s prefers children far along the direction with sign bits s), so that
+// visiting slots in ascending order of (slot ^ ray octant) is roughly
+// near-to-far.  Planes are quantised outward, internal children are numbered
+// and leaf triangles laid out in slot order.
+__device__ __forceinline__ void collapse_emit_group(
+    const BinTree& t, const uint32_t* __restrict__ kids_in, uint32_t k, const uint32_t* __restrict__ off_int,
+    const uint32_t* __restrict__ off_tri, uint32_t level_base, uint32_t next_base, uint32_t tri_next,
+    WideNode* __restrict__ nodes, uint32_t* __restrict__ leaf_root, uint32_t* __restrict__ next_items,
+    uint32_t node_cap, uint32_t tri_cap, uint32_t* err, uint32_t gmask, double& sah_out, double& sahx_out,
+    uint32_t& nleaf_out) {
+  const uint32_t i = threadIdx.x & 7u;
+  const uint32_t kid = kids_in[8 * (size_t)k + i];
+  const bool valid = kid != 0xFFFFFFFFu;
+  const uint32_t vmask = __ballot_sync(gmask, valid) >> (threadIdx.x & 24u) & 0xFFu;
+  const int nk = __popc(vmask);
+  float3 lo = make_float3(0.f, 0.f, 0.f), hi = lo;
+  if (valid) {
+    lo = bt_lo(t, kid);
+    hi = bt_hi(t, kid);
+  }
+  // union box and quantisation frame
+  float3 ulo = valid ? lo : make_float3(INFINITY, INFINITY, INFINITY);
+  float3 uhi = valid ? hi : make_float3(-INFINITY, -INFINITY, -INFINITY);
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    ulo.x = fminf(ulo.x, __shfl_xor_sync(gmask, ulo.x, o, 8));
+    ulo.y = fminf(ulo.y, __shfl_xor_sync(gmask, ulo.y, o, 8));
+    ulo.z = fminf(ulo.z, __shfl_xor_sync(gmask, ulo.z, o, 8));
+    uhi.x = fmaxf(uhi.x, __shfl_xor_sync(gmask, uhi.x, o, 8));
+    uhi.y = fmaxf(uhi.y, __shfl_xor_sync(gmask, uhi.y, o, 8));
+    uhi.z = fmaxf(uhi.z, __shfl_xor_sync(gmask, uhi.z, o, 8));
+  }
+  const uint32_t Ex = exp_for(__fsub_ru(uhi.x, ulo.x));
+  const uint32_t Ey = exp_for(__fsub_ru(uhi.y, ulo.y));
+  const uint32_t Ez = exp_for(__fsub_ru(uhi.z, ulo.z));
+  const float sx = __uint_as_float(Ex << 23), sy = __uint_as_float(Ey << 23), sz = __uint_as_float(Ez << 23);
+  const float ix = __uint_as_float((254u - Ex) << 23), iy = __uint_as_float((254u - Ey) << 23),
+              iz = __uint_as_float((254u - Ez) << 23);
+  // slot costs of this lane's child
+  const float3 pc = make_float3((ulo.x + uhi.x) * 0.5f, (ulo.y + uhi.y) * 0.5f, (ulo.z + uhi.z) * 0.5f);
+  const float dx = (lo.x + hi.x) * 0.5f - pc.x, dy = (lo.y + hi.y) * 0.5f - pc.y, dz = (lo.z + hi.z) * 0.5f - pc.z;
+  float cs[8];
+#pragma unroll
+  for (int s = 0; s < 8; s++) cs[s] = ((s & 1) ? -dx : dx) + ((s & 2) ? -dy : dy) + ((s & 4) ? -dz : dz);
+  // greedy assignment: per round every unplaced child offers its cheapest free
+  // slot; the group takes the least (cost, child, slot)
+  uint32_t used = 0;
+  int my_slot = -1;
+  for (int it = 0; it < nk; it++) {
+    unsigned long long key = ~0ull;
+    if (valid && my_slot < 0) {
+      float bc = INFINITY;
+      int bs = -1;
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        if (used >> s & 1u) continue;
+        if (bs < 0 || cs[s] < bc) {
+          bc = cs[s];
+          bs = s;
+        }
+      }
+      key = ((unsigned long long)f2ord(bc + 0.0f) << 32) | (i << 3) | (uint32_t)bs;  // + 0: -0 ties with +0
+    }
+    const uint32_t khi = __reduce_min_sync(gmask, (uint32_t)(key >> 32));
+    const uint32_t klo = __reduce_min_sync(gmask, (uint32_t)(key >> 32) == khi ? (uint32_t)key : 0xFFFFFFFFu);
+    const uint32_t win = klo >> 3, ws = klo & 7u;
+    used |= 1u << ws;
+    if (win == i) my_slot = (int)ws;
+  }
+  // this child's planes, its part of the SAH, its place among the slots
+  uint32_t qlx = 0, qly = 0, qlz = 0, qhx = 0, qhy = 0, qhz = 0, cnt = 0;
+  bool internal = false;
+  double A = 0.0, Ax = 0.0;
+  if (valid) {
+    const float flx = fminf(fmaxf(floorf(__fsub_rd(lo.x, ulo.x) * ix), 0.f), 255.f);
+    const float fly = fminf(fmaxf(floorf(__fsub_rd(lo.y, ulo.y) * iy), 0.f), 255.f);
+    const float flz = fminf(fmaxf(floorf(__fsub_rd(lo.z, ulo.z) * iz), 0.f), 255.f);
+    const float fhx = fminf(fmaxf(ceilf(__fsub_ru(hi.x, ulo.x) * ix), 0.f), 255.f);
+    const float fhy = fminf(fmaxf(ceilf(__fsub_ru(hi.y, ulo.y) * iy), 0.f), 255.f);
+    const float fhz = fminf(fmaxf(ceilf(__fsub_ru(hi.z, ulo.z) * iz), 0.f), 255.f);
+    qlx = (uint32_t)flx; qly = (uint32_t)fly; qlz = (uint32_t)flz;
+    qhx = (uint32_t)fhx; qhy = (uint32_t)fhy; qhz = (uint32_t)fhz;
+    // decoded (outward-rounded) box, as traversal sees it
+    const float3 dlo = make_float3(__fmaf_rd(flx, sx, ulo.x), __fmaf_rd(fly, sy, ulo.y), __fmaf_rd(flz, sz, ulo.z));
+    const float3 dhi = make_float3(__fmaf_ru(fhx, sx, ulo.x), __fmaf_ru(fhy, sy, ulo.y), __fmaf_ru(fhz, sz, ulo.z));
+    A = (double)fmaxf(0.f, half_area(dlo, dhi));
+    Ax = (double)fmaxf(0.f, half_area(lo, hi));
+    cnt = t.cnt[kid];
+    internal = cnt > t.leaf_max;
+  }
+  const uint32_t slot = valid ? (uint32_t)my_slot : 8u;
+  const uint32_t int_slots = __reduce_or_sync(gmask, internal ? 1u << slot : 0u);
+  uint32_t tri_off = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const uint32_t sj = __shfl_sync(gmask, slot, j, 8);
+    const uint32_t cj = __shfl_sync(gmask, (valid && !internal) ? cnt : 0u, j, 8);
+    if (sj < slot) tri_off += cj;
+  }
+  const uint32_t oi = off_int[k], ot = off_tri[k];
+  const uint32_t child_base = next_base + oi, tri_base = tri_next + ot;
+  uint32_t meta = 0;
+  if (valid && internal) {
+    const uint32_t rank = __popc(int_slots & ((1u << slot) - 1u));
+    meta = 0x80u | slot;
+    if (oi + rank >= node_cap || child_base + rank >= node_cap) atomicOr(err, kErrBuild);
+    else next_items[oi + rank] = kid;
+    sah_out += A;  // inner node term
+    sahx_out += Ax;
+  } else if (valid) {
+    meta = 0x80u | ((cnt - 1u) << 5) | tri_off;
+    // the leaf's triangle records are written after the last level by
+    // k_write_leaves, one thread per leaf: here only its binary subtree is
+    // recorded at the slot of its first triangle
+    if (tri_base + tri_off + cnt > tri_cap) atomicOr(err, kErrBuild);
+    else leaf_root[tri_base + tri_off] = kid;
+    sah_out += A * (double)((cnt + 3) / 4);  // leaf term: area x Triangle4 blocks
+    sahx_out += Ax * (double)((cnt + 3) / 4);
+    nleaf_out++;
+  }
+  // the node's words: byte `slot` of each per-slot array (empty slots: meta 0,
+  // lower planes 255, upper planes 0)
+  const uint32_t sh = 8u * (slot & 3u);
+  const bool hi4 = slot >= 4u && slot < 8u, lo4 = slot < 4u;
+  auto word = [&](uint32_t v, bool part) { return part ? v << sh : 0u; };
+  const uint32_t empty = (~used) & 0xFFu;
+  auto fill = [&](uint32_t m4) {  // 0xFF in the bytes of the empty slots m4 (4 bits)
+    return ((m4 & 1u) ? 0xFFu : 0u) | ((m4 & 2u) ? 0xFF00u : 0u) | ((m4 & 4u) ? 0xFF0000u : 0u) |
+           ((m4 & 8u) ? 0xFF000000u : 0u);
+  };
+  const uint32_t m0 = __reduce_or_sync(gmask, word(meta, lo4)), m1 = __reduce_or_sync(gmask, word(meta, hi4));
+  const uint32_t lx0 = __reduce_or_sync(gmask, word(qlx, lo4)) | fill(empty & 15u);
+  const uint32_t lx1 = __reduce_or_sync(gmask, word(qlx, hi4)) | fill(empty >> 4);
+  const uint32_t ly0 = __reduce_or_sync(gmask, word(qly, lo4)) | fill(empty & 15u);
+  const uint32_t ly1 = __reduce_or_sync(gmask, word(qly, hi4)) | fill(empty >> 4);
+  const uint32_t lz0 = __reduce_or_sync(gmask, word(qlz, lo4)) | fill(empty & 15u);
+  const uint32_t lz1 = __reduce_or_sync(gmask, word(qlz, hi4)) | fill(empty >> 4);
+  const uint32_t hx0 = __reduce_or_sync(gmask, word(qhx, lo4)), hx1 = __reduce_or_sync(gmask, word(qhx, hi4));
+  const uint32_t hy0 = __reduce_or_sync(gmask, word(qhy, lo4)), hy1 = __reduce_or_sync(gmask, word(qhy, hi4));
+  const uint32_t hz0 = __reduce_or_sync(gmask, word(qhz, lo4)), hz1 = __reduce_or_sync(gmask, word(qhz, hi4));
+  if (level_base + k >= node_cap) {
+    if (i == 0) atomicOr(err, kErrBuild);
+    return;
+  }
+  // WideNode as five 16-byte words (gb_common.h layout)
+  uint4* dst = reinterpret_cast<uint4*>(nodes + level_base + k);
+  if (i == 0) {
+    dst[0] = make_uint4(__float_as_uint(ulo.x), __float_as_uint(ulo.y), __float_as_uint(ulo.z),
+                        Ex | (Ey << 8) | (Ez << 16) | ((int_slots & 0xFFu) << 24));
+  } else if (i == 1) {
+    dst[1] = make_uint4(child_base, tri_base, m0, m1);
+  } else if (i == 2) {
+    dst[2] = make_uint4(lx0, lx1, ly0, ly1);
+  } else if (i == 3) {
+    dst[3] = make_uint4(lz0, lz1, hx0, hx1);
+  } else if (i == 4) {
+    dst[4] = make_uint4(hy0, hy1, hz0, hz1);
+  }
+}
 
-// One wide node per thread; the SAH sums and the leaf count are reduced per
-// CTA first (one atomic per CTA instead of one per node).
+constexpr int COLLAPSE_THREADS = 128;
+// Levels of at most this many items are emitted by lane groups (latency-bound:
+// one node's greedy slot choice and reductions spread over 8 lanes), wider ones
+// one node per thread.
+constexpr uint32_t kGroupEmitMax = 16384;
+
+// One wide node per 8-lane group; the SAH sums and the leaf count are reduced
+// per CTA first (one atomic per CTA instead of one per node).
 __global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
     BinTree t, const uint32_t* __restrict__ kids_in, const uint32_t* __restrict__ cstate,
     const uint32_t* __restrict__ off_int, const uint32_t* __restrict__ off_tri, WideNode* __restrict__ nodes,
@@ -1614,14 +1787,21 @@ __global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
   const uint32_t next_base = level_base + nitems;
   double sah = 0.0, sahx = 0.0;
   uint32_t nleaf = 0;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nitems; k += gridDim.x * blockDim.x) {
-    double a = 0.0, b = 0.0;
-    uint32_t l = 0;
-    collapse_emit_node(t, kids_in, k, off_int, off_tri, level_base, next_base, tri_next, nodes, leaf_root, next_items,
-                       node_cap, tri_cap, err, a, b, l);
-    sah += a;
-    sahx += b;
-    nleaf += l;
+  if (nitems <= kGroupEmitMax) {
+    const uint32_t gmask = 0xFFu << (threadIdx.x & 24u);
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; k < nitems; k += (gridDim.x * blockDim.x) >> 3)
+      collapse_emit_group(t, kids_in, k, off_int, off_tri, level_base, next_base, tri_next, nodes, leaf_root,
+                          next_items, node_cap, tri_cap, err, gmask, sah, sahx, nleaf);
+  } else {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nitems; k += gridDim.x * blockDim.x) {
+      double a = 0.0, b = 0.0;
+      uint32_t l = 0;
+      collapse_emit_node(t, kids_in, k, off_int, off_tri, level_base, next_base, tri_next, nodes, leaf_root,
+                         next_items, node_cap, tri_cap, err, a, b, l);
+      sah += a;
+      sahx += b;
+      nleaf += l;
+    }
   }
   nleaf = __reduce_add_sync(0xFFFFFFFFu, nleaf);
   if ((threadIdx.x & 31) == 0 && nleaf) atomicAdd(leaf_count, nleaf);
@@ -1796,15 +1976,23 @@ __global__ void __launch_bounds__(COLLAPSE_ALL_THREADS, 2) k_collapse_all(
       pt += tb;
     }
     __syncthreads();
-    // (3) the wide nodes of this CTA's items (each thread reads back the offsets it wrote)
-    for (uint32_t k = first + threadIdx.x; k < last; k += blockDim.x) {
-      double a = 0.0, b = 0.0;
-      uint32_t l = 0;
-      collapse_emit_node(t, kids, k, nint, ntri, base, base + nitems, tri_next, nodes, leaf_root, next_items,
-                         node_cap, tri_cap, err, a, b, l);
-      sah += a;
-      sahx += b;
-      nleaf += l;
+    // (3) the wide nodes of this CTA's items: one per 8-lane group on narrow
+    // levels, one per thread on wide ones
+    if (nitems <= kGroupEmitMax) {
+      const uint32_t gmask = 0xFFu << (threadIdx.x & 24u);
+      for (uint32_t k = first + (threadIdx.x >> 3); k < last; k += blockDim.x >> 3)
+        collapse_emit_group(t, kids, k, nint, ntri, base, base + nitems, tri_next, nodes, leaf_root, next_items,
+                            node_cap, tri_cap, err, gmask, sah, sahx, nleaf);
+    } else {
+      for (uint32_t k = first + threadIdx.x; k < last; k += blockDim.x) {
+        double a = 0.0, b = 0.0;
+        uint32_t l = 0;
+        collapse_emit_node(t, kids, k, nint, ntri, base, base + nitems, tri_next, nodes, leaf_root, next_items,
+                           node_cap, tri_cap, err, a, b, l);
+        sah += a;
+        sahx += b;
+        nleaf += l;
+      }
     }
     // (4) the next level, alike in every CTA
     if (blockIdx.x == 0 && threadIdx.x == 0 && depth < (uint32_t)kColMaxLevels) cstate[kColLevels + depth] = base;
@@ -2243,8 +2431,9 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     k_collapse_count<<<grid, 128, 0, st>>>(bt, citems, cstate, kids, nint, ntri);
     note_launches(1);
     scan_excl2(nint, ntri, nitems_known, d_tot + 0, d_tot + 1, scan_sums, st, &acc->pad);
-    k_collapse_emit<<<grid, COLLAPSE_THREADS, 0, st>>>(bt, kids, cstate, nint, ntri, wnodes, leaf_root, citems,
-                                                       d_sah, d_leaves, maxw, N, &acc->pad);
+    k_collapse_emit<<<cdiv((uint64_t)nitems_known * (nitems_known <= kGroupEmitMax ? 8 : 1), COLLAPSE_THREADS),
+                      COLLAPSE_THREADS, 0, st>>>(
+        bt, kids, cstate, nint, ntri, wnodes, leaf_root, citems, d_sah, d_leaves, maxw, N, &acc->pad);
     k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels, 0);
     note_launches(2);
     level++;
