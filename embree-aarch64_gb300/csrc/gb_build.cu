@@ -104,12 +104,16 @@ __device__ __forceinline__ int find_geom(const GeomDesc* geoms, int ngeoms, uint
 }
 
 // plo[i] = (lo.xyz, geometry slot), phi[i] = (hi.xyz, primID); invalid
-// triangles get an empty box (+inf,-inf).  Grid-stride: the bounds and the
-// valid count are reduced per thread, per warp and per CTA, so the global
-// atomics are 13 per CTA (a grid of a few CTAs per SM).
+// triangles get an empty box (+inf,-inf).  prec[i] (when non-null) receives
+// primitive i's leaf record -- Triangle4 values v0, e1 = v0 - v1, e2 = v2 - v0
+// (triangle.h:40-41), or v0, v1, v2 in robust scenes (trianglev.h:93-115), or
+// an instance leaf -- read here in primitive order, where the vertex reads
+// coalesce, so that the leaf writer later gathers one 48-byte record per leaf.
+// Grid-stride: the bounds and the valid count are reduced per thread, per warp
+// and per CTA, so the global atomics are 13 per CTA (a grid of a few CTAs per SM).
 __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ geoms, int ngeoms, uint32_t total,
                                                   float4* __restrict__ plo, float4* __restrict__ phi,
-                                                  BoundsAcc* acc) {
+                                                  BoundsAcc* acc, TriRecord* __restrict__ prec, int robust) {
   __shared__ uint32_t s_b[12];
   __shared__ uint32_t s_cnt;
   if (threadIdx.x < 12) s_b[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0xFFFFFFFFu : 0u;
@@ -134,6 +138,10 @@ __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ g
           lo = make_float3(bx.lo[0], bx.lo[1], bx.lo[2]);
           hi = make_float3(bx.hi[0], bx.hi[1], bx.hi[2]);
         }
+        if (prec)
+          prec[gi] = TriRecord{make_float4(0.f, 0.f, 0.f, __uint_as_float(bx.inst)),
+                               make_float4(0.f, 0.f, 0.f, __uint_as_float(bx.geomID)),
+                               make_float4(0.f, 0.f, 0.f, __uint_as_float(kInstanceLeaf))};
       } else {
       const uint3 t = load_tri(g, j);
       if (t.x < g.nverts && t.y < g.nverts && t.z < g.nverts) {
@@ -142,6 +150,13 @@ __global__ void __launch_bounds__(256) k_primrefs(const GeomDesc* __restrict__ g
           ok = true;
           lo = f3min(f3min(a, b), c);
           hi = f3max(f3max(a, b), c);
+          if (prec) {
+            const float3 e1 = robust ? b : make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+            const float3 e2 = robust ? c : make_float3(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z));
+            prec[gi] = TriRecord{make_float4(a.x, a.y, a.z, __uint_as_float(j)),
+                                 make_float4(e1.x, e1.y, e1.z, __uint_as_float(g.geomID)),
+                                 make_float4(e2.x, e2.y, e2.z, 0.f)};
+          }
         }
       }
       }
@@ -2027,7 +2042,8 @@ __global__ void __launch_bounds__(COLLAPSE_ALL_THREADS, 2) k_collapse_all(
 __global__ void __launch_bounds__(256) k_write_leaves(BinTree t, const GeomDesc* __restrict__ geoms,
                                                       const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                       const uint32_t* __restrict__ leaf_root, uint32_t ntris,
-                                                      TriRecord* __restrict__ tris, uint32_t* err) {
+                                                      TriRecord* __restrict__ tris, uint32_t* err,
+                                                      const TriRecord* __restrict__ prec) {
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   if (first >= ntris) return;
   const uint32_t c = leaf_root[first];
@@ -2043,7 +2059,8 @@ __global__ void __launch_bounds__(256) k_write_leaves(BinTree t, const GeomDesc*
         atomicOr(err, kErrBuild);
         return;
       }
-      write_tri(geoms, plo, phi, bt_right(t, x), &tris[first + w], t.robust != 0);
+      if (prec) tris[first + w] = prec[bt_right(t, x)];
+      else write_tri(geoms, plo, phi, bt_right(t, x), &tris[first + w], t.robust != 0);
       w++;
     } else {
       if (sp + 2 > 8) {
@@ -2219,7 +2236,12 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   h_acc.kand = ~0ull;
   h_acc.kor = 0ull;
   GB_CHECK(cudaMemcpyAsync(acc, &h_acc, sizeof(BoundsAcc), cudaMemcpyHostToDevice, st));
-  k_primrefs<<<grid_stride_blocks(total), 256, 0, st>>>(d_geoms, ngeoms, total, plo, phi, acc); note_launches(1);
+  // leaf records in primitive order (read back by k_write_leaves)
+  TriRecord* prec = nullptr;
+  GB_CHECK(arena.alloc(&prec, total));
+  k_primrefs<<<grid_stride_blocks(total), 256, 0, st>>>(d_geoms, ngeoms, total, plo, phi, acc, prec,
+                                                        opt.robust ? 1 : 0);
+  note_launches(1);
 
   uint64_t *keys_a = nullptr, *keys_b = nullptr;
   uint32_t *vals_a = nullptr, *vals_b = nullptr;
@@ -2240,7 +2262,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   for (int d = 0; d < 3; d++) { out->lo[d] = ord2f(h_acc.glo[d]); out->hi[d] = ord2f(h_acc.ghi[d]); }
   if (N == 0) {
     for (int d = 0; d < 3; d++) { out->lo[d] = INFINITY; out->hi[d] = -INFINITY; }
-    arena.free(d_geoms); arena.free(plo); arena.free(phi); arena.free(acc);
+    arena.free(d_geoms); arena.free(plo); arena.free(phi); arena.free(acc); arena.free(prec);
     arena.free(keys_a); arena.free(keys_b); arena.free(vals_a); arena.free(vals_b);
     return cudaStreamSynchronize(st);
   }
@@ -2454,7 +2476,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   }
   const uint32_t num_nodes = level_base, depth = (uint32_t)level_start.size();
   const uint32_t tri_next = level < 1 ? 0u : h_col[kColTri];
-  k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, d_geoms, plo, phi, leaf_root, N, wtris, &acc->pad);
+  k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, d_geoms, plo, phi, leaf_root, N, wtris, &acc->pad, prec);
   note_launches(1);
   GB_CHECK(cudaGetLastError());
   arena.free(leaf_root);
@@ -2486,7 +2508,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   if (d_choice) arena.free(d_choice);
   arena.free(d_tot); arena.free(d_root); arena.free(d_iters); arena.free(scan_sums);
   arena.free(bnlo); arena.free(bnhi); arena.free(bncnt);
-  arena.free(plo); arena.free(phi); arena.free(acc); arena.free(d_geoms);
+  arena.free(plo); arena.free(phi); arena.free(acc); arena.free(d_geoms); arena.free(prec);
   arena.free(keys_a); arena.free(keys_b); arena.free(vals_a); arena.free(vals_b);
   GB_CHECK(cudaEventRecord(ev1, st));
   GB_CHECK(cudaStreamSynchronize(st));
@@ -2592,7 +2614,8 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
       (e = alloc(&g->nint, maxw)) || (e = alloc(&g->ntri, maxw)) || (e = alloc(&g->leaf_root, N)) ||
       (e = alloc(&g->d_sah, 2)) || (e = alloc(&g->d_leaves, 1)) || (e = alloc(&g->cstate, kColStateWords)) ||
       (e = alloc(&g->seg_index, g->nseg)) || (e = alloc(&g->status, 1)) ||
-      (e = alloc(&g->col_sums, 2 * (size_t)g->col_grid)) || (e = alloc(&g->col_bar, 2))) {
+      (e = alloc(&g->col_sums, 2 * (size_t)g->col_grid)) || (e = alloc(&g->col_bar, 2)) ||
+      (e = alloc(&g->prec, T))) {
     graph_build_release(g);
     return e;
   }
@@ -2655,7 +2678,8 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   BoundsAcc* acc = reinterpret_cast<BoundsAcc*>(g.acc);
   const int fixed_grid = 8 * num_sms_build();
   k_acc_init<<<1, 32, 0, st>>>(acc);
-  k_primrefs<<<grid_stride_blocks(T), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc);
+  k_primrefs<<<grid_stride_blocks(T), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc, g.prec,
+                                                    g.opt.robust ? 1 : 0);
   k_morton<<<grid_stride_blocks(T), 256, 0, st>>>(g.plo, g.phi, T, acc, g.keys_a, g.vals_a, g.opt.morton_cube,
                                          g.opt.segmented ? 1 : 0, g.opt.morton_bits == 30 ? 1 : 0);
   note_launches(3);
@@ -2732,7 +2756,8 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
                                 reinterpret_cast<GridBarrier*>(g.col_bar), &acc->pad));
   }
   note_launches(2);
-  k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, g.d_geoms, g.plo, g.phi, g.leaf_root, N, g.tris, &acc->pad);
+  k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, g.d_geoms, g.plo, g.phi, g.leaf_root, N, g.tris, &acc->pad,
+                                                g.prec);
   k_graph_build_check<<<1, 32, 0, st>>>(acc, g.ploc_state, g.cstate, N, g.status);
   note_launches(2);
   return cudaGetLastError();

@@ -77,6 +77,7 @@ struct GraphBuild {
   uint32_t *d_leaves = nullptr, *cstate = nullptr, *seg_index = nullptr, *status = nullptr;
   uint32_t col_grid = 0;                                // CTAs of the cooperative collapse
   uint32_t *col_sums = nullptr, *col_bar = nullptr;     // its per-CTA sums and grid barrier
+  TriRecord* prec = nullptr;                            // leaf records in primitive order
   cudaStream_t body_stream = nullptr;  // captures the bodies of the device-decided build loops
 };
 struct GraphBuildResult {
