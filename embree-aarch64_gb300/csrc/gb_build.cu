@@ -752,6 +752,47 @@ __device__ __forceinline__ void dp_leaf(float4* cost, uint2* choice, uint32_t n,
   dp_store(cost, choice, n, c, make_uint2(0u, 0u));
 }
 
+// Grid barrier of the cooperative build kernels (all CTAs resident).
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+};
+
+// Barrier over all CTAs of a cooperative launch; every thread calls it.  A CTA
+// that waits for more than kLbSpinLimit re-reads (a CTA missing) sets kErrBuild
+// in *err; a CTA that finds *err set does not wait.  Returns false once *err
+// is set, so the grid leaves its loop.
+__device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned int* err) {
+  __shared__ bool s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool ok = lb_load(err) == 0u;
+    if (ok) {
+      const unsigned int g = lb_load(&b->gen);
+      __threadfence();
+      if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+        lb_store(&b->count, 0u);
+        __threadfence();
+        atomicAdd(&b->gen, 1u);
+      } else {
+        uint32_t it = 0;
+        while (lb_load(&b->gen) == g && it < kLbSpinLimit) {
+          __nanosleep(64);
+          it++;
+        }
+        if (it == kLbSpinLimit) {
+          atomicOr(err, kErrBuild);
+          ok = false;
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok;
+}
+
 // ---------------------------------------------------------------------------
 // 4. PLOC
 // ---------------------------------------------------------------------------
@@ -799,7 +840,8 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
 // over the tiles grid-stride, so the grid is any size.
 enum : int { kPlocN = 0, kPlocNext = 1, kPlocRounds = 2, kPlocTiles = 3, kPlocDone = 4, kPlocParity = 5,
              kPlocIters = 6, kPlocStateWords = 8 };
-// device-decided PLOC loops (conditional graph nodes) stop after this many rounds
+// device-decided PLOC loops (the cooperative rounds of captured builds) stop
+// after this many rounds
 constexpr uint32_t kPlocMaxIters = 1024;
 
 // The two cluster buffers of the PLOC rounds; a round reads set ploc_state[kPlocParity]
@@ -811,17 +853,11 @@ struct PlocBufs {
   uint32_t* cidx[2];
 };
 
-// Sets the condition of the conditional graph node that repeats a build loop (when
-// the kernel runs inside such a graph; handle 0 otherwise).
-__device__ __forceinline__ void set_loop(cudaGraphConditionalHandle h, bool again) {
-  if (h) cudaGraphSetConditional(h, again ? 1u : 0u);
-}
 
 // The clusters alternate between two buffers, one round reading A and writing
 // B, the next the reverse; kPlocParity counts (mod 2) the rounds that ran, so
 // the current clusters are in B when it is 1 whatever no-op rounds followed.
-__global__ void k_ploc_state_init(const BoundsAcc* __restrict__ acc, uint32_t* __restrict__ ploc_state,
-                                  cudaGraphConditionalHandle loop) {
+__global__ void k_ploc_state_init(const BoundsAcc* __restrict__ acc, uint32_t* __restrict__ ploc_state) {
   if (threadIdx.x == 0) {
     const uint32_t n = acc->nvalid;
     ploc_state[kPlocN] = n;
@@ -831,8 +867,43 @@ __global__ void k_ploc_state_init(const BoundsAcc* __restrict__ acc, uint32_t* _
     ploc_state[kPlocDone] = n <= PLOC_SMALL ? 1u : 0u;
     ploc_state[kPlocParity] = 0;
     ploc_state[kPlocIters] = 0;
-    set_loop(loop, n > PLOC_SMALL);
   }
+}
+
+// Nearest neighbour (least merged-box area within PLOC_R clusters on either
+// side, same segment) of every cluster of one PLOC_BLOCK tile; the window with
+// its halo is staged in shared memory.
+template <int PLOC_R>
+__device__ __forceinline__ void ploc_nn_tile(const float4* __restrict__ clo, const float4* __restrict__ chi, uint32_t n,
+                                             uint32_t tile, uint32_t* __restrict__ nn, float3* s_lo, float3* s_hi,
+                                             uint32_t* s_seg) {
+  const int base = (int)(tile * PLOC_BLOCK);
+  for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
+    const int j = base - PLOC_R + k;
+    if (j >= 0 && j < (int)n) {
+      const float4 a = clo[j], b = chi[j];
+      s_lo[k] = make_float3(a.x, a.y, a.z);
+      s_hi[k] = make_float3(b.x, b.y, b.z);
+      s_seg[k] = __float_as_uint(a.w);
+    }
+  }
+  __syncthreads();
+  const int i = base + threadIdx.x;
+  if (i < (int)n) {
+    const float3 lo = s_lo[threadIdx.x + PLOC_R], hi = s_hi[threadIdx.x + PLOC_R];
+    const uint32_t seg = s_seg[threadIdx.x + PLOC_R];
+    unsigned long long best = ~0ull;
+#pragma unroll 4
+    for (int o = -PLOC_R; o <= PLOC_R; o++) {
+      const int j = i + o;
+      if (o == 0 || j < 0 || j >= (int)n || s_seg[threadIdx.x + PLOC_R + o] != seg) continue;
+      const float a = half_area(f3min(lo, s_lo[threadIdx.x + PLOC_R + o]), f3max(hi, s_hi[threadIdx.x + PLOC_R + o]));
+      const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
+      best = key < best ? key : best;
+    }
+    nn[i] = best != ~0ull ? (uint32_t)best : (uint32_t)i;  // no neighbour in the segment: stays alone
+  }
+  __syncthreads();  // the window is reloaded for the next tile
 }
 
 template <int PLOC_R>
@@ -843,37 +914,8 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const PlocBufs bufs, con
   if (ploc_state[kPlocDone]) return;
   const uint32_t n = ploc_state[kPlocN];
   const uint32_t par = ploc_state[kPlocParity] & 1u;
-  const float4* __restrict__ clo = bufs.clo[par];
-  const float4* __restrict__ chi = bufs.chi[par];
-  for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x) {
-    const int base = (int)(tile * PLOC_BLOCK);
-    for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_R; k += PLOC_BLOCK) {
-      const int j = base - PLOC_R + k;
-      if (j >= 0 && j < (int)n) {
-        const float4 a = clo[j], b = chi[j];
-        s_lo[k] = make_float3(a.x, a.y, a.z);
-        s_hi[k] = make_float3(b.x, b.y, b.z);
-        s_seg[k] = __float_as_uint(a.w);
-      }
-    }
-    __syncthreads();
-    const int i = base + threadIdx.x;
-    if (i < (int)n) {
-      const float3 lo = s_lo[threadIdx.x + PLOC_R], hi = s_hi[threadIdx.x + PLOC_R];
-      const uint32_t seg = s_seg[threadIdx.x + PLOC_R];
-      unsigned long long best = ~0ull;
-#pragma unroll 4
-      for (int o = -PLOC_R; o <= PLOC_R; o++) {
-        const int j = i + o;
-        if (o == 0 || j < 0 || j >= (int)n || s_seg[threadIdx.x + PLOC_R + o] != seg) continue;
-        const float a = half_area(f3min(lo, s_lo[threadIdx.x + PLOC_R + o]), f3max(hi, s_hi[threadIdx.x + PLOC_R + o]));
-        const unsigned long long key = ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j;
-        best = key < best ? key : best;
-      }
-      nn[i] = best != ~0ull ? (uint32_t)best : (uint32_t)i;  // no neighbour in the segment: stays alone
-    }
-    __syncthreads();  // the window is reloaded for the next tile
-  }
+  for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x)
+    ploc_nn_tile<PLOC_R>(bufs.clo[par], bufs.chi[par], n, tile, nn, s_lo, s_hi, s_seg);
 }
 
 // Survivor and merge counts of every tile of the round.
@@ -912,6 +954,68 @@ __device__ __forceinline__ uint32_t block_excl_scan_flag(int flag, uint32_t* s_w
   return pre + __popc(bal & ((1u << lane) - 1u));
 }
 
+// Survivors and merges of one tile: a cluster whose nearest neighbour is
+// mutual merges with it (the lower index creates the node, the higher one is
+// dropped), the others survive as they are; outputs go to position
+// surv_off + rank among the tile's survivors, new nodes to node_next + merge_off
+// + rank among its merges.  Each new node's collapse costs are computed here.
+__device__ __forceinline__ void ploc_emit_tile(const PlocBufs& bufs, uint32_t par, const uint32_t* __restrict__ nn,
+                                               uint32_t n, uint32_t node_next, uint32_t tile, uint32_t surv_off,
+                                               uint32_t merge_off, float4* __restrict__ bnlo,
+                                               float4* __restrict__ bnhi, uint32_t* __restrict__ bncnt,
+                                               uint32_t node_cap, uint32_t* err, float4* __restrict__ dp_cost,
+                                               uint2* __restrict__ dp_choice, uint32_t leaf_max, uint32_t* s_w) {
+  const float4* __restrict__ clo = bufs.clo[par];
+  const float4* __restrict__ chi = bufs.chi[par];
+  const uint32_t* __restrict__ cidx = bufs.cidx[par];
+  float4* __restrict__ olo = bufs.clo[par ^ 1u];
+  float4* __restrict__ ohi = bufs.chi[par ^ 1u];
+  uint32_t* __restrict__ oidx = bufs.cidx[par ^ 1u];
+  const uint32_t i = tile * PLOC_BLOCK + threadIdx.x;
+  int surv = 0, merge = 0;
+  uint32_t j = 0;
+  if (i < n) {
+    j = nn[i];
+    const bool mutual = (j != i) && nn[j] == i;
+    merge = mutual && i < j;
+    surv = !(mutual && j < i);
+  }
+  const uint32_t rs = block_excl_scan_flag(surv, s_w);
+  const uint32_t rm = block_excl_scan_flag(merge, s_w);
+  if (i >= n || !surv) return;
+  const uint32_t pos = surv_off + rs;
+  const float4 a = clo[i], b = chi[i];
+  if (pos >= n) {
+    atomicOr(err, kErrBuild);
+    return;
+  }
+  if (merge) {
+    const float4 c = clo[j], d = chi[j];
+    const uint32_t id = node_next + merge_off + rm;
+    if (id >= node_cap) {
+      atomicOr(err, kErrBuild);
+      return;
+    }
+    const uint32_t l = cidx[i], r = cidx[j];
+    const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), a.w);
+    const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
+    bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
+    bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
+    const uint32_t cnt = bncnt[l] + bncnt[r];
+    bncnt[id] = cnt;
+    if (dp_cost)
+      dp_node(dp_cost, dp_choice, id, l, r, half_area(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z)),
+              cnt, leaf_max);
+    olo[pos] = lo;
+    ohi[pos] = hi;
+    oidx[pos] = id;
+  } else {
+    olo[pos] = a;
+    ohi[pos] = b;
+    oidx[pos] = cidx[i];
+  }
+}
+
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const PlocBufs bufs, const uint32_t* __restrict__ nn,
                                                           const uint32_t* __restrict__ ploc_state,
                                                           const uint32_t* __restrict__ bsurv_off,
@@ -924,63 +1028,14 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_emit(const PlocBufs bufs, c
   if (ploc_state[kPlocDone]) return;
   const uint32_t n = ploc_state[kPlocN], node_next = ploc_state[kPlocNext];
   const uint32_t par = ploc_state[kPlocParity] & 1u;
-  const float4* __restrict__ clo = bufs.clo[par];
-  const float4* __restrict__ chi = bufs.chi[par];
-  const uint32_t* __restrict__ cidx = bufs.cidx[par];
-  float4* __restrict__ olo = bufs.clo[par ^ 1u];
-  float4* __restrict__ ohi = bufs.chi[par ^ 1u];
-  uint32_t* __restrict__ oidx = bufs.cidx[par ^ 1u];
-  for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x) {
-    const uint32_t i = tile * PLOC_BLOCK + threadIdx.x;
-    int surv = 0, merge = 0;
-    uint32_t j = 0;
-    if (i < n) {
-      j = nn[i];
-      const bool mutual = (j != i) && nn[j] == i;
-      merge = mutual && i < j;
-      surv = !(mutual && j < i);
-    }
-    const uint32_t rs = block_excl_scan_flag(surv, s_w);
-    const uint32_t rm = block_excl_scan_flag(merge, s_w);
-    if (i >= n || !surv) continue;
-    const uint32_t pos = bsurv_off[tile] + rs;
-    const float4 a = clo[i], b = chi[i];
-    if (pos >= n) {
-      atomicOr(err, kErrBuild);
-      continue;
-    }
-    if (merge) {
-      const float4 c = clo[j], d = chi[j];
-      const uint32_t id = node_next + bmerge_off[tile] + rm;
-      if (id >= node_cap) {
-        atomicOr(err, kErrBuild);
-        continue;
-      }
-      const uint32_t l = cidx[i], r = cidx[j];
-      const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), a.w);
-      const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
-      bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
-      bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-      const uint32_t cnt = bncnt[l] + bncnt[r];
-      bncnt[id] = cnt;
-      if (dp_cost)
-        dp_node(dp_cost, dp_choice, id, l, r, half_area(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z)),
-                cnt, leaf_max);
-      olo[pos] = lo;
-      ohi[pos] = hi;
-      oidx[pos] = id;
-    } else {
-      olo[pos] = a;
-      ohi[pos] = b;
-      oidx[pos] = cidx[i];
-    }
-  }
+  for (uint32_t tile = blockIdx.x; tile * PLOC_BLOCK < n; tile += gridDim.x)
+    ploc_emit_tile(bufs, par, nn, n, node_next, tile, bsurv_off[tile], bmerge_off[tile], bnlo, bnhi, bncnt, node_cap,
+                   err, dp_cost, dp_choice, leaf_max, s_w);
 }
 
 // After a round: the survivors are the new clusters, the merges took the next
 // binary node indices; rounds end once n <= PLOC_SMALL or nothing merged.
-__global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ ploc_state,
-                               cudaGraphConditionalHandle loop) {
+__global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ ploc_state) {
   if (threadIdx.x != 0) return;
   if (!ploc_state[kPlocDone]) {
     const uint32_t n = tot[0], merged = tot[1];
@@ -991,10 +1046,115 @@ __global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __res
     ploc_state[kPlocParity] ^= 1u;
     if (n <= PLOC_SMALL || merged == 0) ploc_state[kPlocDone] = 1u;
   }
-  // a device-decided loop also stops at kPlocMaxIters rounds (the one-CTA finish then
-  // finds more than PLOC_SMALL clusters and reports the build as failed)
-  const uint32_t it = ++ploc_state[kPlocIters];
-  set_loop(loop, !ploc_state[kPlocDone] && it < kPlocMaxIters);
+  ++ploc_state[kPlocIters];
+}
+
+// All PLOC rounds above PLOC_SMALL clusters in one cooperative launch (captured
+// builds): per round (A) nearest neighbours, [barrier], (B) survivors and
+// merges of each tile, per-CTA sums, [barrier], (C) this CTA's offsets from the
+// sums and its tiles' outputs, [barrier].  Each CTA takes a contiguous run of
+// tiles and keeps the round state (the k_ploc_advance rules) in registers; CTA 0
+// writes it back to ploc_state.  cta_sums holds 2 * gridDim.x words; *bar is
+// zero on entry.
+template <int PLOC_R>
+__global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_all(const PlocBufs bufs, uint32_t* __restrict__ ploc_state,
+                                                         uint32_t* __restrict__ nn, uint32_t* __restrict__ tile_s,
+                                                         uint32_t* __restrict__ tile_m, uint32_t* __restrict__ cta_sums,
+                                                         float4* __restrict__ bnlo, float4* __restrict__ bnhi,
+                                                         uint32_t* __restrict__ bncnt, uint32_t node_cap,
+                                                         float4* __restrict__ dp_cost, uint2* __restrict__ dp_choice,
+                                                         uint32_t leaf_max, GridBarrier* bar, unsigned int* err) {
+  __shared__ float3 s_lo[PLOC_BLOCK + 2 * PLOC_R], s_hi[PLOC_BLOCK + 2 * PLOC_R];
+  __shared__ uint32_t s_seg[PLOC_BLOCK + 2 * PLOC_R];
+  __shared__ uint32_t s_w[PLOC_BLOCK / 32];
+  __shared__ uint32_t s_red[4][PLOC_BLOCK / 32];
+  uint32_t n = __ldcg(ploc_state + kPlocN), node_next = __ldcg(ploc_state + kPlocNext);
+  uint32_t par = __ldcg(ploc_state + kPlocParity) & 1u, rounds = __ldcg(ploc_state + kPlocRounds);
+  uint32_t iters = __ldcg(ploc_state + kPlocIters);
+  bool done = __ldcg(ploc_state + kPlocDone) != 0u;
+  while (!done && iters < kPlocMaxIters) {
+    const uint32_t ntiles = (n + PLOC_BLOCK - 1) / PLOC_BLOCK;
+    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t0 = min(blockIdx.x * per, ntiles), t1 = min(t0 + per, ntiles);
+    // (A) nearest neighbours
+    for (uint32_t tile = t0; tile < t1; tile++)
+      ploc_nn_tile<PLOC_R>(bufs.clo[par], bufs.chi[par], n, tile, nn, s_lo, s_hi, s_seg);
+    if (!grid_sync(bar, err)) break;
+    // (B) survivors and merges per tile
+    uint32_t cs_sum = 0, cm_sum = 0;
+    for (uint32_t tile = t0; tile < t1; tile++) {
+      const uint32_t i = tile * PLOC_BLOCK + threadIdx.x;
+      int surv = 0, merge = 0;
+      if (i < n) {
+        const uint32_t j = nn[i];
+        const bool mutual = (j != i) && nn[j] == i;
+        merge = mutual && i < j;
+        surv = !(mutual && j < i);
+      }
+      const uint32_t cs = (uint32_t)__syncthreads_count(surv);
+      const uint32_t cm = (uint32_t)__syncthreads_count(merge);
+      if (threadIdx.x == 0) {
+        tile_s[tile] = cs;
+        tile_m[tile] = cm;
+      }
+      cs_sum += cs;
+      cm_sum += cm;
+    }
+    if (threadIdx.x == 0) {
+      __stcg(cta_sums + blockIdx.x, cs_sum);
+      __stcg(cta_sums + gridDim.x + blockIdx.x, cm_sum);
+    }
+    if (!grid_sync(bar, err)) break;
+    // (C) this CTA's offsets and the round's totals, then its tiles' outputs
+    uint32_t v[4] = {0u, 0u, 0u, 0u};  // prefix survivors, prefix merges, total survivors, total merges
+    for (uint32_t c = threadIdx.x; c < gridDim.x; c += blockDim.x) {
+      const uint32_t a = __ldcg(cta_sums + c), b = __ldcg(cta_sums + gridDim.x + c);
+      v[2] += a;
+      v[3] += b;
+      if (c < blockIdx.x) {
+        v[0] += a;
+        v[1] += b;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      v[q] = __reduce_add_sync(0xFFFFFFFFu, v[q]);
+      if ((threadIdx.x & 31) == 0) s_red[q][threadIdx.x >> 5] = v[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      uint32_t t = 0;
+      for (int w = 0; w < PLOC_BLOCK / 32; w++) t += s_red[q][w];
+      v[q] = t;
+    }
+    __syncthreads();  // s_red is reused next round
+    uint32_t ps = v[0], pm = v[1];
+    for (uint32_t tile = t0; tile < t1; tile++) {
+      ploc_emit_tile(bufs, par, nn, n, node_next, tile, ps, pm, bnlo, bnhi, bncnt, node_cap, err, dp_cost, dp_choice,
+                     leaf_max, s_w);
+      ps += tile_s[tile];
+      pm += tile_m[tile];
+    }
+    // next round (the k_ploc_advance rules, alike in every CTA)
+    const uint32_t merged = v[3];
+    n = v[2];
+    node_next += merged;
+    rounds += merged > 0 ? 1u : 0u;
+    par ^= 1u;
+    iters++;
+    if (n <= PLOC_SMALL || merged == 0) done = true;
+    if (!grid_sync(bar, err)) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ploc_state[kPlocN] = n;
+    ploc_state[kPlocNext] = node_next;
+    ploc_state[kPlocRounds] = rounds;
+    ploc_state[kPlocTiles] = (n + PLOC_BLOCK - 1) / PLOC_BLOCK;
+    ploc_state[kPlocParity] = par;
+    ploc_state[kPlocDone] = done ? 1u : 0u;
+    ploc_state[kPlocIters] = iters;
+  }
 }
 
 // Finishes clustering of the n <= PLOC_SMALL clusters left by the rounds
@@ -1340,8 +1500,7 @@ __device__ __forceinline__ uint32_t cta_excl_scan_1024(uint32_t v, uint32_t* s_w
 __global__ void __launch_bounds__(1024) k_collapse_roots(const uint32_t* __restrict__ d_root, uint32_t nseg,
                                                          uint32_t nbin, uint32_t* __restrict__ items,
                                                          uint32_t* __restrict__ seg_index,
-                                                         uint32_t* __restrict__ cstate,
-                                                         cudaGraphConditionalHandle loop) {
+                                                         uint32_t* __restrict__ cstate) {
   __shared__ uint32_t s_w[32];
   uint32_t r[4], cnt = 0;
   const uint32_t s0 = threadIdx.x * 4;
@@ -1364,7 +1523,6 @@ __global__ void __launch_bounds__(1024) k_collapse_roots(const uint32_t* __restr
     cstate[kColBase] = 0;
     cstate[kColTri] = 0;
     cstate[kColDepth] = 0;
-    set_loop(loop, total > 0);
   }
 }
 
@@ -1407,11 +1565,10 @@ __global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const ColItem
 // them itself and has no bound: a chain-like binary tree, e.g. thousands of
 // identical triangles, collapses into thousands of levels).
 __global__ void k_collapse_advance(const uint32_t* __restrict__ tot, uint32_t* __restrict__ cstate, uint32_t node_cap,
-                                   uint32_t max_levels, cudaGraphConditionalHandle loop) {
+                                   uint32_t max_levels) {
   if (threadIdx.x != 0) return;
   const uint32_t n = cstate[kColN];
   if (n == 0) {
-    set_loop(loop, false);
     return;
   }
   const uint32_t d = cstate[kColDepth];
@@ -1427,7 +1584,6 @@ __global__ void k_collapse_advance(const uint32_t* __restrict__ tot, uint32_t* _
   }
   cstate[kColN] = next;
   if (next == 0 && d + 1 <= (uint32_t)kColMaxLevels) cstate[kColLevels + d + 1] = base;  // end of the last level
-  set_loop(loop, next > 0);  // max_levels bounds a device-decided loop: next is 0 beyond it
 }
 
 __device__ __forceinline__ uint32_t exp_for(float ext) {
@@ -1826,49 +1982,10 @@ __global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse_emit(
 // ---- all collapse levels in one cooperative launch (captured builds)
 //
 // A grid barrier between the phases of a level replaces the kernel boundaries
-// of the level-by-level form (count, scan, emit, advance: four launches and a
-// conditional graph node per level).  Every CTA keeps the level state in
-// registers and advances it alike; CTA 0 writes it back to cstate at the end.
+// of the level-by-level form (count, scan, emit, advance: four launches per
+// level).  Every CTA keeps the level state in registers and advances it alike;
+// CTA 0 writes it back to cstate at the end.
 
-struct GridBarrier {
-  unsigned int count;
-  unsigned int gen;
-};
-
-// Barrier over all CTAs of a cooperative launch; every thread calls it.  A CTA
-// that waits for more than kLbSpinLimit re-reads (a CTA missing) sets kErrBuild
-// in *err; a CTA that finds *err set does not wait.  Returns false once *err
-// is set, so the grid leaves its loop.
-__device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned int* err) {
-  __shared__ bool s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    bool ok = lb_load(err) == 0u;
-    if (ok) {
-      const unsigned int g = lb_load(&b->gen);
-      __threadfence();
-      if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
-        lb_store(&b->count, 0u);
-        __threadfence();
-        atomicAdd(&b->gen, 1u);
-      } else {
-        uint32_t it = 0;
-        while (lb_load(&b->gen) == g && it < kLbSpinLimit) {
-          __nanosleep(64);
-          it++;
-        }
-        if (it == kLbSpinLimit) {
-          atomicOr(err, kErrBuild);
-          ok = false;
-        }
-      }
-      __threadfence();
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok;
-}
 
 constexpr int COLLAPSE_ALL_THREADS = 256;
 
@@ -2344,7 +2461,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&ploc_state, kPlocStateWords));
   uint32_t* h_tot = nullptr;
   GB_CHECK(arena.host(&h_tot, kPlocStateWords));
-  k_ploc_state_init<<<1, 32, 0, st>>>(acc, ploc_state, 0);
+  k_ploc_state_init<<<1, 32, 0, st>>>(acc, ploc_state);
   note_launches(1);
   const int radius = opt.ploc_radius == 1 || opt.ploc_radius == 2 || opt.ploc_radius == 4 || opt.ploc_radius == 8
                          ? opt.ploc_radius
@@ -2364,7 +2481,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     scan_excl2(bsurv, bmerge, maxb, d_tot + 0, d_tot + 1, scan_sums, st, &acc->pad, ploc_state + kPlocTiles);
     k_ploc_emit<<<grid, PLOC_BLOCK, 0, st>>>(pb, nn, ploc_state, bsurv, bmerge, bnlo, bnhi, bncnt, nnodes_bin,
                                              &acc->pad, dp_cost, d_choice, leaf_max_used);
-    k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state, 0);
+    k_ploc_advance<<<1, 32, 0, st>>>(d_tot, ploc_state);
     note_launches(2);
     round++;
   };
@@ -2443,7 +2560,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&seg_index, nseg));
   GB_CHECK(arena.host(&h_col, kColStateWords));
   GB_CHECK(cudaMemsetAsync(cstate, 0, sizeof(uint32_t) * kColStateWords, st));
-  k_collapse_roots<<<1, 1024, 0, st>>>(d_root, nseg, nnodes_bin, items_a, seg_index, cstate, 0);
+  k_collapse_roots<<<1, 1024, 0, st>>>(d_root, nseg, nnodes_bin, items_a, seg_index, cstate);
   note_launches(1);
   const ColItems citems{{items_a, items_b}};
   uint32_t level = 0;
@@ -2456,7 +2573,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     k_collapse_emit<<<cdiv((uint64_t)nitems_known * (nitems_known <= kGroupEmitMax ? 8 : 1), COLLAPSE_THREADS),
                       COLLAPSE_THREADS, 0, st>>>(
         bt, kids, cstate, nint, ntri, wnodes, leaf_root, citems, d_sah, d_leaves, maxw, N, &acc->pad);
-    k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels, 0);
+    k_collapse_advance<<<1, 32, 0, st>>>(d_tot, cstate, maxw, max_levels);
     note_launches(2);
     level++;
   };
@@ -2597,6 +2714,14 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
         cudaSuccess)
       return e;
     g->col_grid = (uint32_t)std::max(1, std::min(per_sm, 4)) * (uint32_t)num_sms_build();
+    // and the cooperative PLOC rounds (of the chosen search radius)
+    const void* pk = g->radius == 1   ? (const void*)k_ploc_all<1>
+                     : g->radius == 2 ? (const void*)k_ploc_all<2>
+                     : g->radius == 4 ? (const void*)k_ploc_all<4>
+                     : g->radius == 8 ? (const void*)k_ploc_all<8>
+                                      : (const void*)k_ploc_all<PLOC_R_MAX>;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pk, PLOC_BLOCK, 0)) != cudaSuccess) return e;
+    g->ploc_grid = (uint32_t)std::max(1, std::min(per_sm, 8)) * (uint32_t)num_sms_build();
   }
   if ((e = alloc(&g->d_geoms, ngeoms)) || (e = alloc(&g->plo, T)) || (e = alloc(&g->phi, T)) ||
       (e = alloc(&acc, 1)) || (e = alloc(&g->keys_a, T)) || (e = alloc(&g->keys_b, T)) ||
@@ -2615,7 +2740,8 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
       (e = alloc(&g->d_sah, 2)) || (e = alloc(&g->d_leaves, 1)) || (e = alloc(&g->cstate, kColStateWords)) ||
       (e = alloc(&g->seg_index, g->nseg)) || (e = alloc(&g->status, 1)) ||
       (e = alloc(&g->col_sums, 2 * (size_t)g->col_grid)) || (e = alloc(&g->col_bar, 2)) ||
-      (e = alloc(&g->prec, T))) {
+      (e = alloc(&g->prec, T)) || (e = alloc(&g->ploc_sums, 2 * (size_t)g->ploc_grid)) ||
+      (e = alloc(&g->ploc_bar, 2))) {
     graph_build_release(g);
     return e;
   }
@@ -2626,57 +2752,16 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
     e = cudaMemset(g->scan_sums, 0, sizeof(uint32_t) * 2 * scan_scratch(std::max(g->maxb, maxw)));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_os_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsScatterSmem);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->body_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) graph_build_release(g);
   const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return e;
 }
 
-// A new condition handle of the graph being captured on st; its value is 0 at every
-// launch of the graph until a kernel of the graph sets it.
-static cudaError_t loop_handle(cudaStream_t st, cudaGraphConditionalHandle* h) {
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaGraph_t graph = nullptr;
-  GB_CHECK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, nullptr, nullptr, nullptr));
-  if (cs != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureUnsupported;
-  return cudaGraphConditionalHandleCreate(h, graph, 0u, cudaGraphCondAssignDefault);
-}
-
-// Appends to the capture on st a conditional WHILE node on handle h, whose body --
-// enqueued by body(stream) on body_st, captured into the node's own graph -- runs
-// again as long as the condition is non-zero.  The kernels set the condition: one
-// enqueued before the node (whether to run at all), the body's last (whether to
-// run again).
-template <typename F>
-static cudaError_t capture_while(cudaStream_t st, cudaStream_t body_st, cudaGraphConditionalHandle h, F&& body) {
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaGraph_t graph = nullptr;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t ndeps = 0;
-  GB_CHECK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &ndeps));
-  if (cs != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureUnsupported;
-  cudaGraphNodeParams p{};
-  p.type = cudaGraphNodeTypeConditional;
-  p.conditional.handle = h;
-  p.conditional.type = cudaGraphCondTypeWhile;
-  p.conditional.size = 1;
-  cudaGraphNode_t node = nullptr;
-  GB_CHECK(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &p));
-  GB_CHECK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-  GB_CHECK(cudaStreamBeginCaptureToGraph(body_st, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                         cudaStreamCaptureModeThreadLocal));
-  body(body_st);
-  cudaGraph_t out = nullptr;
-  const cudaError_t e1 = cudaGetLastError();
-  const cudaError_t e2 = cudaStreamEndCapture(body_st, &out);
-  return e1 != cudaSuccess ? e1 : e2;
-}
 
 cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   const uint32_t T = g.total, N = g.plan.valid_tris, maxw = g.maxw;
   BoundsAcc* acc = reinterpret_cast<BoundsAcc*>(g.acc);
-  const int fixed_grid = 8 * num_sms_build();
   k_acc_init<<<1, 32, 0, st>>>(acc);
   k_primrefs<<<grid_stride_blocks(T), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc, g.prec,
                                                     g.opt.robust ? 1 : 0);
@@ -2689,7 +2774,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   // the digits the key width can use: 63-bit keys 8, 30-bit keys 4 (6 with the slot)
   const uint32_t digits = g.opt.morton_bits == 30 ? (g.opt.segmented ? 0x3Fu : 0x0Fu) : 0xFFu;
   GB_CHECK(onesweep_sort(ka, va, kb, vb, T, digits, g.hist, &acc->pad, st));
-  // PLOC: rounds in a loop the device ends (a conditional WHILE node), then the
+  // PLOC: the rounds in one cooperative launch that ends them itself, then the
   // one-CTA finish
   GB_CHECK(cudaMemsetAsync(g.d_root, 0xFF, sizeof(uint32_t) * g.nseg, st));
   GB_CHECK(cudaMemsetAsync(g.d_iters, 0, sizeof(uint32_t), st));
@@ -2698,29 +2783,43 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   uint2* dp_choice = g.opt.collapse == 1 ? g.choice : nullptr;
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(g.plo, g.phi, va, N, &acc->nvalid, g.bnlo, g.bnhi, g.bncnt, g.cidx[0],
                                             g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0, dp_cost, dp_choice);
-  cudaGraphConditionalHandle ploc_loop = 0;
-  GB_CHECK(loop_handle(st, &ploc_loop));
-  k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state, ploc_loop);
+  k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state);
   note_launches(2);
-  const uint32_t pgrid = std::min<uint32_t>(g.maxb, (uint32_t)fixed_grid);
   const uint32_t nbin_cap = 2 * N;
   const PlocBufs pb{{g.clo[0], g.clo[1]}, {g.chi[0], g.chi[1]}, {g.cidx[0], g.cidx[1]}};
-  GB_CHECK(capture_while(st, g.body_stream, ploc_loop, [&](cudaStream_t bs) {
+  // the rounds above PLOC_SMALL clusters in one cooperative launch, then the one-CTA finish
+  GB_CHECK(cudaMemsetAsync(g.ploc_bar, 0, sizeof(GridBarrier), st));
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.ploc_grid);
+    cfg.blockDim = dim3(PLOC_BLOCK);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(g.ploc_bar);
     switch (g.radius) {
-      case 1: k_ploc_nn<1><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
-      case 2: k_ploc_nn<2><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
-      case 4: k_ploc_nn<4><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
-      case 8: k_ploc_nn<8><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
-      default: k_ploc_nn<PLOC_R_MAX><<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.ploc_state, g.nn); break;
+      case 1: GB_CHECK(cudaLaunchKernelEx(&cfg, k_ploc_all<1>, pb, g.ploc_state, g.nn, g.bsurv, g.bmerge, g.ploc_sums,
+                                          g.bnlo, g.bnhi, g.bncnt, nbin_cap, dp_cost, dp_choice, leaf_max, bar,
+                                          &acc->pad)); break;
+      case 2: GB_CHECK(cudaLaunchKernelEx(&cfg, k_ploc_all<2>, pb, g.ploc_state, g.nn, g.bsurv, g.bmerge, g.ploc_sums,
+                                          g.bnlo, g.bnhi, g.bncnt, nbin_cap, dp_cost, dp_choice, leaf_max, bar,
+                                          &acc->pad)); break;
+      case 4: GB_CHECK(cudaLaunchKernelEx(&cfg, k_ploc_all<4>, pb, g.ploc_state, g.nn, g.bsurv, g.bmerge, g.ploc_sums,
+                                          g.bnlo, g.bnhi, g.bncnt, nbin_cap, dp_cost, dp_choice, leaf_max, bar,
+                                          &acc->pad)); break;
+      case 8: GB_CHECK(cudaLaunchKernelEx(&cfg, k_ploc_all<8>, pb, g.ploc_state, g.nn, g.bsurv, g.bmerge, g.ploc_sums,
+                                          g.bnlo, g.bnhi, g.bncnt, nbin_cap, dp_cost, dp_choice, leaf_max, bar,
+                                          &acc->pad)); break;
+      default: GB_CHECK(cudaLaunchKernelEx(&cfg, k_ploc_all<PLOC_R_MAX>, pb, g.ploc_state, g.nn, g.bsurv, g.bmerge,
+                                           g.ploc_sums, g.bnlo, g.bnhi, g.bncnt, nbin_cap, dp_cost, dp_choice,
+                                           leaf_max, bar, &acc->pad)); break;
     }
-    k_ploc_count<<<pgrid, PLOC_BLOCK, 0, bs>>>(g.nn, g.ploc_state, g.bsurv, g.bmerge);
-    scan_excl2(g.bsurv, g.bmerge, g.maxb, g.d_tot + 0, g.d_tot + 1, g.scan_sums, bs, &acc->pad,
-               g.ploc_state + kPlocTiles);
-    k_ploc_emit<<<pgrid, PLOC_BLOCK, 0, bs>>>(pb, g.nn, g.ploc_state, g.bsurv, g.bmerge, g.bnlo, g.bnhi, g.bncnt,
-                                              nbin_cap, &acc->pad, dp_cost, dp_choice, leaf_max);
-    k_ploc_advance<<<1, 32, 0, bs>>>(g.d_tot, g.ploc_state, ploc_loop);
-    note_launches(4);
-  }));
+    note_launches(2);
+  }
   {
     const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(g.clo[0], g.chi[0], g.cidx[0], g.clo[1], g.chi[1], g.cidx[1],
@@ -2737,7 +2836,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   GB_CHECK(cudaMemsetAsync(g.cstate, 0, sizeof(uint32_t) * kColStateWords, st));
   // collapse levels in a loop the device ends
   // all collapse levels in one cooperative launch
-  k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate, 0);
+  k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate);
   GB_CHECK(cudaMemsetAsync(g.col_bar, 0, sizeof(GridBarrier), st));
   {
     const ColItems ci{{g.items[0], g.items[1]}};
@@ -2797,7 +2896,6 @@ cudaError_t graph_build_result(const GraphBuild& g, const float scene_lo[3], con
 
 void graph_build_release(GraphBuild* g) {
   for (void* p : g->allocs) cudaFree(p);
-  if (g->body_stream) cudaStreamDestroy(g->body_stream);
   *g = GraphBuild{};
 }
 

@@ -78,7 +78,8 @@ struct GraphBuild {
   uint32_t col_grid = 0;                                // CTAs of the cooperative collapse
   uint32_t *col_sums = nullptr, *col_bar = nullptr;     // its per-CTA sums and grid barrier
   TriRecord* prec = nullptr;                            // leaf records in primitive order
-  cudaStream_t body_stream = nullptr;  // captures the bodies of the device-decided build loops
+  uint32_t ploc_grid = 0;                               // CTAs of the cooperative PLOC rounds
+  uint32_t *ploc_sums = nullptr, *ploc_bar = nullptr;   // their per-CTA sums and grid barrier
 };
 struct GraphBuildResult {
   uint32_t status = 0;  // 0: the build is complete and consistent; else kGraphBuild* bits
