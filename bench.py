@@ -889,6 +889,15 @@ def run_gpu(args, rank, world):
     bst = sc.build_stats()
     build_ms = statistics.median(b[1] for b in builds)
     build_wall_ms = statistics.median(b[0] for b in builds) * 1e3
+    # where the replayed build's time goes: the same build on a device that stamps its phases
+    pdev = api.Device(f"gpu.device={local},gpu.build_phases=1{',' + args.config if args.config else ''}".encode())
+    psc = api.Scene(pdev, flags=api.RTC_SCENE_FLAG_ROBUST if args.robust else 0)
+    psc.add_mesh(verts, idx)
+    for _ in range(4):
+        psc.commit()
+    build_phases = psc.build_phases()
+    psc.release()
+    pdev.release()
 
     pristine = torch.from_numpy(rays.view(np.uint8)).cuda()
     work = torch.empty_like(pristine)
@@ -1008,7 +1017,10 @@ def run_gpu(args, rank, world):
                       "Mtris_per_s": bst["num_prims"] / (build_ms * 1e-3) / 1e6, "sah": bst["sah"],
                       "sah_exact_boxes": bst["sah_exact"], "leaf_max": bst["leaf_max"],
                       "nodes": bst["num_nodes"], "depth": bst["depth"], "ploc_iterations": bst["ploc_iterations"],
-                      "bvh_MB": bst["bvh_bytes"] / 1e6},
+                      "bvh_MB": bst["bvh_bytes"] / 1e6,
+                      "phases_us": build_phases or None,
+                      "phases_source": "rtcgbGetSceneBuildPhases on a second device with gpu.build_phases=1 "
+                                       "(device timestamps between the phases of the replayed build)"},
             "autotune": tuning,
             "learned": None, "animated": None, "batched": None, "heightfield": None,
         }

@@ -2676,6 +2676,14 @@ __global__ void k_graph_build_check(const BoundsAcc* __restrict__ acc, const uin
   *status = s;
 }
 
+// Device time (globaltimer, ns) into stamps[k]: one thread, enqueued between the
+// phases of a captured build when BuildOptions::phase_stamps is set.
+__global__ void k_phase_stamp(unsigned long long* stamps, int k) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  stamps[k] = t;
+}
+
 cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const BuildOptions& opt,
                                 const GraphBuildPlan& plan, GraphBuild* g) {
   *g = GraphBuild{};
@@ -2741,7 +2749,7 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
       (e = alloc(&g->seg_index, g->nseg)) || (e = alloc(&g->status, 1)) ||
       (e = alloc(&g->col_sums, 2 * (size_t)g->col_grid)) || (e = alloc(&g->col_bar, 2)) ||
       (e = alloc(&g->prec, T)) || (e = alloc(&g->ploc_sums, 2 * (size_t)g->ploc_grid)) ||
-      (e = alloc(&g->ploc_bar, 2))) {
+      (e = alloc(&g->ploc_bar, 2)) || (opt.phase_stamps && (e = alloc(&g->stamps, kBuildPhases + 1)))) {
     graph_build_release(g);
     return e;
   }
@@ -2762,18 +2770,24 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
 cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   const uint32_t T = g.total, N = g.plan.valid_tris, maxw = g.maxw;
   BoundsAcc* acc = reinterpret_cast<BoundsAcc*>(g.acc);
+  auto stamp = [&](int k) {
+    if (g.stamps) k_phase_stamp<<<1, 1, 0, st>>>(g.stamps, k);
+  };
+  stamp(0);
   k_acc_init<<<1, 32, 0, st>>>(acc);
   k_primrefs<<<grid_stride_blocks(T), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc, g.prec,
                                                     g.opt.robust ? 1 : 0);
   k_morton<<<grid_stride_blocks(T), 256, 0, st>>>(g.plo, g.phi, T, acc, g.keys_a, g.vals_a, g.opt.morton_cube,
                                          g.opt.segmented ? 1 : 0, g.opt.morton_bits == 30 ? 1 : 0);
   note_launches(3);
+  stamp(1);
   // all digits of the key width (the ordinary build skips constant ones: the same order)
   uint64_t *ka = g.keys_a, *kb = g.keys_b;
   uint32_t *va = g.vals_a, *vb = g.vals_b;
   // the digits the key width can use: 63-bit keys 8, 30-bit keys 4 (6 with the slot)
   const uint32_t digits = g.opt.morton_bits == 30 ? (g.opt.segmented ? 0x3Fu : 0x0Fu) : 0xFFu;
   GB_CHECK(onesweep_sort(ka, va, kb, vb, T, digits, g.hist, &acc->pad, st));
+  stamp(2);
   // PLOC: the rounds in one cooperative launch that ends them itself, then the
   // one-CTA finish
   GB_CHECK(cudaMemsetAsync(g.d_root, 0xFF, sizeof(uint32_t) * g.nseg, st));
@@ -2783,6 +2797,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   uint2* dp_choice = g.opt.collapse == 1 ? g.choice : nullptr;
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(g.plo, g.phi, va, N, &acc->nvalid, g.bnlo, g.bnhi, g.bncnt, g.cidx[0],
                                             g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0, dp_cost, dp_choice);
+  stamp(3);
   k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state);
   note_launches(2);
   const uint32_t nbin_cap = 2 * N;
@@ -2820,6 +2835,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
     }
     note_launches(2);
   }
+  stamp(4);
   {
     const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(g.clo[0], g.chi[0], g.cidx[0], g.clo[1], g.chi[1], g.cidx[1],
@@ -2828,6 +2844,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
                                                       leaf_max);
     note_launches(1);
   }
+  stamp(5);
   // collapse decisions and levels
   BinTree bt{g.bnlo, g.bnhi, g.bncnt, N, leaf_max, (uint32_t)(g.opt.robust != 0), dp_choice};
   GB_CHECK(cudaMemsetAsync(g.leaf_root, 0xFF, sizeof(uint32_t) * N, st));
@@ -2835,6 +2852,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   GB_CHECK(cudaMemsetAsync(g.d_leaves, 0, sizeof(uint32_t), st));
   GB_CHECK(cudaMemsetAsync(g.cstate, 0, sizeof(uint32_t) * kColStateWords, st));
   // collapse levels in a loop the device ends
+  stamp(6);
   // all collapse levels in one cooperative launch
   k_collapse_roots<<<1, 1024, 0, st>>>(g.d_root, g.nseg, g.nbin, g.items[0], g.seg_index, g.cstate);
   GB_CHECK(cudaMemsetAsync(g.col_bar, 0, sizeof(GridBarrier), st));
@@ -2855,8 +2873,10 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
                                 reinterpret_cast<GridBarrier*>(g.col_bar), &acc->pad));
   }
   note_launches(2);
+  stamp(7);
   k_write_leaves<<<cdiv(N, 256), 256, 0, st>>>(bt, g.d_geoms, g.plo, g.phi, g.leaf_root, N, g.tris, &acc->pad,
                                                 g.prec);
+  stamp(8);
   k_graph_build_check<<<1, 32, 0, st>>>(acc, g.ploc_state, g.cstate, N, g.status);
   note_launches(2);
   return cudaGetLastError();
@@ -2877,7 +2897,13 @@ cudaError_t graph_build_result(const GraphBuild& g, const float scene_lo[3], con
   out->roots.assign(g.nseg, kInvalidID);
   if (g.opt.segmented)
     GB_CHECK(cudaMemcpyAsync(out->roots.data(), g.seg_index, sizeof(uint32_t) * g.nseg, cudaMemcpyDeviceToHost, st));
+  unsigned long long ts[kBuildPhases + 1] = {};
+  if (g.stamps) GB_CHECK(cudaMemcpyAsync(ts, g.stamps, sizeof(ts), cudaMemcpyDeviceToHost, st));
   GB_CHECK(cudaStreamSynchronize(st));
+  if (g.stamps) {
+    out->nphases = kBuildPhases;
+    for (int k = 0; k < kBuildPhases; k++) out->phase_us[k] = (double)(ts[k + 1] - ts[k]) * 1e-3;
+  }
   out->num_nodes = col[kColBase];
   out->depth = std::min<uint32_t>(col[kColDepth], (uint32_t)kColMaxLevels);
   out->level_start.assign(col.begin() + kColLevels, col.begin() + kColLevels + out->depth + 1);
@@ -2969,6 +2995,8 @@ cudaError_t cached_build_run(CachedBuild* c, const GeomDesc* h_geoms, int ngeoms
   stats->num_prims = N;
   stats->depth = r.depth;
   stats->ploc_iterations = r.ploc_rounds;
+  stats->nphases = r.nphases;
+  for (int k = 0; k < kBuildPhases; k++) stats->phase_us[k] = r.phase_us[k];
   return cudaSuccess;
 }
 

@@ -78,6 +78,7 @@ struct GraphBuild {
   uint32_t col_grid = 0;                                // CTAs of the cooperative collapse
   uint32_t *col_sums = nullptr, *col_bar = nullptr;     // its per-CTA sums and grid barrier
   TriRecord* prec = nullptr;                            // leaf records in primitive order
+  unsigned long long* stamps = nullptr;                 // phase timestamps (BuildOptions::phase_stamps)
   uint32_t ploc_grid = 0;                               // CTAs of the cooperative PLOC rounds
   uint32_t *ploc_sums = nullptr, *ploc_bar = nullptr;   // their per-CTA sums and grid barrier
 };
@@ -89,6 +90,8 @@ struct GraphBuildResult {
   std::vector<uint32_t> level_start;
   float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // geometry bounds of the replayed build
   std::vector<uint32_t> roots;  // segmented builds: root node of each geometry slot (kInvalidID: empty)
+  uint32_t nphases = 0;         // phase times (gpu.build_phases=1)
+  double phase_us[kBuildPhases] = {};
 };
 enum : uint32_t { kGraphBuildCount = 1, kGraphBuildRounds = 2, kGraphBuildLevels = 4, kGraphBuildError = 8 };
 cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const BuildOptions& opt,

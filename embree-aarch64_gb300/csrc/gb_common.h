@@ -128,6 +128,9 @@ struct BuildOptions {
   // 3.13 ms against 3.51 (4 radix passes instead of 8) with the same SAH within
   // 0.02 % and the same trace time on the soup and the heightfields.
   int morton_bits = 30;
+  // gpu.build_phases=1: the captured (replayed) build records a device timestamp
+  // between its phases (kBuildPhases intervals, BuildStats::phase_us)
+  int phase_stamps = 0;
 };
 
 // Build statistics reported through the extension API.
@@ -140,7 +143,11 @@ struct BuildStats {
   uint32_t ploc_iterations = 0;
   uint32_t ploc_rounds = 0;  // PLOC rounds over all clusters (before the one-CTA finish) that merged
   uint32_t refit = 0;        // 1 when the last commit refitted instead of rebuilding
+  uint32_t nphases = 0;      // phases timed (replayed builds with gpu.build_phases=1), else 0
+  double phase_us[8] = {};   // primitives + keys, sort, PLOC set-up, PLOC rounds, PLOC finish,
+                             // collapse set-up, collapse levels, leaf records
 };
+constexpr int kBuildPhases = 8;
 
 // Traversal work counters (counting variant of the kernels).
 struct TraceCounters {

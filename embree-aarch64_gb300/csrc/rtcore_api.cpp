@@ -121,7 +121,7 @@ struct Device : RefCounted {
 
   // Config string: comma separated key=value tokens (kernels/common/state.cpp:217-450).
   // Honoured: verbose, benchmark, gpu.device, gpu.leaf_max, gpu.morton, gpu.morton_bits, gpu.collapse, gpu.ploc_radius,
-  // gpu.host_rays, gpu.proposer, gpu.reorder, gpu.graph_rebuild, gpu.trace_shape;
+  // gpu.host_rays, gpu.proposer, gpu.reorder, gpu.graph_rebuild, gpu.build_phases, gpu.trace_shape;
   // the CPU tasking and ISA keys
   // (threads, isa, max_isa, set_affinity, ...) are accepted and ignored.
   void parse(const char* cfg) {
@@ -147,6 +147,7 @@ struct Device : RefCounted {
         else if (k == "gpu.ploc_radius") build_opt.ploc_radius = atoi(v.c_str());
         else if (k == "gpu.morton_bits") build_opt.morton_bits = atoi(v.c_str()) == 63 ? 63 : 30;
         else if (k == "gpu.graph_rebuild") graph_rebuild = atoi(v.c_str()) != 0;
+        else if (k == "gpu.build_phases") build_opt.phase_stamps = atoi(v.c_str()) != 0;
         else if (k == "gpu.host_rays") host_mode = v == "copy" ? 0 : v == "direct" ? 2 : 1;
         else if (k == "gpu.proposer") proposer_mma = (v == "mma");
         else if (k == "gpu.reorder") reorder = atoi(v.c_str());
@@ -722,7 +723,7 @@ struct Scene : RefCounted {
     // and strides are read from the geometry table at run time)
     std::vector<uint64_t> key = {(uint64_t)opt.robust, (uint64_t)opt.segmented, (uint64_t)opt.refit_target,
                                  (uint64_t)opt.leaf_max, (uint64_t)opt.morton_cube, (uint64_t)opt.morton_bits,
-                                 (uint64_t)opt.collapse, (uint64_t)opt.ploc_radius};
+                                 (uint64_t)opt.collapse, (uint64_t)opt.ploc_radius, (uint64_t)opt.phase_stamps};
     for (const gb::GeomDesc& d : descs)
       key.insert(key.end(), {(uint64_t)d.geomID, (uint64_t)d.ntris, (uint64_t)d.nverts, (uint64_t)d.kind});
     const bool cacheable = device->graph_rebuild && iboxes.empty() && !descs.empty();
@@ -2038,6 +2039,18 @@ RTC_API void rtcgbGetSceneBuildStats(RTCScene hs, RTCGBBuildStats* out) {
   out->bvh_bytes = (unsigned long long)s->bvh.num_nodes * sizeof(gb::WideNode) +
                    (unsigned long long)s->bvh.num_tris * sizeof(gb::TriRecord);
   API_END(s ? s->device : nullptr)
+}
+
+RTC_API unsigned int rtcgbGetSceneBuildPhases(RTCScene hs, double* us, unsigned int max_phases) {
+  Scene* s = (Scene*)hs;
+  API_BEGIN
+  VERIFY_HANDLE(hs);
+  if (!s->committed) fail(RTC_ERROR_INVALID_OPERATION, "scene not committed");
+  const unsigned n = s->stats.nphases;
+  for (unsigned k = 0; us && k < n && k < max_phases; k++) us[k] = s->stats.phase_us[k];
+  return n;
+  API_END(s ? s->device : nullptr)
+  return 0;
 }
 
 RTC_API void rtcgbGetLastQueryStats(RTCGBQueryStats* out) {

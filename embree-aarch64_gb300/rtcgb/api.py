@@ -42,7 +42,7 @@ rtcRetainScene rtcReleaseScene rtcAttachGeometry rtcAttachGeometryByID rtcDetach
 rtcCommitScene rtcJoinCommitScene rtcSetSceneProgressMonitorFunction rtcSetSceneBuildQuality rtcSetSceneFlags
 rtcGetSceneFlags rtcGetSceneBounds rtcGetSceneLinearBounds rtcIntersect1 rtcIntersect1M rtcIntersect1Mp
 rtcOccluded1 rtcOccluded1M rtcOccluded1Mp rtcIntersect4 rtcIntersect8 rtcIntersect16 rtcIntersectNM
-rtcIntersectNp rtcOccluded4 rtcOccluded8 rtcOccluded16 rtcOccludedNM rtcOccludedNp rtcgbGetSceneBuildStats rtcgbGetLastQueryStats rtcgbSetQueryCounting
+rtcIntersectNp rtcOccluded4 rtcOccluded8 rtcOccluded16 rtcOccludedNM rtcOccludedNp rtcgbGetSceneBuildStats rtcgbGetSceneBuildPhases rtcgbGetLastQueryStats rtcgbSetQueryCounting
 rtcgbGetKernelLaunchCount rtcgbSetThreadStream rtcgbGetSceneBVH rtcgbRadixSortPairs rtcgbIntersect1MNoAlloc rtcgbGetDeviceHostAccess
 rtcgbGetTraversalShapes rtcgbSetSceneTraversalShape rtcgbGetSceneTraversalShape rtcgbTuneSceneTraversal
 rtcgbNewProposer rtcgbNewProposerEx rtcgbRetainProposer rtcgbReleaseProposer rtcgbProposerTrain rtcgbProposerPredict rtcgbProposerGetStats
@@ -186,6 +186,7 @@ def load(build=True):
         "rtcIntersectNp": (None, [vp, vp, vp, u]), "rtcOccludedNp": (None, [vp, vp, vp, u]),
         "rtcgbGetSceneBuildStats": (None, [vp, ctypes.POINTER(RTCGBBuildStats)]),
         "rtcgbGetLastQueryStats": (None, [ctypes.POINTER(RTCGBQueryStats)]),
+        "rtcgbGetSceneBuildPhases": (u, [vp, ctypes.POINTER(ctypes.c_double), u]),
         "rtcgbSetQueryCounting": (None, [i]),
         "rtcgbGetKernelLaunchCount": (ctypes.c_ulonglong, []),
         "rtcgbSetThreadStream": (None, [vp]),
@@ -373,6 +374,17 @@ class Scene:
         self.L.rtcGetSceneBounds(self.h, ctypes.byref(b))
         self.dev.check("rtcGetSceneBounds")
         return np.array([b.lower_x, b.lower_y, b.lower_z]), np.array([b.upper_x, b.upper_y, b.upper_z])
+
+    BUILD_PHASES = ("primitives_and_keys", "sort", "ploc_setup", "ploc_rounds", "ploc_finish", "collapse_setup",
+                    "collapse_levels", "leaf_records")
+
+    def build_phases(self):
+        """Device microseconds of each phase of the last (replayed) build, as a dict;
+        empty unless the device has gpu.build_phases=1 and the commit was replayed."""
+        us = (ctypes.c_double * 8)()
+        n = self.L.rtcgbGetSceneBuildPhases(self.h, us, 8)
+        self.dev.check("rtcgbGetSceneBuildPhases")
+        return {k: us[i] for i, k in enumerate(self.BUILD_PHASES[:n])}
 
     def build_stats(self):
         s = RTCGBBuildStats()

@@ -42,6 +42,17 @@ typedef struct RTCGBQueryStats {
 /* Statistics of the scene's last commit. */
 RTC_API void rtcgbGetSceneBuildStats(RTCScene scene, RTCGBBuildStats* out);
 
+/* Device time of each phase of the scene's last commit, in microseconds, when
+   that commit was a replayed rebuild (rtcCommitScene of a scene whose layout is
+   unchanged since its previous commit) on a device created with the config key
+   gpu.build_phases=1; returns the number of phases (8) and writes up to
+   max_phases of them, else returns 0.  Phases: primitive references and leaf
+   records + sort keys; radix sort; PLOC set-up; PLOC rounds; PLOC finish (one
+   CTA); collapse set-up; collapse levels; leaf triangle records.  The device
+   timestamps are taken by one-thread kernels between the phases, which add a
+   few microseconds to the build. */
+RTC_API unsigned int rtcgbGetSceneBuildPhases(RTCScene scene, double* us, unsigned int max_phases);
+
 /* Statistics of the calling thread's last rtcIntersect* / rtcOccluded* call. */
 RTC_API void rtcgbGetLastQueryStats(RTCGBQueryStats* out);
 

@@ -243,3 +243,29 @@ def test_replayed_rebuild_falls_back_when_valid_count_changes(rtc, oracle):
     assert_clean(compare_closest(orc, rays, g, r))
     sc.release()
     device.release()
+
+
+def test_build_phase_timestamps(rtc):
+    """gpu.build_phases=1: a replayed rebuild reports the device time of its eight
+    phases (rtcgbGetSceneBuildPhases), which add up to about the build's own time,
+    and the tree is the one built without the timestamps."""
+    meshes = [W.gaussian_soup(80_000, seed=14)]
+    dp, sp = _committed(rtc, b"gpu.build_phases=1", meshes, False)
+    dq, sq = _committed(rtc, b"", meshes, False)
+    sp.commit()
+    sq.commit()
+    assert sp.build_phases() == {}  # the first commit is host-driven
+    for _ in range(3):
+        sp.commit()
+        sq.commit()
+    ph = sp.build_phases()
+    assert list(ph) == list(rtc.Scene.BUILD_PHASES)
+    assert all(v >= 0.0 for v in ph.values()) and ph["ploc_rounds"] > 0 and ph["collapse_levels"] > 0
+    total_ms = sum(ph.values()) * 1e-3
+    assert total_ms <= sp.build_stats()["build_ms"] * 1.05 + 0.05
+    n1, t1 = sp.bvh()
+    n2, t2 = sq.bvh()
+    assert np.array_equal(n1, n2) and np.array_equal(t1.view(np.uint32), t2.view(np.uint32))
+    for s, d in ((sp, dp), (sq, dq)):
+        s.release()
+        d.release()
