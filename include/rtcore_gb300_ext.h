@@ -287,9 +287,9 @@ RTC_API void rtcgbOccluded1MBatched(RTCScene scene, struct RTCRay* ray, unsigned
    batched closest-hit query over device-resident rays, captured once into one
    CUDA graph and replayed with one launch (optionally preceded by a copy of
    `pristine` over `rayhit`, both device memory).  The captured build runs with
-   no host reads: its PLOC rounds and its collapse levels are the bodies of two
-   conditional WHILE graph nodes whose conditions the build's own kernels set,
-   so the device runs exactly as many rounds and levels as the data needs; a
+   no host reads: its PLOC rounds and its collapse levels are two cooperative
+   launches that end them themselves, so the device runs exactly as many
+   rounds and levels as the data needs; a
    replay whose build fails (more than 1024 PLOC rounds, more than 64 levels, a
    different number of valid triangles) reports RTC_ERROR_UNKNOWN.  The scene's
    geometry IDs must be 0..n-1; a new
