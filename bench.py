@@ -787,8 +787,9 @@ def run_batched(api, dev_config, torch, scale, steps, warmup, cpu_seconds):
     # bitwise: the records' integer fields (e.g. instID = 0xFFFFFFFF) are NaN as floats
     same = bool(torch.equal(work.view(torch.int32), separate.view(torch.int32)))
     del separate
-    out["graph"] = {"frame": "ray restore copy + rebuild of all BVHs (PLOC rounds and collapse levels in conditional "
-                             "WHILE nodes the device ends) + batched closest-hit query, one CUDA graph launch",
+    out["graph"] = {"frame": "ray restore copy + rebuild of all BVHs (PLOC rounds and collapse levels in two "
+                             "cooperative launches that end them on the device) + batched closest-hit query, "
+                             "one CUDA graph launch",
                     "ms_per_step": float(statistics.median(fms)),
                     "Mrays_per_s": nrays / (statistics.median(fms) * 1e-3) / 1e6,
                     "restore_copy_ms": float(statistics.median(copy_ms)),
