@@ -230,14 +230,17 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
 // bits30 (gpu.morton_bits=30): 10 bits per axis, the lattice of the reference's
 // Morton builder (kernels/builders/bvh_builder_morton.h:62-86, LATTICE_BITS_PER_DIM
 // 10), so valid keys fit in 30 bits (42 with the slot) and the sort needs 4 (6)
-// digit passes instead of 8; invalid primitives get the all-ones key of that width.
+// digit passes instead of 8; invalid primitives get bit 30 (42) set, above every
+// valid key, so they sort after all valid ones.  key32: the 30-bit keys of an
+// unsegmented build are written as 32-bit words (the sort then moves 4-byte keys).
 constexpr uint32_t kMaxSegments = 4096;
 
 // Grid-stride; the AND / OR of all keys (constant digits are not sorted) is
 // reduced per thread, per warp and per CTA: two global atomics per CTA.
 __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                 uint32_t n, BoundsAcc* acc, uint64_t* __restrict__ keys,
-                                                uint32_t* __restrict__ vals, int cube, int segmented, int bits30) {
+                                                uint32_t* __restrict__ vals, int cube, int segmented, int bits30,
+                                                int key32) {
   __shared__ unsigned long long s_and, s_or;
   if (threadIdx.x == 0) {
     s_and = ~0ull;
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
   __syncthreads();
   unsigned long long ka = ~0ull, ko = 0ull;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint64_t key = bits30 ? (~0ull >> (segmented ? 22 : 34)) : ~0ull;
+    uint64_t key = bits30 ? (1ull << (segmented ? 42 : 30)) : ~0ull;
     {
       const float4 a = plo[i], b = phi[i];
       if (a.x <= b.x) {
@@ -283,7 +286,8 @@ __global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ plo, 
           key = segmented ? ((uint64_t)(__float_as_uint(a.w) & (kMaxSegments - 1)) << 51) | (code >> 12) : code;
         }
       }
-      keys[i] = key;
+      if (key32) reinterpret_cast<uint32_t*>(keys)[i] = (uint32_t)key;
+      else keys[i] = key;
       vals[i] = i;
     }
     ka &= key;
@@ -384,8 +388,9 @@ __device__ __forceinline__ uint32_t lb_exclusive(const uint32_t* status, uint32_
 }
 
 // Counts of every active digit (digit_mask bit d: digit d, bits 8d..8d+7) over all
-// keys; the last CTA writes each digit's exclusive bucket bases.
-__global__ void __launch_bounds__(256) k_os_hist(const uint64_t* __restrict__ keys, uint32_t n, uint32_t digit_mask,
+// keys (K: 32- or 64-bit); the last CTA writes each digit's exclusive bucket bases.
+template <typename K>
+__global__ void __launch_bounds__(256) k_os_hist(const K* __restrict__ keys, uint32_t n, uint32_t digit_mask,
                                                  uint32_t* __restrict__ scratch) {
   __shared__ uint32_t s_h[8][256];
   __shared__ bool s_last;
@@ -394,9 +399,9 @@ __global__ void __launch_bounds__(256) k_os_hist(const uint64_t* __restrict__ ke
   for (int d = 0; d < 8; d++) s_h[d][tid] = 0;
   __syncthreads();
   for (uint32_t i = blockIdx.x * 256u + tid; i < n; i += gridDim.x * 256u) {
-    const uint64_t k = keys[i];
+    const K k = keys[i];
 #pragma unroll
-    for (int d = 0; d < 8; d++)
+    for (int d = 0; d < (int)sizeof(K); d++)
       if (digit_mask >> d & 1u) atomicAdd(&s_h[d][(uint32_t)(k >> (8 * d)) & 0xFFu], 1u);
   }
   __syncthreads();
@@ -437,15 +442,18 @@ __global__ void __launch_bounds__(256) k_os_hist(const uint64_t* __restrict__ ke
 // the keys are placed in shared memory in (digit, original order) order and written
 // out in runs, consecutive threads to consecutive positions of a digit's bucket.
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr size_t kOsScatterSmem = (size_t)RS_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
+template <typename K>
+constexpr size_t os_scatter_smem() { return (size_t)RS_TILE * (sizeof(K) + sizeof(uint32_t)); }
 
-__global__ void __launch_bounds__(RS_THREADS) k_os_scatter(const uint64_t* __restrict__ kin,
+template <typename K>
+__global__ void __launch_bounds__(RS_THREADS) k_os_scatter(const K* __restrict__ kin,
                                                            const uint32_t* __restrict__ vin,
-                                                           uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           K* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, uint32_t* __restrict__ scratch,
                                                            uint32_t pass_slot, uint32_t* __restrict__ status,
                                                            unsigned int* __restrict__ err) {
-  extern __shared__ uint64_t s_keys[];                                   // RS_TILE keys, then RS_TILE values
+  extern __shared__ __align__(16) unsigned char s_stage[];               // RS_TILE keys, then RS_TILE values
+  K* s_keys = reinterpret_cast<K*>(s_stage);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + RS_TILE);
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_wcnt[RS_WARPS][256];  // per-warp digit counts, then per-warp offsets
@@ -462,14 +470,14 @@ __global__ void __launch_bounds__(RS_THREADS) k_os_scatter(const uint64_t* __res
   const uint32_t tile_n = min((uint32_t)RS_TILE, n - base);
   const uint32_t lt = (1u << lane) - 1u;
   // ---- per-warp ranking (warp-synchronous: each warp owns its row of s_wcnt)
-  uint64_t k[RS_ITEMS];
+  K k[RS_ITEMS];
   uint32_t pos[RS_ITEMS];
   const uint32_t wbase = base + (uint32_t)warp * (RS_ITEMS * 32);
 #pragma unroll
   for (int r = 0; r < RS_ITEMS; r++) {
     const uint32_t i = wbase + r * 32 + lane;
     const bool in = i < n;
-    k[r] = in ? kin[i] : 0ull;
+    k[r] = in ? kin[i] : (K)0;
     const uint32_t d = in ? (uint32_t)(k[r] >> shift) & 0xFFu : 256u;
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
     const uint32_t rank = __popc(peers & lt);
@@ -527,7 +535,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_os_scatter(const uint64_t* __res
   __syncthreads();
   // ---- runs out: local index j of digit d goes to s_glob[d] + j
   for (uint32_t j = tid; j < tile_n; j += RS_THREADS) {
-    const uint64_t key = s_keys[j];
+    const K key = s_keys[j];
     const uint32_t out = s_glob[(uint32_t)(key >> shift) & 0xFFu] + j;
     if (out < n) {
       kout[out] = key;
@@ -2248,27 +2256,30 @@ static inline size_t onesweep_scratch_words(uint32_t n, int passes) {
 // (ka, va) name the buffers that hold the result.  scratch: at least
 // onesweep_scratch_words(n, passes) words, zeroed here.  A look-back that gives up
 // sets kErrBuild in *err (or in the scratch's error word when err is null).
-static cudaError_t onesweep_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& vb, uint32_t n,
-                                 uint32_t digit_mask, uint32_t* scratch, unsigned int* err, cudaStream_t st) {
-  const int passes = __builtin_popcount(digit_mask & 0xFFu);
+template <typename K>
+static cudaError_t onesweep_sort(K*& ka, uint32_t*& va, K*& kb, uint32_t*& vb, uint32_t n, uint32_t digit_mask,
+                                 uint32_t* scratch, unsigned int* err, cudaStream_t st) {
+  digit_mask &= (1u << sizeof(K)) - 1u;
+  const int passes = __builtin_popcount(digit_mask);
   if (n == 0 || passes == 0) return cudaSuccess;
   if (n >= kLbValue) return cudaErrorInvalidValue;  // look-back counts are 30-bit
   const uint32_t ntiles = cdiv(n, RS_TILE);
   GB_CHECK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * onesweep_scratch_words(n, passes), st));
   const uint32_t hgrid = std::min<uint32_t>(ntiles, 4u * (uint32_t)num_sms_build());
-  // 48 KB of staged keys and values beyond the static shared memory (per device; a
-  // captured build sets it in graph_build_prepare)
+  // 32 or 48 KB of staged keys and values beyond the static shared memory (per
+  // device; a captured build sets it in graph_build_prepare)
+  constexpr size_t smem = os_scatter_smem<K>();
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   GB_CHECK(cudaStreamIsCapturing(st, &cap));
   if (cap == cudaStreamCaptureStatusNone)
-    GB_CHECK(cudaFuncSetAttribute(k_os_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsScatterSmem));
-  k_os_hist<<<hgrid, 256, 0, st>>>(ka, n, digit_mask & 0xFFu, scratch);
+    GB_CHECK(cudaFuncSetAttribute(k_os_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_os_hist<K><<<hgrid, 256, 0, st>>>(ka, n, digit_mask & ((1u << sizeof(K)) - 1u), scratch);
   uint32_t slot = 0;
-  for (int d = 0; d < 8; d++) {
+  for (int d = 0; d < (int)sizeof(K); d++) {
     if (!(digit_mask >> d & 1u)) continue;
-    k_os_scatter<<<ntiles, RS_THREADS, kOsScatterSmem, st>>>(ka, va, kb, vb, n, 8 * d, scratch, slot,
-                                                 scratch + kOsStatus + (size_t)slot * ntiles * 256u,
-                                                 err ? err : scratch + kOsErr);
+    k_os_scatter<K><<<ntiles, RS_THREADS, smem, st>>>(ka, va, kb, vb, n, 8 * d, scratch, slot,
+                                                      scratch + kOsStatus + (size_t)slot * ntiles * 256u,
+                                                      err ? err : scratch + kOsErr);
     std::swap(ka, kb);
     std::swap(va, vb);
     slot++;
@@ -2369,8 +2380,10 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   const bool segmented = opt.segmented != 0;
   const uint32_t nseg = segmented ? (uint32_t)ngeoms : 1u;
   if (segmented && (uint32_t)ngeoms > kMaxSegments) return cudaErrorInvalidValue;
-  k_morton<<<grid_stride_blocks(total), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube, segmented ? 1 : 0,
-                                             opt.morton_bits == 30 ? 1 : 0);
+  const bool key32 = opt.morton_bits == 30 && !segmented;  // 30-bit keys sorted as 32-bit words
+  k_morton<<<grid_stride_blocks(total), 256, 0, st>>>(plo, phi, total, acc, keys_a, vals_a, opt.morton_cube,
+                                                      segmented ? 1 : 0, opt.morton_bits == 30 ? 1 : 0,
+                                                      key32 ? 1 : 0);
   note_launches(1);
   GB_CHECK(cudaGetLastError());
   GB_CHECK(cudaMemcpyAsync(&h_acc, acc, sizeof(BoundsAcc), cudaMemcpyDeviceToHost, st));
@@ -2384,15 +2397,20 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
     return cudaStreamSynchronize(st);
   }
 
-  // ---- radix sort (all `total` keys; invalid ones carry ~0 and sort last), the
-  // digits that are constant over all keys skipped
+  // ---- radix sort (all `total` keys; invalid ones carry a key above every valid
+  // one and sort last), the digits that are constant over all keys skipped
   {
     uint32_t digit_mask = 0;
     for (int d = 0; d < 8; d++)
       if (((h_acc.kand >> (8 * d)) & 0xFF) != ((h_acc.kor >> (8 * d)) & 0xFF)) digit_mask |= 1u << d;
     uint32_t* hist = nullptr;
     GB_CHECK(arena.alloc(&hist, onesweep_scratch_words(total, __builtin_popcount(digit_mask))));
-    GB_CHECK(onesweep_sort(keys_a, vals_a, keys_b, vals_b, total, digit_mask, hist, &acc->pad, st));
+    if (key32) {
+      uint32_t *ka32 = reinterpret_cast<uint32_t*>(keys_a), *kb32 = reinterpret_cast<uint32_t*>(keys_b);
+      GB_CHECK(onesweep_sort(ka32, vals_a, kb32, vals_b, total, digit_mask, hist, &acc->pad, st));
+    } else {
+      GB_CHECK(onesweep_sort(keys_a, vals_a, keys_b, vals_b, total, digit_mask, hist, &acc->pad, st));
+    }
     arena.free(hist);
   }
 
@@ -2759,7 +2777,11 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
   if (e == cudaSuccess)
     e = cudaMemset(g->scan_sums, 0, sizeof(uint32_t) * 2 * scan_scratch(std::max(g->maxb, maxw)));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_os_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsScatterSmem);
+    e = cudaFuncSetAttribute(k_os_scatter<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)os_scatter_smem<uint64_t>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_os_scatter<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)os_scatter_smem<uint32_t>());
   if (e != cudaSuccess) graph_build_release(g);
   const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -2777,8 +2799,10 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   k_acc_init<<<1, 32, 0, st>>>(acc);
   k_primrefs<<<grid_stride_blocks(T), 256, 0, st>>>(g.d_geoms, g.ngeoms, T, g.plo, g.phi, acc, g.prec,
                                                     g.opt.robust ? 1 : 0);
+  const bool key32 = g.opt.morton_bits == 30 && !g.opt.segmented;  // 30-bit keys sorted as 32-bit words
   k_morton<<<grid_stride_blocks(T), 256, 0, st>>>(g.plo, g.phi, T, acc, g.keys_a, g.vals_a, g.opt.morton_cube,
-                                         g.opt.segmented ? 1 : 0, g.opt.morton_bits == 30 ? 1 : 0);
+                                                  g.opt.segmented ? 1 : 0, g.opt.morton_bits == 30 ? 1 : 0,
+                                                  key32 ? 1 : 0);
   note_launches(3);
   stamp(1);
   // all digits of the key width (the ordinary build skips constant ones: the same order)
@@ -2786,7 +2810,12 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   uint32_t *va = g.vals_a, *vb = g.vals_b;
   // the digits the key width can use: 63-bit keys 8, 30-bit keys 4 (6 with the slot)
   const uint32_t digits = g.opt.morton_bits == 30 ? (g.opt.segmented ? 0x3Fu : 0x0Fu) : 0xFFu;
-  GB_CHECK(onesweep_sort(ka, va, kb, vb, T, digits, g.hist, &acc->pad, st));
+  if (key32) {
+    uint32_t *ka32 = reinterpret_cast<uint32_t*>(ka), *kb32 = reinterpret_cast<uint32_t*>(kb);
+    GB_CHECK(onesweep_sort(ka32, va, kb32, vb, T, digits, g.hist, &acc->pad, st));
+  } else {
+    GB_CHECK(onesweep_sort(ka, va, kb, vb, T, digits, g.hist, &acc->pad, st));
+  }
   stamp(2);
   // PLOC: the rounds in one cooperative launch that ends them itself, then the
   // one-CTA finish

@@ -269,3 +269,35 @@ def test_build_phase_timestamps(rtc):
     for s, d in ((sp, dp), (sq, dq)):
         s.release()
         d.release()
+
+
+@pytest.mark.parametrize("config", [b"", b"gpu.morton_bits=63", b"gpu.graph_rebuild=0"])
+def test_invalid_triangles_sort_after_the_corner_triangle(rtc, config):
+    """Invalid triangles (NaN vertices) get a sort key above every valid one: the
+    triangle whose centroid is the largest on all three axes -- the all-ones Morton
+    code -- stays in the tree even when invalid triangles precede it."""
+    from rtcgb import rays as R
+    rng = np.random.default_rng(5)
+    base = (rng.random((600, 3, 3)) * 0.8 + 0.05).astype(np.float32)
+    bad = np.zeros((10, 3, 3), np.float32)
+    bad[:, 0, 0] = np.nan
+    corner = np.array([[[0.99, 0.99, 1.0], [1.0, 0.99, 0.99], [0.99, 1.0, 0.99]]], np.float32)
+    tris = np.concatenate([bad, base, corner])
+    verts = tris.reshape(-1, 3)
+    idx = np.arange(verts.shape[0], dtype=np.uint32).reshape(-1, 3)
+    device = rtc.Device(config)
+    sc = rtc.Scene(device)
+    sc.add_mesh(verts, idx)
+    for _ in range(3):  # host-driven, then replayed rebuilds
+        sc.commit()
+        ray = np.zeros(1, R.RAYHIT_DTYPE)
+        ray["org_x"], ray["org_y"], ray["org_z"] = 2.0, 2.0, 2.0
+        ray["dir_x"] = ray["dir_y"] = ray["dir_z"] = -1.0
+        ray["tnear"], ray["tfar"] = 0.0, np.inf
+        ray["mask"] = 0xFFFFFFFF
+        ray["geomID"], ray["primID"] = 0xFFFFFFFF, 0xFFFFFFFF
+        sc.intersect(ray)
+        assert ray["geomID"][0] == 0 and ray["primID"][0] == idx.shape[0] - 1, ray
+        assert sc.build_stats()["num_prims"] == idx.shape[0] - 10
+    sc.release()
+    device.release()
