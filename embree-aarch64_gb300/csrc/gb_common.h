@@ -31,7 +31,9 @@ constexpr int kStackSize = 64;       // traversal stack entries (node groups)
 // 80-byte wide node.
 //   meta[s]: 0 = empty slot; otherwise bit 7 is set and, for a leaf, bits
 //            5..6 hold (triangle count - 1) and bits 0..4 the first
-//            triangle's offset from tri_base (0..28).
+//            triangle's offset from tri_base (0..28).  An empty slot's box is
+//            inverted (qlo = 255, qhi = 0 on every axis), so the traversal's
+//            slab test misses it without reading meta.
 //   imask:   bit s set when slot s holds an internal child.
 //   ex/ey/ez: IEEE-754 biased exponent of the per-axis scale 2^(e-127).
 //   decoded child box: lo = p + qlo * scale, hi = p + qhi * scale (the

