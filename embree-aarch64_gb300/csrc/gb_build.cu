@@ -710,19 +710,31 @@ __device__ __forceinline__ void dp_store(float4* cost, uint2* choice, uint32_t n
   __stcg(choice + n, ch);
 }
 
-// cost(n, 1..8) and the choices of binary node n with children l and r, whose
-// costs are stored already; A is n's box area, cnt its triangles.  The PLOC
-// kernels call it as they create each node, so the table is complete when the
-// clustering ends (children are always created before their parent).
-__device__ __forceinline__ void dp_node(float4* cost, uint2* choice, uint32_t n, uint32_t l, uint32_t r, float A,
-                                        uint32_t cnt, uint32_t leaf_max) {
-  float cl[8], cr[8];
-  {
-    const float4 a = __ldcg(cost + 2 * (size_t)l), b = __ldcg(cost + 2 * (size_t)l + 1);
-    const float4 e = __ldcg(cost + 2 * (size_t)r), f = __ldcg(cost + 2 * (size_t)r + 1);
-    cl[0] = a.x; cl[1] = a.y; cl[2] = a.z; cl[3] = a.w; cl[4] = b.x; cl[5] = b.y; cl[6] = b.z; cl[7] = b.w;
-    cr[0] = e.x; cr[1] = e.y; cr[2] = e.z; cr[3] = e.w; cr[4] = f.x; cr[5] = f.y; cr[6] = f.z; cr[7] = f.w;
+// A child's cost(., 1..8): a primitive (one triangle) costs its box area
+// whatever the number of slots (one leaf block), so primitives have no table
+// entries and the caller passes their areas; internal children's costs are
+// stored already.
+__device__ __forceinline__ void dp_child_costs(const float4* cost, uint32_t c, uint32_t cnt_c, float Ac, float (&out)[8]) {
+  if (cnt_c == 1) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) out[i] = Ac;
+    return;
   }
+  const float4 a = __ldcg(cost + 2 * (size_t)c), b = __ldcg(cost + 2 * (size_t)c + 1);
+  out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w; out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+}
+
+// cost(n, 1..8) and the choices of binary node n with children l and r (cnt_l,
+// cnt_r triangles; a child of one triangle is a primitive, whose area Al / Ar
+// the caller passes); A is n's box area.  The PLOC kernels call it as they
+// create each node, so the table is complete when the clustering ends
+// (children are always created before their parent).
+__device__ __forceinline__ void dp_node(float4* cost, uint2* choice, uint32_t n, uint32_t l, uint32_t r, float A,
+                                        uint32_t cnt_l, uint32_t cnt_r, float Al, float Ar, uint32_t leaf_max) {
+  const uint32_t cnt = cnt_l + cnt_r;
+  float cl[8], cr[8];
+  dp_child_costs(cost, l, cnt_l, Al, cl);
+  dp_child_costs(cost, r, cnt_r, Ar, cr);
   float D[9];
   uint32_t K[9];
 #pragma unroll
@@ -754,11 +766,6 @@ __device__ __forceinline__ void dp_node(float4* cost, uint2* choice, uint32_t n,
            make_uint2(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24), b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24)));
 }
 
-// A primitive: one triangle, one block, whatever the number of slots.
-__device__ __forceinline__ void dp_leaf(float4* cost, uint2* choice, uint32_t n, float A) {
-  const float c[8] = {A, A, A, A, A, A, A, A};
-  dp_store(cost, choice, n, c, make_uint2(0u, 0u));
-}
 
 // Grid barrier of the cooperative build kernels (all CTAs resident).
 struct GridBarrier {
@@ -824,8 +831,7 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
                                                    const uint32_t* __restrict__ d_n,
                                                    float4* __restrict__ bnlo, float4* __restrict__ bnhi,
                                                    uint32_t* __restrict__ bncnt, uint32_t* __restrict__ cidx,
-                                                   float4* __restrict__ clo, float4* __restrict__ chi, int segmented,
-                                                   float4* __restrict__ dp_cost, uint2* __restrict__ dp_choice) {
+                                                   float4* __restrict__ clo, float4* __restrict__ chi, int segmented) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || i >= *d_n) return;  // n bounds the grid, *d_n is the count of valid primitives
   const uint32_t p = sorted[i];
@@ -833,7 +839,6 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
   bnlo[i] = make_float4(a.x, a.y, a.z, __int_as_float(-1));
   bnhi[i] = make_float4(b.x, b.y, b.z, __uint_as_float(p));
   bncnt[i] = 1;
-  if (dp_cost) dp_leaf(dp_cost, dp_choice, i, half_area(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)));
   cidx[i] = i;
   clo[i] = make_float4(a.x, a.y, a.z, segmented ? a.w : __uint_as_float(0u));
   chi[i] = make_float4(b.x, b.y, b.z, 0.f);
@@ -1009,11 +1014,12 @@ __device__ __forceinline__ void ploc_emit_tile(const PlocBufs& bufs, uint32_t pa
     const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
     bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
     bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-    const uint32_t cnt = bncnt[l] + bncnt[r];
-    bncnt[id] = cnt;
+    const uint32_t cnt_l = bncnt[l], cnt_r = bncnt[r];
+    bncnt[id] = cnt_l + cnt_r;
     if (dp_cost)
       dp_node(dp_cost, dp_choice, id, l, r, half_area(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z)),
-              cnt, leaf_max);
+              cnt_l, cnt_r, cnt_l == 1 ? half_area(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)) : 0.f,
+              cnt_r == 1 ? half_area(make_float3(c.x, c.y, c.z), make_float3(d.x, d.y, d.z)) : 0.f, leaf_max);
     olo[pos] = lo;
     ohi[pos] = hi;
     oidx[pos] = id;
@@ -1292,15 +1298,17 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
             atomicOr(err, kErrBuild);
             break;
           }
+          const uint32_t cnt_l = bncnt[l], cnt_r = bncnt[r];
+          const float Al = cnt_l == 1 ? half_area(lo, hi) : 0.f;
+          const float Ar = cnt_r == 1 ? half_area(s_lo[j], s_hi[j]) : 0.f;
           lo = f3min(lo, s_lo[j]);
           hi = f3max(hi, s_hi[j]);
           bnlo[nid] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
           bnhi[nid] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-          const uint32_t cnt = bncnt[l] + bncnt[r];
-          bncnt[nid] = cnt;
+          bncnt[nid] = cnt_l + cnt_r;
           // children come from earlier rounds: their costs were stored before
           // this round's barriers
-          if (dp_cost) dp_node(dp_cost, dp_choice, nid, l, r, half_area(lo, hi), cnt, leaf_max);
+          if (dp_cost) dp_node(dp_cost, dp_choice, nid, l, r, half_area(lo, hi), cnt_l, cnt_r, Al, Ar, leaf_max);
           id = nid;
           pm++;
         }
@@ -2457,7 +2465,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   GB_CHECK(arena.alloc(&nn, N));
   const uint32_t leaf_max_used = (uint32_t)std::min(std::max(leaf_max, 1), kLeafMaxLimit);
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(plo, phi, vals_a, N, &acc->nvalid, bnlo, bnhi, bncnt, cidx_a, clo_a,
-                                            chi_a, segmented ? 1 : 0, dp_cost, d_choice);
+                                            chi_a, segmented ? 1 : 0);
   note_launches(1);
   uint32_t *bsurv, *bmerge, *d_tot, *d_root, *d_iters;
   const uint32_t maxb = cdiv(N, PLOC_BLOCK);
@@ -2825,7 +2833,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   float4* dp_cost = g.opt.collapse == 1 ? g.cost : nullptr;
   uint2* dp_choice = g.opt.collapse == 1 ? g.choice : nullptr;
   k_ploc_init<<<cdiv(N, 256), 256, 0, st>>>(g.plo, g.phi, va, N, &acc->nvalid, g.bnlo, g.bnhi, g.bncnt, g.cidx[0],
-                                            g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0, dp_cost, dp_choice);
+                                            g.clo[0], g.chi[0], g.opt.segmented ? 1 : 0);
   stamp(3);
   k_ploc_state_init<<<1, 32, 0, st>>>(acc, g.ploc_state);
   note_launches(2);
