@@ -822,10 +822,14 @@ constexpr int PLOC_R_MAX = 16;
 constexpr int PLOC_BLOCK = 256;
 constexpr uint32_t PLOC_SMALL = 4096;   // finish on one CTA below this many clusters
 constexpr int PLOC_SMALL_THREADS = 1024;
+// k_ploc_small's shared memory: boxes, node ids, nearest neighbours, segments, counts
+constexpr size_t kPlocSmallSmem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 4 * sizeof(uint32_t));
 
 // binary nodes: bnlo[k] = (lo.xyz, left), bnhi[k] = (hi.xyz, right);
 // leaves k < N: left = -1, right = primref index
-// Cluster boxes carry their segment in clo.w (0 unless the build is segmented).
+// Cluster boxes carry their segment in clo.w (0 unless the build is segmented)
+// and their triangle count in chi.w (so a merge has both children's counts
+// with their boxes, without a dependent read of bncnt).
 __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                    const uint32_t* __restrict__ sorted, uint32_t n,
                                                    const uint32_t* __restrict__ d_n,
@@ -841,7 +845,7 @@ __global__ void __launch_bounds__(256) k_ploc_init(const float4* __restrict__ pl
   bncnt[i] = 1;
   cidx[i] = i;
   clo[i] = make_float4(a.x, a.y, a.z, segmented ? a.w : __uint_as_float(0u));
-  chi[i] = make_float4(b.x, b.y, b.z, 0.f);
+  chi[i] = make_float4(b.x, b.y, b.z, __uint_as_float(1u));
 }
 
 // PLOC rounds run back to back without the host.  ploc_state (device memory):
@@ -1011,10 +1015,10 @@ __device__ __forceinline__ void ploc_emit_tile(const PlocBufs& bufs, uint32_t pa
     }
     const uint32_t l = cidx[i], r = cidx[j];
     const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), a.w);
-    const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
+    const uint32_t cnt_l = __float_as_uint(b.w), cnt_r = __float_as_uint(d.w);
+    const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), __uint_as_float(cnt_l + cnt_r));
     bnlo[id] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
     bnhi[id] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-    const uint32_t cnt_l = bncnt[l], cnt_r = bncnt[r];
     bncnt[id] = cnt_l + cnt_r;
     if (dp_cost)
       dp_node(dp_cost, dp_choice, id, l, r, half_area(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z)),
@@ -1194,6 +1198,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
   uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_hi + PLOC_SMALL);
   uint32_t* s_nn = s_idx + PLOC_SMALL;
   uint32_t* s_seg = s_nn + PLOC_SMALL;
+  uint32_t* s_cnt = s_seg + PLOC_SMALL;
   __shared__ uint32_t s_w[32];
   __shared__ uint32_t s_tot[2];
   constexpr int EPT = PLOC_SMALL / PLOC_SMALL_THREADS;  // elements per thread (contiguous)
@@ -1212,6 +1217,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
     s_hi[k] = make_float3(b.x, b.y, b.z);
     s_idx[k] = cidx[k];
     s_seg[k] = __float_as_uint(a.w);
+    s_cnt[k] = __float_as_uint(b.w);
   }
   uint32_t n = n0, node_next = node_next0, iters = 0;
   __syncthreads();
@@ -1282,14 +1288,14 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
     uint32_t ps = excl & 0xFFFFu, pm = excl >> 16;
     // gather outputs into registers
     float3 olo[EPT], ohi[EPT];
-    uint32_t oidx[EPT], opos[EPT], oseg[EPT];
+    uint32_t oidx[EPT], opos[EPT], oseg[EPT], ocnt[EPT];
 #pragma unroll
     for (int e = 0; e < EPT; e++) {
       const uint32_t i = i0 + e;
       opos[e] = 0xFFFFFFFFu;
       if (i < n && fs[e]) {
         float3 lo = s_lo[i], hi = s_hi[i];
-        uint32_t id = s_idx[i];
+        uint32_t id = s_idx[i], cnt = s_cnt[i];
         if (fm[e]) {
           const uint32_t j = s_nn[i];
           const uint32_t nid = node_next + pm;
@@ -1298,14 +1304,15 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
             atomicOr(err, kErrBuild);
             break;
           }
-          const uint32_t cnt_l = bncnt[l], cnt_r = bncnt[r];
+          const uint32_t cnt_l = cnt, cnt_r = s_cnt[j];
           const float Al = cnt_l == 1 ? half_area(lo, hi) : 0.f;
           const float Ar = cnt_r == 1 ? half_area(s_lo[j], s_hi[j]) : 0.f;
           lo = f3min(lo, s_lo[j]);
           hi = f3max(hi, s_hi[j]);
           bnlo[nid] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(l));
           bnhi[nid] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(r));
-          bncnt[nid] = cnt_l + cnt_r;
+          cnt = cnt_l + cnt_r;
+          bncnt[nid] = cnt;
           // children come from earlier rounds: their costs were stored before
           // this round's barriers
           if (dp_cost) dp_node(dp_cost, dp_choice, nid, l, r, half_area(lo, hi), cnt_l, cnt_r, Al, Ar, leaf_max);
@@ -1316,6 +1323,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
         ohi[e] = hi;
         oidx[e] = id;
         oseg[e] = s_seg[i];
+        ocnt[e] = cnt;
         opos[e] = ps++;
       }
     }
@@ -1327,6 +1335,7 @@ __global__ void __launch_bounds__(PLOC_SMALL_THREADS) k_ploc_small(const float4*
         s_hi[opos[e]] = ohi[e];
         s_idx[opos[e]] = oidx[e];
         s_seg[opos[e]] = oseg[e];
+        s_cnt[opos[e]] = ocnt[e];
       }
     }
     const uint32_t merged = s_tot[1];
@@ -2526,7 +2535,7 @@ cudaError_t build_bvh(const GeomDesc* h_geoms, int ngeoms, cudaStream_t st, cons
   // segments it means every segment is down to one cluster (<= kMaxSegments)
   const uint32_t iters = round > 0 ? h_tot[kPlocRounds] : 0u;
   {
-    const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
+    const size_t smem = kPlocSmallSmem;
     GB_CHECK(cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(clo_a, chi_a, cidx_a, clo_b, chi_b, cidx_b, ploc_state, bnlo,
                                                       bnhi, bncnt, d_root, d_iters, nnodes_bin, &acc->pad, nseg,
@@ -2791,7 +2800,7 @@ cudaError_t graph_build_prepare(const GeomDesc* h_geoms, int ngeoms, const Build
     e = cudaFuncSetAttribute(k_os_scatter<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)os_scatter_smem<uint32_t>());
   if (e != cudaSuccess) graph_build_release(g);
-  const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
+  const size_t smem = kPlocSmallSmem;
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return e;
 }
@@ -2874,7 +2883,7 @@ cudaError_t graph_build_enqueue(const GraphBuild& g, cudaStream_t st) {
   }
   stamp(4);
   {
-    const size_t smem = (size_t)PLOC_SMALL * (2 * sizeof(float3) + 3 * sizeof(uint32_t));
+    const size_t smem = kPlocSmallSmem;
     k_ploc_small<<<1, PLOC_SMALL_THREADS, smem, st>>>(g.clo[0], g.chi[0], g.cidx[0], g.clo[1], g.chi[1], g.cidx[1],
                                                       g.ploc_state, g.bnlo, g.bnhi, g.bncnt, g.d_root, g.d_iters,
                                                       nbin_cap, &acc->pad, g.nseg, (int)g.radius, dp_cost, dp_choice,
