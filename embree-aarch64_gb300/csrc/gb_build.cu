@@ -1551,6 +1551,10 @@ __global__ void __launch_bounds__(1024) k_collapse_roots(const uint32_t* __restr
   }
 }
 
+// leaf_root entry of a one-triangle leaf: the primitive index with this bit set
+// (primitive indices and binary node ids are below 2^31)
+constexpr uint32_t kLeafPrim = 0x80000000u;
+
 // The two item buffers of the collapse levels: level d reads items[d & 1] and writes
 // items[(d & 1) ^ 1] (d = cstate[kColDepth]), so every level runs the same kernels
 // with the same arguments.
@@ -1783,7 +1787,7 @@ __device__ __forceinline__ void collapse_emit_node(
         atomicOr(err, kErrBuild);
         return;
       }
-      leaf_root[node.tri_base + tri_off] = c;
+      leaf_root[node.tri_base + tri_off] = cnt == 1 ? bt_right(t, c) | kLeafPrim : c;
       tri_off += cnt;
       sah += A * (double)((cnt + 3) / 4);  // leaf term: area x Triangle4 blocks
       sahx += Ax * (double)((cnt + 3) / 4);
@@ -1920,7 +1924,7 @@ __device__ __forceinline__ void collapse_emit_group(
     // k_write_leaves, one thread per leaf: here only its binary subtree is
     // recorded at the slot of its first triangle
     if (tri_base + tri_off + cnt > tri_cap) atomicOr(err, kErrBuild);
-    else leaf_root[tri_base + tri_off] = kid;
+    else leaf_root[tri_base + tri_off] = cnt == 1 ? bt_right(t, kid) | kLeafPrim : kid;
     sah_out += A * (double)((cnt + 3) / 4);  // leaf term: area x Triangle4 blocks
     sahx_out += Ax * (double)((cnt + 3) / 4);
     nleaf_out++;
@@ -2179,8 +2183,9 @@ __global__ void __launch_bounds__(COLLAPSE_ALL_THREADS, 2) k_collapse_all(
 }
 
 // Writes the triangle records of every leaf: slot t holds the binary subtree of
-// the leaf whose first triangle goes to t (kInvalidID elsewhere); its
-// primitives (at most 4) are written in depth-first order, left first.
+// the leaf whose first triangle goes to t, or for a one-triangle leaf its
+// primitive with kLeafPrim set (kInvalidID elsewhere); a subtree's primitives
+// (at most 4) are written in depth-first order, left first.
 __global__ void __launch_bounds__(256) k_write_leaves(BinTree t, const GeomDesc* __restrict__ geoms,
                                                       const float4* __restrict__ plo, const float4* __restrict__ phi,
                                                       const uint32_t* __restrict__ leaf_root, uint32_t ntris,
@@ -2190,6 +2195,12 @@ __global__ void __launch_bounds__(256) k_write_leaves(BinTree t, const GeomDesc*
   if (first >= ntris) return;
   const uint32_t c = leaf_root[first];
   if (c == kInvalidID) return;
+  if (c & kLeafPrim) {  // one triangle: its primitive, no subtree to walk
+    const uint32_t prim = c & ~kLeafPrim;
+    if (prec) tris[first] = prec[prim];
+    else write_tri(geoms, plo, phi, prim, &tris[first], t.robust != 0);
+    return;
+  }
   uint32_t st[8];
   int sp = 0;
   st[sp++] = c;
