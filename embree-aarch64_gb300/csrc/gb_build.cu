@@ -1396,6 +1396,13 @@ struct BinTree {
 };
 
 __device__ __forceinline__ bool bt_leaf(const BinTree& t, uint32_t k) { return k < t.nleaves; }
+// Triangles of binary node k as the collapse needs them: with one-triangle
+// leaves only "one (a primitive) or more" matters, so no count is read (2
+// stands for any internal node).
+__device__ __forceinline__ uint32_t bt_cnt(const BinTree& t, uint32_t k) {
+  if (t.leaf_max == 1) return bt_leaf(t, k) ? 1u : 2u;
+  return t.cnt[k];
+}
 __device__ __forceinline__ uint32_t bt_left(const BinTree& t, uint32_t k) { return __float_as_uint(t.lo[k].w); }
 __device__ __forceinline__ uint32_t bt_right(const BinTree& t, uint32_t k) { return __float_as_uint(t.hi[k].w); }
 __device__ __forceinline__ float3 bt_lo(const BinTree& t, uint32_t k) {
@@ -1575,7 +1582,7 @@ __global__ void __launch_bounds__(128) k_collapse_count(BinTree t, const ColItem
     for (int i = 0; i < 8; i++) {
       if (i < nk) {
         const uint32_t c = kids[i];
-        const uint32_t cnt = t.cnt[c];
+        const uint32_t cnt = bt_cnt(t, c);
         if (cnt > t.leaf_max) ni++; else nt += cnt;
         kids_out[8 * (size_t)k + i] = c;
       } else {
@@ -1766,7 +1773,7 @@ __device__ __forceinline__ void collapse_emit_node(
     const float3 dhi = make_float3(__fmaf_ru(qhx, sx, ulo.x), __fmaf_ru(qhy, sy, ulo.y), __fmaf_ru(qhz, sz, ulo.z));
     const double A = (double)fmaxf(0.f, half_area(dlo, dhi));
     const double Ax = (double)fmaxf(0.f, half_area(a, b));
-    const uint32_t cnt = t.cnt[c];
+    const uint32_t cnt = bt_cnt(t, c);
     if (cnt > t.leaf_max) {
       node.meta[s] = (uint8_t)(0x80u | (uint32_t)s);
       node.imask |= (uint8_t)(1u << s);
@@ -1896,7 +1903,7 @@ __device__ __forceinline__ void collapse_emit_group(
     const float3 dhi = make_float3(__fmaf_ru(fhx, sx, ulo.x), __fmaf_ru(fhy, sy, ulo.y), __fmaf_ru(fhz, sz, ulo.z));
     A = (double)fmaxf(0.f, half_area(dlo, dhi));
     Ax = (double)fmaxf(0.f, half_area(lo, hi));
-    cnt = t.cnt[kid];
+    cnt = bt_cnt(t, kid);
     internal = cnt > t.leaf_max;
   }
   const uint32_t slot = valid ? (uint32_t)my_slot : 8u;
@@ -2083,7 +2090,7 @@ __global__ void __launch_bounds__(COLLAPSE_ALL_THREADS, 2) k_collapse_all(
       for (int i = 0; i < 8; i++) {
         if (i < nk) {
           const uint32_t c = kk[i];
-          const uint32_t cnt = t.cnt[c];
+          const uint32_t cnt = bt_cnt(t, c);
           if (cnt > t.leaf_max) ni++; else nt += cnt;
           kids[8 * (size_t)k + i] = c;
         } else {
