@@ -923,6 +923,28 @@ __device__ __forceinline__ void ploc_nn_tile(const float4* __restrict__ clo, con
   __syncthreads();  // the window is reloaded for the next tile
 }
 
+// The same nearest neighbour for one cluster h, read from global memory (the
+// halo clusters just outside a CTA's run of tiles; bit-identical to the tile
+// form: same boxes, same area arithmetic, the least (area, index) key).
+template <int PLOC_R>
+__device__ __forceinline__ uint32_t ploc_nn_one(const float4* __restrict__ clo, const float4* __restrict__ chi,
+                                                uint32_t n, int h) {
+  const float4 a = clo[h], b = chi[h];
+  const float3 lo = make_float3(a.x, a.y, a.z), hi = make_float3(b.x, b.y, b.z);
+  const uint32_t seg = __float_as_uint(a.w);
+  unsigned long long best = ~0ull;
+  for (int o = -PLOC_R; o <= PLOC_R; o++) {
+    const int j = h + o;
+    if (o == 0 || j < 0 || j >= (int)n) continue;
+    const float4 c = clo[j], d = chi[j];
+    if (__float_as_uint(c.w) != seg) continue;
+    const float ar = half_area(f3min(lo, make_float3(c.x, c.y, c.z)), f3max(hi, make_float3(d.x, d.y, d.z)));
+    const unsigned long long key = ((unsigned long long)__float_as_uint(ar) << 32) | (uint32_t)j;
+    best = key < best ? key : best;
+  }
+  return best != ~0ull ? (uint32_t)best : (uint32_t)h;
+}
+
 template <int PLOC_R>
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_nn(const PlocBufs bufs, const uint32_t* __restrict__ ploc_state,
                                                         uint32_t* __restrict__ nn) {
@@ -1068,12 +1090,14 @@ __global__ void k_ploc_advance(const uint32_t* __restrict__ tot, uint32_t* __res
 }
 
 // All PLOC rounds above PLOC_SMALL clusters in one cooperative launch (captured
-// builds): per round (A) nearest neighbours, [barrier], (B) survivors and
-// merges of each tile, per-CTA sums, [barrier], (C) this CTA's offsets from the
-// sums and its tiles' outputs, [barrier].  Each CTA takes a contiguous run of
-// tiles and keeps the round state (the k_ploc_advance rules) in registers; CTA 0
-// writes it back to ploc_state.  cta_sums holds 2 * gridDim.x words; *bar is
-// zero on entry.
+// builds): per round (A) nearest neighbours of the CTA's contiguous run of
+// tiles and of the PLOC_R clusters either side of it, (B) survivors and merges
+// of each tile (mutual pairs decided from A alone), per-CTA sums, [barrier],
+// (C) this CTA's offsets from the sums and its tiles' outputs, [barrier]: two
+// grid barriers per round (with a third between A and B the 4M soup rebuilt
+// in 2.50 ms, without it 2.46).  Each CTA keeps the round state (the k_ploc_advance
+// rules) in registers; CTA 0 writes it back to ploc_state.  cta_sums holds
+// 2 * gridDim.x words; *bar is zero on entry.
 template <int PLOC_R>
 __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_all(const PlocBufs bufs, uint32_t* __restrict__ ploc_state,
                                                          uint32_t* __restrict__ nn, uint32_t* __restrict__ tile_s,
@@ -1086,6 +1110,7 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_all(const PlocBufs bufs, ui
   __shared__ uint32_t s_seg[PLOC_BLOCK + 2 * PLOC_R];
   __shared__ uint32_t s_w[PLOC_BLOCK / 32];
   __shared__ uint32_t s_red[4][PLOC_BLOCK / 32];
+  __shared__ uint32_t s_halo_nn[2 * PLOC_R];  // nearest neighbours of the R clusters either side of the run
   uint32_t n = __ldcg(ploc_state + kPlocN), node_next = __ldcg(ploc_state + kPlocNext);
   uint32_t par = __ldcg(ploc_state + kPlocParity) & 1u, rounds = __ldcg(ploc_state + kPlocRounds);
   uint32_t iters = __ldcg(ploc_state + kPlocIters);
@@ -1094,18 +1119,30 @@ __global__ void __launch_bounds__(PLOC_BLOCK) k_ploc_all(const PlocBufs bufs, ui
     const uint32_t ntiles = (n + PLOC_BLOCK - 1) / PLOC_BLOCK;
     const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
     const uint32_t t0 = min(blockIdx.x * per, ntiles), t1 = min(t0 + per, ntiles);
-    // (A) nearest neighbours
+    // (A) nearest neighbours of this CTA's run of tiles [r0, r1), and of the R
+    // clusters either side of it (computed here as their own CTAs compute
+    // them), so that (B) needs no grid barrier before it
+    const int r0 = (int)(t0 * PLOC_BLOCK), r1 = (int)min(t1 * PLOC_BLOCK, n);
     for (uint32_t tile = t0; tile < t1; tile++)
       ploc_nn_tile<PLOC_R>(bufs.clo[par], bufs.chi[par], n, tile, nn, s_lo, s_hi, s_seg);
-    if (!grid_sync(bar, err)) break;
-    // (B) survivors and merges per tile
+    if (threadIdx.x < 2 * PLOC_R && t0 < t1) {
+      const int h = threadIdx.x < PLOC_R ? r0 - PLOC_R + (int)threadIdx.x : r1 + (int)threadIdx.x - PLOC_R;
+      if (h >= 0 && h < (int)n) s_halo_nn[threadIdx.x] = ploc_nn_one<PLOC_R>(bufs.clo[par], bufs.chi[par], n, h);
+    }
+    __syncthreads();
+    // (B) survivors and merges per tile (the run's nn written above by this CTA)
+    auto nn_of = [&](uint32_t j) -> uint32_t {
+      if ((int)j < r0) return s_halo_nn[(int)j - (r0 - PLOC_R)];
+      if ((int)j >= r1) return s_halo_nn[PLOC_R + (int)j - r1];
+      return nn[j];
+    };
     uint32_t cs_sum = 0, cm_sum = 0;
     for (uint32_t tile = t0; tile < t1; tile++) {
       const uint32_t i = tile * PLOC_BLOCK + threadIdx.x;
       int surv = 0, merge = 0;
       if (i < n) {
         const uint32_t j = nn[i];
-        const bool mutual = (j != i) && nn[j] == i;
+        const bool mutual = (j != i) && nn_of(j) == i;
         merge = mutual && i < j;
         surv = !(mutual && j < i);
       }
